@@ -1,0 +1,50 @@
+/*
+ * cuda_cpu_shim.h -- lets the reference's CUDA kernels (which use no shared
+ * memory, no barriers and no atomics) be compiled by g++ and executed on the
+ * CPU, one (block, thread) at a time.  TEST INFRASTRUCTURE ONLY: used to build
+ * oracle/_ref/, the reference's own kernels run on the host, which pins the
+ * C restatement in oracle/amps_oracle.c.
+ *
+ * device_launch_parameters.h declares threadIdx/blockIdx with a __STORAGE__
+ * prefix; defining it empty turns them into ordinary mutable globals that the
+ * launch loop below sets before each "thread" runs.
+ */
+#ifndef CUDA_CPU_SHIM_H
+#define CUDA_CPU_SHIM_H
+#define __STORAGE__
+#include <cuda_runtime.h>
+#include <device_launch_parameters.h>
+#include <cuda_fp16.h>
+#include <mma.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <iostream>
+#include <fstream>
+#include <string>
+#include <sstream>
+#include <unistd.h>
+#include <math.h>
+#include <cmath>
+#include <algorithm>
+namespace nvcuda {}
+#undef __global__
+#define __global__ static
+
+/* Run kernel k over grid g x block b sequentially. */
+template <typename K, typename... A>
+static void shim_launch(dim3 g, dim3 b, K k, A... args)
+{
+    for (unsigned bz = 0; bz < g.z; ++bz)
+        for (unsigned by = 0; by < g.y; ++by)
+            for (unsigned bx = 0; bx < g.x; ++bx)
+                for (unsigned tz = 0; tz < b.z; ++tz)
+                    for (unsigned ty = 0; ty < b.y; ++ty)
+                        for (unsigned tx = 0; tx < b.x; ++tx) {
+                            blockIdx.x = bx; blockIdx.y = by; blockIdx.z = bz;
+                            threadIdx.x = tx; threadIdx.y = ty; threadIdx.z = tz;
+                            blockDim.x = b.x; blockDim.y = b.y; blockDim.z = b.z;
+                            gridDim.x = g.x; gridDim.y = g.y; gridDim.z = g.z;
+                            k(args...);
+                        }
+}
+#endif
