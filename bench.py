@@ -1,0 +1,362 @@
+"""Benchmark: adaptive mixed-precision grain growth, 1024x1024, Q=8 (Fan-Chen,
+gamma=1.5, kappa=2, L=1, dx=1, dt=0.05, periodic, eta_i ~ U[-1e-3, 1e-3]),
+one bench step = one complete 10000-step run from the seeded initial state.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--sim-steps S]
+
+Prints one JSON line.  `value` is Gcell-updates/s (cells x time steps / s)
+with the initial state already in HBM; `e2e` is the same metric through the
+C ABI from pinned host memory, including the host->device copy of the initial
+fields and the device->host read of the final fields.  `plain_fp64` is the
+plain-FP64 path on the same workload and `max_abs_err` the adaptive run's
+error against it.  `roofline` covers the dominant update kernel, timed with
+CUDA events on its launching stream during a profiled run.
+
+--impl reference times the reference's FP64 update restated as a host
+OpenMP loop (the oracle: the reference has no CPU implementation of its own)
+on a bounded sample of the same workload, on all host cores.
+
+Multi-GPU: the path does not shard (one grid per GPU); N ranks run N
+independent replicas (weak scaling).
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = "graingrowth Fan-Chen Q=8 1024x1024 adaptive half/fp32/fp64, 10000 steps per run"
+METRIC = "Gcell-updates/s"
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+                for k, n in enumerate(names):
+                    if r[5 + k].lower().startswith("active"):
+                        reasons.add(n)
+            except Exception:
+                continue
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def oracle_rate(nx, q, steps, threads):
+    """FP64 oracle grain-growth step on the host cores: Gcell-updates/s."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    import oracle_bind as ob
+    import w3914777_gb300 as w
+    p = w.Params.preset("graingrowth", 0, nx=nx, ny=nx, nfields=q)
+    f0 = w.init_host(p, w.INIT_SEEDED)
+    op = ob.gg_params(nx, nx, q=q, dx=1.0, dy=1.0, dt=0.05, mobil=1.0, grcoef=2.0, gamma=1.5)
+    ob.gg_run(op, list(f0), 1)  # warm the thread pool
+    t0 = time.perf_counter()
+    ob.gg_run(op, list(f0), steps)
+    dt = time.perf_counter() - t0
+    return nx * nx * steps / dt / 1e9, dt
+
+
+def run_reference(args):
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return
+    threads = cpu_threads()
+    sample = args.ref_sample_steps
+    rates = []
+    for i in range(args.warmup + args.steps):
+        r, dt = oracle_rate(1024, 8, sample, threads)
+        if i >= args.warmup:
+            rates.append((r, dt))
+    value = statistics.median([r for r, _ in rates])
+    ms = statistics.median([dt for _, dt in rates]) * 1e3
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "Gcell-updates/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "nx": 1024, "ny": 1024, "Q": 8,
+                   "sample": f"{sample} FP64 steps of the 1024^2 Q=8 grid per bench step"},
+        "cpu_baseline": {"value": value, "unit": "Gcell-updates/s", "cores": threads, "kind": "port",
+                         "sample": f"{sample} steps of 1024x1024 Q=8 FP64 (oracle restatement of "
+                                   "graingrowth/function.h:5-30, OpenMP over rows)"},
+        "e2e": {"value": value, "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    import w3914777_gb300 as w
+
+    world, rank, local = dist_setup()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    S = args.sim_steps
+    p = w.Params.preset("graingrowth", 0)
+    if args.tile:
+        p.tile = args.tile
+    nf = p.num_fields
+    cells = p.nx * p.ny
+    host0 = torch.from_numpy(w.init_host(p, w.INIT_SEEDED)).pin_memory()
+    dev0 = host0.to(dev)
+    host_out = torch.empty_like(host0).pin_memory()
+    stream = torch.cuda.Stream(device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # 256 MiB > L2
+
+    sim = w.Simulation(p)
+    sim.set_stream(stream.cuda_stream)
+
+    def one_run_device():
+        sim.set_fields_device(dev0.data_ptr())
+        sim.run(S)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    # warm-up (also captures the CUDA graph of a period)
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            one_run_device()
+    torch.cuda.synchronize()
+
+    # ---- device-resident timing ----
+    evs = []
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t_wall = time.perf_counter()
+        with torch.cuda.stream(stream):
+            for _ in range(args.steps):
+                flush.zero_()
+                a = torch.cuda.Event(enable_timing=True)
+                b = torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                one_run_device()
+                b.record(stream)
+                evs.append((a, b))
+        torch.cuda.synchronize()
+        t_wall = time.perf_counter() - t_wall
+    barrier()
+    ms = [a.elapsed_time(b) for a, b in evs]
+    total_ms = sum(ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * cells * S * args.steps / (total_ms * 1e-3) / 1e9
+    stats = sim.stats()
+    final_mixed = sim.fields()
+
+    # ---- end-to-end through the C ABI from pinned host memory ----
+    e2e_ms = []
+    for _ in range(max(1, args.steps)):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        lib = w.lib()
+        rc = lib.amps_set_fields(sim.h, ctypes.c_void_p(host0.data_ptr()), w.F64, 0)
+        assert rc == 0
+        sim.run(S)
+        rc = lib.amps_get_fields(sim.h, ctypes.c_void_p(host_out.data_ptr()), w.F64, 0)
+        assert rc == 0
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    e2e_total = sum(e2e_ms)
+    if world > 1:
+        t = torch.tensor([e2e_total], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_total = float(t.item())
+    e2e = world * cells * S * len(e2e_ms) / (e2e_total * 1e-3) / 1e9
+    bytes_io = nf * cells * 8
+
+    # ---- profiled run: per-tier kernel durations for the roofline ----
+    sim.set_fields_device(dev0.data_ptr())
+    sim.set_profiling(True)
+    sim.run(S)
+    kms, klaunch, ktiles = sim.kernel_times()
+    sim.set_profiling(False)
+    T = p.tile
+    tier_bytes = [2, 4, 8]
+    names = ["gg_step half", "gg_step fp32", "gg_step fp64"]
+    dom = int(np.argmax(kms))
+    per_launch_bytes = ktiles[dom] * T * T * nf * 2 * tier_bytes[dom] / max(klaunch[dom], 1)
+    per_launch_s = kms[dom] * 1e-3 / max(klaunch[dom], 1)
+    achieved = per_launch_bytes / per_launch_s / 1e9 if per_launch_s > 0 else 0.0
+    peak, peak_kind = peaks()
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        try:
+            with open(tpath) as f:
+                tr = json.load(f)
+            # DRAM bytes per tile-step of this tier kernel, from the ncu capture
+            per_tile = tr.get(names[dom].replace(" ", "_"))
+            if per_tile:
+                traffic = per_tile * ktiles[dom] / max(klaunch[dom], 1)
+        except Exception:
+            traffic = None
+    all_kernels = {names[k]: {"ms": kms[k], "launches": klaunch[k], "tile_steps": ktiles[k],
+                              "GB/s": (ktiles[k] * T * T * nf * 2 * tier_bytes[k] / (kms[k] * 1e-3) / 1e9)
+                              if kms[k] > 0 else None} for k in range(3)}
+
+    # ---- plain FP64 path on the same workload + error of the adaptive run ----
+    pf = p.replace(mode="purehigh", ref_order=0)
+    with w.Simulation(pf) as s64:
+        s64.set_stream(stream.cuda_stream)
+        with torch.cuda.stream(stream):
+            s64.set_fields_device(dev0.data_ptr())
+            s64.run(10)
+            torch.cuda.synchronize()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            s64.set_fields_device(dev0.data_ptr())
+            a.record(stream)
+            s64.run(S)
+            b.record(stream)
+        torch.cuda.synchronize()
+        fp64_ms = a.elapsed_time(b)
+        final64 = s64.fields()
+    plain = cells * S / (fp64_ms * 1e-3) / 1e9
+    err = float(np.max(np.abs(final_mixed - final64)))
+
+    # ---- CPU baseline (oracle port on host cores), rank 0 only ----
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        threads = cpu_threads()
+        r, dt = oracle_rate(1024, 8, args.ref_sample_steps, threads)
+        cpu = {"value": r, "unit": "Gcell-updates/s", "cores": threads, "kind": "port",
+               "sample": f"{args.ref_sample_steps} FP64 steps of the 1024x1024 Q=8 grid ({dt:.1f} s)"}
+
+    launches = sum(klaunch) // 1 if klaunch else 0
+    per_run_launches = launches + S // p.cadence + 4  # update kernels + classifications + set_fields kernels
+    ts = stats["tile_steps"]
+    tot = max(sum(ts), 1)
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "Gcell-updates/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f16+f32+f64 (per-tile adaptive)",
+            "data": "synthetic (seeded uniform eta in [-1e-3,1e-3])",
+            "config": {"workload": WORKLOAD, "nx": p.nx, "ny": p.ny, "Q": nf, "steps_per_run": S, "tile": T,
+                       "monitor": "spatial range, every cell, all fields, every 10 steps",
+                       "thresholds": [p.thr_lo, p.thr_hi], "l2": "flushed between runs (256 MiB write)",
+                       "parallelism": f"replicas x{world}"},
+            "e2e": {"value": e2e, "unit": "Gcell-updates/s", "h2d_bytes_per_step": bytes_io,
+                    "d2h_bytes_per_step": bytes_io, "ms_per_step": e2e_total / len(e2e_ms)},
+            "plain_fp64": {"value": plain, "unit": "Gcell-updates/s", "ms_per_run": fp64_ms},
+            "speedup_vs_plain_fp64": value / plain,
+            "max_abs_err_vs_fp64": err,
+            "tier_mix": {"half": ts[0] / tot, "fp32": ts[1] / tot, "fp64": ts[2] / tot},
+            "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                         "peak_source": f"{peak_kind} hbm_gbs",
+                         "algorithmic_bytes_per_launch": per_launch_bytes,
+                         "note": "algorithmic bytes = tiles x 32^2 cells x Q fields x (read+write) x tier bytes; "
+                                 "the 1024^2 state (16-64 MiB) stays L2-resident within a run"},
+            "kernels": all_kernels,
+            "gpu_launches": per_run_launches * args.steps,
+            "clocks": clk.summary(),
+            "wall_s_timed_region": t_wall,
+        }
+        if cpu:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+    sim.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--sim-steps", type=int, default=10000)
+    ap.add_argument("--ref-sample-steps", type=int, default=100)
+    ap.add_argument("--tile", type=int, default=0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,226 @@
+/*
+ * amps.h -- C ABI of the GB300-native adaptive mixed-precision phase-field
+ * stencil library (libamps.so).
+ *
+ * What it replaces.  The reference drives its hot path from per-app `main`
+ * programs that launch `__global__` kernels on caller-owned managed arrays
+ * (snowflake/purehigh.cu:3-66, snowflake/purelow.cu:3-82,
+ * snowflake/end2end_mix.cu:3-147, graingrowth/{purehigh,purelow,end2end_mix}.cu,
+ * sintering/main.cu:5-635), with the kernel interface in
+ * {snowflake,graingrowth,sintering}/function.h and tools.h and every size and
+ * constant fixed at compile time (snowflake/paras/total.h:18-47).  This header
+ * exposes the same path -- initial state, the purehigh / purelow /
+ * end2end_mix (+ GRAM1/GRAM2) time loops, the per-tile precision monitor and
+ * tier conversion, and the field read-back used for the CSV dump -- as
+ * handle-based calls with runtime parameters.  Each entry point cites the
+ * reference code it stands in for.
+ *
+ * Conventions.  Every call returns an int status (AMPS_OK == 0) and never
+ * exits the process (the reference's CHECK_ERROR exits, snowflake/paras/
+ * total.h:48-56).  amps_last_error() gives the message of the last failure on
+ * a handle.  Work is queued on one CUDA stream per handle (caller-suppliable);
+ * a handle is not re-entrant, distinct handles are independent.
+ *
+ * Fields.  Kobayashi: 0 = phi, 1 = T.  Grain growth: 0..Q-1 = eta_i.
+ * Sintering: 0 = c, 1..N = eta_i.  Field data crosses the ABI as row-major
+ * [ny][nx] arrays of double (dtype AMPS_F64) or float (AMPS_F32), on the host
+ * or on the device.
+ */
+#ifndef AMPS_H
+#define AMPS_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AMPS_ABI_VERSION 1
+
+#if defined(__GNUC__)
+#define AMPS_API __attribute__((visibility("default")))
+#else
+#define AMPS_API
+#endif
+
+/* status codes */
+enum {
+    AMPS_OK = 0,
+    AMPS_ERR_INVALID = 1,     /* bad argument or parameter combination */
+    AMPS_ERR_CUDA = 2,        /* a CUDA runtime call failed */
+    AMPS_ERR_ALLOC = 3,       /* device or host allocation failed */
+    AMPS_ERR_TIMEOUT = 4,     /* a bounded device wait gave up */
+    AMPS_ERR_NUMERIC = 5,     /* NaN or Inf seen by the monitor */
+    AMPS_ERR_UNSUPPORTED = 6  /* valid request this build cannot serve */
+};
+
+/* models: the reference's three apps */
+enum { AMPS_KOBAYASHI = 0, AMPS_GRAINGROWTH = 1, AMPS_SINTERING = 2 };
+
+/* run modes: snowflake/purehigh.cu, snowflake/purelow.cu,
+ * snowflake/end2end_mix.cu (AMSTENCIL), GRAM1/GRAM2 static-ratio baselines
+ * (snowflake/function.h:72-79) */
+enum { AMPS_PUREHIGH = 0, AMPS_PURELOW = 1, AMPS_END2END_MIX = 2, AMPS_GRAM1 = 3, AMPS_GRAM2 = 4 };
+
+/* storage / arithmetic tiers of a tile */
+enum { AMPS_TIER_HALF = 0, AMPS_TIER_FP32 = 1, AMPS_TIER_FP64 = 2 };
+
+/* boundary conditions */
+enum { AMPS_BC_PERIODIC = 0, AMPS_BC_NOFLUX = 1 };
+
+/* monitors: Monitor1 = spatial range (snowflake/tools.h:177-193),
+ * Monitor2 = temporal change over one cadence (snowflake/tools.h:194-211) */
+enum { AMPS_MONITOR_SPA = 1, AMPS_MONITOR_TEM = 2 };
+
+/* dtypes crossing the ABI */
+enum { AMPS_F64 = 0, AMPS_F32 = 1 };
+
+/* initial states */
+enum {
+    AMPS_INIT_REFERENCE = 0, /* snowflake/tools.h:24-33 disc; graingrowth/tools.h:24-38 circle;
+                                sintering/main.cu:45-59 two touching discs */
+    AMPS_INIT_SEEDED = 1     /* seeded synthetic states: Kobayashi disc at the centre;
+                                grain growth i.i.d. uniform noise; sintering N discs placed by
+                                seeded rejection sampling */
+};
+
+/* reductions for amps_reduce */
+enum { AMPS_REDUCE_SUM = 0, AMPS_REDUCE_MIN = 1, AMPS_REDUCE_MAX = 2, AMPS_REDUCE_SUMSQ = 3 };
+
+typedef struct amps_params {
+    int model;            /* AMPS_KOBAYASHI / AMPS_GRAINGROWTH / AMPS_SINTERING */
+    int mode;             /* AMPS_PUREHIGH ... AMPS_GRAM2 */
+    int nx, ny;           /* grid; multiples of tile */
+    int nfields;          /* grain growth: Q order parameters; sintering: N particles */
+    int bc;               /* AMPS_BC_* */
+    int tile;             /* tile side: 16 (the reference's unit) or 32 */
+    int high_tier;        /* the reference's `highprecision`: AMPS_TIER_FP64 or AMPS_TIER_FP32 */
+    int monitor;          /* AMPS_MONITOR_SPA or AMPS_MONITOR_TEM */
+    int monitor_samples;  /* 0: the reference's 4x4 sample lattice; 1: every cell of the tile */
+    int monitor_field;    /* monitored field index; -1 = every field (max over fields) */
+    int cadence;          /* steps between monitor evaluations (reference: 10) */
+    int stencil;          /* grain growth: 0 = reference 8-neighbour Laplacian, 1 = 5-point */
+    int ref_order;        /* 1: FP64 tiles keep the reference's expression order and rounding
+                             (no fused multiply-add) -- the parity path */
+    int mu_lap_fp64;      /* sintering: chemical-potential Laplacian in FP64 on every tier */
+    int max_log;          /* tier maps kept in the decision log (0 = none) */
+    double thr_lo;        /* metric >= thr_lo -> FP32 tier (three-tier mode) */
+    double thr_hi;        /* metric >= thr_hi -> high tier; thr_lo == thr_hi: reference two tiers */
+    double gram_ratio;    /* GRAM1/GRAM2 fraction of half tiles */
+    double dx, dy, dt;
+    /* Kobayashi (snowflake/paras/para*.h) */
+    double tau, epsb, kappa, delta, aniso, alpha, gama, teq, theta0, pi, noise;
+    /* grain growth (graingrowth/paras/para*.h); gamma: cross-term coefficient */
+    double mobil, grcoef, gamma;
+    /* sintering (sintering/paras/para*.h); A, B: bulk free-energy coefficients */
+    double coefm, coefk, coefl, dvol, dvap, dsur, dgrb, A, B;
+    /* initial-state geometry: Kobayashi disc radius^2 and centre offset;
+     * grain-growth circle radius; sintering particle radii range */
+    double init_r2, init_r, rmin, rmax, init_amp;
+    int init_offset;
+    uint64_t seed;
+} amps_params;
+
+typedef struct amps_stats {
+    int64_t steps;                 /* steps advanced */
+    int64_t tile_steps[3];         /* tile-steps computed per tier (half, fp32, fp64) */
+    int64_t monitor_evals;         /* monitor evaluations (classifications) */
+    int64_t promotions, demotions; /* tier changes over all classifications */
+    int32_t tiles;                 /* tiles in the grid */
+    int32_t numeric_error;         /* 1 if the monitor saw NaN or Inf */
+} amps_stats;
+
+typedef struct amps_handle amps_handle;
+
+/* ---- versions and messages ---------------------------------------------- */
+AMPS_API int amps_abi_version(void);
+AMPS_API const char *amps_status_string(int status);
+/* Message of the last failure on h (or of the last failed amps_create when h is NULL). */
+AMPS_API const char *amps_last_error(const amps_handle *h);
+
+/* ---- parameters --------------------------------------------------------- */
+/* Fill *p with a preset.  preset 1..5: the reference's parameter files
+ * (snowflake/paras/para1-5.h, graingrowth/paras/para1-5.h,
+ * sintering/paras/para1-5.h) at the reference's 512x512, 16x16 tiles,
+ * periodic boundaries, threshold 0.99 and Monitor2, i.e. the shipped
+ * header state (snowflake/paras/total.h:18-28).  preset 0: the seeded
+ * large-grid workloads (Kobayashi 512^2 zero-flux with noise; grain growth
+ * 1024^2 Q=8 Fan-Chen gamma=1.5; sintering 1024^2 with 16 particles). */
+AMPS_API int amps_preset(int model, int preset, amps_params *p);
+/* Validate a parameter set without allocating anything. */
+AMPS_API int amps_check_params(const amps_params *p, char *msg, size_t msg_len);
+/* Number of fields of a parameter set (2, Q or N+1). */
+AMPS_API int amps_num_fields(const amps_params *p);
+
+/* ---- handle lifetime ------------------------------------------------------ */
+/* Replaces the cudaMallocManaged block at the top of each driver
+ * (snowflake/end2end_mix.cu:4-40, graingrowth/end2end_mix.cu:4-31,
+ * sintering/main.cu:6-44).  Device memory is owned by the handle. */
+AMPS_API int amps_create(const amps_params *p, amps_handle **out);
+AMPS_API int amps_destroy(amps_handle *h);
+/* Queue work on a caller stream (cudaStream_t passed as void*); NULL restores
+ * the handle's own stream. */
+AMPS_API int amps_set_stream(amps_handle *h, void *stream);
+AMPS_API int amps_synchronize(amps_handle *h);
+
+/* ---- state ------------------------------------------------------------------ */
+/* Initial state (kind AMPS_INIT_*).  Replaces dataprepare_high/half/half2
+ * (snowflake/tools.h:24-58, graingrowth/tools.h:24-82), the sintering host
+ * init (sintering/main.cu:45-59), the warm start of the temporal monitor
+ * (snowflake/end2end_mix.cu:44-46) and highdata_to_low / dataprepare
+ * (snowflake/tools.h:133-146, sintering/tools.h:80-92). */
+AMPS_API int amps_init(amps_handle *h, int kind);
+/* Host-only: write the initial state of (p, kind) into fields[f] (row-major
+ * double [ny][nx] each).  Needs no GPU. */
+AMPS_API int amps_init_host(const amps_params *p, int kind, double *const *fields);
+/* Set / get one field.  on_device: 0 = host pointer, 1 = device pointer.
+ * amps_get_field replaces data_sychro_aftercomputation +
+ * purelow2high_aftercomputing (snowflake/tools.h:108-174). */
+AMPS_API int amps_set_field(amps_handle *h, int field, const void *src, int dtype, int on_device);
+AMPS_API int amps_get_field(amps_handle *h, int field, void *dst, int dtype, int on_device);
+/* All fields at once, contiguous [nfields][ny][nx]. */
+AMPS_API int amps_set_fields(amps_handle *h, const void *src, int dtype, int on_device);
+AMPS_API int amps_get_fields(amps_handle *h, void *dst, int dtype, int on_device);
+
+/* ---- time loop ------------------------------------------------------------- */
+/* Advance nsteps explicit steps (asynchronous on the handle's stream).
+ * Replaces the per-step launch sequences of the drivers
+ * (snowflake/purehigh.cu:23-34, snowflake/end2end_mix.cu:80-105,
+ * graingrowth/end2end_mix.cu:71-98, sintering/main.cu:126-207): fused update
+ * kernels, one per tier in use, with the monitor (get_max_diff1/2) fused into
+ * the epilogue of every cadence-th step, then get_type, and the tier
+ * conversion done in-register by the next step.  Whole cadence periods are
+ * replayed from a CUDA graph. */
+AMPS_API int amps_run(amps_handle *h, int nsteps);
+/* Enable (1) / disable (0) CUDA-graph replay of whole periods (default 1). */
+AMPS_API int amps_set_graphs(amps_handle *h, int enable);
+/* Kernel timing: while enabled, amps_run launches eagerly and brackets every
+ * update-kernel launch with CUDA events on the handle's stream.
+ * amps_get_kernel_times returns, per tier (half, fp32, fp64), the summed
+ * device time in ms, the number of launches and the tile-steps they computed
+ * since profiling was enabled. */
+AMPS_API int amps_set_profiling(amps_handle *h, int enable);
+AMPS_API int amps_get_kernel_times(amps_handle *h, double *ms, int64_t *launches, int64_t *tile_steps);
+
+/* ---- monitor results and diagnostics ---------------------------------------- */
+/* Current tier of every tile, row-major [nty][ntx] (AMPS_TIER_*).  The
+ * reference keeps this as type_curr (1 = half2, 2 = high). */
+AMPS_API int amps_get_tile_tiers(amps_handle *h, uint8_t *out);
+/* Decision log: the tier map after each classification, oldest first,
+ * up to max_entries maps of ntiles bytes.  *n_out = maps written. */
+AMPS_API int amps_get_decision_log(amps_handle *h, uint8_t *out, int max_entries, int *n_out);
+/* Last monitor metric per tile (double [nty][ntx]). */
+AMPS_API int amps_get_tile_metric(amps_handle *h, double *out);
+AMPS_API int amps_get_stats(amps_handle *h, amps_stats *out);
+/* FP64 reduction of one field over the grid (deterministic order).  SUM of c
+ * is the sintering conserved mass. */
+AMPS_API int amps_reduce(amps_handle *h, int field, int kind, double *out);
+/* Max-abs and RMS difference of one field against a row-major double array
+ * (host or device), computed in FP64 on the device. */
+AMPS_API int amps_compare(amps_handle *h, int field, const double *other, int on_device, double *max_abs,
+                 double *rms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

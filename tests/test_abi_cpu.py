@@ -1,0 +1,93 @@
+"""The C ABI without a GPU: the library loads, exports every symbol the
+header declares, and its host-only entry points (presets, validation,
+initial states) agree with the reference-derived oracle."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+import oracle_bind as ob
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def amps():
+    import w3914777_gb300 as w
+    return w
+
+
+def declared_symbols():
+    src = open(os.path.join(ROOT, "include", "amps.h")).read()
+    return sorted(set(re.findall(r"AMPS_API[^;(]*?\b(amps_\w+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol():
+    w = amps()
+    L = w.lib()
+    syms = declared_symbols()
+    assert len(syms) >= 20
+    missing = [s for s in syms if not hasattr(L, s)]
+    assert not missing, missing
+    assert L.amps_abi_version() == 1
+
+
+def test_status_strings_and_errors_never_exit():
+    w = amps()
+    L = w.lib()
+    assert L.amps_status_string(0) == b"ok"
+    assert b"invalid" in L.amps_status_string(1)
+    p = w.Params.preset("graingrowth", 1, nx=100)  # not a multiple of the tile
+    rc, msg = p.check()
+    assert rc == 1 and "multiples" in msg
+    with pytest.raises(w.AmpsError) as e:
+        w.Simulation(p)
+    assert e.value.status == 1
+
+
+@pytest.mark.parametrize("k", [1, 2, 3, 4, 5])
+def test_presets_mirror_reference_parameter_files(k):
+    w = amps()
+    kob = w.Params.preset("kobayashi", k)
+    assert (kob.nx, kob.ny, kob.tile, kob.cadence) == (512, 512, 16, 10)  # snowflake/paras/total.h:20-21
+    assert kob.aniso == [4.0, 6.0, 5.0, 6.0, 4.0][k - 1]                # snowflake/paras/para*.h
+    assert kob.theta0 == [0.0, 0.0, 0.0, 0.4, 0.25][k - 1]
+    gg = w.Params.preset("graingrowth", k)
+    assert gg.mobil == [5.0, 10.0, 5.0, 5.0, 20.0][k - 1] and gg.dt == 0.005  # graingrowth/paras/para*.h
+    si = w.Params.preset("sintering", k)
+    assert si.coefm == [5.0, 5.0, 20.0, 20.0, 20.0][k - 1] and si.dsur == [32, 64, 16, 16, 64][k - 1]
+    if ob.ref_available("snowflake") and k == 2:
+        rp = ob.ref_params("snowflake", 14)
+        assert [kob.dx, kob.dy, kob.tau, kob.epsb, kob.kappa, kob.delta, kob.aniso, kob.alpha, kob.gama,
+                kob.teq, kob.theta0, kob.dt, kob.pi] == list(rp[:13])
+
+
+def test_reference_initial_states_match_oracle():
+    w = amps()
+    f = w.init_host(w.Params.preset("kobayashi", 2), w.INIT_REFERENCE)
+    a, _ = ob.kob_init_disc(512, 512, 264, 264, 10.0)
+    assert np.array_equal(f[0], a) and not f[1].any()
+    f = w.init_host(w.Params.preset("graingrowth", 1), w.INIT_REFERENCE)
+    a, b = ob.gg_init_circle(512, 512, 256, 256, 50)
+    assert np.array_equal(f[0], a) and np.array_equal(f[1], b)
+    f = w.init_host(w.Params.preset("sintering", 5), w.INIT_REFERENCE)
+    c, e1, e2 = ob.sint_init_two(512, 512, 264, 240, 20, 270, 10)
+    assert np.array_equal(f[0], c) and np.array_equal(f[1], e1) and np.array_equal(f[2], e2)
+
+
+def test_seeded_states():
+    w = amps()
+    p = w.Params.preset("graingrowth", 0, nx=128, ny=64)
+    f = w.init_host(p, w.INIT_SEEDED)
+    assert f.shape == (8, 64, 128) and np.abs(f).max() <= 1e-3 and abs(f.mean()) < 5e-5
+    # same RNG as the oracle's counter-based generator
+    u = ob.lib().orc_uniform01(p.seed, 3, 77)
+    assert f[3].ravel()[77] == p.init_amp * (2 * u - 1)
+    s = w.Params.preset("sintering", 0)
+    g = w.init_host(s, w.INIT_SEEDED)
+    assert g.shape == (17, 1024, 1024)
+    eta = g[1:]
+    assert set(np.unique(eta)) <= {0.0, 1.0} and eta.sum(0).max() == 1.0   # one particle per cell
+    assert np.array_equal(g[0], eta.sum(0))                                # c = 1 inside particles
+    assert all(eta[k].sum() > 1000 for k in range(16))                     # all 16 placed, r >= 20
+    assert np.array_equal(g, w.init_host(s, w.INIT_SEEDED))                # deterministic

@@ -1,0 +1,255 @@
+"""GPU parity: the CUDA path (through the C ABI) against the CPU FP64 oracle
+and against the reference's own outputs (tests/golden/).
+
+Tolerances, written per test:
+  * FP64 tiles in reference order (ref_order=1) -- the plain FP64 parity path:
+    every +,-,*,/ is rounded as the reference writes it, so the only source
+    of difference is the device libm (atan2/cos/sin/atan/pow(x,3)) against
+    glibc, at most a few ulp per call.  Bar: max |gpu - ref| <= 1e-12 *
+    max|ref| after N steps.
+  * FP32 tiles: 1e-4 * max|ref| after N steps.
+  * half tiles (purelow) and mixed runs: envelopes stated in each test.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle_bind as ob
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def amps():
+    import w3914777_gb300 as w
+    return w
+
+
+def rel_err(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+# ------------------------------------------------------------- golden ----
+def test_kobayashi_fp64_matches_reference_golden():
+    w = amps()
+    g = np.load(os.path.join(GOLD, "kobayashi_ref.npz"))
+    p = w.Params.preset("kobayashi", 2, mode="purehigh")
+    with w.Simulation(p, init=w.INIT_REFERENCE) as s:
+        s.run(int(g["steps"]))
+        f = s.fields()
+    e_phi, e_T = rel_err(f[0], g["phi"]), rel_err(f[1], g["T"])
+    print(f"kobayashi fp64 vs reference after {int(g['steps'])} steps: phi {e_phi:.3e} T {e_T:.3e}")
+    assert e_phi <= 1e-12 and e_T <= 1e-12
+
+
+def test_graingrowth_fp64_matches_reference_golden():
+    w = amps()
+    g = np.load(os.path.join(GOLD, "graingrowth_ref.npz"))
+    p = w.Params.preset("graingrowth", 1, mode="purehigh")
+    with w.Simulation(p, init=w.INIT_REFERENCE) as s:
+        s.run(int(g["steps"]))
+        f = s.fields()
+    e1, e2 = rel_err(f[0], g["eta1"]), rel_err(f[1], g["eta2"])
+    print(f"graingrowth fp64 vs reference: {e1:.3e} {e2:.3e}")
+    assert e1 <= 1e-12 and e2 <= 1e-12
+
+
+def test_sintering_fp64_matches_reference_golden():
+    w = amps()
+    g = np.load(os.path.join(GOLD, "sintering_ref.npz"))
+    p = w.Params.preset("sintering", 5, mode="purehigh")
+    with w.Simulation(p, init=w.INIT_REFERENCE) as s:
+        s.run(int(g["steps"]))
+        f = s.fields()
+    errs = [rel_err(f[0], g["c"]), rel_err(f[1], g["eta1"]), rel_err(f[2], g["eta2"])]
+    print("sintering fp64 vs reference:", errs)
+    assert max(errs) <= 1e-12
+
+
+# ------------------------------------------------- oracle, other cases ----
+@pytest.mark.parametrize("tile", [16, 32])
+@pytest.mark.parametrize("bc", [0, 1])
+def test_kobayashi_fp64_vs_oracle_bc_tile_noise(tile, bc):
+    """Zero-flux and periodic boundaries, 32x32 tiles, seeded noise; 96 x 64 grid."""
+    w = amps()
+    nx, ny, steps = 96, 64, 30
+    p = w.Params.preset("kobayashi", 4, mode="purehigh", nx=nx, ny=ny, tile=tile, bc=bc, noise=0.01, seed=7,
+                        init_offset=3, init_r2=40.0)
+    f0 = w.init_host(p, w.INIT_REFERENCE)
+    with w.Simulation(p, init=w.INIT_REFERENCE) as s:
+        s.run(steps)
+        f = s.fields()
+    q = ob.kob_params(nx, ny, bc=bc, aniso=p.aniso, theta0=p.theta0, noise=0.01, seed=7)
+    phi, T = ob.kob_run(q, f0[0], f0[1], steps)
+    e = max(rel_err(f[0], phi), rel_err(f[1], T))
+    print(f"kobayashi tile={tile} bc={bc}: {e:.3e}")
+    assert e <= 1e-12
+
+
+@pytest.mark.parametrize("q,stencil,bc", [(2, 0, 0), (5, 0, 1), (3, 1, 0)])
+def test_graingrowth_fp64_vs_oracle_q_general(q, stencil, bc):
+    w = amps()
+    nx, ny, steps = 64, 96, 25
+    p = w.Params.preset("graingrowth", 0, mode="purehigh", nx=nx, ny=ny, nfields=q, stencil=stencil, bc=bc,
+                        ref_order=1, dt=0.05, init_amp=0.3)
+    f0 = w.init_host(p, w.INIT_SEEDED)
+    with w.Simulation(p, init=w.INIT_SEEDED) as s:
+        s.run(steps)
+        f = s.fields()
+    o = ob.gg_run(ob.gg_params(nx, ny, q=q, bc=bc, stencil=stencil, dx=1.0, dy=1.0, dt=0.05, mobil=1.0,
+                               grcoef=2.0, gamma=1.5), list(f0), steps)
+    e = max(rel_err(f[k], o[k]) for k in range(q))
+    print(f"graingrowth Q={q}: {e:.3e}")
+    assert e <= 1e-12
+
+
+def test_sintering_fp64_vs_oracle_n_particles():
+    w = amps()
+    nx = ny = 128
+    p = w.Params.preset("sintering", 0, mode="purehigh", nx=nx, ny=ny, nfields=4, rmin=10, rmax=16, ref_order=1)
+    f0 = w.init_host(p, w.INIT_SEEDED)
+    with w.Simulation(p, init=w.INIT_SEEDED) as s:
+        s.run(20)
+        f = s.fields()
+    op = ob.sint_params(nx, ny, n=4, coefm=p.coefm, coefk=p.coefk, coefl=p.coefl, dsur=p.dsur)
+    c, e = ob.sint_run(op, f0[0], list(f0[1:]), 20)
+    errs = [rel_err(f[0], c)] + [rel_err(f[k + 1], e[k]) for k in range(4)]
+    print("sintering N=4:", errs)
+    assert max(errs) <= 1e-12
+
+
+# --------------------------------------------------------- lower tiers ----
+def test_fp32_high_tier_vs_oracle():
+    w = amps()
+    g = np.load(os.path.join(GOLD, "graingrowth_ref.npz"))
+    p = w.Params.preset("graingrowth", 1, mode="purehigh", high_tier=w.TIER_FP32)
+    with w.Simulation(p, init=w.INIT_REFERENCE) as s:
+        s.run(int(g["steps"]))
+        f = s.fields()
+    e = max(rel_err(f[0], g["eta1"]), rel_err(f[1], g["eta2"]))
+    print(f"graingrowth fp32 vs reference fp64: {e:.3e}")
+    assert e <= 1e-4
+
+
+def test_purelow_half_envelope():
+    """All-half run (snowflake/purelow.cu): the half storage bounds the error."""
+    w = amps()
+    g = np.load(os.path.join(GOLD, "graingrowth_ref.npz"))
+    p = w.Params.preset("graingrowth", 1, mode="purelow")
+    with w.Simulation(p, init=w.INIT_REFERENCE) as s:
+        s.run(int(g["steps"]))
+        f = s.fields()
+    e = max(np.max(np.abs(f[0] - g["eta1"])), np.max(np.abs(f[1] - g["eta2"])))
+    print(f"graingrowth half vs reference fp64: max abs {e:.3e}")
+    assert e <= 2e-2
+
+
+# --------------------------------------------------------------- mixed ----
+def _oracle_decisions(w, s, p, state_prev, state_now):
+    """Oracle get_type on the GPU's own stored state (snowflake/tools.h:177-230)."""
+    T = p.tile
+    fields = range(s.nf) if p.monitor_field < 0 else [p.monitor_field]
+    m = None
+    for k in fields:
+        if p.monitor == w.MONITOR_SPA:
+            mk = ob.monitor_spa(state_now[k], T, p.monitor_samples)
+        else:
+            mk = ob.monitor_tem(state_now[k], state_prev[k], T, p.monitor_samples)
+        m = mk if m is None else np.maximum(m, mk)
+    thr_lo = p.thr_lo if p.high_tier == w.TIER_FP64 else p.thr_hi
+    t = ob.classify(m, thr_lo, p.thr_hi)
+    if p.high_tier == w.TIER_FP32:
+        t = np.where(t == 2, 1, 0).astype(np.uint8)
+    return m, t
+
+
+@pytest.mark.parametrize("monitor,samples", [(1, 0), (2, 0), (1, 1), (2, 1)])
+def test_mixed_decisions_match_oracle(monitor, samples):
+    """The fused monitor + classification against the oracle on the same state."""
+    w = amps()
+    thr = (0.3, 0.6) if monitor == 1 else (1e-4, 1e-2)
+    p = w.Params.preset("kobayashi", 2, mode="end2end_mix", nx=256, ny=256, monitor=monitor,
+                        monitor_samples=samples, thr_lo=thr[0], thr_hi=thr[1], init_r2=400.0, max_log=16)
+    with w.Simulation(p, init=w.INIT_REFERENCE) as s:
+        s.run(40)
+        prev = s.fields()
+        s.run(10)
+        now = s.fields()
+        m_gpu = s.metric()
+        t_gpu = s.tiers()
+        log = s.decision_log()
+    m, t = _oracle_decisions(w, s, p, prev, now)
+    assert np.array_equal(m_gpu, m), f"metric mismatch: {np.max(np.abs(m_gpu - m))}"
+    assert np.array_equal(t_gpu, t)
+    assert np.array_equal(log[-1], t_gpu)
+    assert len(log) == 6  # the resting classification + one per period
+
+
+def test_mixed_error_envelope_kobayashi():
+    """Adaptive run against the FP64 oracle: the monitor keeps the interface in
+    FP64, so the error stays near the half-precision storage floor."""
+    w = amps()
+    steps = 200
+    p = w.Params.preset("kobayashi", 2, mode="end2end_mix", nx=256, ny=256, init_r2=400.0, monitor=1,
+                        monitor_samples=1, thr_lo=0.02, thr_hi=0.2)
+    f0 = w.init_host(p, w.INIT_REFERENCE)
+    with w.Simulation(p, init=w.INIT_REFERENCE) as s:
+        s.run(steps)
+        f = s.fields()
+        st = s.stats()
+    phi, T = ob.kob_run(ob.kob_params(256, 256), f0[0], f0[1], steps)
+    e = max(np.max(np.abs(f[0] - phi)), np.max(np.abs(f[1] - T)))
+    frac = np.array(st["tile_steps"]) / max(sum(st["tile_steps"]), 1)
+    print(f"kobayashi mixed vs fp64 oracle: max abs {e:.3e}; tier mix half/fp32/fp64 {frac}")
+    assert sum(st["tile_steps"]) == steps * s.ntiles[0] * s.ntiles[1]
+    assert e <= 5e-3
+
+
+def test_mixed_graingrowth_envelope():
+    w = amps()
+    steps = 100
+    p = w.Params.preset("graingrowth", 0, nx=128, ny=128, nfields=4)
+    f0 = w.init_host(p, w.INIT_SEEDED)
+    with w.Simulation(p, init=w.INIT_SEEDED) as s:
+        s.run(steps)
+        f = s.fields()
+        st = s.stats()
+    o = ob.gg_run(ob.gg_params(128, 128, q=4, dx=1.0, dy=1.0, dt=0.05, mobil=1.0, grcoef=2.0, gamma=1.5),
+                  list(f0), steps)
+    e = max(np.max(np.abs(f[k] - o[k])) for k in range(4))
+    print(f"graingrowth mixed Q=4 vs fp64 oracle: max abs {e:.3e}; tiles {st['tile_steps']}")
+    assert e <= 1e-3
+
+
+# ------------------------------------------------------------- plumbing ----
+def test_graph_replay_equals_eager():
+    w = amps()
+    p = w.Params.preset("graingrowth", 0, nx=128, ny=128, nfields=4)
+    out = []
+    for graphs in (True, False):
+        with w.Simulation(p, init=w.INIT_SEEDED, graphs=graphs) as s:
+            s.run(23)
+            s.run(17)
+            out.append((s.fields(), s.tiers(), s.stats()))
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
+    assert out[0][2] == out[1][2]
+
+
+def test_set_get_roundtrip_and_reduce():
+    w = amps()
+    p = w.Params.preset("sintering", 1, mode="purehigh", nx=64, ny=64)
+    rng = np.random.default_rng(3)
+    a = rng.random((3, 64, 64))
+    with w.Simulation(p) as s:
+        s.set_fields(a)
+        assert np.array_equal(s.fields(), a)
+        b = rng.random((64, 64))
+        s.set_field(1, b)
+        assert np.array_equal(s.field(1), b) and np.array_equal(s.field(0), a[0])
+        assert abs(s.reduce(0) - a[0].sum()) <= 1e-12 * a[0].size
+        assert s.reduce(0, w.amps.REDUCE_MAX) == a[0].max()
+        mx, rms = s.compare(2, a[2] + 0.5)
+        assert abs(mx - 0.5) < 1e-15 and abs(rms - 0.5) < 1e-15

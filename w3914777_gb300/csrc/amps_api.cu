@@ -1,0 +1,660 @@
+// amps_api.cu -- handle, time loop and state transfer of the C ABI.
+//
+// The time loop issues, per step, one fused update kernel per tier in use
+// (each over a device-side list of the tiles at that tier), and at the end of
+// every monitor period one classification kernel (get_type) that rebuilds the
+// tier map and the per-tier lists.  Whole periods are captured once into a
+// CUDA graph and replayed; the kernels read every step-varying quantity (tier
+// map, lists, counts, step index) from device memory, so one graph serves
+// every period.
+#include "../../include/amps.h"
+#include "amps_kernels.h"
+
+#include <stdio.h>
+#include <string.h>
+
+#include <map>
+#include <string>
+#include <vector>
+
+using namespace amps;
+
+struct amps_handle {
+    amps_params p;
+    int nf = 0, T = 0, ntx = 0, nty = 0, ntiles = 0;
+    int64_t n = 0;
+    bool used[3] = {false, false, false};
+    bool mixed = false, use_mid = false;
+    void *store[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};
+    int parity = 0;
+    bool transition = false;  // next step reads tiles at tier_prev
+    uint8_t *d_tier_prev = nullptr, *d_tier_cur = nullptr;
+    int *d_lists = nullptr, *d_counts = nullptr;
+    double *d_metric = nullptr, *d_snap = nullptr;
+    int nmon = 0;
+    unsigned long long *d_stats = nullptr;
+    int *d_flags = nullptr;
+    uint8_t *d_log = nullptr;
+    int *d_log_n = nullptr;
+    int64_t *d_step_base = nullptr;
+    double *d_stage = nullptr, *d_partials = nullptr, *d_out = nullptr;
+    double *h_pinned = nullptr;  // nf*n doubles, page-locked
+    cudaStream_t own = nullptr, stream = nullptr;
+    int64_t step = 0;
+    bool graphs = true;
+    std::map<int, cudaGraphExec_t> graph;  // key: parity | transition<<1
+    std::string err;
+    // kernel timing
+    bool profiling = false;
+    struct Ev { int tier; cudaEvent_t a, b; };
+    std::vector<Ev> evs;
+    double prof_ms[3] = {0, 0, 0};
+    int64_t prof_launches[3] = {0, 0, 0};
+    unsigned long long prof_stats0[3] = {0, 0, 0};
+};
+
+static std::string g_create_err;
+
+#define FAIL(h, code, ...)                                         \
+    do {                                                           \
+        char _b[512];                                              \
+        snprintf(_b, sizeof _b, __VA_ARGS__);                      \
+        (h)->err = _b;                                             \
+        return (code);                                             \
+    } while (0)
+#define CK(h, call)                                                                              \
+    do {                                                                                         \
+        cudaError_t _e = (call);                                                                 \
+        if (_e != cudaSuccess) FAIL(h, AMPS_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(_e)); \
+    } while (0)
+
+extern "C" const char *amps_status_string(int s)
+{
+    switch (s) {
+    case AMPS_OK: return "ok";
+    case AMPS_ERR_INVALID: return "invalid argument";
+    case AMPS_ERR_CUDA: return "CUDA error";
+    case AMPS_ERR_ALLOC: return "allocation failed";
+    case AMPS_ERR_TIMEOUT: return "device wait timed out";
+    case AMPS_ERR_NUMERIC: return "NaN or Inf in the state";
+    case AMPS_ERR_UNSUPPORTED: return "unsupported";
+    default: return "unknown status";
+    }
+}
+
+extern "C" const char *amps_last_error(const amps_handle *h)
+{
+    return h ? h->err.c_str() : g_create_err.c_str();
+}
+
+static size_t tier_size(int t) { return t == TIER_FP64 ? 8 : (t == TIER_FP32 ? 4 : 2); }
+
+static Phys make_phys(const amps_params &p)
+{
+    Phys ph;
+    memset(&ph, 0, sizeof ph);
+    ph.dx = p.dx; ph.dy = p.dy; ph.dt = p.dt;
+    ph.dxdy = p.dx * p.dy;
+    ph.inv_dxdy = 1.0 / ph.dxdy;
+    ph.tau = p.tau; ph.epsb = p.epsb; ph.kappa = p.kappa; ph.delta = p.delta; ph.aniso = p.aniso;
+    ph.alpha = p.alpha; ph.gama = p.gama; ph.teq = p.teq; ph.theta0 = p.theta0; ph.pi = p.pi; ph.noise = p.noise;
+    ph.mobil = p.mobil; ph.grcoef = p.grcoef; ph.gamma = p.gamma;
+    ph.coefm = p.coefm; ph.coefk = p.coefk; ph.coefl = p.coefl; ph.dvol = p.dvol; ph.dvap = p.dvap;
+    ph.dsur = p.dsur; ph.dgrb = p.dgrb; ph.A = p.A; ph.B = p.B;
+    ph.seed = p.seed;
+    return ph;
+}
+
+static size_t kernel_smem(const amps_params &p, int tier, int nf)
+{
+    if (p.model == AMPS_GRAINGROWTH) return gg_smem_bytes(p.tile, tier, nf);
+    if (p.model == AMPS_KOBAYASHI) return kob_smem_bytes(p.tile, tier);
+    return sint_smem_bytes(p.tile, tier, nf, p.mu_lap_fp64 || tier == TIER_FP64);
+}
+
+static void free_all(amps_handle *h)
+{
+    for (auto &e : h->evs) { cudaEventDestroy(e.a); cudaEventDestroy(e.b); }
+    h->evs.clear();
+    for (auto &kv : h->graph) cudaGraphExecDestroy(kv.second);
+    h->graph.clear();
+    for (int t = 0; t < 3; ++t)
+        for (int q = 0; q < 2; ++q)
+            if (h->store[t][q]) cudaFree(h->store[t][q]);
+    void *ps[] = {h->d_tier_prev, h->d_tier_cur, h->d_lists, h->d_counts, h->d_metric, h->d_snap, h->d_stats,
+                  h->d_flags, h->d_log, h->d_log_n, h->d_step_base, h->d_stage, h->d_partials, h->d_out};
+    for (void *q : ps)
+        if (q) cudaFree(q);
+    if (h->h_pinned) cudaFreeHost(h->h_pinned);
+    if (h->own) cudaStreamDestroy(h->own);
+}
+
+extern "C" int amps_create(const amps_params *p, amps_handle **out)
+{
+    char msg[256];
+    if (!out) return AMPS_ERR_INVALID;
+    *out = nullptr;
+    if (amps_check_params(p, msg, sizeof msg) != AMPS_OK) {
+        g_create_err = msg;
+        return AMPS_ERR_INVALID;
+    }
+    amps_handle *h = new (std::nothrow) amps_handle();
+    if (!h) return AMPS_ERR_ALLOC;
+    h->p = *p;
+    h->nf = amps_num_fields(p);
+    h->T = p->tile;
+    h->ntx = p->nx / p->tile;
+    h->nty = p->ny / p->tile;
+    h->ntiles = h->ntx * h->nty;
+    h->n = (int64_t)p->nx * p->ny;
+    const int high = p->high_tier;
+    h->mixed = p->mode == AMPS_END2END_MIX;
+    h->use_mid = h->mixed && high == TIER_FP64 && p->thr_lo < p->thr_hi;
+    switch (p->mode) {
+    case AMPS_PUREHIGH: h->used[high] = true; break;
+    case AMPS_PURELOW: h->used[TIER_HALF] = true; break;
+    default:
+        h->used[TIER_HALF] = h->used[high] = true;
+        if (h->use_mid) h->used[TIER_FP32] = true;
+    }
+    for (int t = 0; t < 3; ++t)
+        if (h->used[t] && kernel_smem(*p, t, h->nf) > (size_t)kMaxDynSmem) {
+            g_create_err = "tile staging exceeds 226 KB of shared memory: use tile=16 or fewer fields";
+            delete h;
+            return AMPS_ERR_UNSUPPORTED;
+        }
+    auto fail = [&](int code, const char *what) {
+        g_create_err = std::string("allocation failed: ") + what;
+        free_all(h);
+        delete h;
+        return code;
+    };
+#define ALLOC(ptr, bytes, what)                                              \
+    if (cudaMalloc((void **)&(ptr), (bytes)) != cudaSuccess) return fail(AMPS_ERR_ALLOC, what);
+    for (int t = 0; t < 3; ++t)
+        if (h->used[t])
+            for (int q = 0; q < 2; ++q) ALLOC(h->store[t][q], (size_t)h->nf * h->n * tier_size(t), "field storage");
+    ALLOC(h->d_tier_prev, h->ntiles, "tier map");
+    ALLOC(h->d_tier_cur, h->ntiles, "tier map");
+    ALLOC(h->d_lists, sizeof(int) * 3 * h->ntiles, "tile lists");
+    ALLOC(h->d_counts, sizeof(int) * 4, "tile counts");
+    ALLOC(h->d_metric, sizeof(double) * h->ntiles, "monitor metric");
+    h->nmon = p->monitor_field < 0 ? h->nf : 1;
+    const size_t snap = p->monitor_samples ? (size_t)h->nmon * h->n : (size_t)h->nmon * h->ntiles * 16;
+    ALLOC(h->d_snap, sizeof(double) * snap, "monitor snapshot");
+    ALLOC(h->d_stats, sizeof(unsigned long long) * 8, "stats");
+    ALLOC(h->d_flags, sizeof(int) * 4, "flags");
+    ALLOC(h->d_log_n, sizeof(int), "log count");
+    if (p->max_log > 0) ALLOC(h->d_log, (size_t)p->max_log * h->ntiles, "decision log");
+    ALLOC(h->d_step_base, sizeof(int64_t), "step counter");
+    ALLOC(h->d_stage, sizeof(double) * h->nf * h->n, "staging");
+    ALLOC(h->d_partials, sizeof(double) * 2 * 1024, "partials");
+    ALLOC(h->d_out, sizeof(double) * 4, "result");
+    if (cudaMallocHost((void **)&h->h_pinned, sizeof(double) * h->nf * h->n) != cudaSuccess)
+        return fail(AMPS_ERR_ALLOC, "pinned staging");
+#undef ALLOC
+    if (cudaStreamCreateWithFlags(&h->own, cudaStreamNonBlocking) != cudaSuccess)
+        return fail(AMPS_ERR_CUDA, "stream");
+    h->stream = h->own;
+    cudaMemsetAsync(h->d_stats, 0, sizeof(unsigned long long) * 8, h->stream);
+    cudaMemsetAsync(h->d_flags, 0, sizeof(int) * 4, h->stream);
+    cudaMemsetAsync(h->d_log_n, 0, sizeof(int), h->stream);
+    cudaMemsetAsync(h->d_step_base, 0, sizeof(int64_t), h->stream);
+    cudaMemsetAsync(h->d_metric, 0, sizeof(double) * h->ntiles, h->stream);
+    cudaMemsetAsync(h->d_snap, 0, sizeof(double) * snap, h->stream);
+    // zero state at the starting tier so that an un-initialised run is defined
+    for (int t = 0; t < 3; ++t)
+        if (h->used[t])
+            for (int q = 0; q < 2; ++q) cudaMemsetAsync(h->store[t][q], 0, (size_t)h->nf * h->n * tier_size(t), h->stream);
+    for (int t = 0; t < 3; ++t) {
+        if (!h->used[t]) continue;
+        cudaError_t pe;
+        if (p->model == AMPS_GRAINGROWTH) pe = gg_prepare(h->T, t, p->ref_order != 0);
+        else if (p->model == AMPS_KOBAYASHI) pe = kob_prepare(h->T, t, p->ref_order != 0);
+        else pe = sint_prepare(h->T, t, p->ref_order != 0, p->mu_lap_fp64 != 0);
+        if (pe != cudaSuccess) {
+            g_create_err = std::string("kernel attributes: ") + cudaGetErrorString(pe);
+            free_all(h);
+            delete h;
+            return AMPS_ERR_CUDA;
+        }
+    }
+    const int start = p->mode == AMPS_PURELOW ? TIER_HALF : high;
+    cudaMemsetAsync(h->d_tier_cur, start, h->ntiles, h->stream);
+    cudaMemsetAsync(h->d_tier_prev, start, h->ntiles, h->stream);
+    build_lists(h->d_tier_cur, h->ntiles, h->d_lists, h->d_counts, h->stream);
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) {
+        g_create_err = std::string("initialisation: ") + cudaGetErrorString(e);
+        free_all(h);
+        delete h;
+        return AMPS_ERR_CUDA;
+    }
+    *out = h;
+    return AMPS_OK;
+}
+
+extern "C" int amps_destroy(amps_handle *h)
+{
+    if (!h) return AMPS_ERR_INVALID;
+    cudaStreamSynchronize(h->stream);
+    free_all(h);
+    delete h;
+    return AMPS_OK;
+}
+
+extern "C" int amps_set_stream(amps_handle *h, void *stream)
+{
+    if (!h) return AMPS_ERR_INVALID;
+    CK(h, cudaStreamSynchronize(h->stream));
+    h->stream = stream ? (cudaStream_t)stream : h->own;
+    return AMPS_OK;
+}
+
+extern "C" int amps_synchronize(amps_handle *h)
+{
+    if (!h) return AMPS_ERR_INVALID;
+    CK(h, cudaStreamSynchronize(h->stream));
+    int flag = 0;
+    CK(h, cudaMemcpy(&flag, h->d_flags, sizeof(int), cudaMemcpyDeviceToHost));
+    if (flag & 1) FAIL(h, AMPS_ERR_NUMERIC, "NaN or Inf detected by the monitor");
+    return AMPS_OK;
+}
+
+extern "C" int amps_set_graphs(amps_handle *h, int enable)
+{
+    if (!h) return AMPS_ERR_INVALID;
+    h->graphs = enable != 0;
+    return AMPS_OK;
+}
+
+// ------------------------------------------------------------------ state ----
+static Grid grid_view(amps_handle *h, int parity, const uint8_t *tier)
+{
+    Grid g;
+    for (int t = 0; t < 3; ++t) g.store[t] = h->store[t][parity];
+    g.tier = tier;
+    g.nx = h->p.nx; g.ny = h->p.ny; g.ntx = h->ntx; g.nty = h->nty; g.tile = h->T; g.nf = h->nf; g.n = h->n;
+    return g;
+}
+
+static const uint8_t *live_tiers(amps_handle *h) { return h->transition ? h->d_tier_prev : h->d_tier_cur; }
+
+// Tier map of the current period from the monitor on a resting state:
+// Monitor1 classifies the state itself; Monitor2 starts all-high (the
+// reference's warm start phi_old = (phi==0), snowflake/end2end_mix.cu:44-46).
+static int reclassify_resting(amps_handle *h)
+{
+    const amps_params &p = h->p;
+    Grid g = grid_view(h, h->parity, live_tiers(h));
+    if (p.mode == AMPS_END2END_MIX) {
+        if (p.monitor == AMPS_MONITOR_TEM) {
+            CK(h, monitor_state(g, 2, p.monitor_samples, p.monitor_field, nullptr, h->d_snap, 1, h->d_flags, h->stream));
+            // every tile to the high tier for the first period
+            std::vector<double> big(h->ntiles, 1e300);
+            CK(h, cudaMemcpyAsync(h->d_metric, big.data(), sizeof(double) * h->ntiles, cudaMemcpyHostToDevice, h->stream));
+            CK(h, cudaStreamSynchronize(h->stream));
+        } else {
+            CK(h, monitor_state(g, 1, p.monitor_samples, p.monitor_field, h->d_metric, nullptr, 0, h->d_flags, h->stream));
+        }
+        ClassifyArgs c{};
+        c.metric = h->d_metric; c.tier_prev = h->d_tier_prev; c.tier_cur = h->d_tier_cur;
+        c.lists = h->d_lists; c.counts = h->d_counts; c.ntx = h->ntx; c.nty = h->nty;
+        c.thr_lo = p.thr_lo; c.thr_hi = p.thr_hi; c.high_tier = p.high_tier; c.use_mid = h->use_mid;
+        c.stats = h->d_stats; c.log = h->d_log; c.log_n = h->d_log_n; c.max_log = p.max_log;
+        c.step_base = h->d_step_base; c.advance = 0; c.stat_steps = 0;
+        CK(h, classify(c, h->stream));
+        h->transition = true;
+    }
+    return AMPS_OK;
+}
+
+// Static tier maps for the non-adaptive modes.
+static int static_tiers(amps_handle *h)
+{
+    const amps_params &p = h->p;
+    std::vector<uint8_t> m(h->ntiles, (uint8_t)(p.mode == AMPS_PURELOW ? TIER_HALF : p.high_tier));
+    if (p.mode == AMPS_GRAM1 || p.mode == AMPS_GRAM2) {
+        // snowflake/function.h:72-79: GRAM1 tiles below ratio*ntiles are low;
+        // GRAM2 tiles whose index mod 100 is below 100*ratio are low
+        for (int t = 0; t < h->ntiles; ++t) {
+            const bool low = p.mode == AMPS_GRAM1 ? t < h->ntiles * p.gram_ratio : (t % 100) < 100 * p.gram_ratio;
+            m[t] = low ? TIER_HALF : (uint8_t)p.high_tier;
+        }
+    }
+    if (p.mode == AMPS_END2END_MIX) return AMPS_OK;
+    CK(h, cudaMemcpyAsync(h->d_tier_cur, m.data(), h->ntiles, cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaMemcpyAsync(h->d_tier_prev, m.data(), h->ntiles, cudaMemcpyHostToDevice, h->stream));
+    CK(h, build_lists(h->d_tier_cur, h->ntiles, h->d_lists, h->d_counts, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    return AMPS_OK;
+}
+
+// Write the staged [nf][n] doubles (d_stage) as the current state.
+static int commit_stage(amps_handle *h)
+{
+    if (h->p.mode == AMPS_END2END_MIX) {
+        // resting state lives at the high tier until the monitor has looked at it
+        CK(h, cudaMemsetAsync(h->d_tier_cur, h->p.high_tier, h->ntiles, h->stream));
+        CK(h, cudaMemsetAsync(h->d_tier_prev, h->p.high_tier, h->ntiles, h->stream));
+        h->transition = false;
+        Grid g = grid_view(h, h->parity, h->d_tier_cur);
+        CK(h, scatter_fields(g, h->d_stage, 0, h->stream));
+        int r = reclassify_resting(h);
+        if (r) return r;
+    } else {
+        int r = static_tiers(h);
+        if (r) return r;
+        h->transition = false;
+        Grid g = grid_view(h, h->parity, h->d_tier_cur);
+        CK(h, scatter_fields(g, h->d_stage, 0, h->stream));
+    }
+    return AMPS_OK;
+}
+
+extern "C" int amps_init(amps_handle *h, int kind)
+{
+    if (!h) return AMPS_ERR_INVALID;
+    CK(h, cudaStreamSynchronize(h->stream));
+    std::vector<double *> f(h->nf);
+    for (int k = 0; k < h->nf; ++k) f[k] = h->h_pinned + (int64_t)k * h->n;
+    int r = amps_init_host(&h->p, kind, f.data());
+    if (r) FAIL(h, r, "initial state: invalid kind %d or particle placement failed", kind);
+    CK(h, cudaMemcpyAsync(h->d_stage, h->h_pinned, sizeof(double) * h->nf * h->n, cudaMemcpyHostToDevice, h->stream));
+    h->step = 0;
+    CK(h, cudaMemsetAsync(h->d_step_base, 0, sizeof(int64_t), h->stream));
+    return commit_stage(h);
+}
+
+static int set_impl(amps_handle *h, int f0, int nfs, const void *src, int dtype, int on_device)
+{
+    if (!h || !src || (dtype != AMPS_F64 && dtype != AMPS_F32) || f0 < 0 || f0 + nfs > h->nf)
+        return AMPS_ERR_INVALID;
+    // every field must be in the stage: fetch the others first
+    Grid live = grid_view(h, h->parity, live_tiers(h));
+    if (nfs < h->nf) CK(h, gather_fields(live, h->d_stage, 0, 0, h->nf, h->stream));
+    const size_t cnt = (size_t)nfs * h->n;
+    double *dst = h->d_stage + (int64_t)f0 * h->n;
+    if (dtype == AMPS_F64) {
+        CK(h, cudaMemcpyAsync(dst, src, cnt * 8, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->stream));
+    } else {
+        // float input: widen through the pinned buffer (host) or in place (device)
+        if (on_device) {
+            Grid g = live;  // reuse the gather kernel's conversion by copying through d_partials is awkward;
+            (void)g;        // convert on the host side instead
+            CK(h, cudaStreamSynchronize(h->stream));
+            std::vector<float> tmp(cnt);
+            CK(h, cudaMemcpy(tmp.data(), src, cnt * 4, cudaMemcpyDeviceToHost));
+            for (size_t i = 0; i < cnt; ++i) h->h_pinned[i] = tmp[i];
+        } else {
+            CK(h, cudaStreamSynchronize(h->stream));
+            for (size_t i = 0; i < cnt; ++i) h->h_pinned[i] = ((const float *)src)[i];
+        }
+        CK(h, cudaMemcpyAsync(dst, h->h_pinned, cnt * 8, cudaMemcpyHostToDevice, h->stream));
+    }
+    return commit_stage(h);
+}
+
+extern "C" int amps_set_field(amps_handle *h, int field, const void *src, int dtype, int on_device)
+{
+    return set_impl(h, field, 1, src, dtype, on_device);
+}
+
+extern "C" int amps_set_fields(amps_handle *h, const void *src, int dtype, int on_device)
+{
+    return set_impl(h, 0, h ? h->nf : 0, src, dtype, on_device);
+}
+
+static int get_impl(amps_handle *h, int f0, int nfs, void *dst, int dtype, int on_device)
+{
+    if (!h || !dst || (dtype != AMPS_F64 && dtype != AMPS_F32) || f0 < 0 || f0 + nfs > h->nf)
+        return AMPS_ERR_INVALID;
+    Grid g = grid_view(h, h->parity, live_tiers(h));
+    const size_t bytes = (size_t)nfs * h->n * (dtype == AMPS_F64 ? 8 : 4);
+    if (on_device) {
+        CK(h, gather_fields(g, dst, dtype == AMPS_F32, f0, nfs, h->stream));
+        CK(h, cudaStreamSynchronize(h->stream));
+    } else {
+        CK(h, gather_fields(g, h->d_stage, dtype == AMPS_F32, f0, nfs, h->stream));
+        CK(h, cudaMemcpyAsync(dst, h->d_stage, bytes, cudaMemcpyDeviceToHost, h->stream));
+        CK(h, cudaStreamSynchronize(h->stream));
+    }
+    return AMPS_OK;
+}
+
+extern "C" int amps_get_field(amps_handle *h, int field, void *dst, int dtype, int on_device)
+{
+    return get_impl(h, field, 1, dst, dtype, on_device);
+}
+
+extern "C" int amps_get_fields(amps_handle *h, void *dst, int dtype, int on_device)
+{
+    return get_impl(h, 0, h ? h->nf : 0, dst, dtype, on_device);
+}
+
+// -------------------------------------------------------------- time loop ----
+static int launch_step(amps_handle *h, int step_off, bool monitor_now)
+{
+    const amps_params &p = h->p;
+    StepArgs a;
+    memset(&a, 0, sizeof a);
+    for (int t = 0; t < 3; ++t) {
+        a.in[t] = h->store[t][h->parity];
+        a.out[t] = h->store[t][h->parity ^ 1];
+    }
+    a.tier_in = h->transition ? h->d_tier_prev : h->d_tier_cur;
+    a.tier_out = h->d_tier_cur;
+    a.count = h->d_counts;
+    a.nx = p.nx; a.ny = p.ny; a.ntx = h->ntx; a.nty = h->nty; a.nf = h->nf; a.bc = p.bc; a.stencil = p.stencil;
+    a.n = h->n;
+    a.monitor_now = monitor_now ? 1 : 0;
+    a.monitor_kind = p.monitor;
+    a.samples = p.monitor_samples;
+    a.mfield = p.monitor_field;
+    a.mu_lap_fp64 = p.mu_lap_fp64;
+    a.metric = h->d_metric;
+    a.snap = h->d_snap;
+    a.flags = h->d_flags;
+    a.step_base = h->d_step_base;
+    a.step_off = step_off;
+    a.ph = make_phys(p);
+    const bool ref = p.ref_order != 0;
+    for (int t = 2; t >= 0; --t) {
+        if (!h->used[t]) continue;
+        a.list = h->d_lists + t * h->ntiles;
+        cudaError_t e;
+        amps_handle::Ev ev{t, nullptr, nullptr};
+        if (h->profiling) {
+            if (cudaEventCreate(&ev.a) != cudaSuccess || cudaEventCreate(&ev.b) != cudaSuccess)
+                FAIL(h, AMPS_ERR_CUDA, "event create");
+            cudaEventRecord(ev.a, h->stream);
+        }
+        if (p.model == AMPS_GRAINGROWTH) e = gg_launch(h->T, t, ref, a, h->ntiles, h->stream);
+        else if (p.model == AMPS_KOBAYASHI) e = kob_launch(h->T, t, ref, a, h->ntiles, h->stream);
+        else e = sint_launch(h->T, t, ref, p.mu_lap_fp64 != 0, a, h->ntiles, h->stream);
+        if (e != cudaSuccess) FAIL(h, AMPS_ERR_CUDA, "step kernel launch: %s", cudaGetErrorString(e));
+        if (h->profiling) {
+            cudaEventRecord(ev.b, h->stream);
+            h->evs.push_back(ev);
+        }
+    }
+    h->parity ^= 1;
+    h->transition = false;
+    return AMPS_OK;
+}
+
+// Steps [k0, k0+cnt) of a period, then the period's bookkeeping.
+static int enqueue_chunk(amps_handle *h, int k0, int cnt)
+{
+    const amps_params &p = h->p;
+    const bool period_end = k0 + cnt == p.cadence;
+    for (int s = 0; s < cnt; ++s) {
+        const bool mon = h->mixed && period_end && s == cnt - 1;
+        int r = launch_step(h, k0 + s, mon);
+        if (r) return r;
+    }
+    if (h->mixed && period_end) {
+        ClassifyArgs c{};
+        c.metric = h->d_metric; c.tier_prev = h->d_tier_prev; c.tier_cur = h->d_tier_cur;
+        c.lists = h->d_lists; c.counts = h->d_counts; c.ntx = h->ntx; c.nty = h->nty;
+        c.thr_lo = p.thr_lo; c.thr_hi = p.thr_hi; c.high_tier = p.high_tier; c.use_mid = h->use_mid;
+        c.stats = h->d_stats; c.log = h->d_log; c.log_n = h->d_log_n; c.max_log = p.max_log;
+        c.step_base = h->d_step_base; c.advance = p.cadence; c.stat_steps = cnt;
+        CK(h, classify(c, h->stream));
+        h->transition = true;
+    } else {
+        CK(h, advance_period(h->d_step_base, period_end ? p.cadence : 0, cnt, h->d_counts, h->d_stats, h->stream));
+    }
+    return AMPS_OK;
+}
+
+extern "C" int amps_run(amps_handle *h, int nsteps)
+{
+    if (!h || nsteps < 0) return AMPS_ERR_INVALID;
+    const int cad = h->p.cadence;
+    while (nsteps > 0) {
+        const int k0 = (int)(h->step % cad);
+        const int cnt = nsteps < cad - k0 ? nsteps : cad - k0;
+        if (h->graphs && !h->profiling && k0 == 0 && cnt == cad && h->stream != nullptr) {
+            const int key = h->parity | (h->transition ? 2 : 0);
+            auto it = h->graph.find(key);
+            if (it == h->graph.end()) {
+                const int par0 = h->parity;
+                const bool tr0 = h->transition;
+                cudaGraph_t gr;
+                CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+                int r = enqueue_chunk(h, 0, cad);
+                cudaError_t e = cudaStreamEndCapture(h->stream, &gr);
+                if (r) return r;
+                if (e != cudaSuccess) FAIL(h, AMPS_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+                cudaGraphExec_t ex;
+                e = cudaGraphInstantiate(&ex, gr, 0);
+                cudaGraphDestroy(gr);
+                if (e != cudaSuccess) FAIL(h, AMPS_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+                it = h->graph.emplace(key, ex).first;
+                h->parity = par0;  // capture advanced the host-side state; replay does it for real
+                h->transition = tr0;
+            }
+            CK(h, cudaGraphLaunch(it->second, h->stream));
+            // mirror the period's effect on the host-side state
+            if (cad & 1) h->parity ^= 1;
+            h->transition = h->mixed;
+        } else {
+            int r = enqueue_chunk(h, k0, cnt);
+            if (r) return r;
+        }
+        h->step += cnt;
+        nsteps -= cnt;
+    }
+    return AMPS_OK;
+}
+
+// ------------------------------------------------------------- diagnostics ----
+extern "C" int amps_get_tile_tiers(amps_handle *h, uint8_t *out)
+{
+    if (!h || !out) return AMPS_ERR_INVALID;
+    CK(h, cudaStreamSynchronize(h->stream));
+    CK(h, cudaMemcpy(out, h->d_tier_cur, h->ntiles, cudaMemcpyDeviceToHost));
+    return AMPS_OK;
+}
+
+extern "C" int amps_get_tile_metric(amps_handle *h, double *out)
+{
+    if (!h || !out) return AMPS_ERR_INVALID;
+    CK(h, cudaStreamSynchronize(h->stream));
+    CK(h, cudaMemcpy(out, h->d_metric, sizeof(double) * h->ntiles, cudaMemcpyDeviceToHost));
+    return AMPS_OK;
+}
+
+extern "C" int amps_get_decision_log(amps_handle *h, uint8_t *out, int max_entries, int *n_out)
+{
+    if (!h || !n_out) return AMPS_ERR_INVALID;
+    CK(h, cudaStreamSynchronize(h->stream));
+    int n = 0;
+    CK(h, cudaMemcpy(&n, h->d_log_n, sizeof(int), cudaMemcpyDeviceToHost));
+    if (n > max_entries) n = max_entries;
+    if (n > 0 && out) CK(h, cudaMemcpy(out, h->d_log, (size_t)n * h->ntiles, cudaMemcpyDeviceToHost));
+    *n_out = n;
+    return AMPS_OK;
+}
+
+extern "C" int amps_get_stats(amps_handle *h, amps_stats *out)
+{
+    if (!h || !out) return AMPS_ERR_INVALID;
+    CK(h, cudaStreamSynchronize(h->stream));
+    unsigned long long s[8];
+    int flag = 0;
+    CK(h, cudaMemcpy(s, h->d_stats, sizeof s, cudaMemcpyDeviceToHost));
+    CK(h, cudaMemcpy(&flag, h->d_flags, sizeof(int), cudaMemcpyDeviceToHost));
+    out->steps = h->step;
+    for (int k = 0; k < 3; ++k) out->tile_steps[k] = (int64_t)s[k];
+    out->monitor_evals = (int64_t)s[3];
+    out->promotions = (int64_t)s[4];
+    out->demotions = (int64_t)s[5];
+    out->tiles = h->ntiles;
+    out->numeric_error = flag & 1;
+    return AMPS_OK;
+}
+
+extern "C" int amps_reduce(amps_handle *h, int field, int kind, double *out)
+{
+    if (!h || !out || field < 0 || field >= h->nf || kind < 0 || kind > 3) return AMPS_ERR_INVALID;
+    Grid g = grid_view(h, h->parity, live_tiers(h));
+    CK(h, reduce_field(g, field, kind, h->d_partials, h->d_out, h->stream));
+    CK(h, cudaMemcpyAsync(h->h_pinned, h->d_out, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    *out = h->h_pinned[0];
+    return AMPS_OK;
+}
+
+extern "C" int amps_compare(amps_handle *h, int field, const double *other, int on_device, double *max_abs, double *rms)
+{
+    if (!h || !other || field < 0 || field >= h->nf) return AMPS_ERR_INVALID;
+    const double *dev = other;
+    if (!on_device) {
+        CK(h, cudaMemcpyAsync(h->d_stage, other, sizeof(double) * h->n, cudaMemcpyHostToDevice, h->stream));
+        dev = h->d_stage;
+    }
+    Grid g = grid_view(h, h->parity, live_tiers(h));
+    CK(h, compare_field(g, field, dev, h->d_partials, h->d_out, h->stream));
+    CK(h, cudaMemcpyAsync(h->h_pinned, h->d_out, 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    if (max_abs) *max_abs = h->h_pinned[0];
+    if (rms) *rms = h->h_pinned[1];
+    return AMPS_OK;
+}
+
+extern "C" int amps_set_profiling(amps_handle *h, int enable)
+{
+    if (!h) return AMPS_ERR_INVALID;
+    CK(h, cudaStreamSynchronize(h->stream));
+    for (auto &e : h->evs) { cudaEventDestroy(e.a); cudaEventDestroy(e.b); }
+    h->evs.clear();
+    for (int k = 0; k < 3; ++k) { h->prof_ms[k] = 0; h->prof_launches[k] = 0; }
+    CK(h, cudaMemcpy(h->prof_stats0, h->d_stats, sizeof h->prof_stats0, cudaMemcpyDeviceToHost));
+    h->profiling = enable != 0;
+    return AMPS_OK;
+}
+
+extern "C" int amps_get_kernel_times(amps_handle *h, double *ms, int64_t *launches, int64_t *tile_steps)
+{
+    if (!h) return AMPS_ERR_INVALID;
+    CK(h, cudaStreamSynchronize(h->stream));
+    for (auto &e : h->evs) {
+        float t = 0.f;
+        CK(h, cudaEventElapsedTime(&t, e.a, e.b));
+        h->prof_ms[e.tier] += t;
+        h->prof_launches[e.tier] += 1;
+        cudaEventDestroy(e.a);
+        cudaEventDestroy(e.b);
+    }
+    h->evs.clear();
+    unsigned long long s[3];
+    CK(h, cudaMemcpy(s, h->d_stats, sizeof s, cudaMemcpyDeviceToHost));
+    for (int k = 0; k < 3; ++k) {
+        if (ms) ms[k] = h->prof_ms[k];
+        if (launches) launches[k] = h->prof_launches[k];
+        if (tile_steps) tile_steps[k] = (int64_t)(s[k] - h->prof_stats0[k]);
+    }
+    return AMPS_OK;
+}

@@ -1,0 +1,268 @@
+// amps_internal.cuh -- shared types and device helpers of libamps.
+//
+// Data layout in HBM.  Every field has one row-major [ny][nx] array per tier
+// in use (half, float, double) and per ping-pong parity; field f of tier t
+// lives at store[t][parity] + f*n.  A tile (tile x tile cells) is valid in
+// exactly one tier at a time, recorded in a uint8 tier map.  A step reads
+// every tile at its input tier (tier_in) and writes it at its output tier
+// (tier_out), so promotion/demotion costs nothing beyond the step itself: the
+// conversion happens in registers while the tile is staged.
+#pragma once
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace amps {
+
+constexpr int kThreads = 256;  // threads per tile CTA
+constexpr int kMaxFields = 33; // Q <= 32 order parameters / N <= 32 particles + c
+// dynamic shared memory a tile CTA may use (the 227 KB opt-in less room for static shared memory)
+constexpr int kMaxDynSmem = 226 * 1024;
+
+enum { TIER_HALF = 0, TIER_FP32 = 1, TIER_FP64 = 2 };
+
+// Model constants (double; each kernel rounds them to its compute type).
+struct Phys {
+    double dx, dy, dt, dxdy, inv_dxdy;
+    // Kobayashi
+    double tau, epsb, kappa, delta, aniso, alpha, gama, teq, theta0, pi, noise;
+    // grain growth
+    double mobil, grcoef, gamma;
+    // sintering
+    double coefm, coefk, coefl, dvol, dvap, dsur, dgrb, A, B;
+    uint64_t seed;
+};
+
+// Arguments of one tier launch of a fused step kernel.
+struct StepArgs {
+    const void *in[3];        // input parity, per tier (nullptr when the tier is unused)
+    void *out[3];             // output parity, per tier
+    const uint8_t *tier_in;   // tier of every tile's input data
+    const uint8_t *tier_out;  // tier every tile is computed and stored in
+    const int *list;          // tiles whose tier_out == this launch's tier
+    const int *count;         // count[tier]
+    int nx, ny, ntx, nty, nf, bc, stencil;
+    int64_t n;                // nx*ny
+    // monitor (active when monitor_now != 0)
+    int monitor_now, monitor_kind, samples, mfield, mu_lap_fp64;
+    double *metric;           // [ntiles]
+    double *snap;             // temporal snapshot: [nmon][ntiles][16] or [nmon][n]
+    int *flags;               // bit 0: NaN/Inf seen
+    const int64_t *step_base; // step index of the first step of the current period
+    int step_off;             // this step's offset within the period
+    Phys ph;
+};
+
+// ---- boundary mapping ------------------------------------------------------
+// Periodic wrap (snowflake/function.h:13-18) or mirror (zero flux) about the
+// domain face: -1 -> 0, -2 -> 1, n -> n-1, n+1 -> n-2.
+__device__ __forceinline__ int bc_map(int i, int n, int bc)
+{
+    if (bc == 0) return i < 0 ? i + n : (i >= n ? i - n : i);
+    return i < 0 ? -i - 1 : (i >= n ? 2 * n - i - 1 : i);
+}
+
+// ---- typed loads / stores ----------------------------------------------------
+template <typename CT> __device__ __forceinline__ CT load_tier(const StepArgs &a, int tier, int64_t idx)
+{
+    if (tier == TIER_FP64) return (CT)((const double *)a.in[2])[idx];
+    if (tier == TIER_FP32) return (CT)((const float *)a.in[1])[idx];
+    return (CT)__half2float(((const __half *)a.in[0])[idx]);
+}
+
+// 8 consecutive cells from a tier array, 16-byte aligned (idx % 8 == 0).
+template <typename CT> __device__ __forceinline__ void load8_tier(const StepArgs &a, int tier, int64_t idx, CT v[8])
+{
+    if (tier == TIER_FP64) {
+        const double2 *p = (const double2 *)((const double *)a.in[2] + idx);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            double2 d = __ldg(p + k);
+            v[2 * k] = (CT)d.x;
+            v[2 * k + 1] = (CT)d.y;
+        }
+    } else if (tier == TIER_FP32) {
+        const float4 *p = (const float4 *)((const float *)a.in[1] + idx);
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            float4 f = __ldg(p + k);
+            v[4 * k] = (CT)f.x; v[4 * k + 1] = (CT)f.y; v[4 * k + 2] = (CT)f.z; v[4 * k + 3] = (CT)f.w;
+        }
+    } else {
+        uint4 u = __ldg((const uint4 *)((const __half *)a.in[0] + idx));
+        const __half2 *h = (const __half2 *)&u;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            float2 f = __half22float2(h[k]);
+            v[2 * k] = (CT)f.x;
+            v[2 * k + 1] = (CT)f.y;
+        }
+    }
+}
+
+// Storage rounding of a computed value (what the next step will read back).
+template <int TIER, typename CT> __device__ __forceinline__ CT round_to_tier(CT v)
+{
+    if (TIER == TIER_HALF) return (CT)__half2float(__float2half_rn((float)v));
+    if (TIER == TIER_FP32) return (CT)(float)v;
+    return v;
+}
+
+template <int TIER, typename CT> __device__ __forceinline__ void store_tier(const StepArgs &a, int64_t idx, CT v)
+{
+    if (TIER == TIER_FP64) ((double *)a.out[2])[idx] = (double)v;
+    else if (TIER == TIER_FP32) ((float *)a.out[1])[idx] = (float)v;
+    else ((__half *)a.out[0])[idx] = __float2half_rn((float)v);
+}
+
+// ---- staged halo tile in shared memory ----------------------------------------
+// Field f occupies rows 0..T+2R-1 of pitch P = T + 2*O, the interior starting
+// at column O (16-byte aligned), the halo at O-R..O-1 and O+T..O+T+R-1.
+template <typename CT, int T, int R> struct Stage {
+    static constexpr int O = 16 / sizeof(CT) >= R ? 16 / sizeof(CT) : R;
+    static constexpr int P = T + 2 * O;
+    static constexpr int ROWS = T + 2 * R;
+    static constexpr int FIELD = ROWS * P;
+    __device__ static CT &at(CT *sm, int f, int r, int c) { return sm[f * FIELD + r * P + c]; }
+};
+
+// Stage fields [f0, f0+nfs) of tile (tx, ty) with an R-cell halo, every cell
+// read at its owner tile's input tier and converted to CT.  Interior row
+// segments go as 16-byte vector loads; halo columns as scalar loads.
+template <typename CT, int T, int R>
+__device__ __forceinline__ void stage_tile(const StepArgs &a, CT *sm, int tx, int ty, int f0, int nfs)
+{
+    using S = Stage<CT, T, R>;
+    const int x0 = tx * T, y0 = ty * T;
+    constexpr int SEG = T / 8;  // 8-cell segments per interior row
+    const int units = nfs * S::ROWS * SEG;
+    for (int u = threadIdx.x; u < units; u += kThreads) {
+        const int s = u % SEG;
+        const int r = (u / SEG) % S::ROWS;
+        const int f = u / (SEG * S::ROWS);
+        const int gy = bc_map(y0 - R + r, a.ny, a.bc);
+        const int tier = a.tier_in[(gy / T) * a.ntx + tx];
+        CT v[8];
+        load8_tier<CT>(a, tier, (int64_t)(f0 + f) * a.n + (int64_t)gy * a.nx + x0 + 8 * s, v);
+        CT *dst = &S::at(sm, f, r, S::O + 8 * s);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) dst[k] = v[k];
+    }
+    // halo columns: R cells on each side of every staged row
+    const int hunits = nfs * S::ROWS * 2 * R;
+    for (int u = threadIdx.x; u < hunits; u += kThreads) {
+        const int k = u % (2 * R);
+        const int r = (u / (2 * R)) % S::ROWS;
+        const int f = u / (2 * R * S::ROWS);
+        const int gy = bc_map(y0 - R + r, a.ny, a.bc);
+        const int lx = k < R ? x0 - R + k : x0 + T + (k - R);
+        const int gx = bc_map(lx, a.nx, a.bc);
+        const int tier = a.tier_in[(gy / T) * a.ntx + gx / T];
+        const int col = k < R ? S::O - R + k : S::O + T + (k - R);
+        S::at(sm, f, r, col) = load_tier<CT>(a, tier, (int64_t)(f0 + f) * a.n + (int64_t)gy * a.nx + gx);
+    }
+}
+
+// ---- block reductions (warp shuffle + one shared slot per warp) ------------------
+__device__ __forceinline__ double warp_max(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ double warp_min(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+// Max over the block; every thread gets the result.  red: >= 8 doubles of shared memory.
+__device__ __forceinline__ double block_max(double v, double *red)
+{
+    v = warp_max(v);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double r = red[0];
+#pragma unroll
+    for (int w = 1; w < kThreads / 32; ++w) r = fmax(r, red[w]);
+    return r;
+}
+__device__ __forceinline__ double block_min(double v, double *red)
+{
+    v = warp_min(v);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double r = red[0];
+#pragma unroll
+    for (int w = 1; w < kThreads / 32; ++w) r = fmin(r, red[w]);
+    return r;
+}
+
+// Is (row, col) of a tile on the monitor's sample lattice?  kind 1: spatial
+// {0,5,10,15} (snowflake/tools.h:185), kind 2: temporal {2,6,10,14}
+// (snowflake/tools.h:203), scaled to the tile; samples==1: every cell.
+template <int T> __device__ __forceinline__ int sample_index(int kind, int samples, int row, int col)
+{
+    if (samples) return 0;
+    int ir = -1, ic = -1;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int p = kind == 1 ? (k * (T - 1) * 2 + 3) / 6 : T / 8 + k * (T / 4);
+        if (row == p) ir = k;
+        if (col == p) ic = k;
+    }
+    return (ir < 0 || ic < 0) ? -1 : ir * 4 + ic;
+}
+
+// Per-tile monitor accumulator for one field, reduced at the end of the field.
+struct MonAcc {
+    double mn, mx, dmax;
+    int bad;
+};
+
+// Fold one computed (storage-rounded) value into the accumulator.
+template <int T>
+__device__ __forceinline__ void mon_add(const StepArgs &a, MonAcc &m, int mslot, int tile, int row, int col,
+                                        int64_t gidx, double v)
+{
+    if (!(v == v) || isinf(v)) m.bad = 1;
+    const int si = sample_index<T>(a.monitor_kind, a.samples, row, col);
+    if (si < 0) return;
+    if (a.monitor_kind == 1) {
+        m.mn = fmin(m.mn, v);
+        m.mx = fmax(m.mx, v);
+    } else {
+        double *snap = a.samples ? a.snap + (int64_t)mslot * a.n + gidx
+                                 : a.snap + ((int64_t)mslot * a.ntx * a.nty + tile) * 16 + si;
+        m.dmax = fmax(m.dmax, fabs(*snap - v));
+        *snap = v;
+    }
+}
+
+__device__ __forceinline__ void mon_reset(const StepArgs &a, MonAcc &m)
+{
+    // the reference's lattice monitor starts from min=1, max=0 (snowflake/tools.h:184)
+    m.mn = a.samples ? INFINITY : 1.0;
+    m.mx = a.samples ? -INFINITY : 0.0;
+    m.dmax = 0.0;
+    m.bad = 0;
+}
+
+// Reduce one field's accumulator over the block and fold into the tile metric.
+__device__ __forceinline__ double mon_finish(const StepArgs &a, MonAcc &m, double *red, double metric)
+{
+    double v;
+    if (a.monitor_kind == 1) {
+        const double mx = block_max(m.mx, red);
+        const double mn = block_min(m.mn, red);
+        v = mx - mn;
+    } else {
+        v = block_max(m.dmax, red);
+    }
+    if (__syncthreads_or(m.bad) && threadIdx.x == 0) atomicOr(a.flags, 1);
+    return fmax(metric, v);
+}
+
+}  // namespace amps

@@ -1,0 +1,61 @@
+// amps_kernels.h -- host-side launchers of the libamps kernels.
+#pragma once
+#include "amps_internal.cuh"
+
+namespace amps {
+
+cudaError_t gg_launch(int tile, int tier, bool ref, const StepArgs &a, int grid, cudaStream_t s);
+cudaError_t kob_launch(int tile, int tier, bool ref, const StepArgs &a, int grid, cudaStream_t s);
+cudaError_t sint_launch(int tile, int tier, bool ref, bool mu64, const StepArgs &a, int grid, cudaStream_t s);
+size_t gg_smem_bytes(int tile, int tier, int nf);
+// Raise the dynamic shared-memory limit of the kernel a launch would use
+// (must run before any graph capture).
+cudaError_t gg_prepare(int tile, int tier, bool ref);
+cudaError_t kob_prepare(int tile, int tier, bool ref);
+cudaError_t sint_prepare(int tile, int tier, bool ref, bool mu64);
+size_t kob_smem_bytes(int tile, int tier);
+size_t sint_smem_bytes(int tile, int tier, int nf, bool mu64);
+
+// Geometry + storage view used by the utility kernels.
+struct Grid {
+    void *store[3];           // one parity, per tier
+    const uint8_t *tier;      // tier of every tile
+    int nx, ny, ntx, nty, tile, nf;
+    int64_t n;
+};
+
+// Row-major [nf][n] double/float <-> tiered storage.
+cudaError_t scatter_fields(const Grid &g, const void *src, int src_f32, cudaStream_t s);
+cudaError_t gather_fields(const Grid &g, void *dst, int dst_f32, int f0, int nfs, cudaStream_t s);
+// Monitor at time 0 (or after a set_field): metric and temporal snapshot from the state.
+cudaError_t monitor_state(const Grid &g, int kind, int samples, int mfield, double *metric, double *snap,
+                          int write_snap, int *flags, cudaStream_t s);
+// get_type (snowflake/tools.h:212-230) on the device, three tiers, plus
+// ordered per-tier tile lists, stats and the decision log.
+struct ClassifyArgs {
+    const double *metric;
+    uint8_t *tier_prev, *tier_cur;
+    int *lists, *counts;
+    int ntx, nty;
+    double thr_lo, thr_hi;
+    int high_tier, use_mid;
+    unsigned long long *stats;  // [0..2] tile-steps, [3] evals, [4] promotions, [5] demotions
+    uint8_t *log;
+    int *log_n;
+    int max_log;
+    int64_t *step_base;
+    int advance;                // steps to add to *step_base (one period, or 0)
+    int stat_steps;             // steps the current counts ran for (tile-step stats)
+};
+cudaError_t classify(const ClassifyArgs &c, cudaStream_t s);
+// Rebuild lists/counts from tier_cur without reclassifying (static tier maps).
+cudaError_t build_lists(const uint8_t *tier, int ntiles, int *lists, int *counts, cudaStream_t s);
+// Bookkeeping at the end of a period when no classification runs.
+cudaError_t advance_period(int64_t *step_base, int advance, int stat_steps, const int *counts,
+                           unsigned long long *stats, cudaStream_t s);
+// FP64 reductions over one field (block partials, then one ordered pass).
+cudaError_t reduce_field(const Grid &g, int field, int kind, double *partials, double *out, cudaStream_t s);
+cudaError_t compare_field(const Grid &g, int field, const double *other, double *partials, double *out2,
+                          cudaStream_t s);
+
+}  // namespace amps

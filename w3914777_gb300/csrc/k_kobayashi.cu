@@ -1,0 +1,228 @@
+// k_kobayashi.cu -- fused Kobayashi anisotropic-dendrite step (phi, T).
+//
+// The reference splits a step into two kernels and seven full-size
+// intermediate arrays (snowflake/function.h:5-35 kernel1_pure writes lap phi,
+// lap T, phi_x, phi_y, eps, eps'; :36-60 kernel2_pure reads them at the 4
+// neighbours).  Here one CTA per tile stages phi and T with a 2-cell halo,
+// computes phi_x, phi_y, eps, eps' on the tile plus a 1-cell ring in shared
+// memory (phase A), then the update on the tile (phase B).  Nothing but phi
+// and T touches HBM.
+#include "amps_internal.cuh"
+#include "amps_kernels.h"
+#include <type_traits>
+
+namespace amps {
+
+__device__ __forceinline__ double noise_u01(uint64_t seed, uint64_t a, uint64_t b)
+{
+    auto mix = [](uint64_t z) {
+        z += 0x9E3779B97F4A7C15ull;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return z ^ (z >> 31);
+    };
+    return (double)(mix(mix(seed ^ mix(a)) + b) >> 11) * 0x1.0p-53;
+}
+
+template <typename CT> __device__ __forceinline__ CT k_atan2(CT y, CT x) { return atan2(y, x); }
+template <typename CT> __device__ __forceinline__ CT k_cos(CT v) { return cos(v); }
+template <typename CT> __device__ __forceinline__ CT k_sin(CT v) { return sin(v); }
+template <typename CT> __device__ __forceinline__ CT k_atan(CT v) { return atan(v); }
+
+template <int T, int TIER, bool REF>
+__global__ void __launch_bounds__(kThreads) kob_step_kernel(StepArgs a)
+{
+    using CT = typename std::conditional<TIER == TIER_FP64, double, float>::type;
+    constexpr int R = 2;
+    using S = Stage<CT, T, R>;
+    constexpr int E = T + 2;  // phase-A region side (tile + 1-cell ring)
+    extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ double red[kThreads / 32];
+    CT *sm = reinterpret_cast<CT *>(smraw);
+    CT *px = sm + 2 * S::FIELD, *py = px + E * E, *ep = py + E * E, *epd = ep + E * E;
+
+    if ((int)blockIdx.x >= a.count[TIER]) return;
+    const int tile = a.list[blockIdx.x];
+    const int tx = tile % a.ntx, ty = tile / a.ntx;
+    const int x0 = tx * T, y0 = ty * T;
+    stage_tile<CT, T, R>(a, sm, tx, ty, 0, 2);
+    __syncthreads();
+    const Phys &ph = a.ph;
+
+    // phase A: snowflake/function.h:30-34 on the tile + ring.  With zero-flux
+    // boundaries a ring cell outside the domain takes the intermediates of
+    // the cell it mirrors, as an index-mapped read of the full-size arrays does.
+    for (int u = threadIdx.x; u < E * E; u += kThreads) {
+        int i = u % E - 1, j = u / E - 1;
+        if (a.bc != 0) {
+            i = bc_map(x0 + i, a.nx, 1) - x0;
+            j = bc_map(y0 + j, a.ny, 1) - y0;
+        }
+        const int r = j + R, cc = i + S::O;
+        const CT pe = S::at(sm, 0, r, cc + 1), pw = S::at(sm, 0, r, cc - 1);
+        const CT pn = S::at(sm, 0, r + 1, cc), ps = S::at(sm, 0, r - 1, cc);
+        CT phx, phy, e, ed;
+        if (REF) {
+            phx = __ddiv_rn(__dsub_rn(pe, pw), 2.0 * ph.dx);
+            phy = __ddiv_rn(__dsub_rn(pn, ps), 2.0 * ph.dy);
+            const double th = atan2((double)phy, (double)phx);
+            const double arg = __dmul_rn(ph.aniso, __dsub_rn(th, ph.theta0));
+            e = __dmul_rn(ph.epsb, __dadd_rn(1.0, __dmul_rn(ph.delta, cos(arg))));
+            ed = __dmul_rn(__dmul_rn(__dmul_rn(-ph.epsb, ph.aniso), ph.delta), sin(arg));
+        } else {
+            phx = (pe - pw) * CT(0.5 / ph.dx);
+            phy = (pn - ps) * CT(0.5 / ph.dy);
+            const CT arg = CT(ph.aniso) * (k_atan2<CT>(phy, phx) - CT(ph.theta0));
+            e = CT(ph.epsb) * fma(CT(ph.delta), k_cos<CT>(arg), CT(1));
+            ed = CT(-ph.epsb * ph.aniso * ph.delta) * k_sin<CT>(arg);
+        }
+        const int o = u;
+        px[o] = phx; py[o] = phy; ep[o] = e; epd[o] = ed;
+    }
+    __syncthreads();
+
+    // phase B: snowflake/function.h:54-59 on the tile
+    const int64_t step = *a.step_base + a.step_off;
+    double metric = 0.0;
+    MonAcc mon;
+    const bool mon_on = a.monitor_now != 0;
+    if (mon_on) mon_reset(a, mon);
+    const int mslot = 0;
+    for (int u = threadIdx.x; u < T * T; u += kThreads) {
+        const int i = u % T, j = u / T;
+        const int r = j + R, cc = i + S::O;
+        const int o = (j + 1) * E + (i + 1);
+        const CT p0 = S::at(sm, 0, r, cc), t0 = S::at(sm, 1, r, cc);
+        const CT *P = &S::at(sm, 0, r, cc), *Tm = &S::at(sm, 1, r, cc);
+        const int64_t g = (int64_t)(y0 + j) * a.nx + x0 + i;
+        CT pn, tn;
+        if (REF) {
+            const double d = ph.dxdy;
+            // lap: snowflake/function.h:27-28, each term divided separately, left to right
+            double lp = __ddiv_rn(P[-1], d);
+            lp = __dadd_rn(lp, __ddiv_rn(P[-2], d));
+            lp = __dadd_rn(lp, __ddiv_rn(P[1], d));
+            lp = __dadd_rn(lp, __ddiv_rn(P[2], d));
+            lp = __dadd_rn(lp, __ddiv_rn(P[-S::P], d));
+            lp = __dadd_rn(lp, __ddiv_rn(P[-2 * S::P], d));
+            lp = __dadd_rn(lp, __ddiv_rn(P[S::P], d));
+            lp = __dadd_rn(lp, __ddiv_rn(P[2 * S::P], d));
+            lp = __dsub_rn(lp, __ddiv_rn(__dmul_rn(8.0, p0), d));
+            double lt = __ddiv_rn(Tm[-1], d);
+            lt = __dadd_rn(lt, __ddiv_rn(Tm[-2], d));
+            lt = __dadd_rn(lt, __ddiv_rn(Tm[1], d));
+            lt = __dadd_rn(lt, __ddiv_rn(Tm[2], d));
+            lt = __dadd_rn(lt, __ddiv_rn(Tm[-S::P], d));
+            lt = __dadd_rn(lt, __ddiv_rn(Tm[-2 * S::P], d));
+            lt = __dadd_rn(lt, __ddiv_rn(Tm[S::P], d));
+            lt = __dadd_rn(lt, __ddiv_rn(Tm[2 * S::P], d));
+            lt = __dsub_rn(lt, __ddiv_rn(__dmul_rn(8.0, t0), d));
+            const int on = o + E, os = o - E, oe = o + 1, ow = o - 1;
+            const double term1 = __ddiv_rn(__dsub_rn(__dmul_rn(__dmul_rn(ep[on], epd[on]), px[on]),
+                                                     __dmul_rn(__dmul_rn(ep[os], epd[os]), px[os])), 2.0 * ph.dy);
+            const double term2 = -__ddiv_rn(__dsub_rn(__dmul_rn(__dmul_rn(ep[oe], epd[oe]), py[oe]),
+                                                      __dmul_rn(__dmul_rn(ep[ow], epd[ow]), py[ow])), 2.0 * ph.dx);
+            const double m = __dmul_rn(ph.alpha / ph.pi, atan(__dmul_rn(ph.gama, __dsub_rn(ph.teq, t0))));
+            double drive = __dadd_rn(__dsub_rn(p0, 0.5), m);
+            if (ph.noise != 0.0)
+                drive = __dadd_rn(drive, __dmul_rn(ph.noise, __dsub_rn(noise_u01(ph.seed, (uint64_t)step, (uint64_t)g), 0.5)));
+            const double inner = __dadd_rn(__dadd_rn(__dadd_rn(term1, term2), __dmul_rn(__dmul_rn(ep[o], ep[o]), lp)),
+                                           __dmul_rn(__dmul_rn(p0, __dsub_rn(1.0, p0)), drive));
+            pn = __dadd_rn(p0, __dmul_rn(ph.dt / ph.tau, inner));
+            tn = __dadd_rn(__dadd_rn(t0, __dmul_rn(ph.dt, lt)), __dmul_rn(ph.kappa, __dsub_rn(pn, p0)));
+        } else {
+            const CT inv = CT(ph.inv_dxdy);
+            const CT lp = ((P[-1] + P[1]) + (P[-2] + P[2]) + (P[-S::P] + P[S::P]) + (P[-2 * S::P] + P[2 * S::P])
+                           - CT(8) * p0) * inv;
+            const CT lt = ((Tm[-1] + Tm[1]) + (Tm[-2] + Tm[2]) + (Tm[-S::P] + Tm[S::P]) + (Tm[-2 * S::P] + Tm[2 * S::P])
+                           - CT(8) * t0) * inv;
+            const int on = o + E, os = o - E, oe = o + 1, ow = o - 1;
+            const CT term1 = (ep[on] * epd[on] * px[on] - ep[os] * epd[os] * px[os]) * CT(0.5 / ph.dy);
+            const CT term2 = -(ep[oe] * epd[oe] * py[oe] - ep[ow] * epd[ow] * py[ow]) * CT(0.5 / ph.dx);
+            const CT m = CT(ph.alpha / ph.pi) * k_atan<CT>(CT(ph.gama) * (CT(ph.teq) - t0));
+            CT drive = p0 - CT(0.5) + m;
+            if (ph.noise != 0.0)
+                drive += CT(ph.noise) * (CT(noise_u01(ph.seed, (uint64_t)step, (uint64_t)g)) - CT(0.5));
+            const CT inner = term1 + term2 + ep[o] * ep[o] * lp + p0 * (CT(1) - p0) * drive;
+            pn = fma(CT(ph.dt / ph.tau), inner, p0);
+            tn = fma(CT(ph.kappa), pn - p0, fma(CT(ph.dt), lt, t0));
+        }
+        store_tier<TIER>(a, g, pn);
+        store_tier<TIER>(a, a.n + g, tn);
+        if (mon_on && (a.mfield <= 0)) mon_add<T>(a, mon, mslot, tile, j, i, g, (double)round_to_tier<TIER>(pn));
+    }
+    if (mon_on) {
+        metric = mon_finish(a, mon, red, metric);
+        if (a.mfield < 0 || a.mfield == 1) {
+            // second monitored field (T): a second pass over the stored values
+            MonAcc m2;
+            mon_reset(a, m2);
+            __syncthreads();
+            for (int u = threadIdx.x; u < T * T; u += kThreads) {
+                const int i = u % T, j = u / T;
+                const int64_t g = (int64_t)(y0 + j) * a.nx + x0 + i;
+                double v;
+                if (TIER == TIER_FP64) v = ((const double *)a.out[2])[a.n + g];
+                else if (TIER == TIER_FP32) v = ((const float *)a.out[1])[a.n + g];
+                else v = __half2float(((const __half *)a.out[0])[a.n + g]);
+                mon_add<T>(a, m2, a.mfield < 0 ? 1 : 0, tile, j, i, g, v);
+            }
+            metric = mon_finish(a, m2, red, metric);
+        }
+        if (threadIdx.x == 0) a.metric[tile] = metric;
+    }
+}
+
+template <int T, int TIER> static size_t kob_smem()
+{
+    using CT = typename std::conditional<TIER == TIER_FP64, double, float>::type;
+    return (2 * (size_t)Stage<CT, T, 2>::FIELD + 4 * (size_t)(T + 2) * (T + 2)) * sizeof(CT);
+}
+
+template <int T, int TIER, bool REF>
+static cudaError_t kob_launch_t(const StepArgs &a, int grid, cudaStream_t s)
+{
+    const size_t smem = kob_smem<T, TIER>();
+    kob_step_kernel<T, TIER, REF><<<grid, kThreads, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+size_t kob_smem_bytes(int tile, int tier)
+{
+    if (tile == 32) return tier == TIER_FP64 ? kob_smem<32, TIER_FP64>() : kob_smem<32, TIER_FP32>();
+    return tier == TIER_FP64 ? kob_smem<16, TIER_FP64>() : kob_smem<16, TIER_FP32>();
+}
+
+cudaError_t kob_launch(int tile, int tier, bool ref, const StepArgs &a, int grid, cudaStream_t s)
+{
+#define AMPS_KOB(TT)                                                                \
+    switch (tier) {                                                                 \
+    case TIER_HALF: return kob_launch_t<TT, TIER_HALF, false>(a, grid, s);          \
+    case TIER_FP32: return kob_launch_t<TT, TIER_FP32, false>(a, grid, s);          \
+    default:                                                                        \
+        return ref ? kob_launch_t<TT, TIER_FP64, true>(a, grid, s)                  \
+                   : kob_launch_t<TT, TIER_FP64, false>(a, grid, s);                \
+    }
+    if (tile == 32) { AMPS_KOB(32) }
+    AMPS_KOB(16)
+#undef AMPS_KOB
+}
+
+cudaError_t kob_prepare(int tile, int tier, bool ref)
+{
+    const int lim = kMaxDynSmem;
+    const auto attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
+#define AMPS_KOBP(TT)                                                                              \
+    switch (tier) {                                                                               \
+    case TIER_HALF: return cudaFuncSetAttribute(kob_step_kernel<TT, TIER_HALF, false>, attr, lim);  \
+    case TIER_FP32: return cudaFuncSetAttribute(kob_step_kernel<TT, TIER_FP32, false>, attr, lim);  \
+    default:                                                                                      \
+        return ref ? cudaFuncSetAttribute(kob_step_kernel<TT, TIER_FP64, true>, attr, lim)         \
+                   : cudaFuncSetAttribute(kob_step_kernel<TT, TIER_FP64, false>, attr, lim);       \
+    }
+    if (tile == 32) { AMPS_KOBP(32) }
+    AMPS_KOBP(16)
+#undef AMPS_KOBP
+}
+
+}  // namespace amps

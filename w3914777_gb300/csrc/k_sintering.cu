@@ -1,0 +1,236 @@
+// k_sintering.cu -- fused solid-state sintering step: Cahn-Hilliard density c
+// plus one Allen-Cahn order parameter per particle.
+//
+// The reference runs four kernels per step with full-size intermediates
+// (sintering/function.h:51-79 con1_pure: mu; :80-108 con2_pure: c update;
+// :110-159 phi1/phi2_pure: eta updates; sequenced in sintering/main.cu:136-147).
+// Here one CTA per tile stages c with a 2-cell halo and every eta with a
+// 1-cell halo, computes the chemical potential mu on the tile plus a 1-cell
+// ring (phase A), then c' from lap(mu) and every eta' from c' and the old
+// etas (phase B) -- the reference's operator splitting, in one pass.
+// Generalised to N particles: sum_{i<j} 2 eta_i eta_j for the grain-boundary
+// mobility term (the reference's 2*eta1*eta2, sintering/function.h:97) and
+// sums over all eta in the bulk terms.
+#include "amps_internal.cuh"
+#include "amps_kernels.h"
+#include <type_traits>
+
+namespace amps {
+
+template <int T, int TIER, bool REF, bool MU64>
+__global__ void __launch_bounds__(kThreads) sint_step_kernel(StepArgs a)
+{
+    using CT = typename std::conditional<TIER == TIER_FP64, double, float>::type;
+    using MT = typename std::conditional<MU64, double, CT>::type;  // type of mu and lap(mu)
+    using SC = Stage<CT, T, 2>;
+    using SE = Stage<CT, T, 1>;
+    constexpr int E = T + 2;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ double red[kThreads / 32];
+    MT *mu = reinterpret_cast<MT *>(smraw);                       // [E*E]
+    CT *smc = reinterpret_cast<CT *>(smraw + sizeof(MT) * E * E);  // c, 2-cell halo
+    CT *sme = smc + SC::FIELD;                                     // etas, 1-cell halo
+
+    if ((int)blockIdx.x >= a.count[TIER]) return;
+    const int tile = a.list[blockIdx.x];
+    const int tx = tile % a.ntx, ty = tile / a.ntx;
+    const int x0 = tx * T, y0 = ty * T;
+    const int np = a.nf - 1;
+    stage_tile<CT, T, 2>(a, smc, tx, ty, 0, 1);
+    stage_tile<CT, T, 1>(a, sme, tx, ty, 1, np);
+    __syncthreads();
+    const Phys &ph = a.ph;
+
+    // phase A: mu on the tile + ring (sintering/function.h:67-71)
+    for (int u = threadIdx.x; u < E * E; u += kThreads) {
+        int i = u % E - 1, j = u / E - 1;
+        if (a.bc != 0) {
+            i = bc_map(x0 + i, a.nx, 1) - x0;
+            j = bc_map(y0 + j, a.ny, 1) - y0;
+        }
+        const CT *C = &SC::at(smc, 0, j + 2, i + SC::O);
+        const CT cc = C[0];
+        MT m;
+        if (REF) {
+            const double lap = __ddiv_rn(__dsub_rn(__dadd_rn(__dadd_rn(__dadd_rn(C[-1], C[1]), C[-SC::P]), C[SC::P]),
+                                                   __dmul_rn(4.0, cc)), ph.dxdy);
+            double e0 = SE::at(sme, 0, j + 1, i + SE::O);
+            double s2 = __dmul_rn(e0, e0), s3 = pow(e0, 3.0);
+            for (int k = 1; k < np; ++k) {
+                const double e = SE::at(sme, k, j + 1, i + SE::O);
+                s2 = __dadd_rn(s2, __dmul_rn(e, e));
+                s3 = __dadd_rn(s3, pow(e, 3.0));
+            }
+            const double A2 = 2.0 * ph.A;
+            const double dfdc = __dadd_rn(
+                __dsub_rn(__dmul_rn(ph.B, __dsub_rn(__dadd_rn(__dmul_rn(2.0, cc), __dmul_rn(4.0, s3)), __dmul_rn(6.0, s2))),
+                          __dmul_rn(__dmul_rn(A2, __dmul_rn(cc, cc)), __dsub_rn(1.0, cc))),
+                __dmul_rn(__dmul_rn(A2, cc), __dmul_rn(__dsub_rn(1.0, cc), __dsub_rn(1.0, cc))));
+            m = __dsub_rn(dfdc, __dmul_rn(0.5 * ph.coefm, lap));
+        } else {
+            const MT lap = ((MT)C[-1] + (MT)C[1] + (MT)C[-SC::P] + (MT)C[SC::P] - MT(4) * (MT)cc) * MT(ph.inv_dxdy);
+            MT s2 = 0, s3 = 0;
+            for (int k = 0; k < np; ++k) {
+                const MT e = SE::at(sme, k, j + 1, i + SE::O);
+                const MT e2 = e * e;
+                s2 += e2;
+                s3 = fma(e2, e, s3);
+            }
+            const MT c1 = MT(1) - (MT)cc;
+            const MT A2 = MT(2.0 * ph.A);
+            const MT dfdc = MT(ph.B) * (MT(2) * (MT)cc + MT(4) * s3 - MT(6) * s2) + A2 * (MT)cc * c1 * (c1 - (MT)cc);
+            m = dfdc - MT(0.5 * ph.coefm) * lap;
+        }
+        mu[u] = m;
+    }
+    __syncthreads();
+
+    // phase B: c' (sintering/function.h:90-100), then eta_i' (:126-131)
+    double metric = 0.0;
+    MonAcc mon;
+    const bool mon_on = a.monitor_now != 0;
+    if (mon_on) mon_reset(a, mon);
+    for (int u = threadIdx.x; u < T * T; u += kThreads) {
+        const int i = u % T, j = u / T;
+        const int o = (j + 1) * E + (i + 1);
+        const int64_t g = (int64_t)(y0 + j) * a.nx + x0 + i;
+        const CT cc = SC::at(smc, 0, j + 2, i + SC::O);
+        CT cn;
+        double s2ref = 0.0;
+        CT s2f = 0;
+        if (REF) {
+            const double lapm = __ddiv_rn(__dsub_rn(__dadd_rn(__dadd_rn(__dadd_rn(mu[o - 1], mu[o + 1]), mu[o - E]), mu[o + E]),
+                                                    __dmul_rn(4.0, mu[o])), ph.dxdy);
+            const double phi = __dmul_rn(pow((double)cc, 3.0),
+                                         __dadd_rn(__dsub_rn(10.0, __dmul_rn(15.0, cc)), __dmul_rn(6.0, __dmul_rn(cc, cc))));
+            double sum = 0.0;
+            for (int p = 0; p < np; ++p)
+                for (int q = p + 1; q < np; ++q)
+                    sum = __dadd_rn(sum, __dmul_rn(__dmul_rn(SE::at(sme, p, j + 1, i + SE::O), SE::at(sme, q, j + 1, i + SE::O)), 2.0));
+            const double mob = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(ph.dvol, phi), __dmul_rn(ph.dvap, __dsub_rn(1.0, phi))),
+                                                   __dmul_rn(__dmul_rn(ph.dsur, cc), __dsub_rn(1.0, cc))),
+                                         __dmul_rn(ph.dgrb, sum));
+            double v = __dadd_rn(cc, __dmul_rn(__dmul_rn(ph.dt, mob), lapm));
+            if (v >= 1) v = 1;
+            else if (v < 0) v = 0;
+            cn = v;
+            double e0 = SE::at(sme, 0, j + 1, i + SE::O);
+            s2ref = __dmul_rn(e0, e0);
+            for (int k = 1; k < np; ++k) {
+                const double e = SE::at(sme, k, j + 1, i + SE::O);
+                s2ref = __dadd_rn(s2ref, __dmul_rn(e, e));
+            }
+        } else {
+            const MT lapm = (mu[o - 1] + mu[o + 1] + mu[o - E] + mu[o + E] - MT(4) * mu[o]) * MT(ph.inv_dxdy);
+            const CT phi = cc * cc * cc * fma(CT(6) * cc, cc, CT(10) - CT(15) * cc);
+            CT se = 0;
+            for (int k = 0; k < np; ++k) {
+                const CT e = SE::at(sme, k, j + 1, i + SE::O);
+                se += e;
+                s2f = fma(e, e, s2f);
+            }
+            const CT sum = se * se - s2f;  // sum_{i != j} eta_i eta_j
+            const CT mob = CT(ph.dvol) * phi + CT(ph.dvap) * (CT(1) - phi) + CT(ph.dsur) * cc * (CT(1) - cc)
+                         + CT(ph.dgrb) * sum;
+            CT v = (CT)((MT)cc + (MT)(CT(ph.dt) * mob) * lapm);
+            cn = v >= CT(1) ? CT(1) : (v < CT(0) ? CT(0) : v);
+        }
+        store_tier<TIER>(a, g, cn);
+        if (mon_on && a.mfield <= 0) mon_add<T>(a, mon, 0, tile, j, i, g, (double)round_to_tier<TIER>(cn));
+        for (int k = 0; k < np; ++k) {
+            const CT *Ep = &SE::at(sme, k, j + 1, i + SE::O);
+            const CT e = Ep[0];
+            CT en;
+            if (REF) {
+                const double lap = __ddiv_rn(__dsub_rn(__dadd_rn(__dadd_rn(__dadd_rn(Ep[-1], Ep[1]), Ep[-SE::P]), Ep[SE::P]),
+                                                       __dmul_rn(4.0, e)), ph.dxdy);
+                const double cnd = cn;
+                const double dfd = __dmul_rn(ph.B, __dadd_rn(__dadd_rn(
+                    __dmul_rn(__dmul_rn(-12.0, __dmul_rn(e, e)), __dsub_rn(2.0, cnd)),
+                    __dmul_rn(__dmul_rn(12.0, e), __dsub_rn(1.0, cnd))), __dmul_rn(__dmul_rn(12.0, e), s2ref)));
+                double v = __dsub_rn(e, __dmul_rn(ph.dt * ph.coefl, __dsub_rn(dfd, __dmul_rn(0.5 * ph.coefk, lap))));
+                if (v >= 1) v = 1;
+                else if (v < 0) v = 0;
+                en = v;
+            } else {
+                const CT lap = (Ep[-1] + Ep[1] + Ep[-SE::P] + Ep[SE::P] - CT(4) * e) * CT(ph.inv_dxdy);
+                const CT dfd = CT(12.0 * ph.B) * e * (s2f + (CT(1) - cn) - e * (CT(2) - cn));
+                CT v = fma(-CT(ph.dt * ph.coefl), fma(-CT(0.5 * ph.coefk), lap, dfd), e);
+                en = v >= CT(1) ? CT(1) : (v < CT(0) ? CT(0) : v);
+            }
+            store_tier<TIER>(a, (int64_t)(k + 1) * a.n + g, en);
+        }
+    }
+    if (mon_on) {
+        metric = mon_finish(a, mon, red, metric);
+        if (threadIdx.x == 0) a.metric[tile] = metric;
+    }
+}
+
+template <int T, int TIER, bool MU64> static size_t sint_smem(int nf)
+{
+    using CT = typename std::conditional<TIER == TIER_FP64, double, float>::type;
+    using MT = typename std::conditional<MU64, double, CT>::type;
+    return sizeof(MT) * (T + 2) * (T + 2) + sizeof(CT) * ((size_t)Stage<CT, T, 2>::FIELD
+                                                          + (size_t)(nf - 1) * Stage<CT, T, 1>::FIELD);
+}
+
+template <int T, int TIER, bool REF, bool MU64>
+static cudaError_t sint_launch_t(const StepArgs &a, int grid, cudaStream_t s)
+{
+    const size_t smem = sint_smem<T, TIER, MU64>(a.nf);
+    sint_step_kernel<T, TIER, REF, MU64><<<grid, kThreads, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+size_t sint_smem_bytes(int tile, int tier, int nf, bool mu64)
+{
+    if (tile == 32) {
+        if (tier == TIER_FP64) return sint_smem<32, TIER_FP64, true>(nf);
+        return mu64 ? sint_smem<32, TIER_FP32, true>(nf) : sint_smem<32, TIER_FP32, false>(nf);
+    }
+    if (tier == TIER_FP64) return sint_smem<16, TIER_FP64, true>(nf);
+    return mu64 ? sint_smem<16, TIER_FP32, true>(nf) : sint_smem<16, TIER_FP32, false>(nf);
+}
+
+cudaError_t sint_launch(int tile, int tier, bool ref, bool mu64, const StepArgs &a, int grid, cudaStream_t s)
+{
+#define AMPS_SINT(TT)                                                                              \
+    switch (tier) {                                                                                \
+    case TIER_HALF:                                                                                \
+        return mu64 ? sint_launch_t<TT, TIER_HALF, false, true>(a, grid, s)                        \
+                    : sint_launch_t<TT, TIER_HALF, false, false>(a, grid, s);                      \
+    case TIER_FP32:                                                                                \
+        return mu64 ? sint_launch_t<TT, TIER_FP32, false, true>(a, grid, s)                        \
+                    : sint_launch_t<TT, TIER_FP32, false, false>(a, grid, s);                      \
+    default:                                                                                       \
+        return ref ? sint_launch_t<TT, TIER_FP64, true, true>(a, grid, s)                          \
+                   : sint_launch_t<TT, TIER_FP64, false, true>(a, grid, s);                        \
+    }
+    if (tile == 32) { AMPS_SINT(32) }
+    AMPS_SINT(16)
+#undef AMPS_SINT
+}
+
+cudaError_t sint_prepare(int tile, int tier, bool ref, bool mu64)
+{
+    const int lim = kMaxDynSmem;
+    const auto attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
+#define AMPS_SP(TT)                                                                                      \
+    switch (tier) {                                                                                      \
+    case TIER_HALF:                                                                                      \
+        return mu64 ? cudaFuncSetAttribute(sint_step_kernel<TT, TIER_HALF, false, true>, attr, lim)      \
+                    : cudaFuncSetAttribute(sint_step_kernel<TT, TIER_HALF, false, false>, attr, lim);    \
+    case TIER_FP32:                                                                                      \
+        return mu64 ? cudaFuncSetAttribute(sint_step_kernel<TT, TIER_FP32, false, true>, attr, lim)      \
+                    : cudaFuncSetAttribute(sint_step_kernel<TT, TIER_FP32, false, false>, attr, lim);    \
+    default:                                                                                             \
+        return ref ? cudaFuncSetAttribute(sint_step_kernel<TT, TIER_FP64, true, true>, attr, lim)        \
+                   : cudaFuncSetAttribute(sint_step_kernel<TT, TIER_FP64, false, true>, attr, lim);      \
+    }
+    if (tile == 32) { AMPS_SP(32) }
+    AMPS_SP(16)
+#undef AMPS_SP
+}
+
+}  // namespace amps
