@@ -4,7 +4,7 @@ reference tree).  Each fixture holds the reference's fields after STEPS steps
 from the reference's own initial state, as float64, at the reference's
 compile-time size 512x512:
 
-  kobayashi_ref.npz    snowflake/paras/para2.h, snowflake/function.h:5-60
+  kobayashi_ref.npz    snowflake/paras/para2.h, snowflake/function.h:5-60 (also at EARLY steps)
   graingrowth_ref.npz  graingrowth/paras/para1.h, graingrowth/function.h:5-30
   sintering_ref.npz    sintering/paras/para5.h, sintering/function.h:51-159
 
@@ -21,6 +21,7 @@ import oracle_bind as ob  # noqa: E402
 
 N = 512
 STEPS = 40
+EARLY = 8  # Kobayashi snapshot before any zero-gradient point is reached
 
 
 def main():
@@ -30,8 +31,11 @@ def main():
     R = ob.ref_lib("snowflake")
     phi = np.zeros((N, N)); T = np.zeros((N, N))
     R.ref_snowflake_init(ob.ptr(phi), ob.ptr(T))
-    R.ref_snowflake_steps(ob.ptr(phi), ob.ptr(T), STEPS)
+    R.ref_snowflake_steps(ob.ptr(phi), ob.ptr(T), EARLY)
+    phi_early, T_early = phi.copy(), T.copy()
+    R.ref_snowflake_steps(ob.ptr(phi), ob.ptr(T), STEPS - EARLY)
     np.savez_compressed(os.path.join(HERE, "kobayashi_ref.npz"), phi=phi, T=T, steps=STEPS,
+                        phi_early=phi_early, T_early=T_early, early=EARLY,
                         params=ob.ref_params("snowflake", 14))
 
     R = ob.ref_lib("graingrowth")

@@ -33,15 +33,46 @@ def rel_err(a, b):
 
 # ------------------------------------------------------------- golden ----
 def test_kobayashi_fp64_matches_reference_golden():
+    """The reference's own parameters and symmetric seed (snowflake/paras/para2.h,
+    snowflake/tools.h:24-33).  Bar: <= 1e-12 relative at the early snapshot.
+    Later, where the symmetric seed produces an exactly zero gradient, the
+    reference's theta = atan2(phi_y, phi_x) (snowflake/function.h:32) is
+    discontinuous and a one-ulp difference in the device libm makes theta
+    arbitrary there; tests/test_oracle_conditioning.py shows the oracle itself
+    moves by ~1e-4 under a one-ulp perturbation.  Bar after 40 steps: 1e-3
+    relative (phi) / 1e-2 relative (T, whose magnitude is ~1e-3 of phi's)."""
     w = amps()
     g = np.load(os.path.join(GOLD, "kobayashi_ref.npz"))
     p = w.Params.preset("kobayashi", 2, mode="purehigh")
     with w.Simulation(p, init=w.INIT_REFERENCE) as s:
-        s.run(int(g["steps"]))
+        s.run(int(g["early"]))
+        f8 = s.fields()
+        s.run(int(g["steps"]) - int(g["early"]))
         f = s.fields()
+    e8 = max(rel_err(f8[0], g["phi_early"]), rel_err(f8[1], g["T_early"]))
     e_phi, e_T = rel_err(f[0], g["phi"]), rel_err(f[1], g["T"])
-    print(f"kobayashi fp64 vs reference after {int(g['steps'])} steps: phi {e_phi:.3e} T {e_T:.3e}")
-    assert e_phi <= 1e-12 and e_T <= 1e-12
+    print(f"kobayashi fp64 vs reference: {int(g['early'])} steps {e8:.3e}; "
+          f"{int(g['steps'])} steps phi {e_phi:.3e} T {e_T:.3e}")
+    assert e8 <= 1e-12
+    assert e_phi <= 1e-3 and e_T <= 1e-2
+
+
+def test_kobayashi_fp64_reference_params_asymmetric_seed():
+    """Reference parameters (para2) with a seed whose gradient never vanishes
+    exactly: a disc plus a seeded 1e-3 perturbation.  Bar: <= 1e-12 after 40 steps."""
+    w = amps()
+    p = w.Params.preset("kobayashi", 2, mode="purehigh", nx=128, ny=128, init_offset=0, init_r2=60.0)
+    f0 = w.init_host(p, w.INIT_REFERENCE)
+    rng = np.random.default_rng(11)
+    f0[0] += 1e-3 * rng.random(f0[0].shape)
+    with w.Simulation(p) as s:
+        s.set_fields(f0)
+        s.run(40)
+        f = s.fields()
+    phi, T = ob.kob_run(ob.kob_params(128, 128), f0[0], f0[1], 40)
+    e = max(rel_err(f[0], phi), rel_err(f[1], T))
+    print(f"kobayashi para2 asymmetric seed, 40 steps: {e:.3e}")
+    assert e <= 1e-12
 
 
 def test_graingrowth_fp64_matches_reference_golden():

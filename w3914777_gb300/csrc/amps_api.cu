@@ -40,6 +40,11 @@ struct amps_handle {
     double *d_stage = nullptr, *d_partials = nullptr, *d_out = nullptr;
     double *h_pinned = nullptr;  // nf*n doubles, page-locked
     cudaStream_t own = nullptr, stream = nullptr;
+    // the tier kernels of one step run as parallel branches: fork from
+    // `stream` onto aux[], join back before the next step
+    cudaStream_t aux[2] = {nullptr, nullptr};
+    cudaEvent_t ev_fork = nullptr, ev_join[2] = {nullptr, nullptr};
+    int ntiers_used = 0;
     int64_t step = 0;
     bool graphs = true;
     std::map<int, cudaGraphExec_t> graph;  // key: parity | transition<<1
@@ -126,6 +131,11 @@ static void free_all(amps_handle *h)
     for (void *q : ps)
         if (q) cudaFree(q);
     if (h->h_pinned) cudaFreeHost(h->h_pinned);
+    for (int k = 0; k < 2; ++k) {
+        if (h->aux[k]) cudaStreamDestroy(h->aux[k]);
+        if (h->ev_join[k]) cudaEventDestroy(h->ev_join[k]);
+    }
+    if (h->ev_fork) cudaEventDestroy(h->ev_fork);
     if (h->own) cudaStreamDestroy(h->own);
 }
 
@@ -195,6 +205,13 @@ extern "C" int amps_create(const amps_params *p, amps_handle **out)
 #undef ALLOC
     if (cudaStreamCreateWithFlags(&h->own, cudaStreamNonBlocking) != cudaSuccess)
         return fail(AMPS_ERR_CUDA, "stream");
+    for (int k = 0; k < 2; ++k)
+        if (cudaStreamCreateWithFlags(&h->aux[k], cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&h->ev_join[k], cudaEventDisableTiming) != cudaSuccess)
+            return fail(AMPS_ERR_CUDA, "aux stream");
+    if (cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) != cudaSuccess)
+        return fail(AMPS_ERR_CUDA, "event");
+    for (int t = 0; t < 3; ++t) h->ntiers_used += h->used[t] ? 1 : 0;
     h->stream = h->own;
     cudaMemsetAsync(h->d_stats, 0, sizeof(unsigned long long) * 8, h->stream);
     cudaMemsetAsync(h->d_flags, 0, sizeof(int) * 4, h->stream);
@@ -459,23 +476,38 @@ static int launch_step(amps_handle *h, int step_off, bool monitor_now)
     a.step_off = step_off;
     a.ph = make_phys(p);
     const bool ref = p.ref_order != 0;
+    const bool fork = h->ntiers_used > 1;
+    if (fork) {
+        CK(h, cudaEventRecord(h->ev_fork, h->stream));
+        for (int k = 0; k < h->ntiers_used - 1; ++k) CK(h, cudaStreamWaitEvent(h->aux[k], h->ev_fork, 0));
+    }
+    int branch = 0;
     for (int t = 2; t >= 0; --t) {
         if (!h->used[t]) continue;
+        // the first (highest) tier stays on the main stream, the others fork
+        cudaStream_t st = branch == 0 ? h->stream : h->aux[branch - 1];
         a.list = h->d_lists + t * h->ntiles;
         cudaError_t e;
         amps_handle::Ev ev{t, nullptr, nullptr};
         if (h->profiling) {
             if (cudaEventCreate(&ev.a) != cudaSuccess || cudaEventCreate(&ev.b) != cudaSuccess)
                 FAIL(h, AMPS_ERR_CUDA, "event create");
-            cudaEventRecord(ev.a, h->stream);
+            cudaEventRecord(ev.a, st);
         }
-        if (p.model == AMPS_GRAINGROWTH) e = gg_launch(h->T, t, ref, a, h->ntiles, h->stream);
-        else if (p.model == AMPS_KOBAYASHI) e = kob_launch(h->T, t, ref, a, h->ntiles, h->stream);
-        else e = sint_launch(h->T, t, ref, p.mu_lap_fp64 != 0, a, h->ntiles, h->stream);
+        if (p.model == AMPS_GRAINGROWTH) e = gg_launch(h->T, t, ref, a, h->ntiles, st);
+        else if (p.model == AMPS_KOBAYASHI) e = kob_launch(h->T, t, ref, a, h->ntiles, st);
+        else e = sint_launch(h->T, t, ref, p.mu_lap_fp64 != 0, a, h->ntiles, st);
         if (e != cudaSuccess) FAIL(h, AMPS_ERR_CUDA, "step kernel launch: %s", cudaGetErrorString(e));
         if (h->profiling) {
-            cudaEventRecord(ev.b, h->stream);
+            cudaEventRecord(ev.b, st);
             h->evs.push_back(ev);
+        }
+        ++branch;
+    }
+    if (fork) {
+        for (int k = 0; k < h->ntiers_used - 1; ++k) {
+            CK(h, cudaEventRecord(h->ev_join[k], h->aux[k]));
+            CK(h, cudaStreamWaitEvent(h->stream, h->ev_join[k], 0));
         }
     }
     h->parity ^= 1;

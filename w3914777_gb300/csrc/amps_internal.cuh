@@ -126,40 +126,96 @@ template <typename CT, int T, int R> struct Stage {
     __device__ static CT &at(CT *sm, int f, int r, int c) { return sm[f * FIELD + r * P + c]; }
 };
 
+// Tiers of the 3x3 tile neighbourhood of (tx, ty) after the boundary mapping
+// (periodic: wrap; zero flux: the mirrored halo of an edge tile lies in the
+// tile itself).  Filled by threads 0..8; the caller synchronises.
+__device__ __forceinline__ void load_neighbour_tiers(const StepArgs &a, int tx, int ty, uint8_t *nt)
+{
+    if (threadIdx.x < 9) {
+        const int dy = (int)threadIdx.x / 3 - 1, dx = (int)threadIdx.x % 3 - 1;
+        int yy = ty + dy, xx = tx + dx;
+        if (a.bc == 0) {
+            yy = yy < 0 ? yy + a.nty : (yy >= a.nty ? yy - a.nty : yy);
+            xx = xx < 0 ? xx + a.ntx : (xx >= a.ntx ? xx - a.ntx : xx);
+        } else {
+            yy = yy < 0 ? 0 : (yy >= a.nty ? a.nty - 1 : yy);
+            xx = xx < 0 ? 0 : (xx >= a.ntx ? a.ntx - 1 : xx);
+        }
+        nt[threadIdx.x] = a.tier_in[yy * a.ntx + xx];
+    }
+}
+
 // Stage fields [f0, f0+nfs) of tile (tx, ty) with an R-cell halo, every cell
-// read at its owner tile's input tier and converted to CT.  Interior row
-// segments go as 16-byte vector loads; halo columns as scalar loads.
+// read at its owner tile's input tier (nt: load_neighbour_tiers) and
+// converted to CT.  Interior row segments go as 16-byte vector loads; halo
+// columns as scalar loads.  Each thread issues a batch of loads before it
+// stores any of them, so that many loads are in flight at once.
 template <typename CT, int T, int R>
-__device__ __forceinline__ void stage_tile(const StepArgs &a, CT *sm, int tx, int ty, int f0, int nfs)
+__device__ __forceinline__ void stage_tile(const StepArgs &a, CT *sm, const uint8_t *nt, int tx, int ty, int f0,
+                                           int nfs)
 {
     using S = Stage<CT, T, R>;
+    constexpr int PER = sizeof(CT) == 8 ? 2 : 4;  // 8-cell units per batch and thread
     const int x0 = tx * T, y0 = ty * T;
     constexpr int SEG = T / 8;  // 8-cell segments per interior row
     const int units = nfs * S::ROWS * SEG;
-    for (int u = threadIdx.x; u < units; u += kThreads) {
-        const int s = u % SEG;
-        const int r = (u / SEG) % S::ROWS;
-        const int f = u / (SEG * S::ROWS);
-        const int gy = bc_map(y0 - R + r, a.ny, a.bc);
-        const int tier = a.tier_in[(gy / T) * a.ntx + tx];
-        CT v[8];
-        load8_tier<CT>(a, tier, (int64_t)(f0 + f) * a.n + (int64_t)gy * a.nx + x0 + 8 * s, v);
-        CT *dst = &S::at(sm, f, r, S::O + 8 * s);
+    for (int base = threadIdx.x; base < units; base += kThreads * PER) {
+        CT v[PER][8];
 #pragma unroll
-        for (int k = 0; k < 8; ++k) dst[k] = v[k];
+        for (int q = 0; q < PER; ++q) {
+            const int u = base + q * kThreads;
+            if (u < units) {
+                const int s = u % SEG;
+                const int r = (u / SEG) % S::ROWS;
+                const int f = u / (SEG * S::ROWS);
+                const int gy = bc_map(y0 - R + r, a.ny, a.bc);
+                const int tier = nt[(r < R ? 0 : (r < T + R ? 3 : 6)) + 1];
+                load8_tier<CT>(a, tier, (int64_t)(f0 + f) * a.n + (int64_t)gy * a.nx + x0 + 8 * s, v[q]);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < PER; ++q) {
+            const int u = base + q * kThreads;
+            if (u < units) {
+                const int s = u % SEG;
+                const int r = (u / SEG) % S::ROWS;
+                const int f = u / (SEG * S::ROWS);
+                CT *dst = &S::at(sm, f, r, S::O + 8 * s);
+#pragma unroll
+                for (int k = 0; k < 8; ++k) dst[k] = v[q][k];
+            }
+        }
     }
     // halo columns: R cells on each side of every staged row
+    constexpr int HPER = 8;
     const int hunits = nfs * S::ROWS * 2 * R;
-    for (int u = threadIdx.x; u < hunits; u += kThreads) {
-        const int k = u % (2 * R);
-        const int r = (u / (2 * R)) % S::ROWS;
-        const int f = u / (2 * R * S::ROWS);
-        const int gy = bc_map(y0 - R + r, a.ny, a.bc);
-        const int lx = k < R ? x0 - R + k : x0 + T + (k - R);
-        const int gx = bc_map(lx, a.nx, a.bc);
-        const int tier = a.tier_in[(gy / T) * a.ntx + gx / T];
-        const int col = k < R ? S::O - R + k : S::O + T + (k - R);
-        S::at(sm, f, r, col) = load_tier<CT>(a, tier, (int64_t)(f0 + f) * a.n + (int64_t)gy * a.nx + gx);
+    for (int base = threadIdx.x; base < hunits; base += kThreads * HPER) {
+        CT v[HPER];
+#pragma unroll
+        for (int q = 0; q < HPER; ++q) {
+            const int u = base + q * kThreads;
+            if (u < hunits) {
+                const int k = u % (2 * R);
+                const int r = (u / (2 * R)) % S::ROWS;
+                const int f = u / (2 * R * S::ROWS);
+                const int gy = bc_map(y0 - R + r, a.ny, a.bc);
+                const int lx = k < R ? x0 - R + k : x0 + T + (k - R);
+                const int gx = bc_map(lx, a.nx, a.bc);
+                const int tier = nt[(r < R ? 0 : (r < T + R ? 3 : 6)) + (k < R ? 0 : 2)];
+                v[q] = load_tier<CT>(a, tier, (int64_t)(f0 + f) * a.n + (int64_t)gy * a.nx + gx);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < HPER; ++q) {
+            const int u = base + q * kThreads;
+            if (u < hunits) {
+                const int k = u % (2 * R);
+                const int r = (u / (2 * R)) % S::ROWS;
+                const int f = u / (2 * R * S::ROWS);
+                const int col = k < R ? S::O - R + k : S::O + T + (k - R);
+                S::at(sm, f, r, col) = v[q];
+            }
+        }
     }
 }
 

@@ -28,12 +28,15 @@ __global__ void __launch_bounds__(kThreads) gg_step_kernel(StepArgs a)
     constexpr int RPT = T / RG;       // rows per thread
     extern __shared__ __align__(16) unsigned char smraw[];
     __shared__ double red[kThreads / 32];
+    __shared__ uint8_t ntier[9];
     CT *sm = reinterpret_cast<CT *>(smraw);
 
     if ((int)blockIdx.x >= a.count[TIER]) return;
     const int tile = a.list[blockIdx.x];
     const int tx = tile % a.ntx, ty = tile / a.ntx;
-    stage_tile<CT, T, R>(a, sm, tx, ty, 0, a.nf);
+    load_neighbour_tiers(a, tx, ty, ntier);
+    __syncthreads();
+    stage_tile<CT, T, R>(a, sm, ntier, tx, ty, 0, a.nf);
     __syncthreads();
 
     const int col = threadIdx.x % T;

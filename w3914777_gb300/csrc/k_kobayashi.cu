@@ -38,6 +38,7 @@ __global__ void __launch_bounds__(kThreads) kob_step_kernel(StepArgs a)
     constexpr int E = T + 2;  // phase-A region side (tile + 1-cell ring)
     extern __shared__ __align__(16) unsigned char smraw[];
     __shared__ double red[kThreads / 32];
+    __shared__ uint8_t ntier[9];
     CT *sm = reinterpret_cast<CT *>(smraw);
     CT *px = sm + 2 * S::FIELD, *py = px + E * E, *ep = py + E * E, *epd = ep + E * E;
 
@@ -45,7 +46,9 @@ __global__ void __launch_bounds__(kThreads) kob_step_kernel(StepArgs a)
     const int tile = a.list[blockIdx.x];
     const int tx = tile % a.ntx, ty = tile / a.ntx;
     const int x0 = tx * T, y0 = ty * T;
-    stage_tile<CT, T, R>(a, sm, tx, ty, 0, 2);
+    load_neighbour_tiers(a, tx, ty, ntier);
+    __syncthreads();
+    stage_tile<CT, T, R>(a, sm, ntier, tx, ty, 0, 2);
     __syncthreads();
     const Phys &ph = a.ph;
 

@@ -27,6 +27,7 @@ __global__ void __launch_bounds__(kThreads) sint_step_kernel(StepArgs a)
     constexpr int E = T + 2;
     extern __shared__ __align__(16) unsigned char smraw[];
     __shared__ double red[kThreads / 32];
+    __shared__ uint8_t ntier[9];
     MT *mu = reinterpret_cast<MT *>(smraw);                       // [E*E]
     CT *smc = reinterpret_cast<CT *>(smraw + sizeof(MT) * E * E);  // c, 2-cell halo
     CT *sme = smc + SC::FIELD;                                     // etas, 1-cell halo
@@ -36,8 +37,10 @@ __global__ void __launch_bounds__(kThreads) sint_step_kernel(StepArgs a)
     const int tx = tile % a.ntx, ty = tile / a.ntx;
     const int x0 = tx * T, y0 = ty * T;
     const int np = a.nf - 1;
-    stage_tile<CT, T, 2>(a, smc, tx, ty, 0, 1);
-    stage_tile<CT, T, 1>(a, sme, tx, ty, 1, np);
+    load_neighbour_tiers(a, tx, ty, ntier);
+    __syncthreads();
+    stage_tile<CT, T, 2>(a, smc, ntier, tx, ty, 0, 1);
+    stage_tile<CT, T, 1>(a, sme, ntier, tx, ty, 1, np);
     __syncthreads();
     const Phys &ph = a.ph;
 
