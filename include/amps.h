@@ -69,8 +69,10 @@ enum { AMPS_TIER_HALF = 0, AMPS_TIER_FP32 = 1, AMPS_TIER_FP64 = 2 };
 enum { AMPS_BC_PERIODIC = 0, AMPS_BC_NOFLUX = 1 };
 
 /* monitors: Monitor1 = spatial range (snowflake/tools.h:177-193),
- * Monitor2 = temporal change over one cadence (snowflake/tools.h:194-211) */
-enum { AMPS_MONITOR_SPA = 1, AMPS_MONITOR_TEM = 2 };
+ * Monitor2 = temporal change over one cadence (snowflake/tools.h:194-211),
+ * RATE = the change of the cadence's last step times the cadence (an
+ * estimate of Monitor2 that needs no snapshot; no reference counterpart) */
+enum { AMPS_MONITOR_SPA = 1, AMPS_MONITOR_TEM = 2, AMPS_MONITOR_RATE = 3 };
 
 /* dtypes crossing the ABI */
 enum { AMPS_F64 = 0, AMPS_F32 = 1 };
@@ -95,7 +97,7 @@ typedef struct amps_params {
     int bc;               /* AMPS_BC_* */
     int tile;             /* tile side: 16 (the reference's unit) or 32 */
     int high_tier;        /* the reference's `highprecision`: AMPS_TIER_FP64 or AMPS_TIER_FP32 */
-    int monitor;          /* AMPS_MONITOR_SPA or AMPS_MONITOR_TEM */
+    int monitor;          /* AMPS_MONITOR_SPA, AMPS_MONITOR_TEM or AMPS_MONITOR_RATE */
     int monitor_samples;  /* 0: the reference's 4x4 sample lattice; 1: every cell of the tile */
     int monitor_field;    /* monitored field index; -1 = every field (max over fields) */
     int cadence;          /* steps between monitor evaluations (reference: 10) */
@@ -195,10 +197,11 @@ AMPS_API int amps_run(amps_handle *h, int nsteps);
 /* Enable (1) / disable (0) CUDA-graph replay of whole periods (default 1). */
 AMPS_API int amps_set_graphs(amps_handle *h, int enable);
 /* Kernel timing: while enabled, amps_run launches eagerly and brackets every
- * update-kernel launch with CUDA events on the handle's stream.
- * amps_get_kernel_times returns, per tier (half, fp32, fp64), the summed
- * device time in ms, the number of launches and the tile-steps they computed
- * since profiling was enabled. */
+ * update-kernel launch with CUDA events on the stream it is launched on.
+ * amps_get_kernel_times fills arrays of 4: ms and launches of the per-tier
+ * update kernels (index 0 half, 1 fp32, 2 fp64) and of the fused all-tier
+ * update kernel (index 3); tile_steps[0..2] are the tile-steps computed per
+ * tier since profiling was enabled (tile_steps[3] their sum). */
 AMPS_API int amps_set_profiling(amps_handle *h, int enable);
 AMPS_API int amps_get_kernel_times(amps_handle *h, double *ms, int64_t *launches, int64_t *tile_steps);
 

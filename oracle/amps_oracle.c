@@ -312,6 +312,13 @@ void orc_monitor_tem(const double *f, const double *last, int nx, int ny, int ti
         }
 }
 
+void orc_monitor_rate(const double *f, const double *prev, int nx, int ny, int tile, int samples, int cadence,
+                      double *metric)
+{
+    orc_monitor_tem(f, prev, nx, ny, tile, samples, metric);
+    for (int t = 0; t < (nx / tile) * (ny / tile); ++t) metric[t] = metric[t] * cadence;
+}
+
 void orc_classify(const double *metric, int ntx, int nty, double thr_lo, double thr_hi, uint8_t *tier)
 {
     for (int ty = 0; ty < nty; ++ty)

@@ -81,6 +81,10 @@ void orc_monitor_spa(const double *f, int nx, int ny, int tile, int samples, dou
 /* Monitor2 (temporal change): snowflake/tools.h:194-211. */
 void orc_monitor_tem(const double *f, const double *last, int nx, int ny, int tile, int samples,
                      double *metric);
+/* Per-step change times the cadence (no reference counterpart: the
+ * snapshot-free estimate of Monitor2); lattice of the temporal monitor. */
+void orc_monitor_rate(const double *f, const double *prev, int nx, int ny, int tile, int samples, int cadence,
+                      double *metric);
 /* get_type: snowflake/tools.h:212-230 -- max over the tile and its 4 tile
  * neighbours (not periodic), then thresholds.  Three tiers: metric >= thr_hi
  * -> 2 (FP64), >= thr_lo -> 1 (FP32), else 0 (half).  The reference's two-tier

@@ -71,6 +71,8 @@ def lib():
         L.orc_sint_init_two.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_double] * 5 + [_dp, _dp, _dp]
         L.orc_monitor_spa.argtypes = [_dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp]
         L.orc_monitor_tem.argtypes = [_dp, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp]
+        L.orc_monitor_rate.argtypes = [_dp, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                       ctypes.c_int, _dp]
         L.orc_classify.argtypes = [_dp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, _u8p]
         L.orc_uniform01.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64]
         L.orc_uniform01.restype = ctypes.c_double
@@ -172,6 +174,14 @@ def monitor_tem(f, last, tile, samples=0):
     m = np.zeros((ny // tile) * (nx // tile))
     lib().orc_monitor_tem(ptr(np.ascontiguousarray(f)), ptr(np.ascontiguousarray(last)), nx, ny, tile,
                           samples, ptr(m))
+    return m.reshape(ny // tile, nx // tile)
+
+
+def monitor_rate(f, prev, tile, cadence, samples=0):
+    ny, nx = f.shape
+    m = np.zeros((ny // tile) * (nx // tile))
+    lib().orc_monitor_rate(ptr(np.ascontiguousarray(f)), ptr(np.ascontiguousarray(prev)), nx, ny, tile, samples,
+                           cadence, ptr(m))
     return m.reshape(ny // tile, nx // tile)
 
 

@@ -186,6 +186,8 @@ def _oracle_decisions(w, s, p, state_prev, state_now):
     for k in fields:
         if p.monitor == w.MONITOR_SPA:
             mk = ob.monitor_spa(state_now[k], T, p.monitor_samples)
+        elif p.monitor == w.MONITOR_RATE:
+            mk = ob.monitor_rate(state_now[k], state_prev[k], T, p.cadence, p.monitor_samples)
         else:
             mk = ob.monitor_tem(state_now[k], state_prev[k], T, p.monitor_samples)
         m = mk if m is None else np.maximum(m, mk)
@@ -196,17 +198,18 @@ def _oracle_decisions(w, s, p, state_prev, state_now):
     return m, t
 
 
-@pytest.mark.parametrize("monitor,samples", [(1, 0), (2, 0), (1, 1), (2, 1)])
+@pytest.mark.parametrize("monitor,samples", [(1, 0), (2, 0), (1, 1), (2, 1), (3, 0), (3, 1)])
 def test_mixed_decisions_match_oracle(monitor, samples):
     """The fused monitor + classification against the oracle on the same state."""
     w = amps()
     thr = (0.3, 0.6) if monitor == 1 else (1e-4, 1e-2)
     p = w.Params.preset("kobayashi", 2, mode="end2end_mix", nx=256, ny=256, monitor=monitor,
                         monitor_samples=samples, thr_lo=thr[0], thr_hi=thr[1], init_r2=400.0, max_log=16)
+    back = 1 if monitor == 3 else 10  # the rate monitor compares with the previous step
     with w.Simulation(p, init=w.INIT_REFERENCE) as s:
-        s.run(40)
+        s.run(50 - back)
         prev = s.fields()
-        s.run(10)
+        s.run(back)
         now = s.fields()
         m_gpu = s.metric()
         t_gpu = s.tiers()
@@ -236,6 +239,27 @@ def test_mixed_error_envelope_kobayashi():
     print(f"kobayashi mixed vs fp64 oracle: max abs {e:.3e}; tier mix half/fp32/fp64 {frac}")
     assert sum(st["tile_steps"]) == steps * s.ntiles[0] * s.ntiles[1]
     assert e <= 5e-3
+
+
+@pytest.mark.parametrize("monitor,samples", [(1, 1), (2, 1), (3, 1), (2, 0)])
+def test_graingrowth_decisions_match_oracle(monitor, samples):
+    """Fused grain-growth kernel: every tier in one launch; monitor over all fields."""
+    w = amps()
+    thr = (1e-3, 0.5) if monitor == 1 else (1e-5, 3e-3)
+    p = w.Params.preset("graingrowth", 0, nx=256, ny=192, nfields=5, monitor=monitor, monitor_samples=samples,
+                        thr_lo=thr[0], thr_hi=thr[1], max_log=32)
+    back = 1 if monitor == 3 else 10
+    with w.Simulation(p, init=w.INIT_SEEDED) as s:
+        s.run(200 - back)
+        prev = s.fields()
+        s.run(back)
+        now = s.fields()
+        m_gpu, t_gpu, st = s.metric(), s.tiers(), s.stats()
+    m, t = _oracle_decisions(w, s, p, prev, now)
+    assert np.array_equal(m_gpu, m)
+    assert np.array_equal(t_gpu, t)
+    assert sum(st["tile_steps"]) == 200 * t.size
+    print("graingrowth tiers after 200 steps:", np.bincount(t.ravel(), minlength=3))
 
 
 def test_mixed_graingrowth_envelope():

@@ -23,7 +23,7 @@ KOBAYASHI, GRAINGROWTH, SINTERING = 0, 1, 2
 PUREHIGH, PURELOW, END2END_MIX, GRAM1, GRAM2 = 0, 1, 2, 3, 4
 TIER_HALF, TIER_FP32, TIER_FP64 = 0, 1, 2
 BC_PERIODIC, BC_NOFLUX = 0, 1
-MONITOR_SPA, MONITOR_TEM = 1, 2
+MONITOR_SPA, MONITOR_TEM, MONITOR_RATE = 1, 2, 3
 F64, F32 = 0, 1
 INIT_REFERENCE, INIT_SEEDED = 0, 1
 REDUCE_SUM, REDUCE_MIN, REDUCE_MAX, REDUCE_SUMSQ = 0, 1, 2, 3
@@ -271,9 +271,10 @@ class Simulation:
         self._ck(lib().amps_set_profiling(self.h, int(enable)), "amps_set_profiling")
 
     def kernel_times(self):
-        """Per tier (half, fp32, fp64): summed device ms, launches, tile-steps since profiling began."""
-        ms = (ctypes.c_double * 3)()
-        la = (ctypes.c_int64 * 3)()
-        ts = (ctypes.c_int64 * 3)()
+        """[half, fp32, fp64 per-tier kernels, fused all-tier kernel]: summed device ms and launches;
+        tile-steps per tier (index 3: total) since profiling began."""
+        ms = (ctypes.c_double * 4)()
+        la = (ctypes.c_int64 * 4)()
+        ts = (ctypes.c_int64 * 4)()
         self._ck(lib().amps_get_kernel_times(self.h, ms, la, ts), "amps_get_kernel_times")
         return list(ms), list(la), list(ts)

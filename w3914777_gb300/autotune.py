@@ -28,6 +28,7 @@ def default_candidates(params):
     spa = [(1e-3, math.inf), (3e-3, math.inf), (1e-2, math.inf), (2e-2, math.inf), (5e-2, math.inf),
            (1e-3, 1.5), (1e-2, 1.5)]
     tem = [(1e-6, math.inf), (1e-5, math.inf), (1e-4, math.inf), (1e-3, math.inf), (1e-5, 1e-1)]
+    rate = [(1e-5, math.inf), (1e-4, math.inf), (1e-3, math.inf), (1e-4, 1e-1)]
     for t in tiles:
         for lo, hi in spa:
             c.append((f"spa t{t} lo={lo:g} hi={hi:g}",
@@ -36,6 +37,10 @@ def default_candidates(params):
         for lo, hi in tem:
             c.append((f"tem t{t} lo={lo:g} hi={hi:g}",
                       dict(mode=A.END2END_MIX, tile=t, monitor=A.MONITOR_TEM, monitor_samples=1, monitor_field=-1,
+                           thr_lo=lo, thr_hi=hi if math.isfinite(hi) else 1e300)))
+        for lo, hi in rate:
+            c.append((f"rate t{t} lo={lo:g} hi={hi:g}",
+                      dict(mode=A.END2END_MIX, tile=t, monitor=A.MONITOR_RATE, monitor_samples=1, monitor_field=-1,
                            thr_lo=lo, thr_hi=hi if math.isfinite(hi) else 1e300)))
     c.append(("all fp32", dict(mode=A.PUREHIGH, high_tier=A.TIER_FP32)))
     c.append(("all half", dict(mode=A.PURELOW)))

@@ -53,8 +53,8 @@ struct amps_handle {
     bool profiling = false;
     struct Ev { int tier; cudaEvent_t a, b; };
     std::vector<Ev> evs;
-    double prof_ms[3] = {0, 0, 0};
-    int64_t prof_launches[3] = {0, 0, 0};
+    double prof_ms[4] = {0, 0, 0, 0};
+    int64_t prof_launches[4] = {0, 0, 0, 0};
     unsigned long long prof_stats0[3] = {0, 0, 0};
 };
 
@@ -305,8 +305,10 @@ static int reclassify_resting(amps_handle *h)
     const amps_params &p = h->p;
     Grid g = grid_view(h, h->parity, live_tiers(h));
     if (p.mode == AMPS_END2END_MIX) {
-        if (p.monitor == AMPS_MONITOR_TEM) {
-            CK(h, monitor_state(g, 2, p.monitor_samples, p.monitor_field, nullptr, h->d_snap, 1, h->d_flags, h->stream));
+        if (p.monitor != AMPS_MONITOR_SPA) {
+            if (p.monitor == AMPS_MONITOR_TEM)
+                CK(h, monitor_state(g, 2, p.monitor_samples, p.monitor_field, nullptr, h->d_snap, 1, h->d_flags,
+                                    h->stream));
             // every tile to the high tier for the first period
             std::vector<double> big(h->ntiles, 1e300);
             CK(h, cudaMemcpyAsync(h->d_metric, big.data(), sizeof(double) * h->ntiles, cudaMemcpyHostToDevice, h->stream));
@@ -469,6 +471,7 @@ static int launch_step(amps_handle *h, int step_off, bool monitor_now)
     a.samples = p.monitor_samples;
     a.mfield = p.monitor_field;
     a.mu_lap_fp64 = p.mu_lap_fp64;
+    a.cadence = p.cadence;
     a.metric = h->d_metric;
     a.snap = h->d_snap;
     a.flags = h->d_flags;
@@ -476,11 +479,25 @@ static int launch_step(amps_handle *h, int step_off, bool monitor_now)
     a.step_off = step_off;
     a.ph = make_phys(p);
     const bool ref = p.ref_order != 0;
-    const bool fork = h->ntiers_used > 1;
-    if (fork) {
-        CK(h, cudaEventRecord(h->ev_fork, h->stream));
-        for (int k = 0; k < h->ntiers_used - 1; ++k) CK(h, cudaStreamWaitEvent(h->aux[k], h->ev_fork, 0));
+    if (p.model == AMPS_GRAINGROWTH) {
+        // one fused launch covers every tier
+        amps_handle::Ev ev{3, nullptr, nullptr};
+        if (h->profiling) {
+            if (cudaEventCreate(&ev.a) != cudaSuccess || cudaEventCreate(&ev.b) != cudaSuccess)
+                FAIL(h, AMPS_ERR_CUDA, "event create");
+            cudaEventRecord(ev.a, h->stream);
+        }
+        cudaError_t e = gg_launch(h->T, 0, ref, a, h->ntiles, h->stream);
+        if (e != cudaSuccess) FAIL(h, AMPS_ERR_CUDA, "step kernel launch: %s", cudaGetErrorString(e));
+        if (h->profiling) {
+            cudaEventRecord(ev.b, h->stream);
+            h->evs.push_back(ev);
+        }
+        h->parity ^= 1;
+        h->transition = false;
+        return AMPS_OK;
     }
+    const bool fork = h->ntiers_used > 1;
     int branch = 0;
     for (int t = 2; t >= 0; --t) {
         if (!h->used[t]) continue;
@@ -662,7 +679,7 @@ extern "C" int amps_set_profiling(amps_handle *h, int enable)
     CK(h, cudaStreamSynchronize(h->stream));
     for (auto &e : h->evs) { cudaEventDestroy(e.a); cudaEventDestroy(e.b); }
     h->evs.clear();
-    for (int k = 0; k < 3; ++k) { h->prof_ms[k] = 0; h->prof_launches[k] = 0; }
+    for (int k = 0; k < 4; ++k) { h->prof_ms[k] = 0; h->prof_launches[k] = 0; }
     CK(h, cudaMemcpy(h->prof_stats0, h->d_stats, sizeof h->prof_stats0, cudaMemcpyDeviceToHost));
     h->profiling = enable != 0;
     return AMPS_OK;
@@ -683,10 +700,17 @@ extern "C" int amps_get_kernel_times(amps_handle *h, double *ms, int64_t *launch
     h->evs.clear();
     unsigned long long s[3];
     CK(h, cudaMemcpy(s, h->d_stats, sizeof s, cudaMemcpyDeviceToHost));
-    for (int k = 0; k < 3; ++k) {
+    int64_t total = 0;
+    for (int k = 0; k < 4; ++k) {
         if (ms) ms[k] = h->prof_ms[k];
         if (launches) launches[k] = h->prof_launches[k];
-        if (tile_steps) tile_steps[k] = (int64_t)(s[k] - h->prof_stats0[k]);
+        if (k < 3) {
+            const int64_t ts = (int64_t)(s[k] - h->prof_stats0[k]);
+            total += ts;
+            if (tile_steps) tile_steps[k] = ts;
+        } else if (tile_steps) {
+            tile_steps[3] = total;
+        }
     }
     return AMPS_OK;
 }

@@ -162,7 +162,7 @@ extern "C" int amps_check_params(const amps_params *p, char *msg, size_t len)
     if (p->high_tier != AMPS_TIER_FP64 && p->high_tier != AMPS_TIER_FP32) BAD("high_tier must be FP64 or FP32");
     if (p->model == AMPS_GRAINGROWTH && (p->nfields < 1 || p->nfields > 32)) BAD("grain growth Q must be 1..32");
     if (p->model == AMPS_SINTERING && (p->nfields < 1 || p->nfields > 32)) BAD("sintering N must be 1..32");
-    if (p->monitor != AMPS_MONITOR_SPA && p->monitor != AMPS_MONITOR_TEM) BAD("monitor must be 1 or 2");
+    if (p->monitor < AMPS_MONITOR_SPA || p->monitor > AMPS_MONITOR_RATE) BAD("monitor must be 1, 2 or 3");
     const int nf = amps_num_fields(p);
     if (p->monitor_field < -1 || p->monitor_field >= nf) BAD("monitor_field out of range");
     if (p->cadence < 1) BAD("cadence must be >= 1");

@@ -44,7 +44,7 @@ struct StepArgs {
     int nx, ny, ntx, nty, nf, bc, stencil;
     int64_t n;                // nx*ny
     // monitor (active when monitor_now != 0)
-    int monitor_now, monitor_kind, samples, mfield, mu_lap_fp64;
+    int monitor_now, monitor_kind, samples, mfield, mu_lap_fp64, cadence;
     double *metric;           // [ntiles]
     double *snap;             // temporal snapshot: [nmon][ntiles][16] or [nmon][n]
     int *flags;               // bit 0: NaN/Inf seen
@@ -272,28 +272,50 @@ template <int T> __device__ __forceinline__ int sample_index(int kind, int sampl
     return (ir < 0 || ic < 0) ? -1 : ir * 4 + ic;
 }
 
+// Address of the temporal-monitor snapshot of one cell (si: lattice index).
+template <int T>
+__device__ __forceinline__ double *snap_ptr(const StepArgs &a, int mslot, int tile, int64_t gidx, int si)
+{
+    return a.samples ? a.snap + (int64_t)mslot * a.n + gidx
+                     : a.snap + ((int64_t)mslot * a.ntx * a.nty + tile) * 16 + si;
+}
+
+// Snapshot value of one cell for kind 2 (0 elsewhere), read before the cell is computed.
+template <int T>
+__device__ __forceinline__ double snap_prefetch(const StepArgs &a, int mslot, int tile, int row, int col,
+                                                int64_t gidx)
+{
+    if (a.monitor_kind != 2) return 0.0;
+    const int si = sample_index<T>(2, a.samples, row, col);
+    return si < 0 ? 0.0 : *snap_ptr<T>(a, mslot, tile, gidx, si);
+}
+
 // Per-tile monitor accumulator for one field, reduced at the end of the field.
 struct MonAcc {
     double mn, mx, dmax;
     int bad;
 };
 
-// Fold one computed (storage-rounded) value into the accumulator.
+// Fold one computed (storage-rounded) value into the accumulator.  kind 1:
+// spatial range; kind 2: change since the snapshot of the previous monitor
+// step (the snapshot is updated here); kind 3: this step's change `v - old`
+// scaled by the cadence (no snapshot).  `snapv` is the snapshot value the
+// caller prefetched for kind 2.
 template <int T>
 __device__ __forceinline__ void mon_add(const StepArgs &a, MonAcc &m, int mslot, int tile, int row, int col,
-                                        int64_t gidx, double v)
+                                        int64_t gidx, double v, double old, double snapv)
 {
     if (!(v == v) || isinf(v)) m.bad = 1;
-    const int si = sample_index<T>(a.monitor_kind, a.samples, row, col);
+    const int si = sample_index<T>(a.monitor_kind == 1 ? 1 : 2, a.samples, row, col);
     if (si < 0) return;
     if (a.monitor_kind == 1) {
         m.mn = fmin(m.mn, v);
         m.mx = fmax(m.mx, v);
+    } else if (a.monitor_kind == 2) {
+        m.dmax = fmax(m.dmax, fabs(snapv - v));
+        *snap_ptr<T>(a, mslot, tile, gidx, si) = v;
     } else {
-        double *snap = a.samples ? a.snap + (int64_t)mslot * a.n + gidx
-                                 : a.snap + ((int64_t)mslot * a.ntx * a.nty + tile) * 16 + si;
-        m.dmax = fmax(m.dmax, fabs(*snap - v));
-        *snap = v;
+        m.dmax = fmax(m.dmax, fabs(v - old) * a.cadence);
     }
 }
 

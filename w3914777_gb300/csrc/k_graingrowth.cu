@@ -1,10 +1,12 @@
 // k_graingrowth.cu -- fused multi-order-parameter Allen-Cahn (grain growth) step.
 //
-// One CTA per tile.  All Q fields of the tile plus a 1-cell halo are staged in
-// shared memory at the tile's compute precision (each cell converted from its
-// owner tile's input tier), then every thread advances one column of
-// T*T/256 cells for all Q fields and stores them at the tile's output tier.
-// On monitor steps the epilogue also reduces the per-tile monitor metric.
+// One launch per step covers every tile; each CTA advances one tile in that
+// tile's own tier.  Half and FP32 tiles stage all Q fields plus a 1-cell halo
+// in shared memory as float (each cell converted from its owner tile's input
+// tier) and store at half/float; FP64 tiles are bound by the FP64 pipes, so
+// they skip the staging and read their neighbourhood straight through L1.
+// Shared memory is therefore sized by the float staging alone.  On monitor
+// steps the epilogue reduces the per-tile metric.
 //
 // Reference: graingrowth/function.h:5-30 (kernel1_pure, launched once per
 // field, graingrowth/purehigh.cu:31-32) and graingrowth/function.h:33-277
@@ -14,76 +16,127 @@
 //   eta_i' = eta_i - dt*L*(dfd_i - kappa*lap(eta_i)).
 #include "amps_internal.cuh"
 #include "amps_kernels.h"
-#include <type_traits>
 
 namespace amps {
 
-template <int T, int TIER, bool REF>
-__global__ void __launch_bounds__(kThreads) gg_step_kernel(StepArgs a)
+// Half / FP32 tile: staged float neighbourhood, float arithmetic.
+template <int T, int TIER>
+__device__ __forceinline__ void gg_tile_lo(const StepArgs &a, const float *sm, int tile, int tx, int ty, double *red)
 {
-    using CT = typename std::conditional<TIER == TIER_FP64, double, float>::type;
-    constexpr int R = 1;
-    using S = Stage<CT, T, R>;
-    constexpr int RG = kThreads / T;  // row groups
-    constexpr int RPT = T / RG;       // rows per thread
-    extern __shared__ __align__(16) unsigned char smraw[];
-    __shared__ double red[kThreads / 32];
-    __shared__ uint8_t ntier[9];
-    CT *sm = reinterpret_cast<CT *>(smraw);
-
-    if ((int)blockIdx.x >= a.count[TIER]) return;
-    const int tile = a.list[blockIdx.x];
-    const int tx = tile % a.ntx, ty = tile / a.ntx;
-    load_neighbour_tiers(a, tx, ty, ntier);
-    __syncthreads();
-    stage_tile<CT, T, R>(a, sm, ntier, tx, ty, 0, a.nf);
-    __syncthreads();
-
+    using S = Stage<float, T, 1>;
+    constexpr int RPT = T * T / kThreads;  // rows per thread
     const int col = threadIdx.x % T;
     const int r0 = (threadIdx.x / T) * RPT;
     const int c = S::O + col;
     const int nf = a.nf;
     const Phys &ph = a.ph;
-
-    // sum of squares of every field at this thread's cells (FAST form)
-    CT ssum[RPT];
+    float ssum[RPT];
 #pragma unroll
-    for (int j = 0; j < RPT; ++j) ssum[j] = CT(0);
-    if (!REF) {
-        for (int f = 0; f < nf; ++f) {
+    for (int j = 0; j < RPT; ++j) ssum[j] = 0.f;
+    for (int f = 0; f < nf; ++f) {
 #pragma unroll
-            for (int j = 0; j < RPT; ++j) {
-                const CT v = S::at(sm, f, r0 + j + R, c);
-                ssum[j] = fma(v, v, ssum[j]);
-            }
+        for (int j = 0; j < RPT; ++j) {
+            const float v = S::at(const_cast<float *>(sm), f, r0 + j + 1, c);
+            ssum[j] = fmaf(v, v, ssum[j]);
         }
     }
-
-    const CT dtm = CT(ph.dt * ph.mobil);
-    const CT g2 = CT(2.0 * ph.gamma);
-    const CT kap = CT(ph.grcoef);
-    const CT inv = CT(ph.inv_dxdy);
+    const float dtm = (float)(ph.dt * ph.mobil), g2 = (float)(2.0 * ph.gamma), kap = (float)ph.grcoef;
+    const float inv = (float)ph.inv_dxdy;
     const int64_t gbase = (int64_t)(ty * T + r0) * a.nx + tx * T + col;
     double metric = 0.0;
     MonAcc mon;
-
     for (int f = 0; f < nf; ++f) {
         const bool mon_f = a.monitor_now && (a.mfield < 0 || a.mfield == f);
-        if (mon_f) mon_reset(a, mon);
-        CT w[RPT + 2][3];
+        const int mslot = a.mfield < 0 ? f : 0;
+        double snapv[RPT];
+        if (mon_f) {
+            mon_reset(a, mon);
+#pragma unroll
+            for (int j = 0; j < RPT; ++j) snapv[j] = snap_prefetch<T>(a, mslot, tile, r0 + j, col, gbase + (int64_t)j * a.nx);
+        }
+        float w[RPT + 2][3];
 #pragma unroll
         for (int j = 0; j < RPT + 2; ++j) {
-            w[j][0] = S::at(sm, f, r0 + j, c - 1);
-            w[j][1] = S::at(sm, f, r0 + j, c);
-            w[j][2] = S::at(sm, f, r0 + j, c + 1);
+            const float *row = &S::at(const_cast<float *>(sm), f, r0 + j, c);
+            w[j][0] = row[-1];
+            w[j][1] = row[0];
+            w[j][2] = row[1];
         }
 #pragma unroll
         for (int j = 0; j < RPT; ++j) {
-            const CT *rd = w[j], *rc = w[j + 1], *ru = w[j + 2];
-            const CT e = rc[1];
-            CT out;
+            const float *rd = w[j], *rc = w[j + 1], *ru = w[j + 2];
+            const float e = rc[1];
+            float s;
+            if (a.stencil == 0) s = (rd[0] + rd[1] + rd[2]) + (rc[0] + rc[2]) + (ru[0] + ru[1] + ru[2]) - 8.f * e;
+            else s = (rc[0] + rc[2]) + (rd[1] + ru[1]) - 4.f * e;
+            const float lap = s * inv;
+            const float e2 = e * e;
+            const float dfd = e * fmaf(g2, ssum[j] - e2, e2 - 1.f);
+            const float out = fmaf(-dtm, fmaf(-kap, lap, dfd), e);
+            const int64_t g = gbase + (int64_t)j * a.nx;
+            store_tier<TIER>(a, (int64_t)f * a.n + g, out);
+            if (mon_f)
+                mon_add<T>(a, mon, mslot, tile, r0 + j, col, g, (double)round_to_tier<TIER>(out), (double)e, snapv[j]);
+        }
+        if (mon_f) metric = mon_finish(a, mon, red, metric);
+    }
+    if (a.monitor_now && threadIdx.x == 0) a.metric[tile] = metric;
+}
+
+// One cell of the FP64 tile's neighbourhood at tile-local (ly, lx), read at
+// its owner tile's input tier.
+template <int T>
+__device__ __forceinline__ double ld_nb64(const StepArgs &a, const uint8_t *nt, int f, int x0, int y0, int ly, int lx)
+{
+    const int gy = bc_map(y0 + ly, a.ny, a.bc), gx = bc_map(x0 + lx, a.nx, a.bc);
+    const int cls = (ly < 0 ? 0 : (ly < T ? 3 : 6)) + (lx < 0 ? 0 : (lx < T ? 1 : 2));
+    return load_tier<double>(a, nt[cls], (int64_t)f * a.n + (int64_t)gy * a.nx + gx);
+}
+
+// FP64 tile: direct loads, FP64 arithmetic; REF keeps the reference's
+// expression order and rounding (graingrowth/function.h:20-23).
+template <int T, bool REF>
+__device__ __forceinline__ void gg_tile_fp64(const StepArgs &a, const uint8_t *nt, int tile, int tx, int ty, double *red)
+{
+    constexpr int RPT = T * T / kThreads;
+    const int col = threadIdx.x % T;
+    const int r0 = (threadIdx.x / T) * RPT;
+    const int x0 = tx * T, y0 = ty * T;
+    const int nf = a.nf;
+    const Phys &ph = a.ph;
+    double ssum[RPT];
+#pragma unroll
+    for (int j = 0; j < RPT; ++j) ssum[j] = 0.0;
+    if (!REF)
+        for (int f = 0; f < nf; ++f)
+#pragma unroll
+            for (int j = 0; j < RPT; ++j) {
+                const double v = ld_nb64<T>(a, nt, f, x0, y0, r0 + j, col);
+                ssum[j] = fma(v, v, ssum[j]);
+            }
+    const int64_t gbase = (int64_t)(y0 + r0) * a.nx + x0 + col;
+    double metric = 0.0;
+    MonAcc mon;
+    for (int f = 0; f < nf; ++f) {
+        const bool mon_f = a.monitor_now && (a.mfield < 0 || a.mfield == f);
+        const int mslot = a.mfield < 0 ? f : 0;
+        double snapv[RPT];
+        if (mon_f) {
+            mon_reset(a, mon);
+#pragma unroll
+            for (int j = 0; j < RPT; ++j) snapv[j] = snap_prefetch<T>(a, mslot, tile, r0 + j, col, gbase + (int64_t)j * a.nx);
+        }
+        double w[RPT + 2][3];
+#pragma unroll
+        for (int j = 0; j < RPT + 2; ++j)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) w[j][k] = ld_nb64<T>(a, nt, f, x0, y0, r0 + j - 1, col + k - 1);
+#pragma unroll
+        for (int j = 0; j < RPT; ++j) {
+            const double *rd = w[j], *rc = w[j + 1], *ru = w[j + 2];
+            const double e = rc[1];
+            double out;
             if (REF) {
-                // graingrowth/function.h:20-23, rounding every operation as written
                 double lap;
                 if (a.stencil == 0)
                     lap = __ddiv_rn(__dsub_rn(__dadd_rn(__dadd_rn(__dadd_rn(__dadd_rn(__dadd_rn(__dadd_rn(__dadd_rn(
@@ -96,84 +149,85 @@ __global__ void __launch_bounds__(kThreads) gg_step_kernel(StepArgs a)
                 bool first = true;
                 for (int b = 0; b < nf; ++b) {
                     if (b == f) continue;
-                    const double v = S::at(sm, b, r0 + j + R, c);
+                    const double v = ld_nb64<T>(a, nt, b, x0, y0, r0 + j, col);
                     const double s2 = __dmul_rn(v, v);
                     sum = first ? s2 : __dadd_rn(sum, s2);
                     first = false;
                 }
-                const double dfd = __dsub_rn(__dadd_rn(__dmul_rn(__dmul_rn(2.0 * ph.gamma, e), sum), pow((double)e, 3.0)), e);
-                out = (CT)__dsub_rn(e, __dmul_rn(ph.dt * ph.mobil, __dsub_rn(dfd, __dmul_rn(ph.grcoef, lap))));
+                const double dfd = __dsub_rn(__dadd_rn(__dmul_rn(__dmul_rn(2.0 * ph.gamma, e), sum), pow(e, 3.0)), e);
+                out = __dsub_rn(e, __dmul_rn(ph.dt * ph.mobil, __dsub_rn(dfd, __dmul_rn(ph.grcoef, lap))));
             } else {
-                CT s;
-                if (a.stencil == 0) s = (rd[0] + rd[1] + rd[2]) + (rc[0] + rc[2]) + (ru[0] + ru[1] + ru[2]) - CT(8) * e;
-                else s = (rc[0] + rc[2]) + (rd[1] + ru[1]) - CT(4) * e;
-                const CT lap = s * inv;
-                const CT e2 = e * e;
-                const CT dfd = e * fma(g2, ssum[j] - e2, e2 - CT(1));
-                out = fma(-dtm, fma(-kap, lap, dfd), e);
+                double s;
+                if (a.stencil == 0) s = (rd[0] + rd[1] + rd[2]) + (rc[0] + rc[2]) + (ru[0] + ru[1] + ru[2]) - 8.0 * e;
+                else s = (rc[0] + rc[2]) + (rd[1] + ru[1]) - 4.0 * e;
+                const double lap = s * ph.inv_dxdy;
+                const double e2 = e * e;
+                const double dfd = e * fma(2.0 * ph.gamma, ssum[j] - e2, e2 - 1.0);
+                out = fma(-(ph.dt * ph.mobil), fma(-ph.grcoef, lap, dfd), e);
             }
-            const int64_t gidx = (int64_t)f * a.n + gbase + (int64_t)j * a.nx;
-            store_tier<TIER>(a, gidx, out);
-            if (mon_f)
-                mon_add<T>(a, mon, a.mfield < 0 ? f : 0, tile, r0 + j, col, gbase + (int64_t)j * a.nx,
-                           (double)round_to_tier<TIER>(out));
+            const int64_t g = gbase + (int64_t)j * a.nx;
+            ((double *)a.out[TIER_FP64])[(int64_t)f * a.n + g] = out;
+            if (mon_f) mon_add<T>(a, mon, mslot, tile, r0 + j, col, g, out, e, snapv[j]);
         }
         if (mon_f) metric = mon_finish(a, mon, red, metric);
     }
     if (a.monitor_now && threadIdx.x == 0) a.metric[tile] = metric;
 }
 
-template <int T, int TIER, bool REF> static size_t gg_smem(int nf)
+template <int T, bool REF>
+__global__ void __launch_bounds__(kThreads) gg_step_kernel(StepArgs a)
 {
-    using CT = typename std::conditional<TIER == TIER_FP64, double, float>::type;
-    return (size_t)nf * Stage<CT, T, 1>::FIELD * sizeof(CT);
-}
-
-template <int T, int TIER, bool REF>
-static cudaError_t gg_launch_t(const StepArgs &a, int grid, cudaStream_t s)
-{
-    const size_t smem = gg_smem<T, TIER, REF>(a.nf);
-    gg_step_kernel<T, TIER, REF><<<grid, kThreads, smem, s>>>(a);
-    return cudaGetLastError();
+    using S = Stage<float, T, 1>;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ double red[kThreads / 32];
+    __shared__ uint8_t ntier[9];
+    float *sm = reinterpret_cast<float *>(smraw);
+    const int tile = blockIdx.x;
+    const int tier = a.tier_out[tile];
+    const int tx = tile % a.ntx, ty = tile / a.ntx;
+    load_neighbour_tiers(a, tx, ty, ntier);
+    __syncthreads();
+    if (tier == TIER_FP64) {
+        gg_tile_fp64<T, REF>(a, ntier, tile, tx, ty, red);
+        return;
+    }
+    stage_tile<float, T, 1>(a, sm, ntier, tx, ty, 0, a.nf);
+    __syncthreads();
+    if (tier == TIER_FP32) gg_tile_lo<T, TIER_FP32>(a, sm, tile, tx, ty, red);
+    else gg_tile_lo<T, TIER_HALF>(a, sm, tile, tx, ty, red);
+    (void)sizeof(S);
 }
 
 size_t gg_smem_bytes(int tile, int tier, int nf)
 {
-    const int T = tile;
-    if (T == 32) return tier == TIER_FP64 ? gg_smem<32, TIER_FP64, false>(nf) : gg_smem<32, TIER_FP32, false>(nf);
-    return tier == TIER_FP64 ? gg_smem<16, TIER_FP64, false>(nf) : gg_smem<16, TIER_FP32, false>(nf);
+    (void)tier;
+    if (tile == 32) return (size_t)nf * Stage<float, 32, 1>::FIELD * sizeof(float);
+    return (size_t)nf * Stage<float, 16, 1>::FIELD * sizeof(float);
 }
 
 cudaError_t gg_launch(int tile, int tier, bool ref, const StepArgs &a, int grid, cudaStream_t s)
 {
-#define AMPS_GG(TT)                                                                 \
-    switch (tier) {                                                                 \
-    case TIER_HALF: return gg_launch_t<TT, TIER_HALF, false>(a, grid, s);           \
-    case TIER_FP32: return gg_launch_t<TT, TIER_FP32, false>(a, grid, s);           \
-    default:                                                                        \
-        return ref ? gg_launch_t<TT, TIER_FP64, true>(a, grid, s)                   \
-                   : gg_launch_t<TT, TIER_FP64, false>(a, grid, s);                 \
+    (void)tier;
+    const size_t smem = gg_smem_bytes(tile, 0, a.nf);
+    if (tile == 32) {
+        if (ref) gg_step_kernel<32, true><<<grid, kThreads, smem, s>>>(a);
+        else gg_step_kernel<32, false><<<grid, kThreads, smem, s>>>(a);
+    } else {
+        if (ref) gg_step_kernel<16, true><<<grid, kThreads, smem, s>>>(a);
+        else gg_step_kernel<16, false><<<grid, kThreads, smem, s>>>(a);
     }
-    if (tile == 32) { AMPS_GG(32) }
-    AMPS_GG(16)
-#undef AMPS_GG
+    return cudaGetLastError();
 }
 
 cudaError_t gg_prepare(int tile, int tier, bool ref)
 {
+    (void)tier;
     const int lim = kMaxDynSmem;
     const auto attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
-#define AMPS_GGP(TT)                                                                              \
-    switch (tier) {                                                                               \
-    case TIER_HALF: return cudaFuncSetAttribute(gg_step_kernel<TT, TIER_HALF, false>, attr, lim);  \
-    case TIER_FP32: return cudaFuncSetAttribute(gg_step_kernel<TT, TIER_FP32, false>, attr, lim);  \
-    default:                                                                                      \
-        return ref ? cudaFuncSetAttribute(gg_step_kernel<TT, TIER_FP64, true>, attr, lim)         \
-                   : cudaFuncSetAttribute(gg_step_kernel<TT, TIER_FP64, false>, attr, lim);       \
-    }
-    if (tile == 32) { AMPS_GGP(32) }
-    AMPS_GGP(16)
-#undef AMPS_GGP
+    if (tile == 32) return ref ? cudaFuncSetAttribute(gg_step_kernel<32, true>, attr, lim)
+                               : cudaFuncSetAttribute(gg_step_kernel<32, false>, attr, lim);
+    return ref ? cudaFuncSetAttribute(gg_step_kernel<16, true>, attr, lim)
+               : cudaFuncSetAttribute(gg_step_kernel<16, false>, attr, lim);
 }
 
 }  // namespace amps

@@ -152,7 +152,9 @@ __global__ void __launch_bounds__(kThreads) kob_step_kernel(StepArgs a)
         }
         store_tier<TIER>(a, g, pn);
         store_tier<TIER>(a, a.n + g, tn);
-        if (mon_on && (a.mfield <= 0)) mon_add<T>(a, mon, mslot, tile, j, i, g, (double)round_to_tier<TIER>(pn));
+        if (mon_on && (a.mfield <= 0))
+            mon_add<T>(a, mon, mslot, tile, j, i, g, (double)round_to_tier<TIER>(pn), (double)p0,
+                       snap_prefetch<T>(a, mslot, tile, j, i, g));
     }
     if (mon_on) {
         metric = mon_finish(a, mon, red, metric);
@@ -168,7 +170,9 @@ __global__ void __launch_bounds__(kThreads) kob_step_kernel(StepArgs a)
                 if (TIER == TIER_FP64) v = ((const double *)a.out[2])[a.n + g];
                 else if (TIER == TIER_FP32) v = ((const float *)a.out[1])[a.n + g];
                 else v = __half2float(((const __half *)a.out[0])[a.n + g]);
-                mon_add<T>(a, m2, a.mfield < 0 ? 1 : 0, tile, j, i, g, v);
+                const int slot = a.mfield < 0 ? 1 : 0;
+                mon_add<T>(a, m2, slot, tile, j, i, g, v, (double)S::at(sm, 1, j + R, i + S::O),
+                           snap_prefetch<T>(a, slot, tile, j, i, g));
             }
             metric = mon_finish(a, m2, red, metric);
         }

@@ -139,7 +139,9 @@ __global__ void __launch_bounds__(kThreads) sint_step_kernel(StepArgs a)
             cn = v >= CT(1) ? CT(1) : (v < CT(0) ? CT(0) : v);
         }
         store_tier<TIER>(a, g, cn);
-        if (mon_on && a.mfield <= 0) mon_add<T>(a, mon, 0, tile, j, i, g, (double)round_to_tier<TIER>(cn));
+        if (mon_on && a.mfield <= 0)
+            mon_add<T>(a, mon, 0, tile, j, i, g, (double)round_to_tier<TIER>(cn), (double)cc,
+                       snap_prefetch<T>(a, 0, tile, j, i, g));
         for (int k = 0; k < np; ++k) {
             const CT *Ep = &SE::at(sme, k, j + 1, i + SE::O);
             const CT e = Ep[0];
