@@ -99,6 +99,19 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+TUNED = os.path.join(ROOT, "w3914777_gb300", "tuned", "graingrowth_1024_q8.json")
+
+
+def load_tuned():
+    """Monitor, thresholds and tile chosen by w3914777_gb300.autotune for this
+    workload (file written by `python -m w3914777_gb300.autotune graingrowth`)."""
+    try:
+        with open(TUNED) as f:
+            return json.load(f)["best"]
+    except Exception:
+        return None
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -168,6 +181,9 @@ def run_ours(args):
     dev = torch.device("cuda", local)
     S = args.sim_steps
     p = w.Params.preset("graingrowth", 0)
+    tuned = load_tuned()
+    if tuned:
+        p = p.replace(**tuned["overrides"])
     if args.tile:
         p.tile = args.tile
     nf = p.num_fields
@@ -314,8 +330,13 @@ def run_ours(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f16+f32+f64 (per-tile adaptive)",
             "data": "synthetic (seeded uniform eta in [-1e-3,1e-3])",
             "config": {"workload": WORKLOAD, "nx": p.nx, "ny": p.ny, "Q": nf, "steps_per_run": S, "tile": T,
-                       "monitor": "spatial range, every cell, all fields, every 10 steps",
-                       "thresholds": [p.thr_lo, p.thr_hi], "l2": "flushed between runs (256 MiB write)",
+                       "monitor": {1: "spatial range", 2: "temporal change (snapshot)",
+                                   3: "per-step change x cadence"}[p.monitor]
+                                  + (", every cell" if p.monitor_samples else ", 4x4 lattice")
+                                  + (", all fields" if p.monitor_field < 0 else f", field {p.monitor_field}")
+                                  + f", every {p.cadence} steps",
+                       "thresholds": [p.thr_lo, p.thr_hi], "tuned_by": "autotune" if tuned else "preset",
+                       "l2": "flushed between runs (256 MiB write)",
                        "parallelism": f"replicas x{world}"},
             "e2e": {"value": e2e, "unit": "Gcell-updates/s", "h2d_bytes_per_step": bytes_io,
                     "d2h_bytes_per_step": bytes_io, "ms_per_step": e2e_total / len(e2e_ms)},

@@ -315,8 +315,24 @@ void orc_monitor_tem(const double *f, const double *last, int nx, int ny, int ti
 void orc_monitor_rate(const double *f, const double *prev, int nx, int ny, int tile, int samples, int cadence,
                       double *metric)
 {
-    orc_monitor_tem(f, prev, nx, ny, tile, samples, metric);
-    for (int t = 0; t < (nx / tile) * (ny / tile); ++t) metric[t] = metric[t] * cadence;
+    /* defined in FP32 arithmetic: max |float(f) - float(prev)|, times the cadence in double */
+    const int ntx = nx / tile, nty = ny / tile;
+    int pts[4];
+    orc_sample_points(tile, 2, pts);
+    for (int ty = 0; ty < nty; ++ty)
+        for (int tx = 0; tx < ntx; ++tx) {
+            float mx = 0.f;
+            const int cnt = samples ? tile : 4;
+            for (int j = 0; j < cnt; ++j)
+                for (int k = 0; k < cnt; ++k) {
+                    const int y = ty * tile + (samples ? j : pts[j]);
+                    const int x = tx * tile + (samples ? k : pts[k]);
+                    const int64_t i = (int64_t)y * nx + x;
+                    const float d = fabsf((float)f[i] - (float)prev[i]);
+                    if (d > mx) mx = d;
+                }
+            metric[ty * ntx + tx] = (double)mx * cadence;
+        }
 }
 
 void orc_classify(const double *metric, int ntx, int nty, double thr_lo, double thr_hi, uint8_t *tier)

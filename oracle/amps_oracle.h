@@ -82,7 +82,8 @@ void orc_monitor_spa(const double *f, int nx, int ny, int tile, int samples, dou
 void orc_monitor_tem(const double *f, const double *last, int nx, int ny, int tile, int samples,
                      double *metric);
 /* Per-step change times the cadence (no reference counterpart: the
- * snapshot-free estimate of Monitor2); lattice of the temporal monitor. */
+ * snapshot-free estimate of Monitor2), in FP32 arithmetic; lattice of the
+ * temporal monitor. */
 void orc_monitor_rate(const double *f, const double *prev, int nx, int ny, int tile, int samples, int cadence,
                       double *metric);
 /* get_type: snowflake/tools.h:212-230 -- max over the tile and its 4 tile

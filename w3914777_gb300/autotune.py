@@ -96,3 +96,29 @@ def tune(params, init_kind, steps, err_bound=1e-3, candidates=None, reference=No
     ok = [r for r in table[1:] if "err" in r and r["err"] <= err_bound and r["overrides"].get("mode") == A.END2END_MIX]
     best = min(ok, key=lambda r: r["seconds"]) if ok else None
     return best, table
+
+
+def _main():
+    """python -m w3914777_gb300.autotune graingrowth [steps] [err_bound]
+    Tunes the 1024^2 Q=8 grain-growth workload and writes
+    w3914777_gb300/tuned/graingrowth_1024_q8.json."""
+    import json
+    import os
+    import sys
+    model = sys.argv[1] if len(sys.argv) > 1 else "graingrowth"
+    steps = int(sys.argv[2]) if len(sys.argv) > 2 else 10000
+    bound = float(sys.argv[3]) if len(sys.argv) > 3 else 1e-3
+    if model != "graingrowth":
+        raise SystemExit("only the grain-growth workload has a tuning entry point")
+    p = A.Params.preset("graingrowth", 0)
+    best, table = tune(p, A.INIT_SEEDED, steps, bound, log=lambda r: print(json.dumps(r), flush=True))
+    out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuned", "graingrowth_1024_q8.json")
+    os.makedirs(os.path.dirname(out), exist_ok=True)
+    with open(out, "w") as f:
+        json.dump({"workload": "graingrowth preset 0 (1024x1024, Q=8)", "steps": steps, "err_bound": bound,
+                   "best": best, "table": table}, f, indent=1)
+    print("best:", json.dumps(best))
+
+
+if __name__ == "__main__":
+    _main()

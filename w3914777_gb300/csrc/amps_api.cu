@@ -40,11 +40,7 @@ struct amps_handle {
     double *d_stage = nullptr, *d_partials = nullptr, *d_out = nullptr;
     double *h_pinned = nullptr;  // nf*n doubles, page-locked
     cudaStream_t own = nullptr, stream = nullptr;
-    // the tier kernels of one step run as parallel branches: fork from
-    // `stream` onto aux[], join back before the next step
-    cudaStream_t aux[2] = {nullptr, nullptr};
-    cudaEvent_t ev_fork = nullptr, ev_join[2] = {nullptr, nullptr};
-    int ntiers_used = 0;
+
     int64_t step = 0;
     bool graphs = true;
     std::map<int, cudaGraphExec_t> graph;  // key: parity | transition<<1
@@ -110,9 +106,9 @@ static Phys make_phys(const amps_params &p)
     return ph;
 }
 
-static size_t kernel_smem(const amps_params &p, int tier, int nf)
+static size_t kernel_smem(const amps_params &p, int tier, int nf, bool only64)
 {
-    if (p.model == AMPS_GRAINGROWTH) return gg_smem_bytes(p.tile, tier, nf);
+    if (p.model == AMPS_GRAINGROWTH) return gg_smem_bytes(p.tile, only64 ? TIER_FP64 : -1, nf);
     if (p.model == AMPS_KOBAYASHI) return kob_smem_bytes(p.tile, tier);
     return sint_smem_bytes(p.tile, tier, nf, p.mu_lap_fp64 || tier == TIER_FP64);
 }
@@ -131,11 +127,6 @@ static void free_all(amps_handle *h)
     for (void *q : ps)
         if (q) cudaFree(q);
     if (h->h_pinned) cudaFreeHost(h->h_pinned);
-    for (int k = 0; k < 2; ++k) {
-        if (h->aux[k]) cudaStreamDestroy(h->aux[k]);
-        if (h->ev_join[k]) cudaEventDestroy(h->ev_join[k]);
-    }
-    if (h->ev_fork) cudaEventDestroy(h->ev_fork);
     if (h->own) cudaStreamDestroy(h->own);
 }
 
@@ -168,7 +159,8 @@ extern "C" int amps_create(const amps_params *p, amps_handle **out)
         if (h->use_mid) h->used[TIER_FP32] = true;
     }
     for (int t = 0; t < 3; ++t)
-        if (h->used[t] && kernel_smem(*p, t, h->nf) > (size_t)kMaxDynSmem) {
+        if (h->used[t] && kernel_smem(*p, t, h->nf, h->used[TIER_FP64] && !h->used[TIER_FP32] && !h->used[TIER_HALF])
+                              > (size_t)kMaxDynSmem) {
             g_create_err = "tile staging exceeds 226 KB of shared memory: use tile=16 or fewer fields";
             delete h;
             return AMPS_ERR_UNSUPPORTED;
@@ -205,13 +197,7 @@ extern "C" int amps_create(const amps_params *p, amps_handle **out)
 #undef ALLOC
     if (cudaStreamCreateWithFlags(&h->own, cudaStreamNonBlocking) != cudaSuccess)
         return fail(AMPS_ERR_CUDA, "stream");
-    for (int k = 0; k < 2; ++k)
-        if (cudaStreamCreateWithFlags(&h->aux[k], cudaStreamNonBlocking) != cudaSuccess ||
-            cudaEventCreateWithFlags(&h->ev_join[k], cudaEventDisableTiming) != cudaSuccess)
-            return fail(AMPS_ERR_CUDA, "aux stream");
-    if (cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming) != cudaSuccess)
-        return fail(AMPS_ERR_CUDA, "event");
-    for (int t = 0; t < 3; ++t) h->ntiers_used += h->used[t] ? 1 : 0;
+
     h->stream = h->own;
     cudaMemsetAsync(h->d_stats, 0, sizeof(unsigned long long) * 8, h->stream);
     cudaMemsetAsync(h->d_flags, 0, sizeof(int) * 4, h->stream);
@@ -226,7 +212,10 @@ extern "C" int amps_create(const amps_params *p, amps_handle **out)
     for (int t = 0; t < 3; ++t) {
         if (!h->used[t]) continue;
         cudaError_t pe;
-        if (p->model == AMPS_GRAINGROWTH) pe = gg_prepare(h->T, t, p->ref_order != 0);
+        if (p->model == AMPS_GRAINGROWTH) {
+            const bool only64 = h->used[TIER_FP64] && !h->used[TIER_FP32] && !h->used[TIER_HALF];
+            pe = gg_prepare(h->T, only64 ? TIER_FP64 : -1, p->ref_order != 0);
+        }
         else if (p->model == AMPS_KOBAYASHI) pe = kob_prepare(h->T, t, p->ref_order != 0);
         else pe = sint_prepare(h->T, t, p->ref_order != 0, p->mu_lap_fp64 != 0);
         if (pe != cudaSuccess) {
@@ -487,7 +476,9 @@ static int launch_step(amps_handle *h, int step_off, bool monitor_now)
                 FAIL(h, AMPS_ERR_CUDA, "event create");
             cudaEventRecord(ev.a, h->stream);
         }
-        cudaError_t e = gg_launch(h->T, 0, ref, a, h->ntiles, h->stream);
+        // all-FP64 runs use the staged FP64 kernel, every other mode the fused one
+        const bool only64 = h->used[TIER_FP64] && !h->used[TIER_FP32] && !h->used[TIER_HALF];
+        cudaError_t e = gg_launch(h->T, only64 ? TIER_FP64 : -1, ref, a, h->ntiles, h->stream);
         if (e != cudaSuccess) FAIL(h, AMPS_ERR_CUDA, "step kernel launch: %s", cudaGetErrorString(e));
         if (h->profiling) {
             cudaEventRecord(ev.b, h->stream);
@@ -497,12 +488,9 @@ static int launch_step(amps_handle *h, int step_off, bool monitor_now)
         h->transition = false;
         return AMPS_OK;
     }
-    const bool fork = h->ntiers_used > 1;
-    int branch = 0;
     for (int t = 2; t >= 0; --t) {
         if (!h->used[t]) continue;
-        // the first (highest) tier stays on the main stream, the others fork
-        cudaStream_t st = branch == 0 ? h->stream : h->aux[branch - 1];
+        cudaStream_t st = h->stream;
         a.list = h->d_lists + t * h->ntiles;
         cudaError_t e;
         amps_handle::Ev ev{t, nullptr, nullptr};
@@ -511,20 +499,12 @@ static int launch_step(amps_handle *h, int step_off, bool monitor_now)
                 FAIL(h, AMPS_ERR_CUDA, "event create");
             cudaEventRecord(ev.a, st);
         }
-        if (p.model == AMPS_GRAINGROWTH) e = gg_launch(h->T, t, ref, a, h->ntiles, st);
-        else if (p.model == AMPS_KOBAYASHI) e = kob_launch(h->T, t, ref, a, h->ntiles, st);
+        if (p.model == AMPS_KOBAYASHI) e = kob_launch(h->T, t, ref, a, h->ntiles, st);
         else e = sint_launch(h->T, t, ref, p.mu_lap_fp64 != 0, a, h->ntiles, st);
         if (e != cudaSuccess) FAIL(h, AMPS_ERR_CUDA, "step kernel launch: %s", cudaGetErrorString(e));
         if (h->profiling) {
             cudaEventRecord(ev.b, st);
             h->evs.push_back(ev);
-        }
-        ++branch;
-    }
-    if (fork) {
-        for (int k = 0; k < h->ntiers_used - 1; ++k) {
-            CK(h, cudaEventRecord(h->ev_join[k], h->aux[k]));
-            CK(h, cudaStreamWaitEvent(h->stream, h->ev_join[k], 0));
         }
     }
     h->parity ^= 1;

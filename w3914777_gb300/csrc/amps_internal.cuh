@@ -180,9 +180,16 @@ __device__ __forceinline__ void stage_tile(const StepArgs &a, CT *sm, const uint
                 const int s = u % SEG;
                 const int r = (u / SEG) % S::ROWS;
                 const int f = u / (SEG * S::ROWS);
-                CT *dst = &S::at(sm, f, r, S::O + 8 * s);
+                CT *dst = &S::at(sm, f, r, S::O + 8 * s);  // 16-byte aligned: O, P and FIELD are
+                if (sizeof(CT) == 4) {                        // multiples of 16 bytes
+                    float4 *d4 = reinterpret_cast<float4 *>(dst);
+                    d4[0] = make_float4((float)v[q][0], (float)v[q][1], (float)v[q][2], (float)v[q][3]);
+                    d4[1] = make_float4((float)v[q][4], (float)v[q][5], (float)v[q][6], (float)v[q][7]);
+                } else {
+                    double2 *d2 = reinterpret_cast<double2 *>(dst);
 #pragma unroll
-                for (int k = 0; k < 8; ++k) dst[k] = v[q][k];
+                    for (int k = 0; k < 4; ++k) d2[k] = make_double2((double)v[q][2 * k], (double)v[q][2 * k + 1]);
+                }
             }
         }
     }
@@ -315,8 +322,80 @@ __device__ __forceinline__ void mon_add(const StepArgs &a, MonAcc &m, int mslot,
         m.dmax = fmax(m.dmax, fabs(snapv - v));
         *snap_ptr<T>(a, mslot, tile, gidx, si) = v;
     } else {
-        m.dmax = fmax(m.dmax, fabs(v - old) * a.cadence);
+        m.dmax = fmax(m.dmax, (double)fabsf((float)v - (float)old) * a.cadence);
     }
+}
+
+// Float accumulator for half/FP32 tiles: the values are floats, so min/max
+// are exact in float and the range is taken in double once per tile; the
+// rate monitor is defined in FP32 arithmetic; the temporal (snapshot)
+// difference stays in double.  Keeps per-cell work off the FP64 pipe.
+struct MonAccF {
+    float mn, mx, dmaxf;
+    double dmax;
+    int bad;
+};
+
+__device__ __forceinline__ void mon_reset(const StepArgs &a, MonAccF &m)
+{
+    m.mn = a.samples ? INFINITY : 1.0f;
+    m.mx = a.samples ? -INFINITY : 0.0f;
+    m.dmaxf = 0.f;
+    m.dmax = 0.0;
+    m.bad = 0;
+}
+
+template <int T>
+__device__ __forceinline__ void mon_add(const StepArgs &a, MonAccF &m, int mslot, int tile, int row, int col,
+                                        int64_t gidx, float v, float old, double snapv)
+{
+    if (!(v == v) || isinf(v)) m.bad = 1;
+    const int si = sample_index<T>(a.monitor_kind == 1 ? 1 : 2, a.samples, row, col);
+    if (si < 0) return;
+    if (a.monitor_kind == 1) {
+        m.mn = fminf(m.mn, v);
+        m.mx = fmaxf(m.mx, v);
+    } else if (a.monitor_kind == 2) {
+        m.dmax = fmax(m.dmax, fabs(snapv - (double)v));
+        *snap_ptr<T>(a, mslot, tile, gidx, si) = (double)v;
+    } else {
+        m.dmaxf = fmaxf(m.dmaxf, fabsf(v - old));
+    }
+}
+
+__device__ __forceinline__ float warp_maxf(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+__device__ __forceinline__ float block_maxf(float v, float *red)
+{
+    v = warp_maxf(v);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    float r = red[0];
+#pragma unroll
+    for (int w = 1; w < kThreads / 32; ++w) r = fmaxf(r, red[w]);
+    return r;
+}
+
+__device__ __forceinline__ double mon_finish(const StepArgs &a, MonAccF &m, double *red, double metric)
+{
+    float *redf = reinterpret_cast<float *>(red);
+    double v;
+    if (a.monitor_kind == 1) {
+        const float mx = block_maxf(m.mx, redf);
+        const float mn = -block_maxf(-m.mn, redf);
+        v = (double)mx - (double)mn;
+    } else if (a.monitor_kind == 2) {
+        v = block_max(m.dmax, red);
+    } else {
+        v = (double)block_maxf(m.dmaxf, redf) * a.cadence;
+    }
+    if (__syncthreads_or(m.bad) && threadIdx.x == 0) atomicOr(a.flags, 1);
+    return fmax(metric, v);
 }
 
 __device__ __forceinline__ void mon_reset(const StepArgs &a, MonAcc &m)

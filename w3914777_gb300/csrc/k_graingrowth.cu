@@ -19,66 +19,97 @@
 
 namespace amps {
 
-// Half / FP32 tile: staged float neighbourhood, float arithmetic.
+// Half / FP32 tile: staged float neighbourhood, float arithmetic.  Each
+// thread advances CPT consecutive cells of one row (CPT = 4 for 32x32 tiles:
+// one 128-bit shared load plus two halo scalars per row, shared row sums,
+// 128-bit / 64-bit global stores).
+template <int TIER, int CPT>
+__device__ __forceinline__ void store_cells(const StepArgs &a, int64_t idx, const float *v)
+{
+    if (CPT == 4 && TIER == TIER_FP32) {
+        *reinterpret_cast<float4 *>((float *)a.out[TIER_FP32] + idx) = make_float4(v[0], v[1], v[2], v[3]);
+    } else if (CPT == 4 && TIER == TIER_HALF) {
+        __half2 h0 = __floats2half2_rn(v[0], v[1]), h1 = __floats2half2_rn(v[2], v[3]);
+        uint2 u;
+        u.x = *reinterpret_cast<unsigned *>(&h0);
+        u.y = *reinterpret_cast<unsigned *>(&h1);
+        *reinterpret_cast<uint2 *>((__half *)a.out[TIER_HALF] + idx) = u;
+    } else {
+#pragma unroll
+        for (int k = 0; k < CPT; ++k) store_tier<TIER>(a, idx + k, v[k]);
+    }
+}
+
 template <int T, int TIER>
 __device__ __forceinline__ void gg_tile_lo(const StepArgs &a, const float *sm, int tile, int tx, int ty, double *red)
 {
     using S = Stage<float, T, 1>;
-    constexpr int RPT = T * T / kThreads;  // rows per thread
-    const int col = threadIdx.x % T;
-    const int r0 = (threadIdx.x / T) * RPT;
-    const int c = S::O + col;
+    constexpr int CPT = T * T / kThreads;  // cells per thread, along x
+    constexpr int GPR = T / CPT;           // thread groups per row
+    const int row = threadIdx.x / GPR;
+    const int c0 = (threadIdx.x % GPR) * CPT;
     const int nf = a.nf;
     const Phys &ph = a.ph;
-    float ssum[RPT];
+    float *smm = const_cast<float *>(sm);
+    float ssum[CPT];
 #pragma unroll
-    for (int j = 0; j < RPT; ++j) ssum[j] = 0.f;
+    for (int k = 0; k < CPT; ++k) ssum[k] = 0.f;
     for (int f = 0; f < nf; ++f) {
+        const float *ctr = &S::at(smm, f, row + 1, S::O + c0);
 #pragma unroll
-        for (int j = 0; j < RPT; ++j) {
-            const float v = S::at(const_cast<float *>(sm), f, r0 + j + 1, c);
-            ssum[j] = fmaf(v, v, ssum[j]);
-        }
+        for (int k = 0; k < CPT; ++k) ssum[k] = fmaf(ctr[k], ctr[k], ssum[k]);
     }
     const float dtm = (float)(ph.dt * ph.mobil), g2 = (float)(2.0 * ph.gamma), kap = (float)ph.grcoef;
     const float inv = (float)ph.inv_dxdy;
-    const int64_t gbase = (int64_t)(ty * T + r0) * a.nx + tx * T + col;
+    const int64_t gbase = (int64_t)(ty * T + row) * a.nx + tx * T + c0;
     double metric = 0.0;
-    MonAcc mon;
+    MonAccF mon;
     for (int f = 0; f < nf; ++f) {
         const bool mon_f = a.monitor_now && (a.mfield < 0 || a.mfield == f);
         const int mslot = a.mfield < 0 ? f : 0;
-        double snapv[RPT];
+        double snapv[CPT];
         if (mon_f) {
             mon_reset(a, mon);
 #pragma unroll
-            for (int j = 0; j < RPT; ++j) snapv[j] = snap_prefetch<T>(a, mslot, tile, r0 + j, col, gbase + (int64_t)j * a.nx);
+            for (int k = 0; k < CPT; ++k) snapv[k] = snap_prefetch<T>(a, mslot, tile, row, c0 + k, gbase + k);
         }
-        float w[RPT + 2][3];
+        float w[3][CPT + 2];
 #pragma unroll
-        for (int j = 0; j < RPT + 2; ++j) {
-            const float *row = &S::at(const_cast<float *>(sm), f, r0 + j, c);
-            w[j][0] = row[-1];
-            w[j][1] = row[0];
-            w[j][2] = row[1];
+        for (int rr = 0; rr < 3; ++rr) {
+            const float *p = &S::at(smm, f, row + rr, S::O + c0);
+            if (CPT == 4) {
+                const float4 q = *reinterpret_cast<const float4 *>(p);
+                w[rr][1] = q.x; w[rr][2] = q.y; w[rr][3] = q.z; w[rr][4] = q.w;
+            } else {
+#pragma unroll
+                for (int k = 0; k < CPT; ++k) w[rr][k + 1] = p[k];
+            }
+            w[rr][0] = p[-1];
+            w[rr][CPT + 1] = p[CPT];
         }
+        float out[CPT];
 #pragma unroll
-        for (int j = 0; j < RPT; ++j) {
-            const float *rd = w[j], *rc = w[j + 1], *ru = w[j + 2];
-            const float e = rc[1];
+        for (int k = 0; k < CPT; ++k) {
+            const float e = w[1][k + 1];
             float s;
-            if (a.stencil == 0) s = (rd[0] + rd[1] + rd[2]) + (rc[0] + rc[2]) + (ru[0] + ru[1] + ru[2]) - 8.f * e;
-            else s = (rc[0] + rc[2]) + (rd[1] + ru[1]) - 4.f * e;
+            if (a.stencil == 0)
+                s = (w[0][k] + w[0][k + 1] + w[0][k + 2]) + (w[1][k] + w[1][k + 2]) + (w[2][k] + w[2][k + 1] + w[2][k + 2])
+                  - 8.f * e;
+            else
+                s = (w[1][k] + w[1][k + 2]) + (w[0][k + 1] + w[2][k + 1]) - 4.f * e;
             const float lap = s * inv;
             const float e2 = e * e;
-            const float dfd = e * fmaf(g2, ssum[j] - e2, e2 - 1.f);
-            const float out = fmaf(-dtm, fmaf(-kap, lap, dfd), e);
-            const int64_t g = gbase + (int64_t)j * a.nx;
-            store_tier<TIER>(a, (int64_t)f * a.n + g, out);
-            if (mon_f)
-                mon_add<T>(a, mon, mslot, tile, r0 + j, col, g, (double)round_to_tier<TIER>(out), (double)e, snapv[j]);
+            const float dfd = e * fmaf(g2, ssum[k] - e2, e2 - 1.f);
+            out[k] = fmaf(-dtm, fmaf(-kap, lap, dfd), e);
         }
-        if (mon_f) metric = mon_finish(a, mon, red, metric);
+        store_cells<TIER, CPT>(a, (int64_t)f * a.n + gbase, out);
+        if (mon_f) {
+#pragma unroll
+            for (int k = 0; k < CPT; ++k)
+                mon_add<T>(a, mon, mslot, tile, row, c0 + k, gbase + k, round_to_tier<TIER>(out[k]), w[1][k + 1],
+                           snapv[k]);
+            metric = mon_finish(a, mon, red, metric);
+        }
     }
     if (a.monitor_now && threadIdx.x == 0) a.metric[tile] = metric;
 }
@@ -93,8 +124,9 @@ __device__ __forceinline__ double ld_nb64(const StepArgs &a, const uint8_t *nt, 
     return load_tier<double>(a, nt[cls], (int64_t)f * a.n + (int64_t)gy * a.nx + gx);
 }
 
-// FP64 tile: direct loads, FP64 arithmetic; REF keeps the reference's
-// expression order and rounding (graingrowth/function.h:20-23).
+// FP64 tile: direct loads through L1 with a rolling 3-row window, FP64
+// arithmetic; REF keeps the reference's expression order and rounding
+// (graingrowth/function.h:20-23).
 template <int T, bool REF>
 __device__ __forceinline__ void gg_tile_fp64(const StepArgs &a, const uint8_t *nt, int tile, int tx, int ty, double *red)
 {
@@ -120,20 +152,19 @@ __device__ __forceinline__ void gg_tile_fp64(const StepArgs &a, const uint8_t *n
     for (int f = 0; f < nf; ++f) {
         const bool mon_f = a.monitor_now && (a.mfield < 0 || a.mfield == f);
         const int mslot = a.mfield < 0 ? f : 0;
-        double snapv[RPT];
-        if (mon_f) {
-            mon_reset(a, mon);
+        if (mon_f) mon_reset(a, mon);
+        double rd[3], rc[3], ru[3];
 #pragma unroll
-            for (int j = 0; j < RPT; ++j) snapv[j] = snap_prefetch<T>(a, mslot, tile, r0 + j, col, gbase + (int64_t)j * a.nx);
+        for (int k = 0; k < 3; ++k) {
+            rd[k] = ld_nb64<T>(a, nt, f, x0, y0, r0 - 1, col + k - 1);
+            rc[k] = ld_nb64<T>(a, nt, f, x0, y0, r0, col + k - 1);
         }
-        double w[RPT + 2][3];
-#pragma unroll
-        for (int j = 0; j < RPT + 2; ++j)
-#pragma unroll
-            for (int k = 0; k < 3; ++k) w[j][k] = ld_nb64<T>(a, nt, f, x0, y0, r0 + j - 1, col + k - 1);
-#pragma unroll
+#pragma unroll 1
         for (int j = 0; j < RPT; ++j) {
-            const double *rd = w[j], *rc = w[j + 1], *ru = w[j + 2];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) ru[k] = ld_nb64<T>(a, nt, f, x0, y0, r0 + j + 1, col + k - 1);
+            const int64_t g = gbase + (int64_t)j * a.nx;
+            const double snapv = mon_f ? snap_prefetch<T>(a, mslot, tile, r0 + j, col, g) : 0.0;
             const double e = rc[1];
             double out;
             if (REF) {
@@ -162,20 +193,29 @@ __device__ __forceinline__ void gg_tile_fp64(const StepArgs &a, const uint8_t *n
                 else s = (rc[0] + rc[2]) + (rd[1] + ru[1]) - 4.0 * e;
                 const double lap = s * ph.inv_dxdy;
                 const double e2 = e * e;
-                const double dfd = e * fma(2.0 * ph.gamma, ssum[j] - e2, e2 - 1.0);
+                double sj = ssum[0];
+#pragma unroll
+                for (int q = 1; q < RPT; ++q) sj = j == q ? ssum[q] : sj;
+                const double dfd = e * fma(2.0 * ph.gamma, sj - e2, e2 - 1.0);
                 out = fma(-(ph.dt * ph.mobil), fma(-ph.grcoef, lap, dfd), e);
             }
-            const int64_t g = gbase + (int64_t)j * a.nx;
             ((double *)a.out[TIER_FP64])[(int64_t)f * a.n + g] = out;
-            if (mon_f) mon_add<T>(a, mon, mslot, tile, r0 + j, col, g, out, e, snapv[j]);
+            if (mon_f) mon_add<T>(a, mon, mslot, tile, r0 + j, col, g, out, e, snapv);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                rd[k] = rc[k];
+                rc[k] = ru[k];
+            }
         }
         if (mon_f) metric = mon_finish(a, mon, red, metric);
     }
     if (a.monitor_now && threadIdx.x == 0) a.metric[tile] = metric;
 }
 
+// Fused all-tier step: at most 64 registers, so that four CTAs share an SM
+// and the half/FP32 tiles (the common case) keep their occupancy.
 template <int T, bool REF>
-__global__ void __launch_bounds__(kThreads) gg_step_kernel(StepArgs a)
+__global__ void __launch_bounds__(kThreads, 4) gg_step_kernel(StepArgs a)
 {
     using S = Stage<float, T, 1>;
     extern __shared__ __align__(16) unsigned char smraw[];
@@ -198,32 +238,124 @@ __global__ void __launch_bounds__(kThreads) gg_step_kernel(StepArgs a)
     (void)sizeof(S);
 }
 
+// All-FP64 step (plain FP64 mode): the FP64 neighbourhood is staged in
+// shared memory, which suits the FP64-pipe-bound arithmetic better than the
+// fused kernel's direct loads.
+template <int T, bool REF>
+__global__ void __launch_bounds__(kThreads) gg_step_f64_kernel(StepArgs a)
+{
+    using S = Stage<double, T, 1>;
+    constexpr int RPT = T * T / kThreads;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ double red[kThreads / 32];
+    __shared__ uint8_t ntier[9];
+    double *sm = reinterpret_cast<double *>(smraw);
+    const int tile = blockIdx.x;
+    const int tx = tile % a.ntx, ty = tile / a.ntx;
+    load_neighbour_tiers(a, tx, ty, ntier);
+    __syncthreads();
+    stage_tile<double, T, 1>(a, sm, ntier, tx, ty, 0, a.nf);
+    __syncthreads();
+    const int col = threadIdx.x % T;
+    const int r0 = (threadIdx.x / T) * RPT;
+    const int c = S::O + col;
+    const int nf = a.nf;
+    const Phys &ph = a.ph;
+    double ssum[RPT];
+#pragma unroll
+    for (int j = 0; j < RPT; ++j) ssum[j] = 0.0;
+    if (!REF)
+        for (int f = 0; f < nf; ++f)
+#pragma unroll
+            for (int j = 0; j < RPT; ++j) {
+                const double v = S::at(sm, f, r0 + j + 1, c);
+                ssum[j] = fma(v, v, ssum[j]);
+            }
+    const int64_t gbase = (int64_t)(ty * T + r0) * a.nx + tx * T + col;
+    for (int f = 0; f < nf; ++f) {
+        double w[RPT + 2][3];
+#pragma unroll
+        for (int j = 0; j < RPT + 2; ++j) {
+            w[j][0] = S::at(sm, f, r0 + j, c - 1);
+            w[j][1] = S::at(sm, f, r0 + j, c);
+            w[j][2] = S::at(sm, f, r0 + j, c + 1);
+        }
+#pragma unroll
+        for (int j = 0; j < RPT; ++j) {
+            const double *rd = w[j], *rc = w[j + 1], *ru = w[j + 2];
+            const double e = rc[1];
+            double out;
+            if (REF) {
+                double lap;
+                if (a.stencil == 0)
+                    lap = __ddiv_rn(__dsub_rn(__dadd_rn(__dadd_rn(__dadd_rn(__dadd_rn(__dadd_rn(__dadd_rn(__dadd_rn(
+                                      rd[0], rd[1]), rd[2]), rc[0]), rc[2]), ru[0]), ru[1]), ru[2]),
+                                      __dmul_rn(8.0, e)), ph.dxdy);
+                else
+                    lap = __ddiv_rn(__dsub_rn(__dadd_rn(__dadd_rn(__dadd_rn(rc[0], rc[2]), rd[1]), ru[1]),
+                                              __dmul_rn(4.0, e)), ph.dxdy);
+                double sum = 0.0;
+                bool first = true;
+                for (int b = 0; b < nf; ++b) {
+                    if (b == f) continue;
+                    const double v = S::at(sm, b, r0 + j + 1, c);
+                    const double s2 = __dmul_rn(v, v);
+                    sum = first ? s2 : __dadd_rn(sum, s2);
+                    first = false;
+                }
+                const double dfd = __dsub_rn(__dadd_rn(__dmul_rn(__dmul_rn(2.0 * ph.gamma, e), sum), pow(e, 3.0)), e);
+                out = __dsub_rn(e, __dmul_rn(ph.dt * ph.mobil, __dsub_rn(dfd, __dmul_rn(ph.grcoef, lap))));
+            } else {
+                double s;
+                if (a.stencil == 0) s = (rd[0] + rd[1] + rd[2]) + (rc[0] + rc[2]) + (ru[0] + ru[1] + ru[2]) - 8.0 * e;
+                else s = (rc[0] + rc[2]) + (rd[1] + ru[1]) - 4.0 * e;
+                const double lap = s * ph.inv_dxdy;
+                const double e2 = e * e;
+                const double dfd = e * fma(2.0 * ph.gamma, ssum[j] - e2, e2 - 1.0);
+                out = fma(-(ph.dt * ph.mobil), fma(-ph.grcoef, lap, dfd), e);
+            }
+            ((double *)a.out[TIER_FP64])[(int64_t)f * a.n + gbase + (int64_t)j * a.nx] = out;
+        }
+    }
+}
+
+// tier: TIER_FP64 selects the all-FP64 staged kernel; anything else the fused one.
 size_t gg_smem_bytes(int tile, int tier, int nf)
 {
-    (void)tier;
-    if (tile == 32) return (size_t)nf * Stage<float, 32, 1>::FIELD * sizeof(float);
-    return (size_t)nf * Stage<float, 16, 1>::FIELD * sizeof(float);
+    if (tier == TIER_FP64)
+        return (size_t)nf * (tile == 32 ? Stage<double, 32, 1>::FIELD : Stage<double, 16, 1>::FIELD) * sizeof(double);
+    return (size_t)nf * (tile == 32 ? Stage<float, 32, 1>::FIELD : Stage<float, 16, 1>::FIELD) * sizeof(float);
 }
 
 cudaError_t gg_launch(int tile, int tier, bool ref, const StepArgs &a, int grid, cudaStream_t s)
 {
-    (void)tier;
-    const size_t smem = gg_smem_bytes(tile, 0, a.nf);
-    if (tile == 32) {
-        if (ref) gg_step_kernel<32, true><<<grid, kThreads, smem, s>>>(a);
-        else gg_step_kernel<32, false><<<grid, kThreads, smem, s>>>(a);
+    const size_t smem = gg_smem_bytes(tile, tier, a.nf);
+#define AMPS_GGL(K, TT)                                                         \
+    do {                                                                        \
+        if (ref) K<TT, true><<<grid, kThreads, smem, s>>>(a);                   \
+        else K<TT, false><<<grid, kThreads, smem, s>>>(a);                      \
+    } while (0)
+    if (tier == TIER_FP64) {
+        if (tile == 32) AMPS_GGL(gg_step_f64_kernel, 32);
+        else AMPS_GGL(gg_step_f64_kernel, 16);
     } else {
-        if (ref) gg_step_kernel<16, true><<<grid, kThreads, smem, s>>>(a);
-        else gg_step_kernel<16, false><<<grid, kThreads, smem, s>>>(a);
+        if (tile == 32) AMPS_GGL(gg_step_kernel, 32);
+        else AMPS_GGL(gg_step_kernel, 16);
     }
+#undef AMPS_GGL
     return cudaGetLastError();
 }
 
 cudaError_t gg_prepare(int tile, int tier, bool ref)
 {
-    (void)tier;
     const int lim = kMaxDynSmem;
     const auto attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    if (tier == TIER_FP64) {
+        if (tile == 32) return ref ? cudaFuncSetAttribute(gg_step_f64_kernel<32, true>, attr, lim)
+                                   : cudaFuncSetAttribute(gg_step_f64_kernel<32, false>, attr, lim);
+        return ref ? cudaFuncSetAttribute(gg_step_f64_kernel<16, true>, attr, lim)
+                   : cudaFuncSetAttribute(gg_step_f64_kernel<16, false>, attr, lim);
+    }
     if (tile == 32) return ref ? cudaFuncSetAttribute(gg_step_kernel<32, true>, attr, lim)
                                : cudaFuncSetAttribute(gg_step_kernel<32, false>, attr, lim);
     return ref ? cudaFuncSetAttribute(gg_step_kernel<16, true>, attr, lim)
