@@ -223,6 +223,27 @@ AMPS_API int amps_reduce(amps_handle *h, int field, int kind, double *out);
 AMPS_API int amps_compare(amps_handle *h, int field, const double *other, int on_device, double *max_abs,
                  double *rms);
 
+/* ---- reduction that allocates nothing ------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory when they need the result -- e.g. an application whose device
+ * memory is all handed to its own pool at start-up, or code held to a fixed
+ * device-memory budget: amps_reduce needs a handle, and creating one
+ * allocates.  amps_reduce_noalloc folds a caller-owned row-major double
+ * array `data` of n cells on the device (kind AMPS_REDUCE_*) and writes the
+ * result to the caller's device slot `out`, asynchronously on `stream`
+ * (cudaStream_t as void*, NULL = default stream), in a fixed order, so the
+ * result is deterministic.  Its per-block partials live in one fixed
+ * device array of AMPS_REDUCE_NOALLOC_MAX_BLOCKS doubles (32 KiB per device,
+ * kept until the process exits); n above AMPS_REDUCE_NOALLOC_MAX_CELLS is
+ * rejected with AMPS_ERR_UNSUPPORTED.  All calls share that array: calls
+ * whose kernels overlap on the GPU race; order them on one stream.  The
+ * first call on a device looks the array's address up with that device
+ * current; make it before any stream capture on that device. */
+#define AMPS_REDUCE_NOALLOC_CELLS_PER_BLOCK 4096
+#define AMPS_REDUCE_NOALLOC_MAX_BLOCKS 4096
+#define AMPS_REDUCE_NOALLOC_MAX_CELLS (AMPS_REDUCE_NOALLOC_CELLS_PER_BLOCK * AMPS_REDUCE_NOALLOC_MAX_BLOCKS)
+AMPS_API int amps_reduce_noalloc(const double *data, int64_t n, int kind, double *out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
