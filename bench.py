@@ -364,6 +364,23 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def run_profile_case(args):
+    """A short, untimed run of the tuned workload at nx^2 for ncu captures
+    (`--profile-case 2048` puts a 256 MiB FP32 state, larger than L2)."""
+    import torch
+    import w3914777_gb300 as w
+    torch.cuda.set_device(0)
+    p = w.Params.preset("graingrowth", 0, nx=args.profile_case, ny=args.profile_case)
+    tuned = load_tuned()
+    if tuned:
+        p = p.replace(**tuned["overrides"])
+    with w.Simulation(p, init=w.INIT_SEEDED) as s:
+        s.run(args.sim_steps)
+        s.synchronize()
+        st = s.stats()
+    print(json.dumps({"profile_case": args.profile_case, "steps": args.sim_steps, "tile_steps": st["tile_steps"]}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -374,8 +391,11 @@ def main():
     ap.add_argument("--ref-sample-steps", type=int, default=100)
     ap.add_argument("--tile", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile-case", type=int, default=0)
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.profile_case:
+        run_profile_case(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -147,82 +147,83 @@ __device__ __forceinline__ void load_neighbour_tiers(const StepArgs &a, int tx, 
 
 // Stage fields [f0, f0+nfs) of tile (tx, ty) with an R-cell halo, every cell
 // read at its owner tile's input tier (nt: load_neighbour_tiers) and
-// converted to CT.  Interior row segments go as 16-byte vector loads; halo
-// columns as scalar loads.  Each thread issues a batch of loads before it
-// stores any of them, so that many loads are in flight at once.
+// converted to CT.  Each thread owns fixed slots of the field's footprint --
+// an interior 8-cell row segment (16-byte vector loads) or one halo cell --
+// whose coordinates, tier and offsets are computed once; the field loop then
+// only adds the field stride, issuing a batch of loads before any store.
 template <typename CT, int T, int R>
 __device__ __forceinline__ void stage_tile(const StepArgs &a, CT *sm, const uint8_t *nt, int tx, int ty, int f0,
                                            int nfs)
 {
     using S = Stage<CT, T, R>;
-    constexpr int PER = sizeof(CT) == 8 ? 2 : 4;  // 8-cell units per batch and thread
+    constexpr int SEG = T / 8;
+    constexpr int UI = S::ROWS * SEG;    // interior 8-cell segments per field
+    constexpr int UH = S::ROWS * 2 * R;  // halo cells per field
+    constexpr int U = UI + UH;
+    constexpr int SLOTS = (U + kThreads - 1) / kThreads;
+    constexpr int B0 = (sizeof(CT) == 8 ? 2 : 4) / SLOTS;
+    constexpr int B = B0 < 1 ? 1 : B0;   // fields per batch
     const int x0 = tx * T, y0 = ty * T;
-    constexpr int SEG = T / 8;  // 8-cell segments per interior row
-    const int units = nfs * S::ROWS * SEG;
-    for (int base = threadIdx.x; base < units; base += kThreads * PER) {
-        CT v[PER][8];
+    int kind[SLOTS], tier[SLOTS], soff[SLOTS];
+    int64_t goff[SLOTS];
 #pragma unroll
-        for (int q = 0; q < PER; ++q) {
-            const int u = base + q * kThreads;
-            if (u < units) {
-                const int s = u % SEG;
-                const int r = (u / SEG) % S::ROWS;
-                const int f = u / (SEG * S::ROWS);
-                const int gy = bc_map(y0 - R + r, a.ny, a.bc);
-                const int tier = nt[(r < R ? 0 : (r < T + R ? 3 : 6)) + 1];
-                load8_tier<CT>(a, tier, (int64_t)(f0 + f) * a.n + (int64_t)gy * a.nx + x0 + 8 * s, v[q]);
-            }
-        }
-#pragma unroll
-        for (int q = 0; q < PER; ++q) {
-            const int u = base + q * kThreads;
-            if (u < units) {
-                const int s = u % SEG;
-                const int r = (u / SEG) % S::ROWS;
-                const int f = u / (SEG * S::ROWS);
-                CT *dst = &S::at(sm, f, r, S::O + 8 * s);  // 16-byte aligned: O, P and FIELD are
-                if (sizeof(CT) == 4) {                        // multiples of 16 bytes
-                    float4 *d4 = reinterpret_cast<float4 *>(dst);
-                    d4[0] = make_float4((float)v[q][0], (float)v[q][1], (float)v[q][2], (float)v[q][3]);
-                    d4[1] = make_float4((float)v[q][4], (float)v[q][5], (float)v[q][6], (float)v[q][7]);
-                } else {
-                    double2 *d2 = reinterpret_cast<double2 *>(dst);
-#pragma unroll
-                    for (int k = 0; k < 4; ++k) d2[k] = make_double2((double)v[q][2 * k], (double)v[q][2 * k + 1]);
-                }
-            }
+    for (int q = 0; q < SLOTS; ++q) {
+        const int u = threadIdx.x + q * kThreads;
+        kind[q] = 0; tier[q] = 0; soff[q] = 0; goff[q] = 0;
+        if (u < UI) {
+            const int sg = u % SEG, r = u / SEG;
+            const int gy = bc_map(y0 - R + r, a.ny, a.bc);
+            kind[q] = 1;
+            tier[q] = nt[(r < R ? 0 : (r < T + R ? 3 : 6)) + 1];
+            goff[q] = (int64_t)gy * a.nx + x0 + 8 * sg;
+            soff[q] = r * S::P + S::O + 8 * sg;
+        } else if (u < U) {
+            const int h = u - UI, k = h % (2 * R), r = h / (2 * R);
+            const int gy = bc_map(y0 - R + r, a.ny, a.bc);
+            const int lx = k < R ? x0 - R + k : x0 + T + (k - R);
+            const int gx = bc_map(lx, a.nx, a.bc);
+            kind[q] = 2;
+            tier[q] = nt[(r < R ? 0 : (r < T + R ? 3 : 6)) + (k < R ? 0 : 2)];
+            goff[q] = (int64_t)gy * a.nx + gx;
+            soff[q] = r * S::P + (k < R ? S::O - R + k : S::O + T + (k - R));
         }
     }
-    // halo columns: R cells on each side of every staged row
-    constexpr int HPER = 8;
-    const int hunits = nfs * S::ROWS * 2 * R;
-    for (int base = threadIdx.x; base < hunits; base += kThreads * HPER) {
-        CT v[HPER];
+    for (int fb = 0; fb < nfs; fb += B) {
+        CT v[SLOTS][B][8];
 #pragma unroll
-        for (int q = 0; q < HPER; ++q) {
-            const int u = base + q * kThreads;
-            if (u < hunits) {
-                const int k = u % (2 * R);
-                const int r = (u / (2 * R)) % S::ROWS;
-                const int f = u / (2 * R * S::ROWS);
-                const int gy = bc_map(y0 - R + r, a.ny, a.bc);
-                const int lx = k < R ? x0 - R + k : x0 + T + (k - R);
-                const int gx = bc_map(lx, a.nx, a.bc);
-                const int tier = nt[(r < R ? 0 : (r < T + R ? 3 : 6)) + (k < R ? 0 : 2)];
-                v[q] = load_tier<CT>(a, tier, (int64_t)(f0 + f) * a.n + (int64_t)gy * a.nx + gx);
-            }
-        }
+        for (int q = 0; q < SLOTS; ++q)
 #pragma unroll
-        for (int q = 0; q < HPER; ++q) {
-            const int u = base + q * kThreads;
-            if (u < hunits) {
-                const int k = u % (2 * R);
-                const int r = (u / (2 * R)) % S::ROWS;
-                const int f = u / (2 * R * S::ROWS);
-                const int col = k < R ? S::O - R + k : S::O + T + (k - R);
-                S::at(sm, f, r, col) = v[q];
+            for (int b = 0; b < B; ++b) {
+                const int f = fb + b;
+                if (f < nfs) {
+                    const int64_t idx = (int64_t)(f0 + f) * a.n + goff[q];
+                    if (kind[q] == 1) load8_tier<CT>(a, tier[q], idx, v[q][b]);
+                    else if (kind[q] == 2) v[q][b][0] = load_tier<CT>(a, tier[q], idx);
+                }
             }
-        }
+#pragma unroll
+        for (int q = 0; q < SLOTS; ++q)
+#pragma unroll
+            for (int b = 0; b < B; ++b) {
+                const int f = fb + b;
+                if (f < nfs) {
+                    CT *dst = sm + f * S::FIELD + soff[q];
+                    if (kind[q] == 1) {  // 16-byte aligned: O, P and FIELD are multiples of 16 bytes
+                        if (sizeof(CT) == 4) {
+                            float4 *d4 = reinterpret_cast<float4 *>(dst);
+                            d4[0] = make_float4((float)v[q][b][0], (float)v[q][b][1], (float)v[q][b][2], (float)v[q][b][3]);
+                            d4[1] = make_float4((float)v[q][b][4], (float)v[q][b][5], (float)v[q][b][6], (float)v[q][b][7]);
+                        } else {
+                            double2 *d2 = reinterpret_cast<double2 *>(dst);
+#pragma unroll
+                            for (int k = 0; k < 4; ++k)
+                                d2[k] = make_double2((double)v[q][b][2 * k], (double)v[q][b][2 * k + 1]);
+                        }
+                    } else if (kind[q] == 2) {
+                        dst[0] = v[q][b][0];
+                    }
+                }
+            }
     }
 }
 
