@@ -10,7 +10,9 @@
 #include "../../include/amps.h"
 #include "amps_kernels.h"
 
+#include <cudaTypedefs.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <map>
@@ -49,6 +51,10 @@ struct amps_handle {
     bool profiling = false;
     struct Ev { int tier; cudaEvent_t a, b; };
     std::vector<Ev> evs;
+    // grain growth: persistent TMA kernel over the FP32 ping-pong buffers
+    bool use_tma = false;
+    int tma_grid = 0;
+    alignas(64) CUtensorMap tm[2];
     double prof_ms[4] = {0, 0, 0, 0};
     int64_t prof_launches[4] = {0, 0, 0, 0};
     unsigned long long prof_stats0[3] = {0, 0, 0};
@@ -86,6 +92,35 @@ extern "C" const char *amps_status_string(int s)
 extern "C" const char *amps_last_error(const amps_handle *h)
 {
     return h ? h->err.c_str() : g_create_err.c_str();
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no libcuda link).
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
+// [nf][ny][nx] float array -> box {40 columns, 34 rows, nf fields}: a 32x32
+// tile with a 1-cell halo and its columns padded to 16-byte boundaries.
+static bool encode_field_map(CUtensorMap *tm, void *base, int nx, int ny, int nf)
+{
+    auto enc = tensor_map_encoder();
+    if (!enc) return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nf};
+    const cuuint64_t strides[2] = {(cuuint64_t)nx * 4, (cuuint64_t)nx * ny * 4};
+    const cuuint32_t box[3] = {40, 34, (cuuint32_t)nf};
+    const cuuint32_t es[3] = {1, 1, 1};
+    return enc(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
+           CUDA_SUCCESS;
 }
 
 static size_t tier_size(int t) { return t == TIER_FP64 ? 8 : (t == TIER_FP32 ? 4 : 2); }
@@ -225,6 +260,26 @@ extern "C" int amps_create(const amps_params *p, amps_handle **out)
             return AMPS_ERR_CUDA;
         }
     }
+    {
+        // persistent TMA kernel (opt-in, AMPS_ENABLE_TMA=1): grain growth, 32x32 tiles, an FP32 tier, few
+        // enough fields for two buffers.  Measured slower than the 4-CTA/SM staged kernel on GB300 (two
+        // double-buffered CTAs per SM leave 16 warps for a latency-bound compute phase), so not the default.
+        const bool only64 = h->used[TIER_FP64] && !h->used[TIER_FP32] && !h->used[TIER_HALF];
+        const char *on = getenv("AMPS_ENABLE_TMA");
+        if (p->model == AMPS_GRAINGROWTH && p->tile == 32 && h->used[TIER_FP32] && !only64 && h->nf <= kTmaMaxFields &&
+            on && on[0] == '1') {
+            int bps = 0, dev = 0, sms = 0;
+            if (encode_field_map(&h->tm[0], h->store[TIER_FP32][0], p->nx, p->ny, h->nf) &&
+                encode_field_map(&h->tm[1], h->store[TIER_FP32][1], p->nx, p->ny, h->nf) &&
+                gg_prepare_tma(p->ref_order != 0, h->nf, &bps) == cudaSuccess && bps > 0 &&
+                cudaGetDevice(&dev) == cudaSuccess &&
+                cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess) {
+                h->use_tma = true;
+                h->tma_grid = bps * sms < h->ntiles ? bps * sms : h->ntiles;
+            }
+            cudaGetLastError();  // a refused attribute / encode leaves the generic kernel in charge
+        }
+    }
     const int start = p->mode == AMPS_PURELOW ? TIER_HALF : high;
     cudaMemsetAsync(h->d_tier_cur, start, h->ntiles, h->stream);
     cudaMemsetAsync(h->d_tier_prev, start, h->ntiles, h->stream);
@@ -263,6 +318,7 @@ extern "C" int amps_synchronize(amps_handle *h)
     CK(h, cudaStreamSynchronize(h->stream));
     int flag = 0;
     CK(h, cudaMemcpy(&flag, h->d_flags, sizeof(int), cudaMemcpyDeviceToHost));
+    if (flag & 2) FAIL(h, AMPS_ERR_TIMEOUT, "a bounded device wait gave up (tensor copy did not complete)");
     if (flag & 1) FAIL(h, AMPS_ERR_NUMERIC, "NaN or Inf detected by the monitor");
     return AMPS_OK;
 }
@@ -478,7 +534,8 @@ static int launch_step(amps_handle *h, int step_off, bool monitor_now)
         }
         // all-FP64 runs use the staged FP64 kernel, every other mode the fused one
         const bool only64 = h->used[TIER_FP64] && !h->used[TIER_FP32] && !h->used[TIER_HALF];
-        cudaError_t e = gg_launch(h->T, only64 ? TIER_FP64 : -1, ref, a, h->ntiles, h->stream);
+        cudaError_t e = h->use_tma ? gg_launch_tma(ref, h->tm[h->parity], a, h->tma_grid, h->stream)
+                                   : gg_launch(h->T, only64 ? TIER_FP64 : -1, ref, a, h->ntiles, h->stream);
         if (e != cudaSuccess) FAIL(h, AMPS_ERR_CUDA, "step kernel launch: %s", cudaGetErrorString(e));
         if (h->profiling) {
             cudaEventRecord(ev.b, h->stream);

@@ -13,6 +13,11 @@ size_t gg_smem_bytes(int tile, int tier, int nf);
 cudaError_t gg_prepare(int tile, int tier, bool ref);
 cudaError_t kob_prepare(int tile, int tier, bool ref);
 cudaError_t sint_prepare(int tile, int tier, bool ref, bool mu64);
+// Persistent TMA-pipelined grain-growth step (32x32 tiles, FP32 neighbourhoods by tensor copy).
+constexpr int kTmaMaxFields = 16;
+size_t gg_tma_smem_bytes(int nf);
+cudaError_t gg_prepare_tma(bool ref, int nf, int *blocks_per_sm);
+cudaError_t gg_launch_tma(bool ref, const CUtensorMap &tm, const StepArgs &a, int grid, cudaStream_t s);
 size_t kob_smem_bytes(int tile, int tier);
 size_t sint_smem_bytes(int tile, int tier, int nf, bool mu64);
 

@@ -362,4 +362,118 @@ cudaError_t gg_prepare(int tile, int tier, bool ref)
                : cudaFuncSetAttribute(gg_step_kernel<16, false>, attr, lim);
 }
 
+// Persistent, TMA-pipelined fused step for 32x32 tiles (nf <= kTmaMaxFields).
+// Each CTA walks tiles blockIdx.x, +gridDim.x, ...  A tile whose input
+// neighbourhood is entirely FP32 and inside the domain (no wrap, no mirror)
+// is fetched by one 3-D tensor copy -- all nf fields, 34 rows x 40 columns --
+// straight into the float staging layout, issued one tile ahead into the
+// other of two buffers so that the copy overlaps the current tile's
+// arithmetic.  Every other tile (domain edge, a neighbour at another tier,
+// FP64 output) takes the generic staged / direct path.
+template <bool REF>
+__global__ void __launch_bounds__(kThreads, 2)
+    gg_step_tma_kernel(const __grid_constant__ CUtensorMap tm, StepArgs a, int bufstride)
+{
+    constexpr int T = 32;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ __align__(8) uint64_t mbar[2];
+    __shared__ double red[kThreads / 32];
+    __shared__ uint8_t ntier[9];
+    __shared__ int fast_s[2];
+    float *buf0 = reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(smraw) + 1023) & ~uintptr_t(1023));
+    const int ntiles = a.ntx * a.nty;
+    const uint32_t bytes = 40u * 34u * (uint32_t)a.nf * 4u;
+    if (threadIdx.x == 0) {
+        mbar_init(&mbar[0], 1);
+        mbar_init(&mbar[1], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    // thread 0 only: can tile t come by tensor copy?
+    auto is_fast = [&](int t) -> int {
+        const int tx = t % a.ntx, ty = t / a.ntx;
+        if (tx < 1 || ty < 1 || tx > a.ntx - 2 || ty > a.nty - 2) return 0;
+        if (a.tier_out[t] == TIER_FP64) return 0;
+        for (int dy = -1; dy <= 1; ++dy)
+            for (int dx = -1; dx <= 1; ++dx)
+                if (a.tier_in[(ty + dy) * a.ntx + tx + dx] != TIER_FP32) return 0;
+        return 1;
+    };
+    auto issue = [&](int t, int b) {
+        const int tx = t % a.ntx, ty = t / a.ntx;
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(&mbar[b], bytes);
+        tma_load_3d(buf0 + b * bufstride, &tm, tx * T - 4, ty * T - 1, 0, &mbar[b]);
+    };
+    uint32_t ph0 = 0, ph1 = 0;
+    int t = blockIdx.x;
+    if (threadIdx.x == 0) {
+        const int f = t < ntiles ? is_fast(t) : 0;
+        if (f) issue(t, 0);
+        fast_s[0] = f;
+    }
+    __syncthreads();
+    for (int i = 0; t < ntiles; ++i, t += gridDim.x) {
+        const int b = i & 1;
+        const int tn = t + gridDim.x;
+        if (threadIdx.x == 0) {  // prefetch the next tile into the other buffer (free since the last barrier)
+            const int f = tn < ntiles ? is_fast(tn) : 0;
+            if (f) issue(tn, b ^ 1);
+            fast_s[b ^ 1] = f;
+        }
+        const int fast = fast_s[b];
+        const int tx = t % a.ntx, ty = t / a.ntx;
+        const int tier = a.tier_out[t];
+        float *sm = buf0 + b * bufstride;
+        if (fast) {
+            const bool ok = mbar_wait_bounded(&mbar[b], b ? ph1 : ph0);
+            if (b) ph1 ^= 1u; else ph0 ^= 1u;
+            if (__syncthreads_or(!ok)) {
+                // give up: flag it, let the copy already in flight land (bounded), leave
+                if (threadIdx.x == 0) atomicOr(a.flags, 2);
+                if (fast_s[b ^ 1]) mbar_wait_bounded(&mbar[b ^ 1], b ? ph0 : ph1);
+                return;
+            }
+            if (tier == TIER_FP32) gg_tile_lo<T, TIER_FP32>(a, sm, t, tx, ty, red);
+            else gg_tile_lo<T, TIER_HALF>(a, sm, t, tx, ty, red);
+        } else {
+            load_neighbour_tiers(a, tx, ty, ntier);
+            __syncthreads();
+            if (tier == TIER_FP64) {
+                gg_tile_fp64<T, REF>(a, ntier, t, tx, ty, red);
+            } else {
+                stage_tile<float, T, 1>(a, sm, ntier, tx, ty, 0, a.nf);
+                __syncthreads();
+                if (tier == TIER_FP32) gg_tile_lo<T, TIER_FP32>(a, sm, t, tx, ty, red);
+                else gg_tile_lo<T, TIER_HALF>(a, sm, t, tx, ty, red);
+            }
+        }
+        fence_proxy_async_smem();  // this buffer's reads/writes before its next tensor copy
+        __syncthreads();
+    }
+    // a prefetch is issued only for tiles the loop reaches, so nothing is in flight here
+}
+
+int gg_tma_buffer_floats(int nf) { return ((nf * Stage<float, 32, 1>::FIELD * 4 + 1023) / 1024) * 256; }
+size_t gg_tma_smem_bytes(int nf) { return (size_t)2 * gg_tma_buffer_floats(nf) * 4 + 1024; }
+
+cudaError_t gg_launch_tma(bool ref, const CUtensorMap &tm, const StepArgs &a, int grid, cudaStream_t s)
+{
+    const int bs = gg_tma_buffer_floats(a.nf);
+    const size_t smem = gg_tma_smem_bytes(a.nf);
+    if (ref) gg_step_tma_kernel<true><<<grid, kThreads, smem, s>>>(tm, a, bs);
+    else gg_step_tma_kernel<false><<<grid, kThreads, smem, s>>>(tm, a, bs);
+    return cudaGetLastError();
+}
+
+cudaError_t gg_prepare_tma(bool ref, int nf, int *blocks_per_sm)
+{
+    const size_t smem = gg_tma_smem_bytes(nf);
+    cudaError_t e = ref ? cudaFuncSetAttribute(gg_step_tma_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                        : cudaFuncSetAttribute(gg_step_tma_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    return ref ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, gg_step_tma_kernel<true>, kThreads, smem)
+               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, gg_step_tma_kernel<false>, kThreads, smem);
+}
+
 }  // namespace amps
