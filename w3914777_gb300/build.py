@@ -89,7 +89,31 @@ def build(verbose=False, force=False, extra_flags=()):
         cmd = [cc, *ARCH, "-shared", "-o", LIB, *objs, "-cudart", "static", "-Xcompiler", "-fPIC"]
         if run(cmd):
             raise RuntimeError("link failed")
+    build_drivers(cc, run, force or bool(jobs))
     return LIB
+
+
+DRIVER_SRC = os.path.join(HERE, "drivers", "amps_driver.cpp")
+DRIVER = os.path.join(OUT, "amps_driver")
+DRIVER_NAMES = ["snowflake_purehigh", "snowflake_purelow", "snowflake_end2end_mix", "graingrowth_purehigh",
+                "graingrowth_purelow", "graingrowth_end2end_mix", "sintering_main"]
+
+
+def build_drivers(cc, run, force=False):
+    """The reference's driver programs (one executable, one name per program)."""
+    if foreign_binary(DRIVER):
+        os.remove(DRIVER)
+    if force or _newer(DRIVER, [DRIVER_SRC, LIB, os.path.join(ROOT, "include", "amps.h")]):
+        cmd = [cc, "-O2", "-std=c++17", "-x", "cu", DRIVER_SRC, "-o", DRIVER, "-L" + OUT, "-lamps",
+               "-Xlinker", "-rpath,$ORIGIN", "-cudart", "static"]
+        if run(cmd):
+            raise RuntimeError("driver build failed")
+    for name in DRIVER_NAMES:
+        link = os.path.join(OUT, name)
+        if not os.path.islink(link):
+            if os.path.exists(link):
+                os.remove(link)
+            os.symlink("amps_driver", link)
 
 
 if __name__ == "__main__":
