@@ -244,6 +244,29 @@ AMPS_API int amps_compare(amps_handle *h, int field, const double *other, int on
 #define AMPS_REDUCE_NOALLOC_MAX_CELLS (AMPS_REDUCE_NOALLOC_CELLS_PER_BLOCK * AMPS_REDUCE_NOALLOC_MAX_BLOCKS)
 AMPS_API int amps_reduce_noalloc(const double *data, int64_t n, int kind, double *out, void *stream);
 
+/* ---- one explicit step and its adjoint (differentiation) -----------------
+ * No counterpart in the reference (it only runs forward).  Stateless: the
+ * caller owns every array, all row-major on the device, `dtype` AMPS_F64 or
+ * AMPS_F32 for all of them, asynchronous on `stream`.  Models
+ * AMPS_KOBAYASHI (state [phi; T], 2n values) and AMPS_GRAINGROWTH (state
+ * [eta_0 .. eta_{Q-1}], Q = nfields, Q*n values); the step is the one
+ * amps_run takes in AMPS_PUREHIGH mode (same stencils, boundaries and noise
+ * stream, `step` = the noise step index), up to floating-point order.
+ *   amps_step_forward: state_out = step(state_in).
+ *   amps_step_adjoint: grad_in = (d step / d state_in)^T grad_out, and adds
+ *     dL/dparams into grad_params (device doubles, not cleared): Kobayashi
+ *     [delta, kappa (latent heat K), epsb]; grain growth [mobil, grcoef, gamma].
+ *     Zero-flux boundaries are differentiated exactly.  The atan2 of the
+ *     Kobayashi anisotropy has no derivative where grad phi = 0; the adjoint
+ *     takes it as 0 there.
+ * `workspace` holds amps_adjoint_workspace_bytes(p, dtype) bytes (0 for grain
+ * growth, which needs none).  Sintering returns AMPS_ERR_UNSUPPORTED. */
+AMPS_API size_t amps_adjoint_workspace_bytes(const amps_params *p, int dtype);
+AMPS_API int amps_step_forward(const amps_params *p, int dtype, const void *state_in, void *state_out,
+                               void *workspace, int64_t step, void *stream);
+AMPS_API int amps_step_adjoint(const amps_params *p, int dtype, const void *state_in, const void *grad_out,
+                               void *grad_in, double *grad_params, void *workspace, int64_t step, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

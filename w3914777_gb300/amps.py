@@ -127,6 +127,9 @@ def lib():
             "amps_set_profiling": ([vp, ip], ip),
             "amps_get_kernel_times": ([vp, ctypes.POINTER(dp), ctypes.POINTER(ctypes.c_int64),
                                        ctypes.POINTER(ctypes.c_int64)], ip),
+            "amps_adjoint_workspace_bytes": ([P, ip], ctypes.c_size_t),
+            "amps_step_forward": ([P, ip, vp, vp, vp, ctypes.c_int64, vp], ip),
+            "amps_step_adjoint": ([P, ip, vp, vp, vp, vp, vp, ctypes.c_int64, vp], ip),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
