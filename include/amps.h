@@ -249,23 +249,48 @@ AMPS_API int amps_reduce_noalloc(const double *data, int64_t n, int kind, double
  * caller owns every array, all row-major on the device, `dtype` AMPS_F64 or
  * AMPS_F32 for all of them, asynchronous on `stream`.  Models
  * AMPS_KOBAYASHI (state [phi; T], 2n values) and AMPS_GRAINGROWTH (state
- * [eta_0 .. eta_{Q-1}], Q = nfields, Q*n values); the step is the one
+ * [eta_0 .. eta_{Q-1}], Q = nfields <= 32, Q*n values); the step is the one
  * amps_run takes in AMPS_PUREHIGH mode (same stencils, boundaries and noise
  * stream, `step` = the noise step index), up to floating-point order.
  *   amps_step_forward: state_out = step(state_in).
  *   amps_step_adjoint: grad_in = (d step / d state_in)^T grad_out, and adds
- *     dL/dparams into grad_params (device doubles, not cleared): Kobayashi
- *     [delta, kappa (latent heat K), epsb]; grain growth [mobil, grcoef, gamma].
- *     Zero-flux boundaries are differentiated exactly.  The atan2 of the
- *     Kobayashi anisotropy has no derivative where grad phi = 0; the adjoint
- *     takes it as 0 there.
- * `workspace` holds amps_adjoint_workspace_bytes(p, dtype) bytes (0 for grain
- * growth, which needs none).  Sintering returns AMPS_ERR_UNSUPPORTED. */
-AMPS_API size_t amps_adjoint_workspace_bytes(const amps_params *p, int dtype);
-AMPS_API int amps_step_forward(const amps_params *p, int dtype, const void *state_in, void *state_out,
-                               void *workspace, int64_t step, void *stream);
+ *     dL/dparams into grad_params (3 device doubles, not cleared):
+ *     Kobayashi [delta, kappa (latent heat K), epsb]; grain growth
+ *     [mobil, grcoef, gamma].  Zero-flux boundaries are differentiated
+ *     exactly.  The atan2 of the Kobayashi anisotropy has no derivative where
+ *     grad phi = 0; the adjoint takes it as 0 there.
+ * Sintering returns AMPS_ERR_UNSUPPORTED. */
+AMPS_API int amps_step_forward(const amps_params *p, int dtype, const void *state_in, void *state_out, int64_t step,
+                               void *stream);
 AMPS_API int amps_step_adjoint(const amps_params *p, int dtype, const void *state_in, const void *grad_out,
-                               void *grad_in, double *grad_params, void *workspace, int64_t step, void *stream);
+                               void *grad_in, double *grad_params, int64_t step, void *stream);
+
+/* ---- checkpointed rollout and its reverse sweep --------------------------
+ * A handle for N explicit steps of one model on one grid.  amps_adjoint_forward
+ * runs the N steps from state0 and keeps every `segment`-th state
+ * (segment 0 = ceil(sqrt(N)); 1 keeps every state and replays nothing);
+ * amps_adjoint_backward takes the cotangent of the final state and returns
+ * the cotangent of state0 and dL/dparams (3 device doubles, overwritten),
+ * replaying each segment from its checkpoint.  param_values: the three
+ * differentiable parameters (host doubles, same order as above), which
+ * override those in the amps_params; step0: noise step index of the first
+ * step.  All state pointers are device pointers; both calls are asynchronous
+ * on the handle's stream (set_stream; NULL = default stream).  Each sweep is
+ * captured once into a CUDA graph (set_graphs(0) launches kernels directly)
+ * that reads the parameters and step0 from device memory, so calls with new
+ * values replay it.  Memory: amps_adjoint_memory_bytes (one allocation at
+ * create).  Not re-entrant per handle. */
+typedef struct amps_adjoint amps_adjoint;
+AMPS_API size_t amps_adjoint_memory_bytes(const amps_params *p, int dtype, int nsteps, int segment);
+AMPS_API int amps_adjoint_create(const amps_params *p, int dtype, int nsteps, int segment, amps_adjoint **out);
+AMPS_API int amps_adjoint_destroy(amps_adjoint *a);
+AMPS_API int amps_adjoint_set_stream(amps_adjoint *a, void *stream);
+AMPS_API int amps_adjoint_set_graphs(amps_adjoint *a, int enable);
+AMPS_API int amps_adjoint_segment(const amps_adjoint *a);
+AMPS_API const char *amps_adjoint_last_error(const amps_adjoint *a);
+AMPS_API int amps_adjoint_forward(amps_adjoint *a, const double *param_values, const void *state0, void *state_final,
+                                  int64_t step0);
+AMPS_API int amps_adjoint_backward(amps_adjoint *a, const void *grad_final, void *grad_state0, double *grad_params);
 
 #ifdef __cplusplus
 }

@@ -3,11 +3,11 @@
 * The torch restatement of one step (adjoint_ref) equals the oracle's step
   (which is pinned bit-exact to the reference) to 1e-12, for both models and
   both boundary maps, noise included.
-* The checkpoint/replay logic of adjoint._Rollout, driven by a CPU stepper
-  built on adjoint_ref + torch.autograd, gives the same gradients as
-  differentiating the unrolled loop directly, for several checkpoint
-  spacings.
+* The checkpointed rollout's device-memory layout (host-side arithmetic of
+  amps_adjoint_memory_bytes) and its argument checks.
 """
+import ctypes
+
 import numpy as np
 import pytest
 import torch
@@ -68,61 +68,23 @@ def test_graingrowth_torch_step_matches_oracle(bc, stencil):
     assert np.abs(out - ref).max() <= 1e-12
 
 
-class _TorchStepper:
-    """The Stepper interface over adjoint_ref on the CPU (autograd per step)."""
-
-    def __init__(self, p):
-        self.params = p
-        self.dtype = torch.float64
-        self.vals = [p.delta, p.kappa, p.epsb]
-
-    def set_param_values(self, values):
-        self.vals = list(values)
-
-    def _f(self, state, step, pv):
-        return R.kob_step(state, self.params, pv[0], pv[1], pv[2], step)
-
-    def forward(self, state, step, out=None):
-        with torch.no_grad():
-            r = self._f(state, step, torch.tensor(self.vals, dtype=torch.float64))
-        if out is None:
-            return r
-        out.copy_(r)
-        return out
-
-    def adjoint(self, state, grad_out, step, grad_params, grad_in=None):
-        with torch.enable_grad():
-            x = state.detach().clone().requires_grad_(True)
-            pv = torch.tensor(self.vals, dtype=torch.float64, requires_grad=True)
-            gx, gp = torch.autograd.grad(self._f(x, step, pv), (x, pv), grad_out)
-        grad_params += gp
-        if grad_in is None:
-            return gx
-        grad_in.copy_(gx)
-        return grad_in
+@pytest.mark.parametrize("nsteps,segment,nseg,seg", [(1000, 0, 32, 32), (1000, 32, 32, 32), (24, 0, 5, 5),
+                                                      (10, 1, 10, 1), (10, 50, 1, 10)])
+def test_rollout_memory_layout(nsteps, segment, nseg, seg):
+    """Checkpoints: ceil(N/segment) states, plus segment-1 replay states and
+    four ping-pong states (each rounded up to 256 B), plus 256 B of scalars."""
+    p = amps.Params.preset(amps.KOBAYASHI, 0, nx=256, ny=256)
+    sb = 2 * 256 * 256 * 4
+    got = amps.lib().amps_adjoint_memory_bytes(ctypes.byref(p), amps.F32, nsteps, segment)
+    assert got == sb * (nseg + seg - 1 + 4) + 256
 
 
-@pytest.mark.parametrize("segment", [1, 3, 4, 10])
-def test_rollout_checkpointing_matches_unrolled(segment):
-    p = _kob_p(1, 0.01)
-    phi, T = _kob_state(p)
-    x0 = torch.tensor(np.stack([phi, T]))
-    n = 10
-    tgt = torch.zeros_like(x0[0])
-    # direct: autograd through the unrolled loop
-    pv = torch.tensor([p.delta, p.kappa, p.epsb], dtype=torch.float64, requires_grad=True)
-    xa = x0.clone().requires_grad_(True)
-    s = xa
-    for k in range(n):
-        s = R.kob_step(s, p, pv[0], pv[1], pv[2], 5 + k)
-    (0.5 * ((s[0] - tgt) ** 2).sum()).backward()
-    # checkpointed
-    pv2 = torch.tensor([p.delta, p.kappa, p.epsb], dtype=torch.float64, requires_grad=True)
-    xb = x0.clone().requires_grad_(True)
-    out = adjoint._Rollout.apply(xb, pv2, _TorchStepper(p), n, 5, segment)
-    (0.5 * ((out[0] - tgt) ** 2).sum()).backward()
-    assert torch.allclose(xb.grad, xa.grad, rtol=1e-12, atol=1e-14)
-    assert torch.allclose(pv2.grad, pv.grad, rtol=1e-12, atol=0)
+def test_adjoint_abi_rejects_sintering():
+    p = amps.Params.preset(amps.SINTERING, 0, nx=64, ny=64, tile=16)
+    assert amps.lib().amps_adjoint_memory_bytes(ctypes.byref(p), amps.F64, 10, 0) == 0
+    h = ctypes.c_void_p()
+    assert amps.lib().amps_adjoint_create(ctypes.byref(p), amps.F64, 10, 0, ctypes.byref(h)) == 6
+    assert not h.value
 
 
 def test_param_names_cover_models():

@@ -171,7 +171,7 @@ def _misfit_setup(dtype=torch.float64, nsteps=24):
     return p, x, tgt.to(dtype)
 
 
-def _misfit(p, x, tgt, nsteps, pv, dtype=torch.float64, segment=None, t0_dir=None, eps=0.0):
+def _misfit(p, x, tgt, nsteps, pv, dtype=torch.float64, segment=0, t0_dir=None, eps=0.0):
     x0 = dev(x, dtype)
     if t0_dir is not None:
         x0[1] += eps * t0_dir.to(dtype)
@@ -179,10 +179,10 @@ def _misfit(p, x, tgt, nsteps, pv, dtype=torch.float64, segment=None, t0_dir=Non
     return 0.5 * ((out[0] - tgt) ** 2).sum()
 
 
-def _grads(p, x, tgt, nsteps, dtype=torch.float64, segment=None):
+def _grads(p, x, tgt, nsteps, dtype=torch.float64, segment=0, graphs=True):
     pv = torch.tensor([p.delta, p.kappa, p.epsb], dtype=torch.float64, requires_grad=True)
     x0 = dev(x, dtype).requires_grad_(True)
-    out = adjoint.rollout(x0, p, nsteps, param_values=pv, segment=segment)
+    out = adjoint.rollout(x0, p, nsteps, param_values=pv, segment=segment, graphs=graphs)
     loss = 0.5 * ((out[0] - tgt) ** 2).sum()
     loss.backward()
     return pv.grad.clone(), x0.grad.clone(), float(loss.detach())
@@ -228,15 +228,37 @@ def test_rollout_matches_unrolled_autograd():
     assert np.abs(gx.cpu().numpy() - ref).max() <= 1e-9 * np.abs(ref).max()
 
 
-def test_checkpoint_spacing_invariant():
+def test_checkpoint_spacing_and_graphs_invariant():
+    """Checkpoint spacing (keep-all, 5, sqrt N, one segment) and graph vs
+    direct launches change nothing but the parameter sums' atomic order."""
     n = 24
     p, x, tgt = _misfit_setup(nsteps=n)
     ref_p, ref_x, ref_l = _grads(p, x, tgt, n, segment=n)
-    for seg in (1, 5, None):
-        gp_, gx_, l_ = _grads(p, x, tgt, n, segment=seg)
+    for seg, graphs in ((1, True), (5, True), (0, True), (0, False), (7, False)):
+        gp_, gx_, l_ = _grads(p, x, tgt, n, segment=seg, graphs=graphs)
         assert l_ == ref_l
         assert torch.equal(gx_, ref_x)
         assert torch.allclose(gp_, ref_p, rtol=1e-12, atol=0)
+
+
+def test_rollout_handle_reuse_with_new_values():
+    """One handle, two forward/backward rounds with different parameter values
+    and step origins: the captured graphs read the new values."""
+    n = 12
+    p, x, tgt = _misfit_setup(nsteps=n)
+    run = adjoint.Rollout(p, n)
+    res = []
+    for vals, s0 in (([p.delta, p.kappa, p.epsb], 0), ([0.03, 1.7, 0.011], 40)):
+        pv = torch.tensor(vals, dtype=torch.float64, requires_grad=True)
+        x0 = dev(x).requires_grad_(True)
+        out = adjoint.rollout(x0, p, n, param_values=pv, step0=s0, runner=run)
+        (0.5 * ((out[0] - tgt) ** 2).sum()).backward()
+        fresh = adjoint.rollout(dev(x), p.replace(delta=vals[0], kappa=vals[1], epsb=vals[2]), n, step0=s0,
+                                graphs=False)
+        assert torch.equal(out.detach(), fresh)
+        res.append(pv.grad.clone())
+    assert not torch.equal(res[0], res[1])
+    run.close()
 
 
 def test_fp32_adjoint_tracks_fp64():
@@ -279,15 +301,22 @@ def test_graingrowth_rollout_gradients():
 
 
 def test_invalid_arguments():
+    import ctypes
     p = kob_params()
     st = adjoint.Stepper(p)
     x = dev(kob_state(p))
     lib = amps.lib()
-    import ctypes
-    # in-place forward and a missing workspace are refused
+    # in-place forward and adjoint are refused
     assert lib.amps_step_forward(ctypes.byref(st.params), amps.F64, ctypes.c_void_p(x.data_ptr()),
-                                 ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(st.work.data_ptr()), 0, None) != 0
-    assert lib.amps_step_forward(ctypes.byref(st.params), amps.F64, ctypes.c_void_p(x.data_ptr()),
-                                 ctypes.c_void_p(x.data_ptr() + 8), None, 0, None) != 0
-    sp = amps.Params.preset(amps.SINTERING, 0, nx=64, ny=64, tile=16)
-    assert lib.amps_adjoint_workspace_bytes(ctypes.byref(sp), amps.F64) == 0
+                                 ctypes.c_void_p(x.data_ptr()), 0, None) == 1
+    gp = torch.zeros(3, dtype=torch.float64, device=DEV)
+    assert lib.amps_step_adjoint(ctypes.byref(st.params), amps.F64, ctypes.c_void_p(x.data_ptr()),
+                                 ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(x.data_ptr()),
+                                 ctypes.c_void_p(gp.data_ptr()), 0, None) == 1
+    # backward before forward
+    run = adjoint.Rollout(p, 4)
+    with pytest.raises(amps.AmpsError):
+        run.backward(torch.zeros_like(x))
+    with pytest.raises(ValueError):
+        run.forward(x.float())
+    run.close()

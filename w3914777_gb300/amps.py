@@ -127,9 +127,15 @@ def lib():
             "amps_set_profiling": ([vp, ip], ip),
             "amps_get_kernel_times": ([vp, ctypes.POINTER(dp), ctypes.POINTER(ctypes.c_int64),
                                        ctypes.POINTER(ctypes.c_int64)], ip),
-            "amps_adjoint_workspace_bytes": ([P, ip], ctypes.c_size_t),
-            "amps_step_forward": ([P, ip, vp, vp, vp, ctypes.c_int64, vp], ip),
-            "amps_step_adjoint": ([P, ip, vp, vp, vp, vp, vp, ctypes.c_int64, vp], ip),
+            "amps_step_forward": ([P, ip, vp, vp, ctypes.c_int64, vp], ip),
+            "amps_step_adjoint": ([P, ip, vp, vp, vp, vp, ctypes.c_int64, vp], ip),
+            "amps_adjoint_memory_bytes": ([P, ip, ip, ip], ctypes.c_size_t),
+            "amps_adjoint_create": ([P, ip, ip, ip, ctypes.POINTER(vp)], ip),
+            "amps_adjoint_destroy": ([vp], ip), "amps_adjoint_set_stream": ([vp, vp], ip),
+            "amps_adjoint_set_graphs": ([vp, ip], ip), "amps_adjoint_segment": ([vp], ip),
+            "amps_adjoint_last_error": ([vp], ctypes.c_char_p),
+            "amps_adjoint_forward": ([vp, ctypes.POINTER(dp), vp, vp, ctypes.c_int64], ip),
+            "amps_adjoint_backward": ([vp, vp, vp, vp], ip),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
