@@ -358,10 +358,86 @@ def run_ours(args):
         }
         if cpu:
             line["cpu_baseline"] = cpu
+        if not args.no_adjoint:
+            line["adjoint"] = run_adjoint()
         print(json.dumps(line), flush=True)
     sim.close()
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def run_adjoint(steps=1000, segment=32, n=256):
+    """Checkpointed adjoint on the 256^2 Kobayashi dendrite (zero-flux, noise),
+    1000 FP32 steps, 32-step checkpoints; loss = L2 misfit of phi against the
+    FP64 forward with delta = 0.04, K = 1.8.  Times the forward and backward
+    sweeps (CUDA events, median of 3), the keep-every-state variant and one
+    eager step of each; checks the FP32 gradients against FP64 ones and the
+    FP64 delta-gradient against a central difference (h = 1e-4 delta)."""
+    import torch
+    from w3914777_gb300 import adjoint, amps
+
+    p = amps.Params.preset(amps.KOBAYASHI, 0, nx=n, ny=n)
+    x = amps.init_host(p, amps.INIT_REFERENCE)
+    base = [p.delta, p.kappa, p.epsb]
+
+    def med(fn, reps=3):
+        fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn()
+            b.record()
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b))
+        return statistics.median(ts)
+
+    x64 = torch.tensor(x, device="cuda")
+    tgt = adjoint.Rollout(p, steps, torch.float64, segment).forward(x64, [0.04, 1.8, p.epsb])[0]
+
+    def grads(dtype, seg):
+        run = adjoint.Rollout(p, steps, dtype, seg)
+        pv = torch.tensor(base, dtype=torch.float64, requires_grad=True)
+        x0 = torch.tensor(x, dtype=dtype, device="cuda", requires_grad=True)
+        out = adjoint.rollout(x0, p, steps, param_values=pv, runner=run)
+        loss = 0.5 * ((out[0].double() - tgt) ** 2).sum()
+        loss.backward()
+        g = torch.cat([pv.grad, x0.grad[1].double().flatten().cpu()])
+        x0d = x0.detach()
+        gf = torch.ones_like(x0d)
+        tf = med(lambda: run.forward(x0d, base))
+        tb = med(lambda: run.backward(gf))
+        run.close()
+        return g, tf, tb, float(loss.detach())
+
+    g32, tf32, tb32, _ = grads(torch.float32, segment)
+    _, tf_all, tb_all, _ = grads(torch.float32, 1)
+    g64, tf64, tb64, _ = grads(torch.float64, segment)
+    rel32 = float(((g32[:3] - g64[:3]).abs() / g64[:3].abs()).max())
+    relT0 = float((g32[3:] - g64[3:]).norm() / g64[3:].norm())
+    run64 = adjoint.Rollout(p, steps, torch.float64, segment)
+    h = 1e-4 * p.delta
+    lp = float(0.5 * ((run64.forward(x64, [p.delta + h, p.kappa, p.epsb])[0] - tgt) ** 2).sum())
+    lm = float(0.5 * ((run64.forward(x64, [p.delta - h, p.kappa, p.epsb])[0] - tgt) ** 2).sum())
+    fd = (lp - lm) / (2 * h)
+    run64.close()
+    st = adjoint.Stepper(p, torch.float32)
+    xs = torch.tensor(x, dtype=torch.float32, device="cuda")
+    ys, gs, gi = torch.empty_like(xs), torch.ones_like(xs), torch.empty_like(xs)
+    gp = torch.zeros(3, dtype=torch.float64, device="cuda")
+    t_sf = med(lambda: [st.forward(xs, 0, out=ys) for _ in range(50)]) / 50
+    t_sa = med(lambda: [st.adjoint(xs, gs, 0, gp, grad_in=gi) for _ in range(50)]) / 50
+    return {
+        "workload": f"Kobayashi dendrite {n}x{n} zero-flux + noise, {steps} steps FP32, "
+                    f"{segment}-step checkpoints; grads w.r.t. delta, K, epsb, T0",
+        "forward_sweep_ms": tf32, "backward_sweep_ms": tb32, "ratio": tb32 / tf32,
+        "step_forward_us": t_sf * 1e3, "step_adjoint_us": t_sa * 1e3, "step_ratio": t_sa / t_sf,
+        "keep_all_states": {"forward_sweep_ms": tf_all, "backward_sweep_ms": tb_all, "ratio": tb_all / tf_all},
+        "fp64": {"forward_sweep_ms": tf64, "backward_sweep_ms": tb64, "ratio": tb64 / tf64},
+        "fp32_vs_fp64_param_grad_rel": rel32, "fp32_vs_fp64_T0_grad_rel_l2": relT0,
+        "fp64_delta_grad_vs_central_difference_rel": abs(float(g64[0]) - fd) / abs(fd),
+    }
 
 
 def run_profile_case(args):
@@ -391,6 +467,7 @@ def main():
     ap.add_argument("--ref-sample-steps", type=int, default=100)
     ap.add_argument("--tile", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--profile-case", type=int, default=0)
     args = ap.parse_args()
     if args.profile_case:
