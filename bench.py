@@ -360,6 +360,8 @@ def run_ours(args):
             line["cpu_baseline"] = cpu
         if not args.no_adjoint:
             line["adjoint"] = run_adjoint()
+        if not args.no_ensemble:
+            line["ensemble"] = run_ensemble()
         print(json.dumps(line), flush=True)
     sim.close()
     if world > 1:
@@ -440,6 +442,85 @@ def run_adjoint(steps=1000, segment=32, n=256):
     }
 
 
+def run_ensemble(steps=5000, check_steps=1000, count=64, seed=2024):
+    """64 grain-growth runs (sides 128..1024, Q in {4,8,12,16}, kappa ~ U[1,3],
+    L ~ U[0.5,2], per-member stable dt) advanced by one persistent launch per
+    step, at the autotuned monitor and thresholds.  Times `steps` steps of the
+    ensemble; compares, over `check_steps` steps, the same members run one
+    after another through amps_run, and the plain-FP64 ensemble (rate and
+    per-member max-abs error)."""
+    import torch
+    from w3914777_gb300 import amps, ensemble
+
+    tuned = load_tuned()
+    ov = dict(tuned["overrides"]) if tuned else {}
+    ov.pop("tile", None)
+    params = ensemble.member_params(count=count, seed=seed, overrides=ov)
+    cells = ensemble.cells(params)
+    stream = torch.cuda.Stream()
+
+    def timed(fn):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(stream)
+        fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b)
+
+    def build(ps):
+        sims = [amps.Simulation(p, init=amps.INIT_SEEDED) for p in ps]
+        for sm in sims:
+            sm.set_stream(stream.cuda_stream)
+        ens = amps.Ensemble(sims)
+        ens.set_stream(stream.cuda_stream)
+        return sims, ens
+
+    sims, ens = build(params)
+    ens.run(10)  # warm-up period: captures the graphs
+    ms = timed(lambda: ens.run(steps))
+    ens.synchronize()
+    stats = [sm.stats() for sm in sims]
+    ens.close()
+    for sm in sims:
+        sm.close()
+    # the same members, each through its own amps_run, one after another
+    sims = [amps.Simulation(p, init=amps.INIT_SEEDED) for p in params]
+    for sm in sims:
+        sm.set_stream(stream.cuda_stream)
+        sm.run(10)
+    ms_seq = timed(lambda: [sm.run(check_steps) for sm in sims])
+    for sm in sims:
+        sm.close()
+    # adaptive vs plain FP64 over check_steps
+    sims, ens = build(params)
+    ms_mix = timed(lambda: ens.run(check_steps))
+    mixed = [sm.fields() for sm in sims]
+    ens.close()
+    for sm in sims:
+        sm.close()
+    p64 = [p.replace(mode=amps.PUREHIGH, high_tier=amps.TIER_FP64) for p in params]
+    sims, ens = build(p64)
+    ms_64 = timed(lambda: ens.run(check_steps))
+    err = max(float(np.abs(sm.fields() - f).max()) for sm, f in zip(sims, mixed))
+    ens.close()
+    for sm in sims:
+        sm.close()
+    ts = np.sum([st["tile_steps"] for st in stats], axis=0)
+    return {
+        "workload": f"{count} grain-growth runs, sides 128..1024 (multiples of 32), Q in {{4,8,12,16}}, "
+                    f"kappa~U[1,3], L~U[0.5,2], dt=min(0.05, 0.9*2/(12 L kappa)), seeded eta~U[-1e-3,1e-3], "
+                    f"{steps} steps, one persistent tile-queue launch per step",
+        "members": count, "cells_per_step": cells,
+        "value": cells * steps / (ms * 1e-3) / 1e9, "unit": "Gcell-updates/s", "ms": ms,
+        "sequential_amps_run": {"value": cells * check_steps / (ms_seq * 1e-3) / 1e9, "steps": check_steps},
+        "plain_fp64": {"value": cells * check_steps / (ms_64 * 1e-3) / 1e9, "steps": check_steps},
+        "speedup_vs_plain_fp64": ms_64 / ms_mix,
+        "max_abs_err_vs_fp64": err, "err_steps": check_steps,
+        "tier_mix": {k: float(v) / float(ts.sum()) for k, v in zip(("half", "fp32", "fp64"), ts)},
+    }
+
+
 def run_profile_case(args):
     """A short, untimed run of the tuned workload at nx^2 for ncu captures
     (`--profile-case 2048` puts a 256 MiB FP32 state, larger than L2)."""
@@ -468,6 +549,7 @@ def main():
     ap.add_argument("--tile", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--profile-case", type=int, default=0)
     args = ap.parse_args()
     if args.profile_case:

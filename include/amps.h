@@ -292,6 +292,30 @@ AMPS_API int amps_adjoint_forward(amps_adjoint *a, const double *param_values, c
                                   int64_t step0);
 AMPS_API int amps_adjoint_backward(amps_adjoint *a, const void *grad_final, void *grad_state0, double *grad_params);
 
+/* ---- ensembles of grain-growth runs --------------------------------------
+ * No counterpart in the reference (one run per process there).  Advances
+ * `count` grain-growth handles in lockstep: each step is one persistent
+ * launch whose CTAs take (member, tile) work items from a queue ordered by
+ * cost, so members of different sizes, field counts, parameters and tier
+ * maps share the GPU; the members' period-end classifications are one
+ * batched launch, and each cadence period is replayed from a CUDA graph.
+ * Every member keeps its own parameters (dt, mobil, grcoef, gamma,
+ * thresholds...), tier maps, statistics and step counter, and gives the same
+ * results as amps_run on it alone.  Members must share tile, cadence, mode
+ * class (adaptive or not) and ref_order, and stand at the same phase of the
+ * cadence; they stay owned by the caller and must outlive the ensemble; do
+ * not run them individually while the ensemble is in use.  Work is queued
+ * on the ensemble's stream (set_stream; NULL = default stream). */
+typedef struct amps_ensemble amps_ensemble;
+AMPS_API int amps_ensemble_create(amps_handle *const *members, int count, amps_ensemble **out);
+AMPS_API int amps_ensemble_destroy(amps_ensemble *e);
+AMPS_API int amps_ensemble_set_stream(amps_ensemble *e, void *stream);
+AMPS_API int amps_ensemble_set_graphs(amps_ensemble *e, int enable);
+AMPS_API int amps_ensemble_run(amps_ensemble *e, int nsteps);
+/* Waits for the ensemble's work; reports NaN/Inf or a timed-out wait of any member. */
+AMPS_API int amps_ensemble_synchronize(amps_ensemble *e);
+AMPS_API const char *amps_ensemble_last_error(const amps_ensemble *e);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,122 @@
+"""Ensemble of grain-growth runs (amps_ensemble_*): one persistent launch per
+step over every member's tiles must give each member exactly the results
+amps_run gives it alone -- fields, tier maps, statistics -- for members of
+different sizes, field counts, coefficients and time steps, in adaptive and
+plain modes, over whole and partial cadence periods, with and without
+graphs."""
+import numpy as np
+import pytest
+
+from w3914777_gb300 import amps, ensemble
+
+pytestmark = pytest.mark.gpu
+
+MIXED = dict(mode=amps.END2END_MIX, monitor=amps.MONITOR_RATE, monitor_samples=1, monitor_field=-1)
+_THR = []
+
+
+def mixed():
+    """MIXED with thresholds at the 40% / 75% quantiles of one probe member's
+    tile metrics after a period, so that the members mix all three tiers."""
+    if not _THR:
+        p = small_members(dict(MIXED, thr_lo=0.0, thr_hi=0.0))[2]
+        with amps.Simulation(p, init=amps.INIT_SEEDED) as s:
+            s.run(10)
+            m = s.metric().ravel()
+        _THR.extend([float(np.quantile(m, 0.4)), float(np.quantile(m, 0.75))])
+    return dict(MIXED, thr_lo=_THR[0], thr_hi=_THR[1])
+
+
+def small_members(extra=None):
+    specs = [(64, 4, 2.0, 1.0), (96, 2, 1.3, 1.7), (128, 8, 2.7, 0.6), (64, 12, 1.1, 1.9), (32, 3, 2.2, 1.2)]
+    out = []
+    for i, (side, q, kap, mob) in enumerate(specs):
+        p = amps.Params.preset(amps.GRAINGROWTH, 0, nx=side, ny=side, nfields=q, grcoef=kap, mobil=mob, tile=32,
+                               seed=100 + i, init_amp=0.3)
+        p.dt = ensemble.stable_dt(mob, kap)
+        for k, v in (extra or {}).items():
+            setattr(p, k, v)
+        out.append(p)
+    return out
+
+
+def run_alone(params, steps):
+    res = []
+    for p in params:
+        with amps.Simulation(p, init=amps.INIT_SEEDED) as s:
+            s.run(steps)
+            s.synchronize()
+            res.append((s.fields(), s.tiers(), s.stats()))
+    return res
+
+
+def run_together(params, steps, graphs=True, chunks=None):
+    sims = [amps.Simulation(p, init=amps.INIT_SEEDED) for p in params]
+    with amps.Ensemble(sims, graphs=graphs) as ens:
+        for c in (chunks or [steps]):
+            ens.run(c)
+        ens.synchronize()
+    res = [(s.fields(), s.tiers(), s.stats()) for s in sims]
+    for s in sims:
+        s.close()
+    return res
+
+
+@pytest.mark.parametrize("graphs", [True, False])
+def test_ensemble_matches_individual_runs_adaptive(graphs):
+    params = small_members(mixed())
+    alone = run_alone(params, 37)
+    together = run_together(params, 37, graphs=graphs, chunks=[20, 3, 14])
+    for (fa, ta, sa), (fb, tb, sb) in zip(alone, together):
+        assert np.array_equal(fa, fb)
+        assert np.array_equal(ta, tb)
+        assert sa == sb
+    # the thresholds must actually mix tiers for this to test anything (the
+    # FP32 tile path is covered by the plain FP32 case)
+    mix = np.concatenate([t.ravel() for _, t, _ in alone])
+    assert len(np.unique(mix)) >= 2
+
+
+@pytest.mark.parametrize("tier", [amps.TIER_FP32, amps.TIER_FP64])
+def test_ensemble_matches_individual_runs_plain(tier):
+    params = small_members(dict(mode=amps.PUREHIGH, high_tier=tier))
+    alone = run_alone(params, 23)
+    together = run_together(params, 23)
+    for (fa, _, sa), (fb, _, sb) in zip(alone, together):
+        # the all-FP64 single run uses the staged FP64 kernel, the ensemble the
+        # fused kernel's FP64 tile path: same arithmetic, rounding may differ
+        if tier == amps.TIER_FP64:
+            assert np.abs(fa - fb).max() <= 1e-13
+        else:
+            assert np.array_equal(fa, fb)
+        assert sa["steps"] == sb["steps"]
+
+
+def test_ensemble_members_keep_their_own_step_counters_and_stats():
+    params = small_members(mixed())
+    sims = [amps.Simulation(p, init=amps.INIT_SEEDED) for p in params]
+    with amps.Ensemble(sims) as ens:
+        ens.run(30)
+        ens.synchronize()
+    for s, p in zip(sims, params):
+        st = s.stats()
+        assert st["steps"] == 30
+        assert sum(st["tile_steps"]) == 30 * (p.nx // 32) * (p.ny // 32)
+        assert st["monitor_evals"] == 1 + 3  # the classification at init, then one per period
+        s.close()
+
+
+def test_ensemble_rejects_incompatible_members():
+    a = amps.Simulation(small_members(mixed())[0], init=amps.INIT_SEEDED)
+    b = amps.Simulation(amps.Params.preset(amps.GRAINGROWTH, 0, nx=64, ny=64, nfields=2, tile=16, **mixed()),
+                        init=amps.INIT_SEEDED)
+    k = amps.Simulation(amps.Params.preset(amps.KOBAYASHI, 0, nx=64, ny=64, tile=32), init=amps.INIT_REFERENCE)
+    for members in ([a, b], [a, a], [a, k]):
+        with pytest.raises(amps.AmpsError):
+            amps.Ensemble(members)
+    a.run(3)  # a different phase of the cadence
+    c = amps.Simulation(small_members(mixed())[1], init=amps.INIT_SEEDED)
+    with pytest.raises(amps.AmpsError):
+        amps.Ensemble([a, c])
+    for s in (a, b, k, c):
+        s.close()

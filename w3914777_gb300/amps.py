@@ -136,6 +136,10 @@ def lib():
             "amps_adjoint_last_error": ([vp], ctypes.c_char_p),
             "amps_adjoint_forward": ([vp, ctypes.POINTER(dp), vp, vp, ctypes.c_int64], ip),
             "amps_adjoint_backward": ([vp, vp, vp, vp], ip),
+            "amps_ensemble_create": ([ctypes.POINTER(vp), ip, ctypes.POINTER(vp)], ip),
+            "amps_ensemble_destroy": ([vp], ip), "amps_ensemble_set_stream": ([vp, vp], ip),
+            "amps_ensemble_set_graphs": ([vp, ip], ip), "amps_ensemble_run": ([vp, ip], ip),
+            "amps_ensemble_synchronize": ([vp], ip), "amps_ensemble_last_error": ([vp], ctypes.c_char_p),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -287,3 +291,51 @@ class Simulation:
         ts = (ctypes.c_int64 * 4)()
         self._ck(lib().amps_get_kernel_times(self.h, ms, la, ts), "amps_get_kernel_times")
         return list(ms), list(la), list(ts)
+
+
+class Ensemble:
+    """Grain-growth `Simulation`s advanced in lockstep by one persistent
+    kernel per step (amps_ensemble_*).  The members stay usable for reads
+    (fields, tiers, stats) and must outlive the ensemble."""
+
+    def __init__(self, members, graphs=True):
+        self.members = list(members)
+        arr = (ctypes.c_void_p * len(self.members))(*[m.h.value for m in self.members])
+        h = ctypes.c_void_p()
+        rc = lib().amps_ensemble_create(arr, len(self.members), ctypes.byref(h))
+        if rc != 0:
+            raise AmpsError(rc, "amps_ensemble_create: " + lib().amps_ensemble_last_error(None).decode())
+        self.h = h
+        if not graphs:
+            lib().amps_ensemble_set_graphs(self.h, 0)
+
+    def _ck(self, rc, what):
+        if rc != 0:
+            raise AmpsError(rc, f"{what}: {lib().amps_ensemble_last_error(self.h).decode()}")
+
+    def set_stream(self, stream_ptr):
+        self._ck(lib().amps_ensemble_set_stream(self.h, ctypes.c_void_p(stream_ptr)), "amps_ensemble_set_stream")
+
+    def run(self, nsteps):
+        self._ck(lib().amps_ensemble_run(self.h, int(nsteps)), "amps_ensemble_run")
+        return self
+
+    def synchronize(self):
+        self._ck(lib().amps_ensemble_synchronize(self.h), "amps_ensemble_synchronize")
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().amps_ensemble_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

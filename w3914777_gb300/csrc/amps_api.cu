@@ -15,7 +15,9 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <map>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -497,16 +499,18 @@ extern "C" int amps_get_fields(amps_handle *h, void *dst, int dtype, int on_devi
 }
 
 // -------------------------------------------------------------- time loop ----
-static int launch_step(amps_handle *h, int step_off, bool monitor_now)
+// Arguments of the step at offset step_off of a period, from parity
+// `parity` (transition: this step reads tiles at their previous tier).
+static StepArgs step_args(const amps_handle *h, int parity, bool transition, int step_off, bool monitor_now)
 {
     const amps_params &p = h->p;
     StepArgs a;
     memset(&a, 0, sizeof a);
     for (int t = 0; t < 3; ++t) {
-        a.in[t] = h->store[t][h->parity];
-        a.out[t] = h->store[t][h->parity ^ 1];
+        a.in[t] = h->store[t][parity];
+        a.out[t] = h->store[t][parity ^ 1];
     }
-    a.tier_in = h->transition ? h->d_tier_prev : h->d_tier_cur;
+    a.tier_in = transition ? h->d_tier_prev : h->d_tier_cur;
     a.tier_out = h->d_tier_cur;
     a.count = h->d_counts;
     a.nx = p.nx; a.ny = p.ny; a.ntx = h->ntx; a.nty = h->nty; a.nf = h->nf; a.bc = p.bc; a.stencil = p.stencil;
@@ -523,6 +527,13 @@ static int launch_step(amps_handle *h, int step_off, bool monitor_now)
     a.step_base = h->d_step_base;
     a.step_off = step_off;
     a.ph = make_phys(p);
+    return a;
+}
+
+static int launch_step(amps_handle *h, int step_off, bool monitor_now)
+{
+    const amps_params &p = h->p;
+    StepArgs a = step_args(h, h->parity, h->transition, step_off, monitor_now);
     const bool ref = p.ref_order != 0;
     if (p.model == AMPS_GRAINGROWTH) {
         // one fused launch covers every tier
@@ -569,6 +580,18 @@ static int launch_step(amps_handle *h, int step_off, bool monitor_now)
     return AMPS_OK;
 }
 
+static ClassifyArgs classify_args(const amps_handle *h, int advance, int stat_steps)
+{
+    const amps_params &p = h->p;
+    ClassifyArgs c{};
+    c.metric = h->d_metric; c.tier_prev = h->d_tier_prev; c.tier_cur = h->d_tier_cur;
+    c.lists = h->d_lists; c.counts = h->d_counts; c.ntx = h->ntx; c.nty = h->nty;
+    c.thr_lo = p.thr_lo; c.thr_hi = p.thr_hi; c.high_tier = p.high_tier; c.use_mid = h->use_mid;
+    c.stats = h->d_stats; c.log = h->d_log; c.log_n = h->d_log_n; c.max_log = p.max_log;
+    c.step_base = h->d_step_base; c.advance = advance; c.stat_steps = stat_steps;
+    return c;
+}
+
 // Steps [k0, k0+cnt) of a period, then the period's bookkeeping.
 static int enqueue_chunk(amps_handle *h, int k0, int cnt)
 {
@@ -580,13 +603,7 @@ static int enqueue_chunk(amps_handle *h, int k0, int cnt)
         if (r) return r;
     }
     if (h->mixed && period_end) {
-        ClassifyArgs c{};
-        c.metric = h->d_metric; c.tier_prev = h->d_tier_prev; c.tier_cur = h->d_tier_cur;
-        c.lists = h->d_lists; c.counts = h->d_counts; c.ntx = h->ntx; c.nty = h->nty;
-        c.thr_lo = p.thr_lo; c.thr_hi = p.thr_hi; c.high_tier = p.high_tier; c.use_mid = h->use_mid;
-        c.stats = h->d_stats; c.log = h->d_log; c.log_n = h->d_log_n; c.max_log = p.max_log;
-        c.step_base = h->d_step_base; c.advance = p.cadence; c.stat_steps = cnt;
-        CK(h, classify(c, h->stream));
+        CK(h, classify(classify_args(h, p.cadence, cnt), h->stream));
         h->transition = true;
     } else {
         CK(h, advance_period(h->d_step_base, period_end ? p.cadence : 0, cnt, h->d_counts, h->d_stats, h->stream));
@@ -748,6 +765,257 @@ extern "C" int amps_get_kernel_times(amps_handle *h, double *ms, int64_t *launch
         } else if (tile_steps) {
             tile_steps[3] = total;
         }
+    }
+    return AMPS_OK;
+}
+
+// -------------------------------------------------------------- ensembles ----
+// Many grain-growth handles advanced in lockstep: every step is ONE
+// persistent launch over the (member, tile) work items of all members, and
+// the period-end classification of all members is one batched launch.  A
+// whole cadence period is captured once per (parity, transition) pattern of
+// the members and replayed.
+struct amps_ensemble {
+    std::vector<amps_handle *> m;
+    int T = 0, cad = 0, maxnf = 0;
+    bool ref = false, mixed = false;
+    cudaStream_t stream = nullptr, capture = nullptr;
+    int2 *d_items = nullptr;
+    int nitems = 0, grid = 0;
+    size_t smem = 0;
+    int *d_queue = nullptr;
+    ClassifyArgs *d_cls = nullptr;      // whole periods: advance = stat_steps = cadence
+    ClassifyArgs *d_cls_tmp = nullptr;  // partial periods (eager)
+    StepArgs *d_tmp = nullptr;          // partial periods (eager): cadence x members
+    bool graphs = true;
+    struct Period {
+        StepArgs *table = nullptr;
+        cudaGraphExec_t exec = nullptr;
+    };
+    std::map<std::vector<uint8_t>, Period> periods;
+    std::string err;
+};
+
+#define EFAIL(e, code, ...)                                        \
+    do {                                                           \
+        char _b[512];                                              \
+        snprintf(_b, sizeof _b, __VA_ARGS__);                      \
+        (e)->err = _b;                                             \
+        return (code);                                             \
+    } while (0)
+#define ECK(e, call)                                                                              \
+    do {                                                                                          \
+        cudaError_t _e = (call);                                                                  \
+        if (_e != cudaSuccess) EFAIL(e, AMPS_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(_e)); \
+    } while (0)
+
+static void ens_free(amps_ensemble *e)
+{
+    for (auto &kv : e->periods) {
+        if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+        if (kv.second.table) cudaFree(kv.second.table);
+    }
+    e->periods.clear();
+    cudaFree(e->d_items);
+    cudaFree(e->d_queue);
+    cudaFree(e->d_cls);
+    cudaFree(e->d_cls_tmp);
+    cudaFree(e->d_tmp);
+    if (e->capture) cudaStreamDestroy(e->capture);
+}
+
+extern "C" int amps_ensemble_create(amps_handle *const *members, int count, amps_ensemble **out)
+{
+    if (!out) return AMPS_ERR_INVALID;
+    *out = nullptr;
+    if (!members || count < 1) return AMPS_ERR_INVALID;
+    amps_handle *h0 = members[0];
+    for (int i = 0; i < count; ++i) {
+        amps_handle *h = members[i];
+        if (!h || h->p.model != AMPS_GRAINGROWTH || h->T != h0->T || h->p.cadence != h0->p.cadence ||
+            h->mixed != h0->mixed || (h->p.ref_order != 0) != (h0->p.ref_order != 0) ||
+            h->step % h->p.cadence != h0->step % h0->p.cadence)
+            return AMPS_ERR_INVALID;
+        for (int j = 0; j < i; ++j)
+            if (members[j] == h) return AMPS_ERR_INVALID;
+    }
+    amps_ensemble *e = new (std::nothrow) amps_ensemble;
+    if (!e) return AMPS_ERR_ALLOC;
+    e->m.assign(members, members + count);
+    e->T = h0->T;
+    e->cad = h0->p.cadence;
+    e->mixed = h0->mixed;
+    e->ref = h0->p.ref_order != 0;
+    // work items: members with more fields first (costliest tiles first)
+    std::vector<int> order(count);
+    for (int i = 0; i < count; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return members[a]->nf > members[b]->nf; });
+    std::vector<int2> items;
+    for (int i : order) {
+        e->maxnf = std::max(e->maxnf, members[i]->nf);
+        for (int t = 0; t < members[i]->ntiles; ++t) items.push_back(make_int2(i, t));
+    }
+    e->nitems = (int)items.size();
+    std::vector<ClassifyArgs> cls(count);
+    for (int i = 0; i < count; ++i) cls[i] = classify_args(members[i], e->cad, e->cad);
+    int bps = 0, sms = 0, dev = 0;
+    e->smem = gg_ens_smem_bytes(e->T, e->maxnf);
+    cudaError_t ce = gg_prepare_ens(e->T, e->ref, e->maxnf, &bps);
+    if (ce == cudaSuccess) ce = cudaGetDevice(&dev);
+    if (ce == cudaSuccess) ce = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (ce == cudaSuccess && bps < 1) ce = cudaErrorInvalidConfiguration;
+    e->grid = std::max(1, std::min(e->nitems, bps * sms));
+    if (ce == cudaSuccess) ce = cudaMalloc(&e->d_items, sizeof(int2) * items.size());
+    if (ce == cudaSuccess) ce = cudaMalloc(&e->d_queue, 2 * sizeof(int));
+    if (ce == cudaSuccess) ce = cudaMalloc(&e->d_cls, sizeof(ClassifyArgs) * count);
+    if (ce == cudaSuccess) ce = cudaMalloc(&e->d_cls_tmp, sizeof(ClassifyArgs) * count);
+    if (ce == cudaSuccess) ce = cudaMalloc(&e->d_tmp, sizeof(StepArgs) * (size_t)count * e->cad);
+    if (ce == cudaSuccess) ce = cudaMemcpy(e->d_items, items.data(), sizeof(int2) * items.size(), cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) ce = cudaMemset(e->d_queue, 0, 2 * sizeof(int));
+    if (ce == cudaSuccess) ce = cudaMemcpy(e->d_cls, cls.data(), sizeof(ClassifyArgs) * count, cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&e->capture, cudaStreamNonBlocking);
+    if (ce != cudaSuccess) {
+        g_create_err = std::string("amps_ensemble_create: ") + cudaGetErrorString(ce);
+        cudaGetLastError();
+        ens_free(e);
+        delete e;
+        return ce == cudaErrorMemoryAllocation ? AMPS_ERR_ALLOC : AMPS_ERR_CUDA;
+    }
+    *out = e;
+    return AMPS_OK;
+}
+
+extern "C" int amps_ensemble_destroy(amps_ensemble *e)
+{
+    if (!e) return AMPS_ERR_INVALID;
+    cudaStreamSynchronize(e->stream);
+    ens_free(e);
+    delete e;
+    return AMPS_OK;
+}
+
+extern "C" int amps_ensemble_set_stream(amps_ensemble *e, void *stream)
+{
+    if (!e) return AMPS_ERR_INVALID;
+    e->stream = (cudaStream_t)stream;
+    return AMPS_OK;
+}
+
+extern "C" int amps_ensemble_set_graphs(amps_ensemble *e, int enable)
+{
+    if (!e) return AMPS_ERR_INVALID;
+    e->graphs = enable != 0;
+    return AMPS_OK;
+}
+
+extern "C" const char *amps_ensemble_last_error(const amps_ensemble *e)
+{
+    return e ? e->err.c_str() : g_create_err.c_str();
+}
+
+// Step tables of steps [k0, k0+cnt) of a period for every member, from the
+// members' current host-side parity/transition (table[s * M + i]).
+static std::vector<StepArgs> ens_tables(const amps_ensemble *e, int k0, int cnt)
+{
+    const int M = (int)e->m.size();
+    const bool period_end = k0 + cnt == e->cad;
+    std::vector<StepArgs> t((size_t)cnt * M);
+    for (int i = 0; i < M; ++i) {
+        const amps_handle *h = e->m[i];
+        int par = h->parity;
+        bool tr = h->transition;
+        for (int s = 0; s < cnt; ++s) {
+            const bool mon = e->mixed && period_end && s == cnt - 1;
+            t[(size_t)s * M + i] = step_args(h, par, tr, k0 + s, mon);
+            par ^= 1;
+            tr = false;
+        }
+    }
+    return t;
+}
+
+static int ens_enqueue(amps_ensemble *e, const StepArgs *table, const ClassifyArgs *cls, int cnt, bool period_end,
+                       cudaStream_t s)
+{
+    const int M = (int)e->m.size();
+    for (int k = 0; k < cnt; ++k)
+        ECK(e, gg_launch_ens(e->T, e->ref, table + (size_t)k * M, e->d_items, e->nitems, e->d_queue, e->grid, e->smem, s));
+    if (e->mixed && period_end) ECK(e, classify_batch(cls, M, s));
+    else ECK(e, advance_batch(cls, M, s));
+    return AMPS_OK;
+}
+
+static void ens_advance_host(amps_ensemble *e, int cnt, bool period_end)
+{
+    for (amps_handle *h : e->m) {
+        if (cnt & 1) h->parity ^= 1;
+        if (cnt > 0) h->transition = e->mixed && period_end;
+        h->step += cnt;
+    }
+}
+
+extern "C" int amps_ensemble_run(amps_ensemble *e, int nsteps)
+{
+    if (!e || nsteps < 0) return AMPS_ERR_INVALID;
+    const int M = (int)e->m.size();
+    for (amps_handle *h : e->m) {
+        if (h->step % e->cad != e->m[0]->step % e->cad)
+            EFAIL(e, AMPS_ERR_INVALID, "ensemble members are at different phases of the monitor cadence");
+        ECK(e, cudaStreamSynchronize(h->stream));  // members' own queued work first
+    }
+    while (nsteps > 0) {
+        const int k0 = (int)(e->m[0]->step % e->cad);
+        const int cnt = nsteps < e->cad - k0 ? nsteps : e->cad - k0;
+        const bool period_end = k0 + cnt == e->cad;
+        if (e->graphs && k0 == 0 && cnt == e->cad) {
+            std::vector<uint8_t> key(M);
+            for (int i = 0; i < M; ++i) key[i] = (uint8_t)(e->m[i]->parity | (e->m[i]->transition ? 2 : 0));
+            auto it = e->periods.find(key);
+            if (it == e->periods.end()) {
+                amps_ensemble::Period per;
+                std::vector<StepArgs> tab = ens_tables(e, 0, cnt);
+                ECK(e, cudaMalloc(&per.table, sizeof(StepArgs) * tab.size()));
+                it = e->periods.emplace(key, per).first;
+                ECK(e, cudaMemcpy(it->second.table, tab.data(), sizeof(StepArgs) * tab.size(), cudaMemcpyHostToDevice));
+                cudaGraph_t gr = nullptr;
+                ECK(e, cudaStreamBeginCapture(e->capture, cudaStreamCaptureModeThreadLocal));
+                const int r = ens_enqueue(e, it->second.table, e->d_cls, cnt, true, e->capture);
+                const cudaError_t ce = cudaStreamEndCapture(e->capture, &gr);
+                if (r) return r;
+                if (ce != cudaSuccess) EFAIL(e, AMPS_ERR_CUDA, "ensemble graph capture: %s", cudaGetErrorString(ce));
+                const cudaError_t ci = cudaGraphInstantiate(&it->second.exec, gr, 0);
+                cudaGraphDestroy(gr);
+                if (ci != cudaSuccess) {
+                    it->second.exec = nullptr;
+                    EFAIL(e, AMPS_ERR_CUDA, "ensemble graph instantiate: %s", cudaGetErrorString(ci));
+                }
+            }
+            ECK(e, cudaGraphLaunch(it->second.exec, e->stream));
+        } else {
+            // partial period: upload this chunk's tables into the scratch slots once they are free
+            std::vector<StepArgs> tab = ens_tables(e, k0, cnt);
+            std::vector<ClassifyArgs> cls(M);
+            for (int i = 0; i < M; ++i) cls[i] = classify_args(e->m[i], period_end ? e->cad : 0, cnt);
+            ECK(e, cudaStreamSynchronize(e->stream));
+            ECK(e, cudaMemcpy(e->d_tmp, tab.data(), sizeof(StepArgs) * tab.size(), cudaMemcpyHostToDevice));
+            ECK(e, cudaMemcpy(e->d_cls_tmp, cls.data(), sizeof(ClassifyArgs) * M, cudaMemcpyHostToDevice));
+            if (int r = ens_enqueue(e, e->d_tmp, e->d_cls_tmp, cnt, period_end, e->stream)) return r;
+        }
+        ens_advance_host(e, cnt, period_end);
+        nsteps -= cnt;
+    }
+    return AMPS_OK;
+}
+
+extern "C" int amps_ensemble_synchronize(amps_ensemble *e)
+{
+    if (!e) return AMPS_ERR_INVALID;
+    ECK(e, cudaStreamSynchronize(e->stream));
+    for (size_t i = 0; i < e->m.size(); ++i) {
+        int flag = 0;
+        ECK(e, cudaMemcpy(&flag, e->m[i]->d_flags, sizeof(int), cudaMemcpyDeviceToHost));
+        if (flag & 1) EFAIL(e, AMPS_ERR_NUMERIC, "member %d: NaN or Inf detected by the monitor", (int)i);
+        if (flag & 2) EFAIL(e, AMPS_ERR_TIMEOUT, "member %d: a bounded device wait gave up", (int)i);
     }
     return AMPS_OK;
 }

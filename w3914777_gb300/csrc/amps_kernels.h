@@ -18,6 +18,14 @@ constexpr int kTmaMaxFields = 16;
 size_t gg_tma_smem_bytes(int nf);
 cudaError_t gg_prepare_tma(bool ref, int nf, int *blocks_per_sm);
 cudaError_t gg_launch_tma(bool ref, const CUtensorMap &tm, const StepArgs &a, int grid, cudaStream_t s);
+// Ensemble step: a persistent kernel over the (member, tile) work items
+// items[nitems] (.x member, .y tile), member m's arguments table[m]; work is
+// taken from the counter queue[0] (queue[1] counts finished CTAs; the last
+// CTA resets both to 0 for the next launch).
+size_t gg_ens_smem_bytes(int tile, int max_nf);
+cudaError_t gg_prepare_ens(int tile, bool ref, int max_nf, int *blocks_per_sm);
+cudaError_t gg_launch_ens(int tile, bool ref, const StepArgs *table, const int2 *items, int nitems, int *queue,
+                          int grid, size_t smem, cudaStream_t s);
 size_t kob_smem_bytes(int tile, int tier);
 size_t sint_smem_bytes(int tile, int tier, int nf, bool mu64);
 
@@ -53,6 +61,10 @@ struct ClassifyArgs {
     int stat_steps;             // steps the current counts ran for (tile-step stats)
 };
 cudaError_t classify(const ClassifyArgs &c, cudaStream_t s);
+// Ensembles: classify (or do the period bookkeeping of) count members whose
+// arguments are the device array cs[count], one launch for all.
+cudaError_t classify_batch(const ClassifyArgs *cs, int count, cudaStream_t s);
+cudaError_t advance_batch(const ClassifyArgs *cs, int count, cudaStream_t s);
 // Rebuild lists/counts from tier_cur without reclassifying (static tier maps).
 cudaError_t build_lists(const uint8_t *tier, int ntiles, int *lists, int *counts, cudaStream_t s);
 // Bookkeeping at the end of a period when no classification runs.

@@ -170,7 +170,7 @@ __device__ void lists_from_tiers(const uint8_t *tier, int ntiles, int *lists, in
     if (threadIdx.x < 3) counts[threadIdx.x] = (int)((base >> (21 * threadIdx.x)) & 0x1FFFFF);
 }
 
-__global__ void __launch_bounds__(1024) classify_kernel(ClassifyArgs c)
+__device__ void classify_body(const ClassifyArgs &c)
 {
     __shared__ unsigned long long ws[32];
     __shared__ int prom, dem;
@@ -221,9 +221,20 @@ __global__ void __launch_bounds__(1024) classify_kernel(ClassifyArgs c)
     }
 }
 
+__global__ void __launch_bounds__(1024) classify_kernel(ClassifyArgs c) { classify_body(c); }
+
+// One CTA per ensemble member; member b's arguments are cs[b].
+__global__ void __launch_bounds__(1024) classify_batch_kernel(const ClassifyArgs *cs) { classify_body(cs[blockIdx.x]); }
+
 cudaError_t classify(const ClassifyArgs &c, cudaStream_t s)
 {
     classify_kernel<<<1, 1024, 0, s>>>(c);
+    return cudaGetLastError();
+}
+
+cudaError_t classify_batch(const ClassifyArgs *cs, int count, cudaStream_t s)
+{
+    classify_batch_kernel<<<count, 1024, 0, s>>>(cs);
     return cudaGetLastError();
 }
 
@@ -250,6 +261,23 @@ cudaError_t advance_period(int64_t *step_base, int advance, int stat_steps, cons
                            unsigned long long *stats, cudaStream_t s)
 {
     advance_kernel<<<1, 1, 0, s>>>(step_base, advance, stat_steps, counts, stats);
+    return cudaGetLastError();
+}
+
+// Period bookkeeping of every ensemble member without a classification
+// (one thread per member; advance and stat_steps from each member's args).
+__global__ void advance_batch_kernel(const ClassifyArgs *cs, int count)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= count) return;
+    const ClassifyArgs &c = cs[b];
+    for (int k = 0; k < 3; ++k) c.stats[k] += (unsigned long long)c.counts[k] * (unsigned long long)c.stat_steps;
+    *c.step_base += c.advance;
+}
+
+cudaError_t advance_batch(const ClassifyArgs *cs, int count, cudaStream_t s)
+{
+    advance_batch_kernel<<<(count + 127) / 128, 128, 0, s>>>(cs, count);
     return cudaGetLastError();
 }
 

@@ -476,4 +476,95 @@ cudaError_t gg_prepare_tma(bool ref, int nf, int *blocks_per_sm)
                : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, gg_step_tma_kernel<false>, kThreads, smem);
 }
 
+// Ensemble step: persistent CTAs take (member, tile) work items from a
+// global counter; items are ordered by cost (most fields first), so the
+// dynamic queue approximates longest-first scheduling across members of
+// different sizes and field counts.  A tile's arithmetic is the fused
+// kernel's (same per-tile code, same results); the member's arguments are
+// copied into shared memory when the member changes.  No waits: the counter
+// only hands out indices, and the last CTA to finish resets it.
+template <int T, bool REF>
+__global__ void __launch_bounds__(kThreads, 2)
+    gg_ens_kernel(const StepArgs *__restrict__ table, const int2 *__restrict__ items, int nitems, int *queue)
+{
+    extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ double red[kThreads / 32];
+    __shared__ uint8_t ntier[9];
+    __shared__ __align__(16) StepArgs sa;
+    __shared__ int sw;
+    float *sm = reinterpret_cast<float *>(smraw);
+    static_assert(sizeof(StepArgs) % 4 == 0, "StepArgs copied as 32-bit words");
+    int member = -1;
+    for (;;) {
+        if (threadIdx.x == 0) sw = atomicAdd(&queue[0], 1);
+        __syncthreads();
+        const int w = sw;
+        if (w >= nitems) break;
+        const int2 it = items[w];
+        if (it.x != member) {
+            const int *src = reinterpret_cast<const int *>(table + it.x);
+            int *dst = reinterpret_cast<int *>(&sa);
+            for (int k = threadIdx.x; k < (int)(sizeof(StepArgs) / 4); k += kThreads) dst[k] = src[k];
+            member = it.x;
+        }
+        __syncthreads();
+        const StepArgs &a = sa;
+        const int t = it.y, tx = t % a.ntx, ty = t / a.ntx;
+        const int tier = a.tier_out[t];
+        load_neighbour_tiers(a, tx, ty, ntier);
+        __syncthreads();
+        if (tier == TIER_FP64) {
+            gg_tile_fp64<T, REF>(a, ntier, t, tx, ty, red);
+        } else {
+            stage_tile<float, T, 1>(a, sm, ntier, tx, ty, 0, a.nf);
+            __syncthreads();
+            if (tier == TIER_FP32) gg_tile_lo<T, TIER_FP32>(a, sm, t, tx, ty, red);
+            else gg_tile_lo<T, TIER_HALF>(a, sm, t, tx, ty, red);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&queue[1], 1) == (int)gridDim.x - 1) {
+            queue[0] = 0;
+            queue[1] = 0;
+            __threadfence();
+        }
+    }
+}
+
+size_t gg_ens_smem_bytes(int tile, int max_nf) { return gg_smem_bytes(tile, -1, max_nf); }
+
+cudaError_t gg_prepare_ens(int tile, bool ref, int max_nf, int *blocks_per_sm)
+{
+    const size_t smem = gg_ens_smem_bytes(tile, max_nf);
+    const auto attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
+#define AMPS_GGE(TT, RR)                                                                                   \
+    do {                                                                                                   \
+        cudaError_t e = cudaFuncSetAttribute(gg_ens_kernel<TT, RR>, attr, (int)smem);                      \
+        if (e != cudaSuccess) return e;                                                                    \
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, gg_ens_kernel<TT, RR>, kThreads, smem); \
+    } while (0)
+    if (tile == 32) {
+        if (ref) AMPS_GGE(32, true);
+        AMPS_GGE(32, false);
+    }
+    if (ref) AMPS_GGE(16, true);
+    AMPS_GGE(16, false);
+#undef AMPS_GGE
+}
+
+cudaError_t gg_launch_ens(int tile, bool ref, const StepArgs *table, const int2 *items, int nitems, int *queue,
+                          int grid, size_t smem, cudaStream_t s)
+{
+    if (tile == 32) {
+        if (ref) gg_ens_kernel<32, true><<<grid, kThreads, smem, s>>>(table, items, nitems, queue);
+        else gg_ens_kernel<32, false><<<grid, kThreads, smem, s>>>(table, items, nitems, queue);
+    } else {
+        if (ref) gg_ens_kernel<16, true><<<grid, kThreads, smem, s>>>(table, items, nitems, queue);
+        else gg_ens_kernel<16, false><<<grid, kThreads, smem, s>>>(table, items, nitems, queue);
+    }
+    return cudaGetLastError();
+}
+
 }  // namespace amps
