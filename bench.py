@@ -238,6 +238,7 @@ def run_ours(args):
     value = world * cells * S * args.steps / (total_ms * 1e-3) / 1e9
     stats = sim.stats()
     final_mixed = sim.fields()
+    grains_mixed = sim.grains(threshold=0.5)
 
     # ---- end-to-end through the C ABI from pinned host memory ----
     e2e_ms = []
@@ -309,6 +310,9 @@ def run_ours(args):
         torch.cuda.synchronize()
         fp64_ms = a.elapsed_time(b)
         final64 = s64.fields()
+        grains64 = s64.grains(threshold=0.5)
+        # the reference's error metric: mean |a - b| over the grid (graingrowth/end2enderror.py:34)
+        mean_abs = max(s64.compare_all(f, final_mixed[f])["mean_abs"] for f in range(nf))
     plain = cells * S / (fp64_ms * 1e-3) / 1e9
     err = float(np.max(np.abs(final_mixed - final64)))
 
@@ -343,6 +347,9 @@ def run_ours(args):
             "plain_fp64": {"value": plain, "unit": "Gcell-updates/s", "ms_per_run": fp64_ms},
             "speedup_vs_plain_fp64": value / plain,
             "max_abs_err_vs_fp64": err,
+            "mean_abs_err_vs_fp64": mean_abs,
+            "grains": {"adaptive": grains_mixed, "fp64": grains64,
+                       "note": "connected regions of the dominant eta (>= 0.5), periodic"},
             "tier_mix": {"half": ts[0] / tot, "fp32": ts[1] / tot, "fp64": ts[2] / tot},
             "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,

@@ -223,6 +223,31 @@ AMPS_API int amps_reduce(amps_handle *h, int field, int kind, double *out);
 AMPS_API int amps_compare(amps_handle *h, int field, const double *other, int on_device, double *max_abs,
                  double *rms);
 
+/* ---- microstructure diagnostics (no reference counterpart) ---------------
+ * All on the device in FP64 over the current state, deterministic.
+ * amps_compare_all: out = {max |f - other|, RMS, mean |f - other|} (the mean
+ *   absolute difference is the reference's error metric,
+ *   graingrowth/end2enderror.py:34).
+ * amps_interface: the level set {f >= level}: out = {cells, area (cells*dx*dy),
+ *   perimeter (4-neighbour edges crossing the level: x-edges*dy + y-edges*dx,
+ *   exact for axis-aligned fronts, up to sqrt 2 long on diagonal ones),
+ *   xmin, xmax, ymin, ymax (cell indices; -1 if empty)} -- e.g. the dendrite
+ *   tips.
+ * amps_grains: cells labelled by their dominant order parameter
+ *   (grain growth: eta_0..eta_{Q-1}; sintering: eta_1..eta_N where c >= level)
+ *   wherever its value is >= threshold; connected components of equal labels
+ *   (4-neighbour, through periodic wraps): out = {grains, labelled cells},
+ *   *mean_area = labelled cells * dx * dy / grains.
+ * amps_boundary_lengths: boundary length between every pair of labels
+ *   (every cell labelled by its dominant order parameter; sintering: only
+ *   where c >= level, so the pair lengths are the neck widths), row-major
+ *   q x q symmetric into `lengths` (q = Q or N <= 32), same edge measure as
+ *   the perimeter.  Kobayashi: AMPS_ERR_INVALID for the last two. */
+AMPS_API int amps_compare_all(amps_handle *h, int field, const double *other, int on_device, double out[3]);
+AMPS_API int amps_interface(amps_handle *h, int field, double level, double out[7]);
+AMPS_API int amps_grains(amps_handle *h, double threshold, double level, int64_t out[2], double *mean_area);
+AMPS_API int amps_boundary_lengths(amps_handle *h, double level, double *lengths);
+
 /* ---- reduction that allocates nothing ------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device
  * memory when they need the result -- e.g. an application whose device

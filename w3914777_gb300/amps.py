@@ -136,6 +136,10 @@ def lib():
             "amps_adjoint_last_error": ([vp], ctypes.c_char_p),
             "amps_adjoint_forward": ([vp, ctypes.POINTER(dp), vp, vp, ctypes.c_int64], ip),
             "amps_adjoint_backward": ([vp, vp, vp, vp], ip),
+            "amps_compare_all": ([vp, ip, vp, ip, ctypes.POINTER(dp)], ip),
+            "amps_interface": ([vp, ip, dp, ctypes.POINTER(dp)], ip),
+            "amps_grains": ([vp, dp, dp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(dp)], ip),
+            "amps_boundary_lengths": ([vp, dp, ctypes.POINTER(dp)], ip),
             "amps_ensemble_create": ([ctypes.POINTER(vp), ip, ctypes.POINTER(vp)], ip),
             "amps_ensemble_destroy": ([vp], ip), "amps_ensemble_set_stream": ([vp, vp], ip),
             "amps_ensemble_set_graphs": ([vp, ip], ip), "amps_ensemble_run": ([vp, ip], ip),
@@ -279,6 +283,36 @@ class Simulation:
         self._ck(lib().amps_compare(self.h, k, a.ctypes.data, 0, ctypes.byref(mx), ctypes.byref(rms)),
                  "amps_compare")
         return mx.value, rms.value
+
+    def compare_all(self, k, other):
+        """{max_abs, rms, mean_abs} of field k against `other` (the mean absolute
+        difference is the reference's error metric)."""
+        a = np.ascontiguousarray(other, dtype=np.float64)
+        out = (ctypes.c_double * 3)()
+        self._ck(lib().amps_compare_all(self.h, k, a.ctypes.data, 0, out), "amps_compare_all")
+        return {"max_abs": out[0], "rms": out[1], "mean_abs": out[2]}
+
+    def interface(self, k, level=0.5):
+        """Level set {field k >= level}: cells, area, perimeter, bounding box."""
+        out = (ctypes.c_double * 7)()
+        self._ck(lib().amps_interface(self.h, k, float(level), out), "amps_interface")
+        return {"cells": int(out[0]), "area": out[1], "perimeter": out[2],
+                "xmin": int(out[3]), "xmax": int(out[4]), "ymin": int(out[5]), "ymax": int(out[6])}
+
+    def grains(self, threshold=0.5, level=0.5):
+        """Connected grains of the dominant order parameter: count, labelled cells, mean area."""
+        out = (ctypes.c_int64 * 2)()
+        area = ctypes.c_double()
+        self._ck(lib().amps_grains(self.h, float(threshold), float(level), out, ctypes.byref(area)), "amps_grains")
+        return {"grains": out[0], "cells": out[1], "mean_area": area.value}
+
+    def boundary_lengths(self, level=0.5):
+        """Boundary length between every pair of order parameters (q x q)."""
+        q = self.nf - (1 if self.params.model == SINTERING else 0)
+        out = np.zeros((q, q))
+        self._ck(lib().amps_boundary_lengths(self.h, float(level), out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))),
+                 "amps_boundary_lengths")
+        return out
 
     def set_profiling(self, enable=True):
         self._ck(lib().amps_set_profiling(self.h, int(enable)), "amps_set_profiling")

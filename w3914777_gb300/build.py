@@ -22,7 +22,7 @@ OBJ = os.path.join(OUT, "obj-" + platform.machine())
 _ELF_MACHINE = {"x86_64": 62, "aarch64": 183}
 
 SOURCES = ["amps_api.cu", "amps_host.cpp", "k_common.cu", "k_graingrowth.cu", "k_kobayashi.cu",
-           "k_sintering.cu", "k_noalloc.cu", "k_adjoint.cu"]
+           "k_sintering.cu", "k_noalloc.cu", "k_adjoint.cu", "k_diag.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
               "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include")]

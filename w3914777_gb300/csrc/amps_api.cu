@@ -57,6 +57,9 @@ struct amps_handle {
     bool use_tma = false;
     int tma_grid = 0;
     alignas(64) CUtensorMap tm[2];
+    // diagnostics scratch (allocated on first use): lab, parent (n ints each),
+    // one FP64 field, counters, bounding box
+    char *d_diag = nullptr;
     double prof_ms[4] = {0, 0, 0, 0};
     int64_t prof_launches[4] = {0, 0, 0, 0};
     unsigned long long prof_stats0[3] = {0, 0, 0};
@@ -160,7 +163,8 @@ static void free_all(amps_handle *h)
         for (int q = 0; q < 2; ++q)
             if (h->store[t][q]) cudaFree(h->store[t][q]);
     void *ps[] = {h->d_tier_prev, h->d_tier_cur, h->d_lists, h->d_counts, h->d_metric, h->d_snap, h->d_stats,
-                  h->d_flags, h->d_log, h->d_log_n, h->d_step_base, h->d_stage, h->d_partials, h->d_out};
+                  h->d_flags, h->d_log, h->d_log_n, h->d_step_base, h->d_stage, h->d_partials, h->d_out,
+                  h->d_diag};
     for (void *q : ps)
         if (q) cudaFree(q);
     if (h->h_pinned) cudaFreeHost(h->h_pinned);
@@ -724,6 +728,133 @@ extern "C" int amps_compare(amps_handle *h, int field, const double *other, int 
     CK(h, cudaStreamSynchronize(h->stream));
     if (max_abs) *max_abs = h->h_pinned[0];
     if (rms) *rms = h->h_pinned[1];
+    return AMPS_OK;
+}
+
+// ------------------------------------------------------------ diagnostics ----
+namespace {
+constexpr int kDiagAcc = 2 * 32 * 32 + 8;  // boundary counters for up to 32 labels
+struct DiagScratch {
+    int *lab, *parent, *box;
+    double *field;
+    unsigned long long *acc;
+};
+}  // namespace
+
+static int diag_scratch(amps_handle *h, DiagScratch *d)
+{
+    const size_t ints = (size_t)2 * h->n * sizeof(int), dbl = (size_t)h->n * sizeof(double);
+    const size_t off_f = (ints + 255) & ~(size_t)255, off_a = off_f + ((dbl + 255) & ~(size_t)255);
+    const size_t total = off_a + kDiagAcc * sizeof(unsigned long long) + 256;
+    if (!h->d_diag) CK(h, cudaMalloc(&h->d_diag, total));
+    d->lab = (int *)h->d_diag;
+    d->parent = d->lab + h->n;
+    d->field = (double *)(h->d_diag + off_f);
+    d->acc = (unsigned long long *)(h->d_diag + off_a);
+    d->box = (int *)(d->acc + kDiagAcc);
+    return AMPS_OK;
+}
+
+// all fields, FP64 row-major, into d_stage
+static int diag_gather(amps_handle *h)
+{
+    Grid g = grid_view(h, h->parity, live_tiers(h));
+    CK(h, gather_fields(g, h->d_stage, 0, 0, h->nf, h->stream));
+    return AMPS_OK;
+}
+
+extern "C" int amps_compare_all(amps_handle *h, int field, const double *other, int on_device, double out[3])
+{
+    if (!h || !other || !out || field < 0 || field >= h->nf) return AMPS_ERR_INVALID;
+    DiagScratch d;
+    if (int r = diag_scratch(h, &d)) return r;
+    if (int r = diag_gather(h)) return r;
+    CK(h, cudaMemcpyAsync(d.field, other, sizeof(double) * h->n,
+                          on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->stream));
+    CK(h, diag_compare3(h->d_stage + (int64_t)field * h->n, d.field, h->n, h->d_partials, 512, h->d_out, h->stream));
+    CK(h, cudaMemcpyAsync(h->h_pinned, h->d_out, 3 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    for (int k = 0; k < 3; ++k) out[k] = h->h_pinned[k];
+    return AMPS_OK;
+}
+
+extern "C" int amps_interface(amps_handle *h, int field, double level, double out[7])
+{
+    if (!h || !out || field < 0 || field >= h->nf) return AMPS_ERR_INVALID;
+    DiagScratch d;
+    if (int r = diag_scratch(h, &d)) return r;
+    if (int r = diag_gather(h)) return r;
+    const amps_params &p = h->p;
+    CK(h, diag_interface(h->d_stage + (int64_t)field * h->n, p.nx, p.ny, p.bc, level, d.acc, d.box, h->stream));
+    unsigned long long acc[3];
+    int box[4];
+    CK(h, cudaMemcpyAsync(acc, d.acc, sizeof acc, cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaMemcpyAsync(box, d.box, sizeof box, cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    out[0] = (double)acc[0];
+    out[1] = (double)acc[0] * p.dx * p.dy;
+    out[2] = (double)acc[1] * p.dy + (double)acc[2] * p.dx;
+    for (int k = 0; k < 4; ++k) out[3 + k] = acc[0] ? (double)box[k] : -1.0;
+    return AMPS_OK;
+}
+
+// order parameters of the model: (first field, count, concentration field or -1)
+static bool order_params(const amps_handle *h, int *e0, int *q, int *cfield)
+{
+    if (h->p.model == AMPS_GRAINGROWTH) {
+        *e0 = 0; *q = h->nf; *cfield = -1;
+        return true;
+    }
+    if (h->p.model == AMPS_SINTERING) {
+        *e0 = 1; *q = h->nf - 1; *cfield = 0;
+        return true;
+    }
+    return false;
+}
+
+extern "C" int amps_grains(amps_handle *h, double threshold, double level, int64_t out[2], double *mean_area)
+{
+    int e0, q, cf;
+    if (!h || !out || !order_params(h, &e0, &q, &cf)) return AMPS_ERR_INVALID;
+    DiagScratch d;
+    if (int r = diag_scratch(h, &d)) return r;
+    if (int r = diag_gather(h)) return r;
+    const amps_params &p = h->p;
+    const double *conc = cf >= 0 ? h->d_stage + (int64_t)cf * h->n : nullptr;
+    CK(h, diag_grains(h->d_stage, e0, q, p.nx, p.ny, p.bc, threshold, conc, level, d.lab, d.parent, d.acc,
+                      h->d_flags, h->stream));
+    unsigned long long acc[2];
+    int flag = 0;
+    CK(h, cudaMemcpyAsync(acc, d.acc, sizeof acc, cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaMemcpyAsync(&flag, h->d_flags, sizeof flag, cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    if (flag & 4) FAIL(h, AMPS_ERR_TIMEOUT, "grain labelling: a union-find walk exceeded the cell count");
+    out[0] = (int64_t)acc[0];
+    out[1] = (int64_t)acc[1];
+    if (mean_area) *mean_area = acc[0] ? (double)acc[1] * p.dx * p.dy / (double)acc[0] : 0.0;
+    return AMPS_OK;
+}
+
+extern "C" int amps_boundary_lengths(amps_handle *h, double level, double *lengths)
+{
+    int e0, q, cf;
+    if (!h || !lengths || !order_params(h, &e0, &q, &cf) || q > 32) return AMPS_ERR_INVALID;
+    DiagScratch d;
+    if (int r = diag_scratch(h, &d)) return r;
+    if (int r = diag_gather(h)) return r;
+    const amps_params &p = h->p;
+    const double *conc = cf >= 0 ? h->d_stage + (int64_t)cf * h->n : nullptr;
+    CK(h, diag_boundaries(h->d_stage, e0, q, p.nx, p.ny, p.bc, conc, level, d.lab, d.acc, h->stream));
+    std::vector<unsigned long long> acc((size_t)2 * q * q);
+    CK(h, cudaMemcpyAsync(acc.data(), d.acc, acc.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                          h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    for (int a = 0; a < q; ++a)
+        for (int b = 0; b < q; ++b) {
+            const int lo = a < b ? a : b, hi = a < b ? b : a;
+            const size_t k = ((size_t)lo * q + hi) * 2;
+            lengths[(size_t)a * q + b] = a == b ? 0.0 : (double)acc[k] * p.dy + (double)acc[k + 1] * p.dx;
+        }
     return AMPS_OK;
 }
 

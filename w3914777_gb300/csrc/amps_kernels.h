@@ -75,4 +75,17 @@ cudaError_t reduce_field(const Grid &g, int field, int kind, double *partials, d
 cudaError_t compare_field(const Grid &g, int field, const double *other, double *partials, double *out2,
                           cudaStream_t s);
 
+// Diagnostics on row-major FP64 fields (k_diag.cu).  acc/box/lab/parent are
+// device scratch: acc >= max(3, 2*q*q) counters, box 4 ints, lab and parent
+// n ints each; flags bit 2: a union-find walk hit its cap.
+cudaError_t diag_interface(const double *f, int nx, int ny, int bc, double level, unsigned long long *acc, int *box,
+                           cudaStream_t s);
+cudaError_t diag_grains(const double *fields, int e0, int q, int nx, int ny, int bc, double thr, const double *conc,
+                        double clevel, int *lab, int *parent, unsigned long long *acc, int *flags, cudaStream_t s);
+cudaError_t diag_boundaries(const double *fields, int e0, int q, int nx, int ny, int bc, const double *conc,
+                            double clevel, int *lab, unsigned long long *acc, cudaStream_t s);
+// out = {max |a-b|, rms, mean |a-b|}; partials: 3*np doubles
+cudaError_t diag_compare3(const double *a, const double *b, int64_t n, double *partials, int np, double *out,
+                          cudaStream_t s);
+
 }  // namespace amps
