@@ -1069,8 +1069,11 @@ static int ens_enqueue(amps_ensemble *e, const StepArgs *table, const ClassifyAr
                        cudaStream_t s)
 {
     const int M = (int)e->m.size();
-    for (int k = 0; k < cnt; ++k)
-        ECK(e, gg_launch_ens(e->T, e->ref, table + (size_t)k * M, e->d_items, e->nitems, e->d_queue, e->grid, e->smem, s));
+    for (int k = 0; k < cnt; ++k) {
+        const bool mon = e->mixed && period_end && k == cnt - 1;  // as in ens_tables
+        ECK(e, gg_launch_ens(e->T, e->ref, mon, table + (size_t)k * M, e->d_items, e->nitems, e->d_queue, e->grid,
+                             e->smem, s));
+    }
     if (e->mixed && period_end) ECK(e, classify_batch(cls, M, s));
     else ECK(e, advance_batch(cls, M, s));
     return AMPS_OK;

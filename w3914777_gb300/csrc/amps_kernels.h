@@ -24,8 +24,8 @@ cudaError_t gg_launch_tma(bool ref, const CUtensorMap &tm, const StepArgs &a, in
 // CTA resets both to 0 for the next launch).
 size_t gg_ens_smem_bytes(int tile, int max_nf);
 cudaError_t gg_prepare_ens(int tile, bool ref, int max_nf, int *blocks_per_sm);
-cudaError_t gg_launch_ens(int tile, bool ref, const StepArgs *table, const int2 *items, int nitems, int *queue,
-                          int grid, size_t smem, cudaStream_t s);
+cudaError_t gg_launch_ens(int tile, bool ref, bool monitor, const StepArgs *table, const int2 *items, int nitems,
+                          int *queue, int grid, size_t smem, cudaStream_t s);
 size_t kob_smem_bytes(int tile, int tier);
 size_t sint_smem_bytes(int tile, int tier, int nf, bool mu64);
 

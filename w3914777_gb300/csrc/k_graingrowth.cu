@@ -40,24 +40,93 @@ __device__ __forceinline__ void store_cells(const StepArgs &a, int64_t idx, cons
     }
 }
 
-template <int T, int TIER>
-__device__ __forceinline__ void gg_tile_lo(const StepArgs &a, const float *sm, int tile, int tx, int ty, double *red)
+// Where a half/FP32 tile step reads its neighbourhood from:
+//  SRC_SMEM: the staged float neighbourhood `sm` (16^2 tiles, the TMA kernel);
+//  SRC_G32:  the tile and all eight neighbours hold FP32 input -- three rows
+//            and two halo columns per field straight from the FP32 array
+//            through L1 (no staging copy, no barrier, no shared memory);
+//  SRC_GMIX: any mix of input tiers -- each row segment and halo cell read at
+//            its owner tile's tier and converted to float, as staging would.
+// The arithmetic is the same for all three.
+enum { SRC_SMEM = 0, SRC_G32 = 1, SRC_GMIX = 2 };
+
+// Cells [c0-1, c0+4] of one mapped row of field f into w[0..5] as float:
+// the centre four from the tier `tc` (16/8/32-byte aligned vector), the halo
+// cells from tiers tl / tr.
+__device__ __forceinline__ void ld_row6(const StepArgs &a, int64_t base, int gx0, int gxl, int gxr, int tc, int tl,
+                                        int tr, float *w)
+{
+    if (tc == TIER_FP32) {
+        const float4 q = __ldg(reinterpret_cast<const float4 *>((const float *)a.in[TIER_FP32] + base + gx0));
+        w[1] = q.x; w[2] = q.y; w[3] = q.z; w[4] = q.w;
+    } else if (tc == TIER_HALF) {
+        const uint2 u = __ldg(reinterpret_cast<const uint2 *>((const __half *)a.in[TIER_HALF] + base + gx0));
+        const float2 lo = __half22float2(*reinterpret_cast<const __half2 *>(&u.x));
+        const float2 hi = __half22float2(*reinterpret_cast<const __half2 *>(&u.y));
+        w[1] = lo.x; w[2] = lo.y; w[3] = hi.x; w[4] = hi.y;
+    } else {
+        const double2 *d = reinterpret_cast<const double2 *>((const double *)a.in[TIER_FP64] + base + gx0);
+        const double2 d0 = __ldg(d), d1 = __ldg(d + 1);
+        w[1] = (float)d0.x; w[2] = (float)d0.y; w[3] = (float)d1.x; w[4] = (float)d1.y;
+    }
+    w[0] = load_tier<float>(a, tl, base + gxl);
+    w[5] = load_tier<float>(a, tr, base + gxr);
+}
+
+// MON: this step evaluates the monitor (compiled out of the other steps, so
+// their loop carries no monitor state).
+template <int T, int TIER, int SRC, bool MON>
+__device__ __forceinline__ void gg_tile_lo_impl(const StepArgs &a, const float *sm, const uint8_t *nt, int tile,
+                                                int tx, int ty, double *red)
 {
     using S = Stage<float, T, 1>;
     constexpr int CPT = T * T / kThreads;  // cells per thread, along x
     constexpr int GPR = T / CPT;           // thread groups per row
+    static_assert(SRC == SRC_SMEM || CPT == 4, "direct reads need 4 cells per thread (32^2 tiles)");
     const int row = threadIdx.x / GPR;
     const int c0 = (threadIdx.x % GPR) * CPT;
     const int nf = a.nf;
     const Phys &ph = a.ph;
     float *smm = const_cast<float *>(sm);
+    // direct reads: mapped offsets of rows row-1, row, row+1 and the mapped
+    // halo columns; GMIX: the tier of each row's centre and halo parts
+    int64_t grow[3] = {0, 0, 0};
+    int gxl = 0, gxr = 0, tcs[3] = {0, 0, 0}, tls[3] = {0, 0, 0}, trs[3] = {0, 0, 0};
+    const int gx0 = tx * T + c0;
+    if (SRC != SRC_SMEM) {
+#pragma unroll
+        for (int rr = 0; rr < 3; ++rr) {
+            const int lr = row - 1 + rr;
+            grow[rr] = (int64_t)bc_map(ty * T + lr, a.ny, a.bc) * a.nx;
+            const int rc = (lr < 0 ? 0 : (lr < T ? 3 : 6));
+            tcs[rr] = nt[rc + 1];
+            tls[rr] = nt[rc + (c0 == 0 ? 0 : 1)];
+            trs[rr] = nt[rc + (c0 + CPT == T ? 2 : 1)];
+        }
+        gxl = bc_map(gx0 - 1, a.nx, a.bc);
+        gxr = bc_map(gx0 + CPT, a.nx, a.bc);
+    }
+    const float *g32 = (const float *)a.in[TIER_FP32];
     float ssum[CPT];
 #pragma unroll
     for (int k = 0; k < CPT; ++k) ssum[k] = 0.f;
     for (int f = 0; f < nf; ++f) {
-        const float *ctr = &S::at(smm, f, row + 1, S::O + c0);
+        float c[CPT];
+        if (SRC == SRC_G32) {
+            const float4 q = __ldg(reinterpret_cast<const float4 *>(g32 + f * a.n + grow[1] + gx0));
+            c[0] = q.x; c[1] = q.y; c[2] = q.z; c[3] = q.w;
+        } else if (SRC == SRC_GMIX) {
+            float w6[6];
+            ld_row6(a, f * a.n + grow[1], gx0, gxl, gxr, tcs[1], tls[1], trs[1], w6);
 #pragma unroll
-        for (int k = 0; k < CPT; ++k) ssum[k] = fmaf(ctr[k], ctr[k], ssum[k]);
+            for (int k = 0; k < CPT; ++k) c[k] = w6[k + 1];
+        } else {
+            const float *ctr = &S::at(smm, f, row + 1, S::O + c0);
+#pragma unroll
+            for (int k = 0; k < CPT; ++k) c[k] = ctr[k];
+        }
+#pragma unroll
+        for (int k = 0; k < CPT; ++k) ssum[k] = fmaf(c[k], c[k], ssum[k]);
     }
     const float dtm = (float)(ph.dt * ph.mobil), g2 = (float)(2.0 * ph.gamma), kap = (float)ph.grcoef;
     const float inv = (float)ph.inv_dxdy;
@@ -65,7 +134,7 @@ __device__ __forceinline__ void gg_tile_lo(const StepArgs &a, const float *sm, i
     double metric = 0.0;
     MonAccF mon;
     for (int f = 0; f < nf; ++f) {
-        const bool mon_f = a.monitor_now && (a.mfield < 0 || a.mfield == f);
+        const bool mon_f = MON && (a.mfield < 0 || a.mfield == f);
         const int mslot = a.mfield < 0 ? f : 0;
         double snapv[CPT];
         if (mon_f) {
@@ -76,16 +145,26 @@ __device__ __forceinline__ void gg_tile_lo(const StepArgs &a, const float *sm, i
         float w[3][CPT + 2];
 #pragma unroll
         for (int rr = 0; rr < 3; ++rr) {
-            const float *p = &S::at(smm, f, row + rr, S::O + c0);
-            if (CPT == 4) {
-                const float4 q = *reinterpret_cast<const float4 *>(p);
+            if (SRC == SRC_G32) {
+                const float *b = g32 + f * a.n + grow[rr];
+                const float4 q = __ldg(reinterpret_cast<const float4 *>(b + gx0));
                 w[rr][1] = q.x; w[rr][2] = q.y; w[rr][3] = q.z; w[rr][4] = q.w;
+                w[rr][0] = __ldg(b + gxl);
+                w[rr][CPT + 1] = __ldg(b + gxr);
+            } else if (SRC == SRC_GMIX) {
+                ld_row6(a, f * a.n + grow[rr], gx0, gxl, gxr, tcs[rr], tls[rr], trs[rr], w[rr]);
             } else {
+                const float *p = &S::at(smm, f, row + rr, S::O + c0);
+                if (CPT == 4) {
+                    const float4 q = *reinterpret_cast<const float4 *>(p);
+                    w[rr][1] = q.x; w[rr][2] = q.y; w[rr][3] = q.z; w[rr][4] = q.w;
+                } else {
 #pragma unroll
-                for (int k = 0; k < CPT; ++k) w[rr][k + 1] = p[k];
+                    for (int k = 0; k < CPT; ++k) w[rr][k + 1] = p[k];
+                }
+                w[rr][0] = p[-1];
+                w[rr][CPT + 1] = p[CPT];
             }
-            w[rr][0] = p[-1];
-            w[rr][CPT + 1] = p[CPT];
         }
         float out[CPT];
 #pragma unroll
@@ -111,7 +190,15 @@ __device__ __forceinline__ void gg_tile_lo(const StepArgs &a, const float *sm, i
             metric = mon_finish(a, mon, red, metric);
         }
     }
-    if (a.monitor_now && threadIdx.x == 0) a.metric[tile] = metric;
+    if (MON && threadIdx.x == 0) a.metric[tile] = metric;
+}
+
+template <int T, int TIER, int SRC = SRC_SMEM>
+__device__ __forceinline__ void gg_tile_lo(const StepArgs &a, const float *sm, const uint8_t *nt, int tile, int tx,
+                                           int ty, double *red)
+{
+    if (a.monitor_now) gg_tile_lo_impl<T, TIER, SRC, true>(a, sm, nt, tile, tx, ty, red);
+    else gg_tile_lo_impl<T, TIER, SRC, false>(a, sm, nt, tile, tx, ty, red);
 }
 
 // One cell of the FP64 tile's neighbourhood at tile-local (ly, lx), read at
@@ -214,7 +301,43 @@ __device__ __forceinline__ void gg_tile_fp64(const StepArgs &a, const uint8_t *n
 
 // Fused all-tier step: at most 64 registers, so that four CTAs share an SM
 // and the half/FP32 tiles (the common case) keep their occupancy.
+// every tile of the 3x3 neighbourhood (after the boundary map) holds FP32 input
+__device__ __forceinline__ bool all_fp32(const uint8_t *nt)
+{
+    bool ok = true;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) ok &= nt[k] == TIER_FP32;
+    return ok;
+}
+
+// Tiles off the all-FP32 path (mixed-tier neighbourhoods, half tiles, FP64
+// tiles), kept out of line so that their register demand does not spill the
+// hot path.
+template <int T, bool MON>
+__device__ __noinline__ void gg_tile_mixed_call(const StepArgs &a, const uint8_t *nt, int tier, int tile, int tx,
+                                                int ty, double *red)
+{
+    if (tier == TIER_FP32) gg_tile_lo_impl<T, TIER_FP32, SRC_GMIX, MON>(a, nullptr, nt, tile, tx, ty, red);
+    else gg_tile_lo_impl<T, TIER_HALF, SRC_GMIX, MON>(a, nullptr, nt, tile, tx, ty, red);
+}
+
 template <int T, bool REF>
+__device__ __noinline__ void gg_tile_fp64_call(const StepArgs &a, const uint8_t *nt, int tile, int tx, int ty,
+                                               double *red)
+{
+    gg_tile_fp64<T, REF>(a, nt, tile, tx, ty, red);
+}
+
+// Fused all-tier step: at most 64 registers, so that four CTAs share an SM.
+// MON (the monitor steps, one in `cadence`) is a separate instantiation, so
+// the other steps' kernel carries no monitor code.  Half/FP32 tiles stage
+// their neighbourhood in shared memory.  (Reading it directly through L1 --
+// SRC_G32 -- runs 18.5 against 22.5 us per 1024^2 Q=8 step for an all-FP32
+// grid in isolation, but in the full adaptive run, with monitor steps and
+// mixed-tier neighbourhoods, this kernel measured 22.5 us per step staged
+// against 25.2 direct; the ensemble kernel, whose tile order mixes members,
+// gains from it and uses it.)
+template <int T, bool REF, bool MON>
 __global__ void __launch_bounds__(kThreads, 4) gg_step_kernel(StepArgs a)
 {
     using S = Stage<float, T, 1>;
@@ -233,8 +356,8 @@ __global__ void __launch_bounds__(kThreads, 4) gg_step_kernel(StepArgs a)
     }
     stage_tile<float, T, 1>(a, sm, ntier, tx, ty, 0, a.nf);
     __syncthreads();
-    if (tier == TIER_FP32) gg_tile_lo<T, TIER_FP32>(a, sm, tile, tx, ty, red);
-    else gg_tile_lo<T, TIER_HALF>(a, sm, tile, tx, ty, red);
+    if (tier == TIER_FP32) gg_tile_lo_impl<T, TIER_FP32, SRC_SMEM, MON>(a, sm, ntier, tile, tx, ty, red);
+    else gg_tile_lo_impl<T, TIER_HALF, SRC_SMEM, MON>(a, sm, ntier, tile, tx, ty, red);
     (void)sizeof(S);
 }
 
@@ -335,14 +458,25 @@ cudaError_t gg_launch(int tile, int tier, bool ref, const StepArgs &a, int grid,
         if (ref) K<TT, true><<<grid, kThreads, smem, s>>>(a);                   \
         else K<TT, false><<<grid, kThreads, smem, s>>>(a);                      \
     } while (0)
+#define AMPS_GGM(TT)                                                                        \
+    do {                                                                                    \
+        if (a.monitor_now) {                                                                \
+            if (ref) gg_step_kernel<TT, true, true><<<grid, kThreads, smem, s>>>(a);        \
+            else gg_step_kernel<TT, false, true><<<grid, kThreads, smem, s>>>(a);           \
+        } else {                                                                            \
+            if (ref) gg_step_kernel<TT, true, false><<<grid, kThreads, smem, s>>>(a);       \
+            else gg_step_kernel<TT, false, false><<<grid, kThreads, smem, s>>>(a);          \
+        }                                                                                   \
+    } while (0)
     if (tier == TIER_FP64) {
         if (tile == 32) AMPS_GGL(gg_step_f64_kernel, 32);
         else AMPS_GGL(gg_step_f64_kernel, 16);
     } else {
-        if (tile == 32) AMPS_GGL(gg_step_kernel, 32);
-        else AMPS_GGL(gg_step_kernel, 16);
+        if (tile == 32) AMPS_GGM(32);
+        else AMPS_GGM(16);
     }
 #undef AMPS_GGL
+#undef AMPS_GGM
     return cudaGetLastError();
 }
 
@@ -356,10 +490,21 @@ cudaError_t gg_prepare(int tile, int tier, bool ref)
         return ref ? cudaFuncSetAttribute(gg_step_f64_kernel<16, true>, attr, lim)
                    : cudaFuncSetAttribute(gg_step_f64_kernel<16, false>, attr, lim);
     }
-    if (tile == 32) return ref ? cudaFuncSetAttribute(gg_step_kernel<32, true>, attr, lim)
-                               : cudaFuncSetAttribute(gg_step_kernel<32, false>, attr, lim);
-    return ref ? cudaFuncSetAttribute(gg_step_kernel<16, true>, attr, lim)
-               : cudaFuncSetAttribute(gg_step_kernel<16, false>, attr, lim);
+    cudaError_t e;
+    if (tile == 32) {
+        e = ref ? cudaFuncSetAttribute(gg_step_kernel<32, true, false>, attr, lim)
+                : cudaFuncSetAttribute(gg_step_kernel<32, false, false>, attr, lim);
+        if (e == cudaSuccess)
+            e = ref ? cudaFuncSetAttribute(gg_step_kernel<32, true, true>, attr, lim)
+                    : cudaFuncSetAttribute(gg_step_kernel<32, false, true>, attr, lim);
+        return e;
+    }
+    e = ref ? cudaFuncSetAttribute(gg_step_kernel<16, true, false>, attr, lim)
+            : cudaFuncSetAttribute(gg_step_kernel<16, false, false>, attr, lim);
+    if (e == cudaSuccess)
+        e = ref ? cudaFuncSetAttribute(gg_step_kernel<16, true, true>, attr, lim)
+                : cudaFuncSetAttribute(gg_step_kernel<16, false, true>, attr, lim);
+    return e;
 }
 
 // Persistent, TMA-pipelined fused step for 32x32 tiles (nf <= kTmaMaxFields).
@@ -434,8 +579,8 @@ __global__ void __launch_bounds__(kThreads, 2)
                 if (fast_s[b ^ 1]) mbar_wait_bounded(&mbar[b ^ 1], b ? ph0 : ph1);
                 return;
             }
-            if (tier == TIER_FP32) gg_tile_lo<T, TIER_FP32>(a, sm, t, tx, ty, red);
-            else gg_tile_lo<T, TIER_HALF>(a, sm, t, tx, ty, red);
+            if (tier == TIER_FP32) gg_tile_lo<T, TIER_FP32>(a, sm, ntier, t, tx, ty, red);
+            else gg_tile_lo<T, TIER_HALF>(a, sm, ntier, t, tx, ty, red);
         } else {
             load_neighbour_tiers(a, tx, ty, ntier);
             __syncthreads();
@@ -444,8 +589,8 @@ __global__ void __launch_bounds__(kThreads, 2)
             } else {
                 stage_tile<float, T, 1>(a, sm, ntier, tx, ty, 0, a.nf);
                 __syncthreads();
-                if (tier == TIER_FP32) gg_tile_lo<T, TIER_FP32>(a, sm, t, tx, ty, red);
-                else gg_tile_lo<T, TIER_HALF>(a, sm, t, tx, ty, red);
+                if (tier == TIER_FP32) gg_tile_lo<T, TIER_FP32>(a, sm, ntier, t, tx, ty, red);
+                else gg_tile_lo<T, TIER_HALF>(a, sm, ntier, t, tx, ty, red);
             }
         }
         fence_proxy_async_smem();  // this buffer's reads/writes before its next tensor copy
@@ -483,7 +628,7 @@ cudaError_t gg_prepare_tma(bool ref, int nf, int *blocks_per_sm)
 // kernel's (same per-tile code, same results); the member's arguments are
 // copied into shared memory when the member changes.  No waits: the counter
 // only hands out indices, and the last CTA to finish resets it.
-template <int T, bool REF>
+template <int T, bool REF, bool MON>
 __global__ void __launch_bounds__(kThreads, 2)
     gg_ens_kernel(const StepArgs *__restrict__ table, const int2 *__restrict__ items, int nitems, int *queue)
 {
@@ -513,13 +658,20 @@ __global__ void __launch_bounds__(kThreads, 2)
         const int tier = a.tier_out[t];
         load_neighbour_tiers(a, tx, ty, ntier);
         __syncthreads();
-        if (tier == TIER_FP64) {
+        if constexpr (T == 32) {
+            if (tier == TIER_FP32 && all_fp32(ntier))
+                gg_tile_lo_impl<T, TIER_FP32, SRC_G32, MON>(a, nullptr, ntier, t, tx, ty, red);
+            else if (tier == TIER_FP64)
+                gg_tile_fp64_call<T, REF>(a, ntier, t, tx, ty, red);
+            else
+                gg_tile_mixed_call<T, MON>(a, ntier, tier, t, tx, ty, red);
+        } else if (tier == TIER_FP64) {
             gg_tile_fp64<T, REF>(a, ntier, t, tx, ty, red);
         } else {
             stage_tile<float, T, 1>(a, sm, ntier, tx, ty, 0, a.nf);
             __syncthreads();
-            if (tier == TIER_FP32) gg_tile_lo<T, TIER_FP32>(a, sm, t, tx, ty, red);
-            else gg_tile_lo<T, TIER_HALF>(a, sm, t, tx, ty, red);
+            if (tier == TIER_FP32) gg_tile_lo<T, TIER_FP32>(a, sm, ntier, t, tx, ty, red);
+            else gg_tile_lo<T, TIER_HALF>(a, sm, ntier, t, tx, ty, red);
         }
         __syncthreads();
     }
@@ -533,17 +685,20 @@ __global__ void __launch_bounds__(kThreads, 2)
     }
 }
 
-size_t gg_ens_smem_bytes(int tile, int max_nf) { return gg_smem_bytes(tile, -1, max_nf); }
+// 32^2 ensemble tiles read their neighbourhoods directly (no shared memory)
+size_t gg_ens_smem_bytes(int tile, int max_nf) { return tile == 32 ? 0 : gg_smem_bytes(tile, -1, max_nf); }
 
 cudaError_t gg_prepare_ens(int tile, bool ref, int max_nf, int *blocks_per_sm)
 {
     const size_t smem = gg_ens_smem_bytes(tile, max_nf);
     const auto attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    cudaError_t e = cudaSuccess;
 #define AMPS_GGE(TT, RR)                                                                                   \
     do {                                                                                                   \
-        cudaError_t e = cudaFuncSetAttribute(gg_ens_kernel<TT, RR>, attr, (int)smem);                      \
+        e = cudaFuncSetAttribute(gg_ens_kernel<TT, RR, false>, attr, (int)smem);                           \
+        if (e == cudaSuccess) e = cudaFuncSetAttribute(gg_ens_kernel<TT, RR, true>, attr, (int)smem);      \
         if (e != cudaSuccess) return e;                                                                    \
-        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, gg_ens_kernel<TT, RR>, kThreads, smem); \
+        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, gg_ens_kernel<TT, RR, false>, kThreads, smem); \
     } while (0)
     if (tile == 32) {
         if (ref) AMPS_GGE(32, true);
@@ -554,16 +709,22 @@ cudaError_t gg_prepare_ens(int tile, bool ref, int max_nf, int *blocks_per_sm)
 #undef AMPS_GGE
 }
 
-cudaError_t gg_launch_ens(int tile, bool ref, const StepArgs *table, const int2 *items, int nitems, int *queue,
-                          int grid, size_t smem, cudaStream_t s)
+cudaError_t gg_launch_ens(int tile, bool ref, bool monitor, const StepArgs *table, const int2 *items, int nitems,
+                          int *queue, int grid, size_t smem, cudaStream_t s)
 {
+#define AMPS_GGEL(TT, RR)                                                                                      \
+    do {                                                                                                       \
+        if (monitor) gg_ens_kernel<TT, RR, true><<<grid, kThreads, smem, s>>>(table, items, nitems, queue);    \
+        else gg_ens_kernel<TT, RR, false><<<grid, kThreads, smem, s>>>(table, items, nitems, queue);           \
+    } while (0)
     if (tile == 32) {
-        if (ref) gg_ens_kernel<32, true><<<grid, kThreads, smem, s>>>(table, items, nitems, queue);
-        else gg_ens_kernel<32, false><<<grid, kThreads, smem, s>>>(table, items, nitems, queue);
+        if (ref) AMPS_GGEL(32, true);
+        else AMPS_GGEL(32, false);
     } else {
-        if (ref) gg_ens_kernel<16, true><<<grid, kThreads, smem, s>>>(table, items, nitems, queue);
-        else gg_ens_kernel<16, false><<<grid, kThreads, smem, s>>>(table, items, nitems, queue);
+        if (ref) AMPS_GGEL(16, true);
+        else AMPS_GGEL(16, false);
     }
+#undef AMPS_GGEL
     return cudaGetLastError();
 }
 
