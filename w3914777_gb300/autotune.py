@@ -98,25 +98,45 @@ def tune(params, init_kind, steps, err_bound=1e-3, candidates=None, reference=No
     return best, table
 
 
+WORKLOADS = {
+    # name: (preset model, tuned file, description, default steps, initial state, candidate tiles)
+    "graingrowth": ("graingrowth", "graingrowth_1024_q8.json", "graingrowth preset 0 (1024x1024, Q=8)", 10000,
+                    A.INIT_SEEDED, (32, 16)),
+    "kobayashi": ("kobayashi", "kobayashi_512.json",
+                  "kobayashi preset 0 (512x512 zero-flux, seeded noise)", 2000, A.INIT_SEEDED, (32, 16)),
+    "sintering": ("sintering", "sintering_1024_n16.json", "sintering preset 0 (1024x1024, 16 particles)", 2000,
+                  A.INIT_SEEDED, (32,)),
+}
+
+
+def workload_params(name):
+    """Parameters, initial-state kind and default tuning length of a named workload."""
+    model, _, _, steps, init, _ = WORKLOADS[name]
+    return A.Params.preset(model, 0), init, steps
+
+
 def _main():
-    """python -m w3914777_gb300.autotune graingrowth [steps] [err_bound]
-    Tunes the 1024^2 Q=8 grain-growth workload and writes
-    w3914777_gb300/tuned/graingrowth_1024_q8.json."""
+    """python -m w3914777_gb300.autotune {graingrowth|kobayashi|sintering} [steps] [err_bound] [out]
+    Tunes the named preset-0 workload and writes w3914777_gb300/tuned/<file>.json
+    (or `out`)."""
     import json
     import os
     import sys
-    model = sys.argv[1] if len(sys.argv) > 1 else "graingrowth"
-    steps = int(sys.argv[2]) if len(sys.argv) > 2 else 10000
+    name = sys.argv[1] if len(sys.argv) > 1 else "graingrowth"
+    if name not in WORKLOADS:
+        raise SystemExit(f"unknown workload {name!r}: one of {sorted(WORKLOADS)}")
+    p, init, default_steps = workload_params(name)
+    steps = int(sys.argv[2]) if len(sys.argv) > 2 else default_steps
     bound = float(sys.argv[3]) if len(sys.argv) > 3 else 1e-3
-    if model != "graingrowth":
-        raise SystemExit("only the grain-growth workload has a tuning entry point")
-    p = A.Params.preset("graingrowth", 0)
-    best, table = tune(p, A.INIT_SEEDED, steps, bound, log=lambda r: print(json.dumps(r), flush=True))
-    out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuned", "graingrowth_1024_q8.json")
+    tiles = WORKLOADS[name][5]
+    cands = [c for c in default_candidates(p) if c[1].get("tile", tiles[0]) in tiles]
+    best, table = tune(p, init, steps, bound, candidates=cands, log=lambda r: print(json.dumps(r), flush=True))
+    out = sys.argv[4] if len(sys.argv) > 4 else os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuned",
+                                                               WORKLOADS[name][1])
     os.makedirs(os.path.dirname(out), exist_ok=True)
     with open(out, "w") as f:
-        json.dump({"workload": "graingrowth preset 0 (1024x1024, Q=8)", "steps": steps, "err_bound": bound,
-                   "best": best, "table": table}, f, indent=1)
+        json.dump({"workload": WORKLOADS[name][2], "steps": steps, "err_bound": bound, "best": best, "table": table},
+                  f, indent=1)
     print("best:", json.dumps(best))
 
 

@@ -259,6 +259,8 @@ extern "C" int amps_create(const amps_params *p, amps_handle **out)
         }
         else if (p->model == AMPS_KOBAYASHI) pe = kob_prepare(h->T, t, p->ref_order != 0);
         else pe = sint_prepare(h->T, t, p->ref_order != 0, p->mu_lap_fp64 != 0);
+        if (pe == cudaSuccess && p->model != AMPS_GRAINGROWTH && t == TIER_FP32 && h->used[TIER_HALF])
+            pe = p->model == AMPS_KOBAYASHI ? kob_prepare_lo(h->T) : sint_prepare_lo(h->T, p->mu_lap_fp64 != 0);
         if (pe != cudaSuccess) {
             g_create_err = std::string("kernel attributes: ") + cudaGetErrorString(pe);
             free_all(h);
@@ -560,18 +562,23 @@ static int launch_step(amps_handle *h, int step_off, bool monitor_now)
         h->transition = false;
         return AMPS_OK;
     }
+    // half + FP32 in use: one launch covers both (profiled as index 3)
+    const bool lo_fused = h->used[TIER_HALF] && h->used[TIER_FP32];
     for (int t = 2; t >= 0; --t) {
-        if (!h->used[t]) continue;
+        if (!h->used[t] || (lo_fused && t == TIER_HALF)) continue;
+        const bool fused = lo_fused && t == TIER_FP32;
         cudaStream_t st = h->stream;
         a.list = h->d_lists + t * h->ntiles;
         cudaError_t e;
-        amps_handle::Ev ev{t, nullptr, nullptr};
+        amps_handle::Ev ev{fused ? 3 : t, nullptr, nullptr};
         if (h->profiling) {
             if (cudaEventCreate(&ev.a) != cudaSuccess || cudaEventCreate(&ev.b) != cudaSuccess)
                 FAIL(h, AMPS_ERR_CUDA, "event create");
             cudaEventRecord(ev.a, st);
         }
-        if (p.model == AMPS_KOBAYASHI) e = kob_launch(h->T, t, ref, a, h->ntiles, st);
+        if (fused) e = p.model == AMPS_KOBAYASHI ? kob_launch_lo(h->T, a, h->ntiles, st)
+                                                 : sint_launch_lo(h->T, p.mu_lap_fp64 != 0, a, h->ntiles, st);
+        else if (p.model == AMPS_KOBAYASHI) e = kob_launch(h->T, t, ref, a, h->ntiles, st);
         else e = sint_launch(h->T, t, ref, p.mu_lap_fp64 != 0, a, h->ntiles, st);
         if (e != cudaSuccess) FAIL(h, AMPS_ERR_CUDA, "step kernel launch: %s", cudaGetErrorString(e));
         if (h->profiling) {

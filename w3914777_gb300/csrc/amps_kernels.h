@@ -8,6 +8,12 @@ cudaError_t gg_launch(int tile, int tier, bool ref, const StepArgs &a, int grid,
 cudaError_t kob_launch(int tile, int tier, bool ref, const StepArgs &a, int grid, cudaStream_t s);
 cudaError_t sint_launch(int tile, int tier, bool ref, bool mu64, const StepArgs &a, int grid, cudaStream_t s);
 size_t gg_smem_bytes(int tile, int tier, int nf);
+// Kobayashi / sintering: the half and FP32 tiles of a step in one launch
+// (grid = all tiles; FP64 tiles are skipped, left to the FP64 tier launch).
+cudaError_t kob_launch_lo(int tile, const StepArgs &a, int grid, cudaStream_t s);
+cudaError_t sint_launch_lo(int tile, bool mu64, const StepArgs &a, int grid, cudaStream_t s);
+cudaError_t kob_prepare_lo(int tile);
+cudaError_t sint_prepare_lo(int tile, bool mu64);
 // Raise the dynamic shared-memory limit of the kernel a launch would use
 // (must run before any graph capture).
 cudaError_t gg_prepare(int tile, int tier, bool ref);

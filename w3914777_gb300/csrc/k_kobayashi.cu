@@ -29,21 +29,18 @@ template <typename CT> __device__ __forceinline__ CT k_cos(CT v) { return cos(v)
 template <typename CT> __device__ __forceinline__ CT k_sin(CT v) { return sin(v); }
 template <typename CT> __device__ __forceinline__ CT k_atan(CT v) { return atan(v); }
 
+// One tile of one step at tier TIER (smraw: the kernel's dynamic shared
+// memory, kob_smem<T, TIER> bytes; red / ntier: its static scratch).
 template <int T, int TIER, bool REF>
-__global__ void __launch_bounds__(kThreads) kob_step_kernel(StepArgs a)
+__device__ __forceinline__ void kob_tile(const StepArgs &a, unsigned char *smraw, double *red, uint8_t *ntier,
+                                         int tile)
 {
     using CT = typename std::conditional<TIER == TIER_FP64, double, float>::type;
     constexpr int R = 2;
     using S = Stage<CT, T, R>;
     constexpr int E = T + 2;  // phase-A region side (tile + 1-cell ring)
-    extern __shared__ __align__(16) unsigned char smraw[];
-    __shared__ double red[kThreads / 32];
-    __shared__ uint8_t ntier[9];
     CT *sm = reinterpret_cast<CT *>(smraw);
     CT *px = sm + 2 * S::FIELD, *py = px + E * E, *ep = py + E * E, *epd = ep + E * E;
-
-    if ((int)blockIdx.x >= a.count[TIER]) return;
-    const int tile = a.list[blockIdx.x];
     const int tx = tile % a.ntx, ty = tile / a.ntx;
     const int x0 = tx * T, y0 = ty * T;
     load_neighbour_tiers(a, tx, ty, ntier);
@@ -180,6 +177,33 @@ __global__ void __launch_bounds__(kThreads) kob_step_kernel(StepArgs a)
     }
 }
 
+// The tiles of one tier (list / count built by the classification).
+template <int T, int TIER, bool REF>
+__global__ void __launch_bounds__(kThreads) kob_step_kernel(StepArgs a)
+{
+    extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ double red[kThreads / 32];
+    __shared__ uint8_t ntier[9];
+    if ((int)blockIdx.x >= a.count[TIER]) return;
+    kob_tile<T, TIER, REF>(a, smraw, red, ntier, a.list[blockIdx.x]);
+}
+
+// The half and FP32 tiles of a step in one launch (one CTA per tile; FP64
+// tiles are left to the FP64 launch).  Per-tier launches would each cover
+// only part of the grid -- at 512^2 with 32^2 tiles less than one wave apiece
+// -- and run one after the other.
+template <int T>
+__global__ void __launch_bounds__(kThreads) kob_step_lo_kernel(StepArgs a)
+{
+    extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ double red[kThreads / 32];
+    __shared__ uint8_t ntier[9];
+    const int tile = blockIdx.x;
+    const int tier = a.tier_out[tile];
+    if (tier == TIER_FP32) kob_tile<T, TIER_FP32, false>(a, smraw, red, ntier, tile);
+    else if (tier == TIER_HALF) kob_tile<T, TIER_HALF, false>(a, smraw, red, ntier, tile);
+}
+
 template <int T, int TIER> static size_t kob_smem()
 {
     using CT = typename std::conditional<TIER == TIER_FP64, double, float>::type;
@@ -213,6 +237,20 @@ cudaError_t kob_launch(int tile, int tier, bool ref, const StepArgs &a, int grid
     if (tile == 32) { AMPS_KOB(32) }
     AMPS_KOB(16)
 #undef AMPS_KOB
+}
+
+cudaError_t kob_launch_lo(int tile, const StepArgs &a, int grid, cudaStream_t s)
+{
+    if (tile == 32) kob_step_lo_kernel<32><<<grid, kThreads, kob_smem<32, TIER_FP32>(), s>>>(a);
+    else kob_step_lo_kernel<16><<<grid, kThreads, kob_smem<16, TIER_FP32>(), s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t kob_prepare_lo(int tile)
+{
+    const auto attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    return tile == 32 ? cudaFuncSetAttribute(kob_step_lo_kernel<32>, attr, kMaxDynSmem)
+                      : cudaFuncSetAttribute(kob_step_lo_kernel<16>, attr, kMaxDynSmem);
 }
 
 cudaError_t kob_prepare(int tile, int tier, bool ref)

@@ -17,23 +17,20 @@
 
 namespace amps {
 
+// One tile of one step at tier TIER (smraw: the kernel's dynamic shared
+// memory, sint_smem<T, TIER, MU64> bytes; red / ntier: its static scratch).
 template <int T, int TIER, bool REF, bool MU64>
-__global__ void __launch_bounds__(kThreads) sint_step_kernel(StepArgs a)
+__device__ __forceinline__ void sint_tile(const StepArgs &a, unsigned char *smraw, double *red, uint8_t *ntier,
+                                          int tile)
 {
     using CT = typename std::conditional<TIER == TIER_FP64, double, float>::type;
     using MT = typename std::conditional<MU64, double, CT>::type;  // type of mu and lap(mu)
     using SC = Stage<CT, T, 2>;
     using SE = Stage<CT, T, 1>;
     constexpr int E = T + 2;
-    extern __shared__ __align__(16) unsigned char smraw[];
-    __shared__ double red[kThreads / 32];
-    __shared__ uint8_t ntier[9];
     MT *mu = reinterpret_cast<MT *>(smraw);                       // [E*E]
     CT *smc = reinterpret_cast<CT *>(smraw + sizeof(MT) * E * E);  // c, 2-cell halo
     CT *sme = smc + SC::FIELD;                                     // etas, 1-cell halo
-
-    if ((int)blockIdx.x >= a.count[TIER]) return;
-    const int tile = a.list[blockIdx.x];
     const int tx = tile % a.ntx, ty = tile / a.ntx;
     const int x0 = tx * T, y0 = ty * T;
     const int np = a.nf - 1;
@@ -172,6 +169,33 @@ __global__ void __launch_bounds__(kThreads) sint_step_kernel(StepArgs a)
     }
 }
 
+// The tiles of one tier (list / count built by the classification).
+template <int T, int TIER, bool REF, bool MU64>
+__global__ void __launch_bounds__(kThreads) sint_step_kernel(StepArgs a)
+{
+    extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ double red[kThreads / 32];
+    __shared__ uint8_t ntier[9];
+    if ((int)blockIdx.x >= a.count[TIER]) return;
+    sint_tile<T, TIER, REF, MU64>(a, smraw, red, ntier, a.list[blockIdx.x]);
+}
+
+// The half and FP32 tiles of a step in one launch (one CTA per tile; FP64
+// tiles, whose double staging needs more shared memory, are left to the FP64
+// launch).  Separate half and FP32 launches would each cover only part of
+// the grid and run one after the other.
+template <int T, bool MU64>
+__global__ void __launch_bounds__(kThreads) sint_step_lo_kernel(StepArgs a)
+{
+    extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ double red[kThreads / 32];
+    __shared__ uint8_t ntier[9];
+    const int tile = blockIdx.x;
+    const int tier = a.tier_out[tile];
+    if (tier == TIER_FP32) sint_tile<T, TIER_FP32, false, MU64>(a, smraw, red, ntier, tile);
+    else if (tier == TIER_HALF) sint_tile<T, TIER_HALF, false, MU64>(a, smraw, red, ntier, tile);
+}
+
 template <int T, int TIER, bool MU64> static size_t sint_smem(int nf)
 {
     using CT = typename std::conditional<TIER == TIER_FP64, double, float>::type;
@@ -215,6 +239,30 @@ cudaError_t sint_launch(int tile, int tier, bool ref, bool mu64, const StepArgs 
     if (tile == 32) { AMPS_SINT(32) }
     AMPS_SINT(16)
 #undef AMPS_SINT
+}
+
+cudaError_t sint_launch_lo(int tile, bool mu64, const StepArgs &a, int grid, cudaStream_t s)
+{
+#define AMPS_SLO(TT, MM) sint_step_lo_kernel<TT, MM><<<grid, kThreads, sint_smem<TT, TIER_FP32, MM>(a.nf), s>>>(a)
+    if (tile == 32) {
+        if (mu64) AMPS_SLO(32, true);
+        else AMPS_SLO(32, false);
+    } else {
+        if (mu64) AMPS_SLO(16, true);
+        else AMPS_SLO(16, false);
+    }
+#undef AMPS_SLO
+    return cudaGetLastError();
+}
+
+cudaError_t sint_prepare_lo(int tile, bool mu64)
+{
+    const auto attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    if (tile == 32)
+        return mu64 ? cudaFuncSetAttribute(sint_step_lo_kernel<32, true>, attr, kMaxDynSmem)
+                    : cudaFuncSetAttribute(sint_step_lo_kernel<32, false>, attr, kMaxDynSmem);
+    return mu64 ? cudaFuncSetAttribute(sint_step_lo_kernel<16, true>, attr, kMaxDynSmem)
+                : cudaFuncSetAttribute(sint_step_lo_kernel<16, false>, attr, kMaxDynSmem);
 }
 
 cudaError_t sint_prepare(int tile, int tier, bool ref, bool mu64)
