@@ -369,6 +369,8 @@ def run_ours(args):
             line["adjoint"] = run_adjoint()
         if not args.no_ensemble:
             line["ensemble"] = run_ensemble()
+        if not args.no_configs:
+            line["configs"] = run_configs()
         print(json.dumps(line), flush=True)
     sim.close()
     if world > 1:
@@ -528,6 +530,94 @@ def run_ensemble(steps=5000, check_steps=1000, count=64, seed=2024):
     }
 
 
+def run_configs(kob_steps=2000, sint_steps=20000):
+    """The other two models' seeded workloads at their tuned settings
+    (w3914777_gb300/tuned/*.json), each against its plain FP64 run from the
+    same initial state: Kobayashi dendrite 512^2 zero-flux with noise, 2000
+    steps (plus the all-FP32 run); sintering 1024^2 with 16 particles, 20000
+    steps, with the conserved-mass drift and the neck widths.  Device-timed
+    (CUDA events) graph replays; the states (4-34 MiB per tier) stay
+    L2-resident."""
+    import torch
+    import w3914777_gb300 as w
+
+    def tuned(name):
+        with open(os.path.join(ROOT, "w3914777_gb300", "tuned", name)) as f:
+            return json.load(f)["best"]["overrides"]
+
+    stream = torch.cuda.Stream()
+
+    def run(p, init, steps):
+        with w.Simulation(p) as s:
+            s.set_stream(stream.cuda_stream)
+            s.set_fields(init)
+            s.run(2 * p.cadence)  # captures the period graphs
+            s.set_fields(init)
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            s.run(steps)
+            b.record(stream)
+            s.synchronize()
+            ms = a.elapsed_time(b)
+            extra = {}
+            if p.model == w.KOBAYASHI:
+                extra["interface"] = s.interface(0, 0.5)
+            if p.model == w.SINTERING:
+                extra["mass"] = s.reduce(0, w.REDUCE_SUM)
+                bl = s.boundary_lengths(0.5)
+                iu = np.triu_indices(bl.shape[0], 1)
+                necks = bl[iu][bl[iu] > 0]
+                extra["necks"] = {"count": int(necks.size), "mean_width": float(necks.mean()) if necks.size else 0.0,
+                                  "max_width": float(necks.max()) if necks.size else 0.0}
+            st = s.stats()
+            ts = st["tile_steps"]
+            tot = max(sum(ts), 1)
+            return ms, s.fields(), extra, [t / tot for t in ts]
+
+    out = {}
+    # Kobayashi dendrite
+    p = w.Params.preset("kobayashi", 0)
+    init = w.init_host(p, w.INIT_SEEDED)
+    ms_a, f_a, x_a, mix = run(p.replace(**tuned("kobayashi_512.json")), init, kob_steps)
+    ms_64, f_64, x_64, _ = run(p.replace(mode=w.PUREHIGH, high_tier=w.TIER_FP64), init, kob_steps)
+    ms_32, f_32, _, _ = run(p.replace(mode=w.PUREHIGH, high_tier=w.TIER_FP32), init, kob_steps)
+    cells = p.nx * p.ny * kob_steps
+    out["kobayashi"] = {
+        "workload": f"Kobayashi dendrite {p.nx}x{p.ny} zero-flux, seeded noise, disc r^2<{p.init_r2:g} at the centre, "
+                    f"{kob_steps} steps, tuned spatial monitor",
+        "value": cells / (ms_a * 1e-3) / 1e9, "unit": "Gcell-updates/s",
+        "plain_fp64": cells / (ms_64 * 1e-3) / 1e9, "all_fp32": cells / (ms_32 * 1e-3) / 1e9,
+        "speedup_vs_plain_fp64": ms_64 / ms_a,
+        "max_abs_err_vs_fp64": float(np.abs(f_a - f_64).max()),
+        "mean_abs_err_vs_fp64": float(np.abs(f_a - f_64).mean()),
+        "all_fp32_max_abs_err": float(np.abs(f_32 - f_64).max()),
+        "interface": {"adaptive": x_a["interface"], "fp64": x_64["interface"]},
+        "tier_mix": dict(zip(("half", "fp32", "fp64"), mix)),
+    }
+    # sintering
+    p = w.Params.preset("sintering", 0)
+    init = w.init_host(p, w.INIT_SEEDED)
+    m0 = float(init[0].sum())
+    ms_a, f_a, x_a, mix = run(p.replace(**tuned("sintering_1024_n16.json")), init, sint_steps)
+    ms_64, f_64, x_64, _ = run(p.replace(mode=w.PUREHIGH, high_tier=w.TIER_FP64), init, sint_steps)
+    cells = p.nx * p.ny * sint_steps
+    out["sintering"] = {
+        "workload": f"sintering {p.nx}x{p.ny}, {p.nfields} particles (seeded non-overlapping discs), "
+                    f"{sint_steps} steps, FP64 chemical-potential Laplacian, tuned spatial monitor",
+        "value": cells / (ms_a * 1e-3) / 1e9, "unit": "Gcell-updates/s",
+        "plain_fp64": cells / (ms_64 * 1e-3) / 1e9, "speedup_vs_plain_fp64": ms_64 / ms_a,
+        "max_abs_err_vs_fp64": float(np.abs(f_a - f_64).max()),
+        "mean_abs_err_vs_fp64": float(np.abs(f_a - f_64).mean()),
+        "mass_drift": {"adaptive": (x_a["mass"] - m0) / m0, "fp64": (x_64["mass"] - m0) / m0,
+                       "note": "relative change of the FP64 sum of c; the reference clamps c to [0,1] after each "
+                               "step (sintering/function.h:100-101), which removes mass in both runs"},
+        "necks": {"adaptive": x_a["necks"], "fp64": x_64["necks"]},
+        "tier_mix": dict(zip(("half", "fp32", "fp64"), mix)),
+    }
+    return out
+
+
 def run_profile_case(args):
     """A short, untimed run of the tuned workload at nx^2 for ncu captures
     (`--profile-case 2048` puts a 256 MiB FP32 state, larger than L2)."""
@@ -557,6 +647,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true")
+    ap.add_argument("--no-configs", action="store_true")
     ap.add_argument("--profile-case", type=int, default=0)
     args = ap.parse_args()
     if args.profile_case:

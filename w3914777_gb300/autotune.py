@@ -26,9 +26,10 @@ def default_candidates(params):
     c = []
     tiles = [32, 16]
     spa = [(1e-3, math.inf), (3e-3, math.inf), (1e-2, math.inf), (2e-2, math.inf), (5e-2, math.inf),
-           (1e-3, 1.5), (1e-2, 1.5)]
-    tem = [(1e-6, math.inf), (1e-5, math.inf), (1e-4, math.inf), (1e-3, math.inf), (1e-5, 1e-1)]
-    rate = [(1e-5, math.inf), (1e-4, math.inf), (1e-3, math.inf), (1e-4, 1e-1)]
+           (1e-3, 1.5), (1e-2, 1.5), (1e-3, 0.9), (1e-3, 0.5)]
+    tem = [(1e-6, math.inf), (1e-5, math.inf), (1e-4, math.inf), (1e-3, math.inf), (1e-5, 1e-1), (1e-5, 1e-2),
+           (1e-5, 1e-3)]
+    rate = [(1e-5, math.inf), (1e-4, math.inf), (1e-3, math.inf), (1e-4, 1e-1), (1e-4, 1e-2), (1e-4, 1e-3)]
     for t in tiles:
         for lo, hi in spa:
             c.append((f"spa t{t} lo={lo:g} hi={hi:g}",
