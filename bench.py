@@ -576,12 +576,14 @@ def run_configs(kob_steps=2000, sint_steps=20000):
             return ms, s.fields(), extra, [t / tot for t in ts]
 
     out = {}
-    # Kobayashi dendrite
-    p = w.Params.preset("kobayashi", 0)
+    # Kobayashi dendrite (the FMA form throughout; the preset's reference-order
+    # arithmetic is for parity with the reference)
+    p = w.Params.preset("kobayashi", 0).replace(ref_order=0)
     init = w.init_host(p, w.INIT_SEEDED)
     ms_a, f_a, x_a, mix = run(p.replace(**tuned("kobayashi_512.json")), init, kob_steps)
-    ms_64, f_64, x_64, _ = run(p.replace(mode=w.PUREHIGH, high_tier=w.TIER_FP64), init, kob_steps)
-    ms_32, f_32, _, _ = run(p.replace(mode=w.PUREHIGH, high_tier=w.TIER_FP32), init, kob_steps)
+    # plain runs in the FMA form (ref_order=0), as the adaptive run's FP64 tiles
+    ms_64, f_64, x_64, _ = run(p.replace(mode=w.PUREHIGH, high_tier=w.TIER_FP64, ref_order=0), init, kob_steps)
+    ms_32, f_32, _, _ = run(p.replace(mode=w.PUREHIGH, high_tier=w.TIER_FP32, ref_order=0), init, kob_steps)
     cells = p.nx * p.ny * kob_steps
     out["kobayashi"] = {
         "workload": f"Kobayashi dendrite {p.nx}x{p.ny} zero-flux, seeded noise, disc r^2<{p.init_r2:g} at the centre, "
@@ -600,7 +602,7 @@ def run_configs(kob_steps=2000, sint_steps=20000):
     init = w.init_host(p, w.INIT_SEEDED)
     m0 = float(init[0].sum())
     ms_a, f_a, x_a, mix = run(p.replace(**tuned("sintering_1024_n16.json")), init, sint_steps)
-    ms_64, f_64, x_64, _ = run(p.replace(mode=w.PUREHIGH, high_tier=w.TIER_FP64), init, sint_steps)
+    ms_64, f_64, x_64, _ = run(p.replace(mode=w.PUREHIGH, high_tier=w.TIER_FP64, ref_order=0), init, sint_steps)
     cells = p.nx * p.ny * sint_steps
     out["sintering"] = {
         "workload": f"sintering {p.nx}x{p.ny}, {p.nfields} particles (seeded non-overlapping discs), "
