@@ -1,0 +1,82 @@
+/*
+ * amps_compat.h -- the reference's kernel names as host launch wrappers.
+ *
+ * For a driver written against the reference's kernel interface
+ * (snowflake/function.h, graingrowth/function.h, sintering/function.h and
+ * the monitor tools in snowflake/tools.h): each function below takes the
+ * same device arrays, in the same order and with the same roles, as the
+ * reference kernel it is named after, and computes the same values (FP64,
+ * the reference's expression order, no fused multiply-add), so a reference
+ * time loop can swap `kernel<<<grid, block>>>(args)` for
+ * `amps_<app>_kernel(&params, args, stream)` line by line.  What the
+ * reference fixes at compile time -- grid size, tile size, physical
+ * constants, the threshold -- comes from an amps_params (amps_preset gives
+ * the reference's parameter files).  Arrays are row-major [ny][nx] doubles
+ * in device memory, allocated by the caller; the neighbour map follows
+ * p->bc (the reference's pure kernels are periodic).  Work is queued on
+ * `stream` (cudaStream_t as void*, NULL = default stream); the calls return
+ * an amps status.
+ *
+ * This is the compatibility path: one thread per cell, intermediates in
+ * full-size arrays, several launches per step, as in the reference.  The
+ * fast path for the same time loop is amps_run (include/amps.h).
+ */
+#ifndef AMPS_COMPAT_H
+#define AMPS_COMPAT_H
+#include "amps.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* snowflake/function.h:5-35 -- phi_lap, tempr_lap, phidx, phidy, epsilon,
+ * epsilon_deri from phi and tempr. */
+AMPS_API int amps_snowflake_kernel1_pure(const amps_params *p, const double *phi, double *phi_lap, const double *tempr,
+                                         double *tempr_lap, double *phidx, double *phidy, double *epsilon,
+                                         double *epsilon_deri, void *stream);
+/* snowflake/function.h:36-60 -- advances phi and tempr in place from the
+ * intermediates of kernel1_pure. */
+AMPS_API int amps_snowflake_kernel2_pure(const amps_params *p, double *phi, const double *phi_lap,
+                                         const double *epsilon, const double *epsilon_deri, const double *phidx,
+                                         const double *phidy, double *tempr, const double *tempr_lap, void *stream);
+/* snowflake/tools.h:24-33 -- sets phi = 1 inside the reference's seed disc
+ * (r^2 < p->init_r2 about the centre + p->init_offset); other cells untouched. */
+AMPS_API int amps_snowflake_dataprepare_high(const amps_params *p, double *phi, void *stream);
+
+/* graingrowth/function.h:5-31 -- one order parameter: etaa_lap, dfdetaa and
+ * etaa_out from etaa and the other one, etab (the reference's two-grain
+ * energy, cross coefficient 1). */
+AMPS_API int amps_graingrowth_kernel1_pure(const amps_params *p, const double *etaa, const double *etab,
+                                           double *etaa_lap, double *dfdetaa, double *etaa_out, void *stream);
+
+/* sintering/function.h:51-79 -- con_lap, dfdcon and dummy (the chemical
+ * potential) from con, eta1, eta2.  `step` is the reference's unused step index. */
+AMPS_API int amps_sintering_con1_pure(const amps_params *p, const double *con, double *con_lap, const double *eta1,
+                                      const double *eta2, double *dfdcon, double *dummy, int step, void *stream);
+/* sintering/function.h:80-108 -- dummy_lap, then con in place (clamped to [0,1]). */
+AMPS_API int amps_sintering_con2_pure(const amps_params *p, const double *dummy, double *dummy_lap, double *con,
+                                      const double *eta1, const double *eta2, int step, void *stream);
+/* sintering/function.h:110-134 and :135-159 -- one particle's eta: eta_lap,
+ * dfdeta and eta_out (clamped to [0,1]) from eta, the other particle and con. */
+AMPS_API int amps_sintering_phi1_pure(const amps_params *p, const double *eta1, double *eta1_out, const double *eta2,
+                                      double *eta1_lap, double *dfdeta1, const double *con, int step, void *stream);
+AMPS_API int amps_sintering_phi2_pure(const amps_params *p, const double *eta2, double *eta2_out, const double *eta1,
+                                      double *eta2_lap, double *dfdeta2, const double *con, int step, void *stream);
+
+/* snowflake/tools.h:177-193 -- Monitor1: per tile, the range of `con` over
+ * the 4x4 sample lattice (scaled to p->tile); max_diff_con [nty][ntx]. */
+AMPS_API int amps_get_max_diff1(const amps_params *p, const double *con, double *max_diff_con, void *stream);
+/* snowflake/tools.h:194-211 -- Monitor2: per tile, max |last - now| over the
+ * lattice {2,6,10,14} (scaled). */
+AMPS_API int amps_get_max_diff2(const amps_params *p, const double *test_data_last, const double *test_data,
+                                double *max_diffs, void *stream);
+/* snowflake/tools.h:212-230 -- tile types: type_old = type_con; type_con =
+ * 2 where the 5-point (non-periodic) max of max_diff_con >= p->thr_hi,
+ * else 1.  int arrays [nty][ntx]. */
+AMPS_API int amps_get_type(const amps_params *p, const double *max_diff_con, int *type_old, int *type_con,
+                           void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -18,7 +18,7 @@ def amps():
 
 
 def declared_symbols():
-    src = open(os.path.join(ROOT, "include", "amps.h")).read()
+    src = "".join(open(os.path.join(ROOT, "include", h)).read() for h in ("amps.h", "amps_compat.h"))
     return sorted(set(re.findall(r"AMPS_API[^;(]*?\b(amps_\w+)\s*\(", src)))
 
 

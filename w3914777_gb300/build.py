@@ -22,7 +22,9 @@ OBJ = os.path.join(OUT, "obj-" + platform.machine())
 _ELF_MACHINE = {"x86_64": 62, "aarch64": 183}
 
 SOURCES = ["amps_api.cu", "amps_host.cpp", "k_common.cu", "k_graingrowth.cu", "k_kobayashi.cu",
-           "k_sintering.cu", "k_noalloc.cu", "k_adjoint.cu", "k_diag.cu"]
+           "k_sintering.cu", "k_noalloc.cu", "k_adjoint.cu", "k_diag.cu", "compat.cu"]
+# per-file flags: the reference-named kernels keep the reference's rounding (no fused multiply-add)
+FILE_FLAGS = {"compat.cu": ["-fmad=false"]}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
               "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include")]
@@ -61,7 +63,7 @@ def build(verbose=False, force=False, extra_flags=()):
         if foreign_binary(path):
             os.remove(path)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
-    headers.append(os.path.join(ROOT, "include", "amps.h"))
+    headers += [os.path.join(ROOT, "include", h) for h in ("amps.h", "amps_compat.h")]
     cc = nvcc()
     jobs = []
     objs = []
@@ -70,7 +72,7 @@ def build(verbose=False, force=False, extra_flags=()):
         obj = os.path.join(OBJ, src + ".o")
         objs.append(obj)
         if force or _newer(obj, [path] + headers):
-            cmd = [cc, *ARCH, *NVCC_FLAGS, *extra_flags, "-c", path, "-o", obj]
+            cmd = [cc, *ARCH, *NVCC_FLAGS, *FILE_FLAGS.get(src, []), *extra_flags, "-c", path, "-o", obj]
             if src.endswith(".cpp"):
                 cmd = [cc, *NVCC_FLAGS, "-x", "c++", "-c", path, "-o", obj]
             jobs.append(cmd)
