@@ -119,6 +119,24 @@ def dist_setup():
     return world, rank, local
 
 
+def max_over_ranks(x, world, device="cpu"):
+    """The largest of every rank's x (the job's time is its slowest rank's);
+    x itself when there is one rank.  `device`: where the collective's tensor
+    lives (the GPU for NCCL, the CPU for gloo)."""
+    if world <= 1:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(world, cells, steps_per_run, runs, total_ms):
+    """Whole-job Gcell-updates/s: every rank advances its own grid (weak
+    scaling, replicas), timed by the slowest rank."""
+    return world * cells * steps_per_run * runs / (total_ms * 1e-3) / 1e9
+
+
 def cpu_threads():
     try:
         return len(os.sched_getaffinity(0))
@@ -230,12 +248,8 @@ def run_ours(args):
         t_wall = time.perf_counter() - t_wall
     barrier()
     ms = [a.elapsed_time(b) for a, b in evs]
-    total_ms = sum(ms)
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * cells * S * args.steps / (total_ms * 1e-3) / 1e9
+    total_ms = max_over_ranks(sum(ms), world, dev)
+    value = job_rate(world, cells, S, args.steps, total_ms)
     stats = sim.stats()
     final_mixed = sim.fields()
     grains_mixed = sim.grains(threshold=0.5)
@@ -253,12 +267,8 @@ def run_ours(args):
         rc = lib.amps_get_fields(sim.h, ctypes.c_void_p(host_out.data_ptr()), w.F64, 0)
         assert rc == 0
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
-    e2e_total = sum(e2e_ms)
-    if world > 1:
-        t = torch.tensor([e2e_total], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_total = float(t.item())
-    e2e = world * cells * S * len(e2e_ms) / (e2e_total * 1e-3) / 1e9
+    e2e_total = max_over_ranks(sum(e2e_ms), world, dev)
+    e2e = job_rate(world, cells, S, len(e2e_ms), e2e_total)
     bytes_io = nf * cells * 8
 
     # ---- profiled run: per-tier kernel durations for the roofline ----
@@ -365,11 +375,12 @@ def run_ours(args):
         }
         if cpu:
             line["cpu_baseline"] = cpu
-        if not args.no_adjoint:
+        # single-GPU evidence: measured at N=1 only
+        if world == 1 and not args.no_adjoint:
             line["adjoint"] = run_adjoint()
-        if not args.no_ensemble:
+        if world == 1 and not args.no_ensemble:
             line["ensemble"] = run_ensemble()
-        if not args.no_configs:
+        if world == 1 and not args.no_configs:
             line["configs"] = run_configs()
         print(json.dumps(line), flush=True)
     sim.close()
