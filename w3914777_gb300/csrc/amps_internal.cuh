@@ -270,6 +270,53 @@ __device__ __forceinline__ void stage_tile(const StepArgs &a, CT *sm, const uint
     }
 }
 
+// Stage fields [0, nfs) of a tile whose whole 3x3 neighbourhood holds FP32
+// input (no conversion) with an R-cell halo, by asynchronous global->shared
+// copies: 16-byte copies for the interior 8-cell row segments (L2 only, the
+// values are read once from global memory) and 4-byte copies for the halo
+// cells, every field in flight at once, no register round trip.  Same slot
+// layout and the same floats as stage_tile; the caller synchronises after
+// the final wait issued here.
+template <int T, int R>
+__device__ __forceinline__ void stage_tile_async32(const StepArgs &a, float *sm, int tx, int ty, int nfs)
+{
+    using S = Stage<float, T, R>;
+    constexpr int SEG = T / 8;
+    constexpr int UI = S::ROWS * SEG;
+    constexpr int UH = S::ROWS * 2 * R;
+    const float *src = (const float *)a.in[TIER_FP32];
+    const int x0 = tx * T, y0 = ty * T;
+    for (int u = threadIdx.x; u < UI + UH; u += kThreads) {
+        int64_t goff;
+        int soff;
+        bool seg;
+        if (u < UI) {
+            const int sg = u % SEG, r = u / SEG;
+            goff = (int64_t)bc_map(y0 - R + r, a.ny, a.bc) * a.nx + x0 + 8 * sg;
+            soff = r * S::P + S::O + 8 * sg;
+            seg = true;
+        } else {
+            const int h = u - UI, k = h % (2 * R), r = h / (2 * R);
+            const int lx = k < R ? x0 - R + k : x0 + T + (k - R);
+            goff = (int64_t)bc_map(y0 - R + r, a.ny, a.bc) * a.nx + bc_map(lx, a.nx, a.bc);
+            soff = r * S::P + (k < R ? S::O - R + k : S::O + T + (k - R));
+            seg = false;
+        }
+        for (int f = 0; f < nfs; ++f) {
+            const float *g = src + (int64_t)f * a.n + goff;
+            const uint32_t d = smem_u32(sm + f * S::FIELD + soff);
+            if (seg) {
+                asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(g) : "memory");
+                asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d + 16), "l"(g + 4) : "memory");
+            } else {
+                asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(g) : "memory");
+            }
+        }
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+}
+
 // ---- block reductions (warp shuffle + one shared slot per warp) ------------------
 __device__ __forceinline__ double warp_max(double v)
 {

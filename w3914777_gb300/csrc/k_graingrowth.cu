@@ -354,7 +354,8 @@ __global__ void __launch_bounds__(kThreads, 4) gg_step_kernel(StepArgs a)
         gg_tile_fp64<T, REF>(a, ntier, tile, tx, ty, red);
         return;
     }
-    stage_tile<float, T, 1>(a, sm, ntier, tx, ty, 0, a.nf);
+    if (all_fp32(ntier)) stage_tile_async32<T, 1>(a, sm, tx, ty, a.nf);
+    else stage_tile<float, T, 1>(a, sm, ntier, tx, ty, 0, a.nf);
     __syncthreads();
     if (tier == TIER_FP32) gg_tile_lo_impl<T, TIER_FP32, SRC_SMEM, MON>(a, sm, ntier, tile, tx, ty, red);
     else gg_tile_lo_impl<T, TIER_HALF, SRC_SMEM, MON>(a, sm, ntier, tile, tx, ty, red);
