@@ -201,6 +201,69 @@ __device__ __forceinline__ void gg_tile_lo(const StepArgs &a, const float *sm, c
     else gg_tile_lo_impl<T, TIER, SRC, false>(a, sm, nt, tile, tx, ty, red);
 }
 
+// Half/FP32 tile on a step without the monitor, 32^2 tiles, from the staged
+// float neighbourhood: each thread advances 2 rows x 4 cells, reading 4
+// staged rows (instead of 3 per output row), and the CTA's two halves take
+// alternate fields.  Per cell the arithmetic is gg_tile_lo_impl's.
+template <int TIER>
+__device__ __forceinline__ void gg_tile_lo_2row(const StepArgs &a, const float *sm, int tx, int ty)
+{
+    constexpr int T = 32, CPT = 4, GPR = T / CPT;
+    using S = Stage<float, T, 1>;
+    float *smm = const_cast<float *>(sm);
+    const int half = threadIdx.x / (kThreads / 2), t = threadIdx.x % (kThreads / 2);
+    const int r0 = 2 * (t / GPR), c0 = (t % GPR) * CPT;  // tile-local rows r0, r0 + 1
+    const int nf = a.nf;
+    const Phys &ph = a.ph;
+    float ssum[2][CPT];
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+#pragma unroll
+        for (int k = 0; k < CPT; ++k) ssum[r][k] = 0.f;
+    for (int f = 0; f < nf; ++f)
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+            const float4 q = *reinterpret_cast<const float4 *>(&S::at(smm, f, r0 + 1 + r, S::O + c0));
+            ssum[r][0] = fmaf(q.x, q.x, ssum[r][0]);
+            ssum[r][1] = fmaf(q.y, q.y, ssum[r][1]);
+            ssum[r][2] = fmaf(q.z, q.z, ssum[r][2]);
+            ssum[r][3] = fmaf(q.w, q.w, ssum[r][3]);
+        }
+    const float dtm = (float)(ph.dt * ph.mobil), g2 = (float)(2.0 * ph.gamma), kap = (float)ph.grcoef;
+    const float inv = (float)ph.inv_dxdy;
+    const int64_t gbase = (int64_t)(ty * T + r0) * a.nx + tx * T + c0;
+    for (int f = half; f < nf; f += 2) {
+        float w[4][CPT + 2];
+#pragma unroll
+        for (int rr = 0; rr < 4; ++rr) {
+            const float *p = &S::at(smm, f, r0 + rr, S::O + c0);
+            const float4 q = *reinterpret_cast<const float4 *>(p);
+            w[rr][1] = q.x; w[rr][2] = q.y; w[rr][3] = q.z; w[rr][4] = q.w;
+            w[rr][0] = p[-1];
+            w[rr][CPT + 1] = p[CPT];
+        }
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+            float out[CPT];
+#pragma unroll
+            for (int k = 0; k < CPT; ++k) {
+                const float e = w[r + 1][k + 1];
+                float s;
+                if (a.stencil == 0)
+                    s = (w[r][k] + w[r][k + 1] + w[r][k + 2]) + (w[r + 1][k] + w[r + 1][k + 2]) +
+                        (w[r + 2][k] + w[r + 2][k + 1] + w[r + 2][k + 2]) - 8.f * e;
+                else
+                    s = (w[r + 1][k] + w[r + 1][k + 2]) + (w[r][k + 1] + w[r + 2][k + 1]) - 4.f * e;
+                const float lap = s * inv;
+                const float e2 = e * e;
+                const float dfd = e * fmaf(g2, ssum[r][k] - e2, e2 - 1.f);
+                out[k] = fmaf(-dtm, fmaf(-kap, lap, dfd), e);
+            }
+            store_cells<TIER, CPT>(a, (int64_t)f * a.n + gbase + (int64_t)r * a.nx, out);
+        }
+    }
+}
+
 // One cell of the FP64 tile's neighbourhood at tile-local (ly, lx), read at
 // its owner tile's input tier.
 template <int T>
@@ -357,6 +420,11 @@ __global__ void __launch_bounds__(kThreads, 4) gg_step_kernel(StepArgs a)
     if (all_fp32(ntier)) stage_tile_async32<T, 1>(a, sm, tx, ty, a.nf);
     else stage_tile<float, T, 1>(a, sm, ntier, tx, ty, 0, a.nf);
     __syncthreads();
+    if constexpr (T == 32 && !MON) {
+        if (tier == TIER_FP32) gg_tile_lo_2row<TIER_FP32>(a, sm, tx, ty);
+        else gg_tile_lo_2row<TIER_HALF>(a, sm, tx, ty);
+        return;
+    }
     if (tier == TIER_FP32) gg_tile_lo_impl<T, TIER_FP32, SRC_SMEM, MON>(a, sm, ntier, tile, tx, ty, red);
     else gg_tile_lo_impl<T, TIER_HALF, SRC_SMEM, MON>(a, sm, ntier, tile, tx, ty, red);
     (void)sizeof(S);
