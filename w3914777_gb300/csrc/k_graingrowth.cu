@@ -201,12 +201,16 @@ __device__ __forceinline__ void gg_tile_lo(const StepArgs &a, const float *sm, c
     else gg_tile_lo_impl<T, TIER, SRC, false>(a, sm, nt, tile, tx, ty, red);
 }
 
-// Half/FP32 tile on a step without the monitor, 32^2 tiles, from the staged
-// float neighbourhood: each thread advances 2 rows x 4 cells, reading 4
-// staged rows (instead of 3 per output row), and the CTA's two halves take
-// alternate fields.  Per cell the arithmetic is gg_tile_lo_impl's.
-template <int TIER>
-__device__ __forceinline__ void gg_tile_lo_2row(const StepArgs &a, const float *sm, int tx, int ty)
+// Half/FP32 tile, 32^2 tiles, from the staged float neighbourhood: each
+// thread advances 2 rows x 4 cells, reading 4 staged rows (instead of 3 per
+// output row), and the CTA's two halves take alternate fields.  Per cell the
+// arithmetic is gg_tile_lo_impl's.  MON (temporal or rate monitor only): the
+// tile metric is a maximum over fields and cells, so each thread folds every
+// field it computes into one accumulator and the block reduces once at the
+// end -- the same metric as one reduction per field.
+template <int TIER, bool MON>
+__device__ __forceinline__ void gg_tile_lo_2row(const StepArgs &a, const float *sm, int tile, int tx, int ty,
+                                                double *red)
 {
     constexpr int T = 32, CPT = 4, GPR = T / CPT;
     using S = Stage<float, T, 1>;
@@ -232,7 +236,11 @@ __device__ __forceinline__ void gg_tile_lo_2row(const StepArgs &a, const float *
     const float dtm = (float)(ph.dt * ph.mobil), g2 = (float)(2.0 * ph.gamma), kap = (float)ph.grcoef;
     const float inv = (float)ph.inv_dxdy;
     const int64_t gbase = (int64_t)(ty * T + r0) * a.nx + tx * T + c0;
+    MonAccF mon;
+    if (MON) mon_reset(a, mon);
     for (int f = half; f < nf; f += 2) {
+        const bool mon_f = MON && (a.mfield < 0 || a.mfield == f);
+        const int mslot = a.mfield < 0 ? f : 0;
         float w[4][CPT + 2];
 #pragma unroll
         for (int rr = 0; rr < 4; ++rr) {
@@ -259,8 +267,20 @@ __device__ __forceinline__ void gg_tile_lo_2row(const StepArgs &a, const float *
                 const float dfd = e * fmaf(g2, ssum[r][k] - e2, e2 - 1.f);
                 out[k] = fmaf(-dtm, fmaf(-kap, lap, dfd), e);
             }
-            store_cells<TIER, CPT>(a, (int64_t)f * a.n + gbase + (int64_t)r * a.nx, out);
+            const int64_t g = (int64_t)f * a.n + gbase + (int64_t)r * a.nx;
+            store_cells<TIER, CPT>(a, g, out);
+            if (mon_f) {
+                const int64_t gi = gbase + (int64_t)r * a.nx;
+#pragma unroll
+                for (int k = 0; k < CPT; ++k)
+                    mon_add<T>(a, mon, mslot, tile, r0 + r, c0 + k, gi + k, round_to_tier<TIER>(out[k]),
+                               w[r + 1][k + 1], snap_prefetch<T>(a, mslot, tile, r0 + r, c0 + k, gi + k));
+            }
         }
+    }
+    if (MON) {
+        const double metric = mon_finish(a, mon, red, 0.0);
+        if (threadIdx.x == 0) a.metric[tile] = metric;
     }
 }
 
@@ -420,10 +440,12 @@ __global__ void __launch_bounds__(kThreads, 4) gg_step_kernel(StepArgs a)
     if (all_fp32(ntier)) stage_tile_async32<T, 1>(a, sm, tx, ty, a.nf);
     else stage_tile<float, T, 1>(a, sm, ntier, tx, ty, 0, a.nf);
     __syncthreads();
-    if constexpr (T == 32 && !MON) {
-        if (tier == TIER_FP32) gg_tile_lo_2row<TIER_FP32>(a, sm, tx, ty);
-        else gg_tile_lo_2row<TIER_HALF>(a, sm, tx, ty);
-        return;
+    if constexpr (T == 32) {
+        if (!MON || a.monitor_kind != 1) {  // the spatial range needs one reduction per field
+            if (tier == TIER_FP32) gg_tile_lo_2row<TIER_FP32, MON>(a, sm, tile, tx, ty, red);
+            else gg_tile_lo_2row<TIER_HALF, MON>(a, sm, tile, tx, ty, red);
+            return;
+        }
     }
     if (tier == TIER_FP32) gg_tile_lo_impl<T, TIER_FP32, SRC_SMEM, MON>(a, sm, ntier, tile, tx, ty, red);
     else gg_tile_lo_impl<T, TIER_HALF, SRC_SMEM, MON>(a, sm, ntier, tile, tx, ty, red);
