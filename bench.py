@@ -378,6 +378,7 @@ def run_ours(args):
         # single-GPU evidence: measured at N=1 only
         if world == 1 and not args.no_adjoint:
             line["adjoint"] = run_adjoint()
+            line["adjoint"]["graingrowth"] = run_adjoint_gg()
         if world == 1 and not args.no_ensemble:
             line["ensemble"] = run_ensemble()
         if world == 1 and not args.no_configs:
@@ -460,6 +461,80 @@ def run_adjoint(steps=1000, segment=32, n=256):
         "fp32_vs_fp64_param_grad_rel": rel32, "fp32_vs_fp64_T0_grad_rel_l2": relT0,
         "fp64_delta_grad_vs_central_difference_rel": abs(float(g64[0]) - fd) / abs(fd),
     }
+
+
+def run_adjoint_gg(steps=200, n=1024, q=8):
+    """Checkpointed adjoint of 200 grain-growth steps at 1024^2, Q = 8
+    (sqrt(N)-step checkpoints) from the coarsening state after 1000 FP64
+    steps of the seeded multi-grain start (the first steps amplify the
+    start's noise, and with it rounding); loss = L2 misfit of all order parameters against
+    the FP64 forward with L scaled by 1.1.  Times one eager step
+    and its adjoint, and the forward and backward sweeps (CUDA events,
+    median of 3), FP32 and FP64; checks the FP32 gradients against FP64 ones
+    and the FP64 L-gradient against a central difference (h = 1e-4 L)."""
+    import torch
+    from w3914777_gb300 import adjoint, amps
+
+    p = amps.Params.preset(amps.GRAINGROWTH, 0, nx=n, ny=n, nfields=q)
+    base = [p.mobil, p.grcoef, p.gamma]
+
+    def med(fn, reps=3):
+        fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn()
+            b.record()
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b))
+        return statistics.median(ts)
+
+    warm = adjoint.Stepper(p, torch.float64)
+    x64 = torch.tensor(amps.init_host(p, amps.INIT_SEEDED), device="cuda")
+    nxt = torch.empty_like(x64)
+    for i in range(1000):
+        warm.forward(x64, i, out=nxt)
+        x64, nxt = nxt, x64
+    x = x64.cpu().numpy()
+    run64 = adjoint.Rollout(p, steps, torch.float64)
+    tgt = run64.forward(x64, [1.1 * p.mobil, p.grcoef, p.gamma]).clone()
+
+    def loss_at(vals):
+        return float(0.5 * ((run64.forward(x64, vals) - tgt) ** 2).sum())
+
+    out = {"workload": f"grain growth {n}x{n}, Q={q}, {steps} steps from step 1000, sqrt(N)-step checkpoints; "
+                       "grads w.r.t. L, kappa, gamma, eta0"}
+    grads = {}
+    for name, dtype in (("fp32", torch.float32), ("fp64", torch.float64)):
+        run = run64 if dtype == torch.float64 else adjoint.Rollout(p, steps, dtype)
+        pv = torch.tensor(base, dtype=torch.float64, requires_grad=True)
+        x0 = torch.tensor(x, dtype=dtype, device="cuda", requires_grad=True)
+        y = adjoint.rollout(x0, p, steps, param_values=pv, runner=run)
+        (0.5 * ((y.double() - tgt) ** 2).sum()).backward()
+        grads[name] = (pv.grad.clone(), x0.grad.double())
+        x0d = x0.detach()
+        gf = torch.ones_like(x0d)
+        tf = med(lambda: run.forward(x0d, base))
+        tb = med(lambda: run.backward(gf))
+        st = adjoint.Stepper(p, dtype)
+        ys, gi = torch.empty_like(x0d), torch.empty_like(x0d)
+        gp = torch.zeros(3, dtype=torch.float64, device="cuda")
+        t_sf = med(lambda: [st.forward(x0d, 0, out=ys) for _ in range(50)]) / 50
+        t_sa = med(lambda: [st.adjoint(x0d, gf, 0, gp, grad_in=gi) for _ in range(50)]) / 50
+        out[name] = {"forward_sweep_ms": tf, "backward_sweep_ms": tb, "ratio": tb / tf,
+                     "step_forward_us": t_sf * 1e3, "step_adjoint_us": t_sa * 1e3, "step_ratio": t_sa / t_sf}
+        if run is not run64:
+            run.close()
+    g32, g64 = grads["fp32"], grads["fp64"]
+    out["fp32_vs_fp64_param_grad_rel"] = float(((g32[0] - g64[0]).abs() / g64[0].abs()).max())
+    out["fp32_vs_fp64_eta0_grad_rel_l2"] = float((g32[1] - g64[1]).norm() / g64[1].norm())
+    h = 1e-4 * p.mobil
+    fd = (loss_at([p.mobil + h, p.grcoef, p.gamma]) - loss_at([p.mobil - h, p.grcoef, p.gamma])) / (2 * h)
+    out["fp64_L_grad_vs_central_difference_rel"] = abs(float(g64[0][0]) - fd) / abs(fd)
+    run64.close()
+    return out
 
 
 def run_ensemble(steps=5000, check_steps=1000, count=64, seed=2024):

@@ -399,21 +399,54 @@ __global__ void __launch_bounds__(kAdjThreads)
 constexpr int kGX = 32, kGY = 8;
 using GReg = Reg<kGX, kGY, 1>;
 
-// Stage q fields of f (row-major [q][n]) over the halo-1 region.  zero_out:
+// One element from global to shared memory by an asynchronous copy (the
+// copies of all rows stay in flight until gg_stage_wait).
+template <typename R> __device__ __forceinline__ void cp_elem(R *d, const R *g)
+{
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(d);
+    if constexpr (sizeof(R) == 4)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sa), "l"(g) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sa), "l"(g) : "memory");
+}
+
+__device__ __forceinline__ void gg_stage_wait()
+{
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+}
+
+// Stage q fields of f (row-major [q][n]) over the halo-1 region, one warp
+// per region row (a coalesced copy of the row's kGX interior cells, two
+// lanes for its halo cells); complete after gg_stage_wait.  zero_out:
 // zero-flux cotangents are zero outside the domain (the transpose adds the
 // mirrored preimages itself).
 template <typename R>
 __device__ __forceinline__ void gg_stage(R *s, const R *f, int q, int x0, int y0, const GgAdj &p, bool zero_out)
 {
+    static_assert(kGX == 32, "one lane per interior column");
     const int64_t n = (int64_t)p.nx * p.ny;
-    for (int u = threadIdx.x; u < q * GReg::N; u += kAdjThreads) {
-        const int k = u / GReg::N, r = u - k * GReg::N;
-        const int gx = x0 - 1 + r % GReg::W, gy = y0 - 1 + r / GReg::W;
-        R v = R(0);
-        const bool dom = gx >= 0 && gx < p.nx && gy >= 0 && gy < p.ny;
-        if (gx <= p.nx && gy <= p.ny && !(zero_out && p.bc == 1 && !dom))
-            v = f[k * n + (int64_t)nbmap(gy, p.ny, p.bc) * p.nx + nbmap(gx, p.nx, p.bc)];
-        s[u] = v;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const bool zf = zero_out && p.bc == 1;
+    for (int rr = warp; rr < q * GReg::HT; rr += kAdjThreads / 32) {
+        const int k = rr / GReg::HT, ry = rr - k * GReg::HT;
+        const int gy = y0 - 1 + ry;
+        const bool rowok = gy <= p.ny && !(zf && (gy < 0 || gy >= p.ny));
+        const R *row = f + k * n + (int64_t)(rowok ? nbmap(gy, p.ny, p.bc) : 0) * p.nx;
+        R *dst = s + k * GReg::N + ry * GReg::W;
+        const int gx = x0 + lane;
+        if (rowok && gx <= p.nx && !(zf && gx >= p.nx))
+            cp_elem(dst + 1 + lane, row + nbmap(gx, p.nx, p.bc));
+        else
+            dst[1 + lane] = R(0);
+        if (lane < 2) {
+            const int hx = lane == 0 ? x0 - 1 : x0 + kGX;
+            R *d = dst + (lane == 0 ? 0 : GReg::W - 1);
+            if (rowok && hx <= p.nx && !(zf && (hx < 0 || hx >= p.nx)))
+                cp_elem(d, row + nbmap(hx, p.nx, p.bc));
+            else
+                *d = R(0);
+        }
     }
 }
 
@@ -434,6 +467,9 @@ template <typename R> __device__ __forceinline__ R gg_lap_s(const R *s, int o, i
 template <typename R>
 __device__ __forceinline__ R gg_lap_t_s(const R *s, int o, int x0, int y0, int gx, int gy, const GgAdj &p, R inv)
 {
+    // the stencil is symmetric: where no mirrored preimage exists (periodic
+    // grids, and cells off a zero-flux edge) its transpose is itself
+    if (p.bc == 0 || (gx >= 1 && gx < p.nx - 1 && gy >= 1 && gy < p.ny - 1)) return gg_lap_s(s, o, p.stencil, inv);
     R v;
     if (p.stencil == 0) {
         v = -R(8) * s[o];
@@ -460,6 +496,7 @@ __global__ void __launch_bounds__(kAdjThreads) gg_fwd_kernel(GgAdj p, ParamSrc p
     load_params(ps, mobil, grcoef, gamma, step);
     const int x0 = blockIdx.x * kGX, y0 = blockIdx.y * kGY;
     gg_stage(se, eta, p.q, x0, y0, p, false);
+    gg_stage_wait();
     __syncthreads();
     const int i = threadIdx.x % kGX, j = threadIdx.x / kGX, gx = x0 + i, gy = y0 + j;
     if (gx >= p.nx || gy >= p.ny) return;
@@ -491,6 +528,7 @@ __global__ void __launch_bounds__(kAdjThreads) gg_adj_kernel(GgAdj p, ParamSrc p
     const int x0 = blockIdx.x * kGX, y0 = blockIdx.y * kGY;
     gg_stage(se, eta, p.q, x0, y0, p, false);
     gg_stage(sg, gout, p.q, x0, y0, p, true);
+    gg_stage_wait();
     __syncthreads();
     const int i = threadIdx.x % kGX, j = threadIdx.x / kGX, gx = x0 + i, gy = y0 + j;
     R gl = R(0), gkap = R(0), ggam = R(0);
