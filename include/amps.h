@@ -196,8 +196,13 @@ AMPS_API int amps_get_fields(amps_handle *h, void *dst, int dtype, int on_device
 AMPS_API int amps_run(amps_handle *h, int nsteps);
 /* Enable (1) / disable (0) CUDA-graph replay of whole periods (default 1). */
 AMPS_API int amps_set_graphs(amps_handle *h, int enable);
-/* Kernel timing: while enabled, amps_run launches eagerly and brackets every
- * update-kernel launch with CUDA events on the stream it is launched on.
+/* Kernel timing: while enabled, amps_run brackets update-kernel launches with
+ * CUDA events on the stream they are launched on -- every launch of the
+ * Kobayashi and sintering kernels; for grain growth one pair around each
+ * run of consecutive step launches (ms / launches is then the average launch
+ * duration as the launches run back to back).  With a stream set and graphs
+ * on, each whole period is captured, events included, into a one-off graph,
+ * so no host-side gap falls inside a pair.
  * amps_get_kernel_times fills arrays of 4: ms and launches of the per-tier
  * update kernels (index 0 half, 1 fp32, 2 fp64) and of the fused all-tier
  * update kernel (index 3); tile_steps[0..2] are the tile-steps computed per

@@ -293,6 +293,37 @@ def test_graph_replay_equals_eager():
     assert out[0][2] == out[1][2]
 
 
+@pytest.mark.parametrize("model", ["graingrowth", "kobayashi"])
+def test_profiled_run_equals_plain_and_times_every_launch(model):
+    """Profiling (whole periods captured with their event records as graph
+    nodes, the partial period eager) changes no result and times each step."""
+    import torch
+
+    w = amps()
+    p = w.Params.preset(model, 0, nx=128, ny=128)
+    stream = torch.cuda.Stream()
+    out = []
+    for prof in (False, True):
+        with w.Simulation(p, init=w.INIT_SEEDED) as s:
+            s.set_stream(stream.cuda_stream)
+            s.run(3)
+            s.set_profiling(prof)
+            s.run(2 * p.cadence + 3)
+            s.synchronize()
+            if prof:
+                ms, launches, tiles = s.kernel_times()
+                st = s.stats()
+            out.append((s.fields(), s.tiers()))
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
+    steps = 2 * p.cadence + 3
+    if model == "graingrowth":
+        assert launches[3] == steps and ms[3] > 0
+    else:
+        assert sum(launches) >= steps and all(m >= 0 for m in ms) and sum(ms) > 0
+    assert tiles[3] > 0 and st["tile_steps"]
+
+
 def test_set_get_roundtrip_and_reduce():
     w = amps()
     p = w.Params.preset("sintering", 1, mode="purehigh", nx=64, ny=64)

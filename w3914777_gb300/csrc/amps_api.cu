@@ -51,8 +51,9 @@ struct amps_handle {
     std::string err;
     // kernel timing
     bool profiling = false;
-    struct Ev { int tier; cudaEvent_t a, b; };
+    struct Ev { int tier; cudaEvent_t a, b; int n; };  // n launches between a and b
     std::vector<Ev> evs;
+    std::vector<cudaEvent_t> ev_stash;  // created ahead of a captured profiled period
     // grain growth: persistent TMA kernel over the FP32 ping-pong buffers
     bool use_tma = false;
     int tma_grid = 0;
@@ -157,6 +158,8 @@ static void free_all(amps_handle *h)
 {
     for (auto &e : h->evs) { cudaEventDestroy(e.a); cudaEventDestroy(e.b); }
     h->evs.clear();
+    for (cudaEvent_t e : h->ev_stash) cudaEventDestroy(e);
+    h->ev_stash.clear();
     for (auto &kv : h->graph) cudaGraphExecDestroy(kv.second);
     h->graph.clear();
     for (int t = 0; t < 3; ++t)
@@ -536,28 +539,45 @@ static StepArgs step_args(const amps_handle *h, int parity, bool transition, int
     return a;
 }
 
+// Records a profiling event on the handle's stream; while the stream is
+// being captured the record becomes a graph node, so the pair around a
+// kernel brackets it on the device with no host gap in between.
+static cudaError_t prof_record(amps_handle *h, cudaEvent_t e)
+{
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (h->stream) cudaStreamIsCapturing(h->stream, &cs);
+    return cs == cudaStreamCaptureStatusActive ? cudaEventRecordWithFlags(e, h->stream, cudaEventRecordExternal)
+                                               : cudaEventRecord(e, h->stream);
+}
+
+// Event pair of one profiled launch (from the stash when there is one) and
+// the record of its first event.
+static int prof_begin(amps_handle *h, amps_handle::Ev &ev)
+{
+    for (cudaEvent_t *e : {&ev.a, &ev.b}) {
+        if (!h->ev_stash.empty()) {
+            *e = h->ev_stash.back();
+            h->ev_stash.pop_back();
+        } else if (cudaEventCreate(e) != cudaSuccess) {
+            FAIL(h, AMPS_ERR_CUDA, "event create");
+        }
+    }
+    CK(h, prof_record(h, ev.a));
+    return AMPS_OK;
+}
+
 static int launch_step(amps_handle *h, int step_off, bool monitor_now)
 {
     const amps_params &p = h->p;
     StepArgs a = step_args(h, h->parity, h->transition, step_off, monitor_now);
     const bool ref = p.ref_order != 0;
     if (p.model == AMPS_GRAINGROWTH) {
-        // one fused launch covers every tier
-        amps_handle::Ev ev{3, nullptr, nullptr};
-        if (h->profiling) {
-            if (cudaEventCreate(&ev.a) != cudaSuccess || cudaEventCreate(&ev.b) != cudaSuccess)
-                FAIL(h, AMPS_ERR_CUDA, "event create");
-            cudaEventRecord(ev.a, h->stream);
-        }
+        // one fused launch covers every tier (profiled per chunk by enqueue_chunk)
         // all-FP64 runs use the staged FP64 kernel, every other mode the fused one
         const bool only64 = h->used[TIER_FP64] && !h->used[TIER_FP32] && !h->used[TIER_HALF];
         cudaError_t e = h->use_tma ? gg_launch_tma(ref, h->tm[h->parity], a, h->tma_grid, h->stream)
                                    : gg_launch(h->T, only64 ? TIER_FP64 : -1, ref, a, h->ntiles, h->stream);
         if (e != cudaSuccess) FAIL(h, AMPS_ERR_CUDA, "step kernel launch: %s", cudaGetErrorString(e));
-        if (h->profiling) {
-            cudaEventRecord(ev.b, h->stream);
-            h->evs.push_back(ev);
-        }
         h->parity ^= 1;
         h->transition = false;
         return AMPS_OK;
@@ -570,11 +590,10 @@ static int launch_step(amps_handle *h, int step_off, bool monitor_now)
         cudaStream_t st = h->stream;
         a.list = h->d_lists + t * h->ntiles;
         cudaError_t e;
-        amps_handle::Ev ev{fused ? 3 : t, nullptr, nullptr};
+        amps_handle::Ev ev{fused ? 3 : t, nullptr, nullptr, 1};
         if (h->profiling) {
-            if (cudaEventCreate(&ev.a) != cudaSuccess || cudaEventCreate(&ev.b) != cudaSuccess)
-                FAIL(h, AMPS_ERR_CUDA, "event create");
-            cudaEventRecord(ev.a, st);
+            const int r = prof_begin(h, ev);
+            if (r) return r;
         }
         if (fused) e = p.model == AMPS_KOBAYASHI ? kob_launch_lo(h->T, a, h->ntiles, st)
                                                  : sint_launch_lo(h->T, p.mu_lap_fp64 != 0, a, h->ntiles, st);
@@ -582,7 +601,7 @@ static int launch_step(amps_handle *h, int step_off, bool monitor_now)
         else e = sint_launch(h->T, t, ref, p.mu_lap_fp64 != 0, a, h->ntiles, st);
         if (e != cudaSuccess) FAIL(h, AMPS_ERR_CUDA, "step kernel launch: %s", cudaGetErrorString(e));
         if (h->profiling) {
-            cudaEventRecord(ev.b, st);
+            CK(h, prof_record(h, ev.b));
             h->evs.push_back(ev);
         }
     }
@@ -608,10 +627,23 @@ static int enqueue_chunk(amps_handle *h, int k0, int cnt)
 {
     const amps_params &p = h->p;
     const bool period_end = k0 + cnt == p.cadence;
+    // grain growth: one event pair spans the chunk's back-to-back step
+    // launches (a pair around each ~20 us launch would time its launch
+    // latency too, which consecutive launches otherwise overlap)
+    const bool span = h->profiling && p.model == AMPS_GRAINGROWTH;
+    amps_handle::Ev ev{3, nullptr, nullptr, cnt};
+    if (span) {
+        const int r = prof_begin(h, ev);
+        if (r) return r;
+    }
     for (int s = 0; s < cnt; ++s) {
         const bool mon = h->mixed && period_end && s == cnt - 1;
         int r = launch_step(h, k0 + s, mon);
         if (r) return r;
+    }
+    if (span) {
+        CK(h, prof_record(h, ev.b));
+        h->evs.push_back(ev);
     }
     if (h->mixed && period_end) {
         CK(h, classify(classify_args(h, p.cadence, cnt), h->stream));
@@ -629,7 +661,29 @@ extern "C" int amps_run(amps_handle *h, int nsteps)
     while (nsteps > 0) {
         const int k0 = (int)(h->step % cad);
         const int cnt = nsteps < cad - k0 ? nsteps : cad - k0;
-        if (h->graphs && !h->profiling && k0 == 0 && cnt == cad && h->stream != nullptr) {
+        if (h->graphs && h->profiling && k0 == 0 && cnt == cad && h->stream != nullptr) {
+            // a profiled period runs as a one-off graph with its event records
+            // as nodes (the host enqueues eager launches and event records
+            // slower than the GPU runs them, and would time its own gaps)
+            while (h->ev_stash.size() < (size_t)6 * cad) {
+                cudaEvent_t e;
+                CK(h, cudaEventCreate(&e));
+                h->ev_stash.push_back(e);
+            }
+            cudaGraph_t gr;
+            CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+            int r = enqueue_chunk(h, 0, cad);
+            cudaError_t e = cudaStreamEndCapture(h->stream, &gr);
+            if (r) return r;
+            if (e != cudaSuccess) FAIL(h, AMPS_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+            cudaGraphExec_t ex;
+            e = cudaGraphInstantiate(&ex, gr, 0);
+            cudaGraphDestroy(gr);
+            if (e != cudaSuccess) FAIL(h, AMPS_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+            e = cudaGraphLaunch(ex, h->stream);
+            cudaGraphExecDestroy(ex);  // freed once the launch completes
+            if (e != cudaSuccess) FAIL(h, AMPS_ERR_CUDA, "graph launch: %s", cudaGetErrorString(e));
+        } else if (h->graphs && !h->profiling && k0 == 0 && cnt == cad && h->stream != nullptr) {
             const int key = h->parity | (h->transition ? 2 : 0);
             auto it = h->graph.find(key);
             if (it == h->graph.end()) {
@@ -885,7 +939,7 @@ extern "C" int amps_get_kernel_times(amps_handle *h, double *ms, int64_t *launch
         float t = 0.f;
         CK(h, cudaEventElapsedTime(&t, e.a, e.b));
         h->prof_ms[e.tier] += t;
-        h->prof_launches[e.tier] += 1;
+        h->prof_launches[e.tier] += e.n;
         cudaEventDestroy(e.a);
         cudaEventDestroy(e.b);
     }
