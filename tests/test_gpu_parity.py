@@ -324,6 +324,25 @@ def test_profiled_run_equals_plain_and_times_every_launch(model):
     assert tiles[3] > 0 and st["tile_steps"]
 
 
+@pytest.mark.parametrize("monitor", [1, 2, 3])
+def test_monitor_flags_non_finite_values(monitor):
+    """A NaN in the input state reaches the monitor step of every monitor kind
+    and sets the numeric-error flag; a clean run leaves it clear."""
+    w = amps()
+    # FP32 high tier: the monitor steps run on the half/FP32 path from the start
+    p = w.Params.preset("graingrowth", 0, nx=128, ny=128, nfields=4, tile=32, mode="end2end_mix",
+                        monitor=monitor, monitor_samples=1, thr_lo=1e-5, high_tier=w.TIER_FP32)
+    f0 = w.init_host(p, w.INIT_SEEDED)
+    for poison in (False, True):
+        f = f0.copy()
+        if poison:
+            f[2, 70, 45] = np.nan
+        with w.Simulation(p) as s:
+            s.set_fields(f)
+            s.run(2 * p.cadence)
+            assert s.stats()["numeric_error"] == int(poison)
+
+
 def test_set_get_roundtrip_and_reduce():
     w = amps()
     p = w.Params.preset("sintering", 1, mode="purehigh", nx=64, ny=64)

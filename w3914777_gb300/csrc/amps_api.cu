@@ -144,6 +144,10 @@ static Phys make_phys(const amps_params &p)
     ph.coefm = p.coefm; ph.coefk = p.coefk; ph.coefl = p.coefl; ph.dvol = p.dvol; ph.dvap = p.dvap;
     ph.dsur = p.dsur; ph.dgrb = p.dgrb; ph.A = p.A; ph.B = p.B;
     ph.seed = p.seed;
+    ph.gg_dtm = (float)(ph.dt * ph.mobil);
+    ph.gg_g2 = (float)(2.0 * ph.gamma);
+    ph.gg_kap = (float)ph.grcoef;
+    ph.gg_inv = (float)ph.inv_dxdy;
     return ph;
 }
 

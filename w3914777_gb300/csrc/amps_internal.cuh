@@ -32,6 +32,10 @@ struct Phys {
     // sintering
     double coefm, coefk, coefl, dvol, dvap, dsur, dgrb, A, B;
     uint64_t seed;
+    // grain growth's FP32-tile constants, rounded once on the host (on GB300
+    // a handful of FP64 conversions per thread and tile cost ~18% of a step):
+    // (float)(dt*L), (float)(2*gamma), (float)kappa, (float)(1/dxdy)
+    float gg_dtm, gg_g2, gg_kap, gg_inv;
 };
 
 // Arguments of one tier launch of a fused step kernel.
@@ -425,6 +429,7 @@ struct MonAccF {
     float mn, mx, dmaxf;
     double dmax;
     int bad;
+    float chk;  // NaN-propagating max of |v| (mon_add_k): non-finite iff a value was
 };
 
 __device__ __forceinline__ void mon_reset(const StepArgs &a, MonAccF &m)
@@ -434,6 +439,14 @@ __device__ __forceinline__ void mon_reset(const StepArgs &a, MonAccF &m)
     m.dmaxf = 0.f;
     m.dmax = 0.0;
     m.bad = 0;
+    m.chk = 0.f;
+}
+
+__device__ __forceinline__ float fmax_nan(float x, float y)
+{
+    float r;
+    asm("max.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(x), "f"(y));
+    return r;
 }
 
 template <int T>
@@ -487,6 +500,41 @@ __device__ __forceinline__ double mon_finish(const StepArgs &a, MonAccF &m, doub
     }
     if (__syncthreads_or(m.bad) && threadIdx.x == 0) atomicOr(a.flags, 1);
     return fmax(metric, v);
+}
+
+// mon_add for a monitor kind fixed at compile time (2: temporal, 3: rate),
+// so that no other kind's code -- above all kind 2's FP64 -- is predicated
+// into every cell of the others.  Same metric and flag as mon_add.
+template <int T, int KIND>
+__device__ __forceinline__ void mon_add_k(const StepArgs &a, MonAccF &m, int mslot, int tile, int row, int col,
+                                          int64_t gidx, float v, float old)
+{
+    static_assert(KIND == 2 || KIND == 3, "temporal or rate monitor");
+    m.chk = fmax_nan(m.chk, fabsf(v));
+    if constexpr (KIND == 3) {
+        m.dmaxf = fmaxf(m.dmaxf, fabsf(v - old));
+    } else {
+        const int si = sample_index<T>(2, a.samples, row, col);
+        if (si < 0) return;
+        double *sp = snap_ptr<T>(a, mslot, tile, gidx, si);
+        m.dmax = fmax(m.dmax, fabs(*sp - (double)v));
+        *sp = (double)v;
+    }
+}
+
+// Tile metric of mon_add_k's accumulator (valid in thread 0) and the NaN/Inf flag.
+template <int KIND>
+__device__ __forceinline__ double mon_finish_k(const StepArgs &a, MonAccF &m, double *red)
+{
+    double v;
+    if constexpr (KIND == 3) {
+        const float mx = block_maxf(m.dmaxf, reinterpret_cast<float *>(red));
+        v = threadIdx.x == 0 ? fmax(0.0, (double)mx * a.cadence) : 0.0;
+    } else {
+        v = fmax(0.0, block_max(m.dmax, red));
+    }
+    if (__syncthreads_or(!(m.chk <= 3.402823466e38f)) && threadIdx.x == 0) atomicOr(a.flags, 1);
+    return v;
 }
 
 __device__ __forceinline__ void mon_reset(const StepArgs &a, MonAcc &m)

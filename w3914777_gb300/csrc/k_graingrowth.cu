@@ -128,8 +128,7 @@ __device__ __forceinline__ void gg_tile_lo_impl(const StepArgs &a, const float *
 #pragma unroll
         for (int k = 0; k < CPT; ++k) ssum[k] = fmaf(c[k], c[k], ssum[k]);
     }
-    const float dtm = (float)(ph.dt * ph.mobil), g2 = (float)(2.0 * ph.gamma), kap = (float)ph.grcoef;
-    const float inv = (float)ph.inv_dxdy;
+    const float dtm = ph.gg_dtm, g2 = ph.gg_g2, kap = ph.gg_kap, inv = ph.gg_inv;
     const int64_t gbase = (int64_t)(ty * T + row) * a.nx + tx * T + c0;
     double metric = 0.0;
     MonAccF mon;
@@ -204,11 +203,12 @@ __device__ __forceinline__ void gg_tile_lo(const StepArgs &a, const float *sm, c
 // Half/FP32 tile, 32^2 tiles, from the staged float neighbourhood: each
 // thread advances 2 rows x 4 cells, reading 4 staged rows (instead of 3 per
 // output row), and the CTA's two halves take alternate fields.  Per cell the
-// arithmetic is gg_tile_lo_impl's.  MON (temporal or rate monitor only): the
-// tile metric is a maximum over fields and cells, so each thread folds every
-// field it computes into one accumulator and the block reduces once at the
-// end -- the same metric as one reduction per field.
-template <int TIER, bool MON>
+// arithmetic is gg_tile_lo_impl's.  MK, the monitor kind of a monitor step
+// (0: no monitor, 2: temporal, 3: rate; the spatial range takes
+// gg_tile_lo_impl): the tile metric is a maximum over fields and cells, so
+// each thread folds every field it computes into one accumulator and the
+// block reduces once at the end -- the same metric as one reduction per field.
+template <int TIER, int MK>
 __device__ __forceinline__ void gg_tile_lo_2row(const StepArgs &a, const float *sm, int tile, int tx, int ty,
                                                 double *red)
 {
@@ -233,13 +233,12 @@ __device__ __forceinline__ void gg_tile_lo_2row(const StepArgs &a, const float *
             ssum[r][2] = fmaf(q.z, q.z, ssum[r][2]);
             ssum[r][3] = fmaf(q.w, q.w, ssum[r][3]);
         }
-    const float dtm = (float)(ph.dt * ph.mobil), g2 = (float)(2.0 * ph.gamma), kap = (float)ph.grcoef;
-    const float inv = (float)ph.inv_dxdy;
+    const float dtm = ph.gg_dtm, g2 = ph.gg_g2, kap = ph.gg_kap, inv = ph.gg_inv;
     const int64_t gbase = (int64_t)(ty * T + r0) * a.nx + tx * T + c0;
     MonAccF mon;
-    if (MON) mon_reset(a, mon);
+    if (MK) mon_reset(a, mon);
     for (int f = half; f < nf; f += 2) {
-        const bool mon_f = MON && (a.mfield < 0 || a.mfield == f);
+        const bool mon_f = MK && (a.mfield < 0 || a.mfield == f);
         const int mslot = a.mfield < 0 ? f : 0;
         float w[4][CPT + 2];
 #pragma unroll
@@ -269,17 +268,19 @@ __device__ __forceinline__ void gg_tile_lo_2row(const StepArgs &a, const float *
             }
             const int64_t g = (int64_t)f * a.n + gbase + (int64_t)r * a.nx;
             store_cells<TIER, CPT>(a, g, out);
-            if (mon_f) {
-                const int64_t gi = gbase + (int64_t)r * a.nx;
+            if constexpr (MK != 0) {
+                if (mon_f) {
+                    const int64_t gi = gbase + (int64_t)r * a.nx;
 #pragma unroll
-                for (int k = 0; k < CPT; ++k)
-                    mon_add<T>(a, mon, mslot, tile, r0 + r, c0 + k, gi + k, round_to_tier<TIER>(out[k]),
-                               w[r + 1][k + 1], snap_prefetch<T>(a, mslot, tile, r0 + r, c0 + k, gi + k));
+                    for (int k = 0; k < CPT; ++k)
+                        mon_add_k<T, MK>(a, mon, mslot, tile, r0 + r, c0 + k, gi + k, round_to_tier<TIER>(out[k]),
+                                         w[r + 1][k + 1]);
+                }
             }
         }
     }
-    if (MON) {
-        const double metric = mon_finish(a, mon, red, 0.0);
+    if constexpr (MK != 0) {
+        const double metric = mon_finish_k<MK>(a, mon, red);
         if (threadIdx.x == 0) a.metric[tile] = metric;
     }
 }
@@ -441,9 +442,20 @@ __global__ void __launch_bounds__(kThreads, 4) gg_step_kernel(StepArgs a)
     else stage_tile<float, T, 1>(a, sm, ntier, tx, ty, 0, a.nf);
     __syncthreads();
     if constexpr (T == 32) {
-        if (!MON || a.monitor_kind != 1) {  // the spatial range needs one reduction per field
-            if (tier == TIER_FP32) gg_tile_lo_2row<TIER_FP32, MON>(a, sm, tile, tx, ty, red);
-            else gg_tile_lo_2row<TIER_HALF, MON>(a, sm, tile, tx, ty, red);
+        // the spatial range needs one reduction per field: gg_tile_lo_impl
+        if (!MON) {
+            if (tier == TIER_FP32) gg_tile_lo_2row<TIER_FP32, 0>(a, sm, tile, tx, ty, red);
+            else gg_tile_lo_2row<TIER_HALF, 0>(a, sm, tile, tx, ty, red);
+            return;
+        }
+        if (a.monitor_kind == 3) {
+            if (tier == TIER_FP32) gg_tile_lo_2row<TIER_FP32, 3>(a, sm, tile, tx, ty, red);
+            else gg_tile_lo_2row<TIER_HALF, 3>(a, sm, tile, tx, ty, red);
+            return;
+        }
+        if (a.monitor_kind == 2) {
+            if (tier == TIER_FP32) gg_tile_lo_2row<TIER_FP32, 2>(a, sm, tile, tx, ty, red);
+            else gg_tile_lo_2row<TIER_HALF, 2>(a, sm, tile, tx, ty, red);
             return;
         }
     }
