@@ -148,6 +148,18 @@ static Phys make_phys(const amps_params &p)
     ph.gg_g2 = (float)(2.0 * ph.gamma);
     ph.gg_kap = (float)ph.grcoef;
     ph.gg_inv = (float)ph.inv_dxdy;
+    double *k = ph.kd;
+    if (p.model == AMPS_KOBAYASHI) {
+        k[KB_HX] = 0.5 / ph.dx; k[KB_HY] = 0.5 / ph.dy; k[KB_ANISO] = ph.aniso; k[KB_THETA0] = ph.theta0;
+        k[KB_EPSB] = ph.epsb; k[KB_DELTA] = ph.delta; k[KB_ED] = -ph.epsb * ph.aniso * ph.delta;
+        k[KB_M] = ph.alpha / ph.pi; k[KB_GAMA] = ph.gama; k[KB_TEQ] = ph.teq; k[KB_NOISE] = ph.noise;
+        k[KB_DTT] = ph.dt / ph.tau; k[KB_KAPPA] = ph.kappa; k[KB_DT] = ph.dt; k[KB_INV] = ph.inv_dxdy;
+    } else if (p.model == AMPS_SINTERING) {
+        k[SN_INV] = ph.inv_dxdy; k[SN_B] = ph.B; k[SN_A2] = 2.0 * ph.A; k[SN_HCM] = 0.5 * ph.coefm;
+        k[SN_DVOL] = ph.dvol; k[SN_DVAP] = ph.dvap; k[SN_DSUR] = ph.dsur; k[SN_DGRB] = ph.dgrb; k[SN_DT] = ph.dt;
+        k[SN_B12] = 12.0 * ph.B; k[SN_DTL] = ph.dt * ph.coefl; k[SN_HCK] = 0.5 * ph.coefk;
+    }
+    for (int i = 0; i < KCONST_MAX; ++i) ph.kf[i] = (float)ph.kd[i];
     return ph;
 }
 

@@ -36,7 +36,27 @@ struct Phys {
     // a handful of FP64 conversions per thread and tile cost ~18% of a step):
     // (float)(dt*L), (float)(2*gamma), (float)kappa, (float)(1/dxdy)
     float gg_dtm, gg_g2, gg_kap, gg_inv;
+    // Kobayashi and sintering constants of the non-reference-order tiles,
+    // derived on the host in double (kd) and rounded to float (kf), the same
+    // values the tiles would derive per thread (index: enum KConst)
+    double kd[24];
+    float kf[24];
 };
+
+enum KConst {
+    // Kobayashi: 0.5/dx, 0.5/dy, aniso, theta0, epsb, delta, -epsb*aniso*delta,
+    // alpha/pi, gama, teq, noise, dt/tau, kappa, dt, 1/dxdy
+    KB_HX, KB_HY, KB_ANISO, KB_THETA0, KB_EPSB, KB_DELTA, KB_ED, KB_M, KB_GAMA, KB_TEQ, KB_NOISE, KB_DTT,
+    KB_KAPPA, KB_DT, KB_INV,
+    // sintering: 1/dxdy, B, 2A, 0.5*coefm, dvol, dvap, dsur, dgrb, dt, 12B, dt*coefl, 0.5*coefk
+    SN_INV = 0, SN_B, SN_A2, SN_HCM, SN_DVOL, SN_DVAP, SN_DSUR, SN_DGRB, SN_DT, SN_B12, SN_DTL, SN_HCK,
+    KCONST_MAX = 24
+};
+
+// Constant i of Phys::kd / Phys::kf at the tile's compute type.
+template <typename CT> __device__ __forceinline__ CT kc(const Phys &ph, int i);
+template <> __device__ __forceinline__ double kc<double>(const Phys &ph, int i) { return ph.kd[i]; }
+template <> __device__ __forceinline__ float kc<float>(const Phys &ph, int i) { return ph.kf[i]; }
 
 // Arguments of one tier launch of a fused step kernel.
 struct StepArgs {
@@ -449,6 +469,16 @@ __device__ __forceinline__ float fmax_nan(float x, float y)
     return r;
 }
 
+// Kind 2 (temporal) step of the float accumulator, out of line: its FP64
+// would otherwise be predicated into every cell of the other kinds.
+template <int T>
+__device__ __noinline__ void mon_add_tem(const StepArgs &a, MonAccF &m, int mslot, int tile, int64_t gidx, int si,
+                                         float v, double snapv)
+{
+    m.dmax = fmax(m.dmax, fabs(snapv - (double)v));
+    *snap_ptr<T>(a, mslot, tile, gidx, si) = (double)v;
+}
+
 template <int T>
 __device__ __forceinline__ void mon_add(const StepArgs &a, MonAccF &m, int mslot, int tile, int row, int col,
                                         int64_t gidx, float v, float old, double snapv)
@@ -460,8 +490,7 @@ __device__ __forceinline__ void mon_add(const StepArgs &a, MonAccF &m, int mslot
         m.mn = fminf(m.mn, v);
         m.mx = fmaxf(m.mx, v);
     } else if (a.monitor_kind == 2) {
-        m.dmax = fmax(m.dmax, fabs(snapv - (double)v));
-        *snap_ptr<T>(a, mslot, tile, gidx, si) = (double)v;
+        mon_add_tem<T>(a, m, mslot, tile, gidx, si, v, snapv);
     } else {
         m.dmaxf = fmaxf(m.dmaxf, fabsf(v - old));
     }

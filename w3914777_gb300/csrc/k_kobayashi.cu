@@ -24,6 +24,28 @@ __device__ __forceinline__ double noise_u01(uint64_t seed, uint64_t a, uint64_t 
     return (double)(mix(mix(seed ^ mix(a)) + b) >> 11) * 0x1.0p-53;
 }
 
+// noise_u01 at the tile's compute type.  Float: the 53-bit integer rounded
+// once to float and scaled by 2^-53 (exact), which is (float)noise_u01 --
+// without three FP64 operations per cell.
+template <typename CT> __device__ __forceinline__ CT noise_u01_t(uint64_t seed, uint64_t a, uint64_t b);
+template <> __device__ __forceinline__ double noise_u01_t<double>(uint64_t seed, uint64_t a, uint64_t b)
+{
+    return noise_u01(seed, a, b);
+}
+template <> __device__ __forceinline__ float noise_u01_t<float>(uint64_t seed, uint64_t a, uint64_t b)
+{
+    auto mix = [](uint64_t z) {
+        z += 0x9E3779B97F4A7C15ull;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return z ^ (z >> 31);
+    };
+    return __ull2float_rn(mix(mix(seed ^ mix(a)) + b) >> 11) * 0x1.0p-53f;
+}
+
+// x != 0 for a double parameter, by an integer test of its bits (no FP64 op)
+__device__ __forceinline__ bool nonzero(double x) { return (__double_as_longlong(x) << 1) != 0; }
+
 template <typename CT> __device__ __forceinline__ CT k_atan2(CT y, CT x) { return atan2(y, x); }
 template <typename CT> __device__ __forceinline__ CT k_cos(CT v) { return cos(v); }
 template <typename CT> __device__ __forceinline__ CT k_sin(CT v) { return sin(v); }
@@ -70,11 +92,11 @@ __device__ __forceinline__ void kob_tile(const StepArgs &a, unsigned char *smraw
             e = __dmul_rn(ph.epsb, __dadd_rn(1.0, __dmul_rn(ph.delta, cos(arg))));
             ed = __dmul_rn(__dmul_rn(__dmul_rn(-ph.epsb, ph.aniso), ph.delta), sin(arg));
         } else {
-            phx = (pe - pw) * CT(0.5 / ph.dx);
-            phy = (pn - ps) * CT(0.5 / ph.dy);
-            const CT arg = CT(ph.aniso) * (k_atan2<CT>(phy, phx) - CT(ph.theta0));
-            e = CT(ph.epsb) * fma(CT(ph.delta), k_cos<CT>(arg), CT(1));
-            ed = CT(-ph.epsb * ph.aniso * ph.delta) * k_sin<CT>(arg);
+            phx = (pe - pw) * kc<CT>(ph, KB_HX);
+            phy = (pn - ps) * kc<CT>(ph, KB_HY);
+            const CT arg = kc<CT>(ph, KB_ANISO) * (k_atan2<CT>(phy, phx) - kc<CT>(ph, KB_THETA0));
+            e = kc<CT>(ph, KB_EPSB) * fma(kc<CT>(ph, KB_DELTA), k_cos<CT>(arg), CT(1));
+            ed = kc<CT>(ph, KB_ED) * k_sin<CT>(arg);
         }
         const int o = u;
         px[o] = phx; py[o] = phy; ep[o] = e; epd[o] = ed;
@@ -84,7 +106,10 @@ __device__ __forceinline__ void kob_tile(const StepArgs &a, unsigned char *smraw
     // phase B: snowflake/function.h:54-59 on the tile
     const int64_t step = *a.step_base + a.step_off;
     double metric = 0.0;
-    MonAcc mon;
+    // half/FP32 tiles fold their float values into a float accumulator (the
+    // same metric, without FP64 operations per cell)
+    using MA = typename std::conditional<TIER == TIER_FP64, MonAcc, MonAccF>::type;
+    MA mon;
     const bool mon_on = a.monitor_now != 0;
     if (mon_on) mon_reset(a, mon);
     const int mslot = 0;
@@ -131,44 +156,44 @@ __device__ __forceinline__ void kob_tile(const StepArgs &a, unsigned char *smraw
             pn = __dadd_rn(p0, __dmul_rn(ph.dt / ph.tau, inner));
             tn = __dadd_rn(__dadd_rn(t0, __dmul_rn(ph.dt, lt)), __dmul_rn(ph.kappa, __dsub_rn(pn, p0)));
         } else {
-            const CT inv = CT(ph.inv_dxdy);
+            const CT inv = kc<CT>(ph, KB_INV);
             const CT lp = ((P[-1] + P[1]) + (P[-2] + P[2]) + (P[-S::P] + P[S::P]) + (P[-2 * S::P] + P[2 * S::P])
                            - CT(8) * p0) * inv;
             const CT lt = ((Tm[-1] + Tm[1]) + (Tm[-2] + Tm[2]) + (Tm[-S::P] + Tm[S::P]) + (Tm[-2 * S::P] + Tm[2 * S::P])
                            - CT(8) * t0) * inv;
             const int on = o + E, os = o - E, oe = o + 1, ow = o - 1;
-            const CT term1 = (ep[on] * epd[on] * px[on] - ep[os] * epd[os] * px[os]) * CT(0.5 / ph.dy);
-            const CT term2 = -(ep[oe] * epd[oe] * py[oe] - ep[ow] * epd[ow] * py[ow]) * CT(0.5 / ph.dx);
-            const CT m = CT(ph.alpha / ph.pi) * k_atan<CT>(CT(ph.gama) * (CT(ph.teq) - t0));
+            const CT term1 = (ep[on] * epd[on] * px[on] - ep[os] * epd[os] * px[os]) * kc<CT>(ph, KB_HY);
+            const CT term2 = -(ep[oe] * epd[oe] * py[oe] - ep[ow] * epd[ow] * py[ow]) * kc<CT>(ph, KB_HX);
+            const CT m = kc<CT>(ph, KB_M) * k_atan<CT>(kc<CT>(ph, KB_GAMA) * (kc<CT>(ph, KB_TEQ) - t0));
             CT drive = p0 - CT(0.5) + m;
-            if (ph.noise != 0.0)
-                drive += CT(ph.noise) * (CT(noise_u01(ph.seed, (uint64_t)step, (uint64_t)g)) - CT(0.5));
+            if (nonzero(ph.noise))
+                drive += kc<CT>(ph, KB_NOISE) * (noise_u01_t<CT>(ph.seed, (uint64_t)step, (uint64_t)g) - CT(0.5));
             const CT inner = term1 + term2 + ep[o] * ep[o] * lp + p0 * (CT(1) - p0) * drive;
-            pn = fma(CT(ph.dt / ph.tau), inner, p0);
-            tn = fma(CT(ph.kappa), pn - p0, fma(CT(ph.dt), lt, t0));
+            pn = fma(kc<CT>(ph, KB_DTT), inner, p0);
+            tn = fma(kc<CT>(ph, KB_KAPPA), pn - p0, fma(kc<CT>(ph, KB_DT), lt, t0));
         }
         store_tier<TIER>(a, g, pn);
         store_tier<TIER>(a, a.n + g, tn);
         if (mon_on && (a.mfield <= 0))
-            mon_add<T>(a, mon, mslot, tile, j, i, g, (double)round_to_tier<TIER>(pn), (double)p0,
+            mon_add<T>(a, mon, mslot, tile, j, i, g, (CT)round_to_tier<TIER>(pn), p0,
                        snap_prefetch<T>(a, mslot, tile, j, i, g));
     }
     if (mon_on) {
         metric = mon_finish(a, mon, red, metric);
         if (a.mfield < 0 || a.mfield == 1) {
             // second monitored field (T): a second pass over the stored values
-            MonAcc m2;
+            MA m2;
             mon_reset(a, m2);
             __syncthreads();
             for (int u = threadIdx.x; u < T * T; u += kThreads) {
                 const int i = u % T, j = u / T;
                 const int64_t g = (int64_t)(y0 + j) * a.nx + x0 + i;
-                double v;
-                if (TIER == TIER_FP64) v = ((const double *)a.out[2])[a.n + g];
-                else if (TIER == TIER_FP32) v = ((const float *)a.out[1])[a.n + g];
+                CT v;
+                if constexpr (TIER == TIER_FP64) v = ((const double *)a.out[2])[a.n + g];
+                else if constexpr (TIER == TIER_FP32) v = ((const float *)a.out[1])[a.n + g];
                 else v = __half2float(((const __half *)a.out[0])[a.n + g]);
                 const int slot = a.mfield < 0 ? 1 : 0;
-                mon_add<T>(a, m2, slot, tile, j, i, g, v, (double)S::at(sm, 1, j + R, i + S::O),
+                mon_add<T>(a, m2, slot, tile, j, i, g, v, S::at(sm, 1, j + R, i + S::O),
                            snap_prefetch<T>(a, slot, tile, j, i, g));
             }
             metric = mon_finish(a, m2, red, metric);

@@ -68,7 +68,7 @@ __device__ __forceinline__ void sint_tile(const StepArgs &a, unsigned char *smra
                 __dmul_rn(__dmul_rn(A2, cc), __dmul_rn(__dsub_rn(1.0, cc), __dsub_rn(1.0, cc))));
             m = __dsub_rn(dfdc, __dmul_rn(0.5 * ph.coefm, lap));
         } else {
-            const MT lap = ((MT)C[-1] + (MT)C[1] + (MT)C[-SC::P] + (MT)C[SC::P] - MT(4) * (MT)cc) * MT(ph.inv_dxdy);
+            const MT lap = ((MT)C[-1] + (MT)C[1] + (MT)C[-SC::P] + (MT)C[SC::P] - MT(4) * (MT)cc) * kc<MT>(ph, SN_INV);
             MT s2 = 0, s3 = 0;
             for (int k = 0; k < np; ++k) {
                 const MT e = SE::at(sme, k, j + 1, i + SE::O);
@@ -77,9 +77,9 @@ __device__ __forceinline__ void sint_tile(const StepArgs &a, unsigned char *smra
                 s3 = fma(e2, e, s3);
             }
             const MT c1 = MT(1) - (MT)cc;
-            const MT A2 = MT(2.0 * ph.A);
-            const MT dfdc = MT(ph.B) * (MT(2) * (MT)cc + MT(4) * s3 - MT(6) * s2) + A2 * (MT)cc * c1 * (c1 - (MT)cc);
-            m = dfdc - MT(0.5 * ph.coefm) * lap;
+            const MT A2 = kc<MT>(ph, SN_A2);
+            const MT dfdc = kc<MT>(ph, SN_B) * (MT(2) * (MT)cc + MT(4) * s3 - MT(6) * s2) + A2 * (MT)cc * c1 * (c1 - (MT)cc);
+            m = dfdc - kc<MT>(ph, SN_HCM) * lap;
         }
         mu[u] = m;
     }
@@ -87,7 +87,10 @@ __device__ __forceinline__ void sint_tile(const StepArgs &a, unsigned char *smra
 
     // phase B: c' (sintering/function.h:90-100), then eta_i' (:126-131)
     double metric = 0.0;
-    MonAcc mon;
+    // half/FP32 tiles fold their float values into a float accumulator (the
+    // same metric, without FP64 operations per cell)
+    using MA = typename std::conditional<TIER == TIER_FP64, MonAcc, MonAccF>::type;
+    MA mon;
     const bool mon_on = a.monitor_now != 0;
     if (mon_on) mon_reset(a, mon);
     for (int u = threadIdx.x; u < T * T; u += kThreads) {
@@ -121,7 +124,7 @@ __device__ __forceinline__ void sint_tile(const StepArgs &a, unsigned char *smra
                 s2ref = __dadd_rn(s2ref, __dmul_rn(e, e));
             }
         } else {
-            const MT lapm = (mu[o - 1] + mu[o + 1] + mu[o - E] + mu[o + E] - MT(4) * mu[o]) * MT(ph.inv_dxdy);
+            const MT lapm = (mu[o - 1] + mu[o + 1] + mu[o - E] + mu[o + E] - MT(4) * mu[o]) * kc<MT>(ph, SN_INV);
             const CT phi = cc * cc * cc * fma(CT(6) * cc, cc, CT(10) - CT(15) * cc);
             CT se = 0;
             for (int k = 0; k < np; ++k) {
@@ -130,14 +133,14 @@ __device__ __forceinline__ void sint_tile(const StepArgs &a, unsigned char *smra
                 s2f = fma(e, e, s2f);
             }
             const CT sum = se * se - s2f;  // sum_{i != j} eta_i eta_j
-            const CT mob = CT(ph.dvol) * phi + CT(ph.dvap) * (CT(1) - phi) + CT(ph.dsur) * cc * (CT(1) - cc)
-                         + CT(ph.dgrb) * sum;
-            CT v = (CT)((MT)cc + (MT)(CT(ph.dt) * mob) * lapm);
+            const CT mob = kc<CT>(ph, SN_DVOL) * phi + kc<CT>(ph, SN_DVAP) * (CT(1) - phi) + kc<CT>(ph, SN_DSUR) * cc * (CT(1) - cc)
+                         + kc<CT>(ph, SN_DGRB) * sum;
+            CT v = (CT)((MT)cc + (MT)(kc<CT>(ph, SN_DT) * mob) * lapm);
             cn = v >= CT(1) ? CT(1) : (v < CT(0) ? CT(0) : v);
         }
         store_tier<TIER>(a, g, cn);
         if (mon_on && a.mfield <= 0)
-            mon_add<T>(a, mon, 0, tile, j, i, g, (double)round_to_tier<TIER>(cn), (double)cc,
+            mon_add<T>(a, mon, 0, tile, j, i, g, (CT)round_to_tier<TIER>(cn), cc,
                        snap_prefetch<T>(a, 0, tile, j, i, g));
         for (int k = 0; k < np; ++k) {
             const CT *Ep = &SE::at(sme, k, j + 1, i + SE::O);
@@ -155,9 +158,9 @@ __device__ __forceinline__ void sint_tile(const StepArgs &a, unsigned char *smra
                 else if (v < 0) v = 0;
                 en = v;
             } else {
-                const CT lap = (Ep[-1] + Ep[1] + Ep[-SE::P] + Ep[SE::P] - CT(4) * e) * CT(ph.inv_dxdy);
-                const CT dfd = CT(12.0 * ph.B) * e * (s2f + (CT(1) - cn) - e * (CT(2) - cn));
-                CT v = fma(-CT(ph.dt * ph.coefl), fma(-CT(0.5 * ph.coefk), lap, dfd), e);
+                const CT lap = (Ep[-1] + Ep[1] + Ep[-SE::P] + Ep[SE::P] - CT(4) * e) * kc<CT>(ph, SN_INV);
+                const CT dfd = kc<CT>(ph, SN_B12) * e * (s2f + (CT(1) - cn) - e * (CT(2) - cn));
+                CT v = fma(-kc<CT>(ph, SN_DTL), fma(-kc<CT>(ph, SN_HCK), lap, dfd), e);
                 en = v >= CT(1) ? CT(1) : (v < CT(0) ? CT(0) : v);
             }
             store_tier<TIER>(a, (int64_t)(k + 1) * a.n + g, en);
