@@ -12,19 +12,21 @@ from w3914777_gb300 import amps, ensemble
 pytestmark = pytest.mark.gpu
 
 MIXED = dict(mode=amps.END2END_MIX, monitor=amps.MONITOR_RATE, monitor_samples=1, monitor_field=-1)
-_THR = []
+_THR = {}
 
 
-def mixed():
-    """MIXED with thresholds at the 40% / 75% quantiles of one probe member's
-    tile metrics after a period, so that the members mix all three tiers."""
-    if not _THR:
-        p = small_members(dict(MIXED, thr_lo=0.0, thr_hi=0.0))[2]
+def mixed(monitor=amps.MONITOR_RATE):
+    """MIXED (with the given monitor) with thresholds at the 40% / 75%
+    quantiles of one probe member's tile metrics after a period, so that the
+    members mix all three tiers."""
+    if monitor not in _THR:
+        p = small_members(dict(MIXED, monitor=monitor, thr_lo=0.0, thr_hi=0.0))[2]
         with amps.Simulation(p, init=amps.INIT_SEEDED) as s:
             s.run(10)
             m = s.metric().ravel()
-        _THR.extend([float(np.quantile(m, 0.4)), float(np.quantile(m, 0.75))])
-    return dict(MIXED, thr_lo=_THR[0], thr_hi=_THR[1])
+        _THR[monitor] = (float(np.quantile(m, 0.4)), float(np.quantile(m, 0.75)))
+    lo, hi = _THR[monitor]
+    return dict(MIXED, monitor=monitor, thr_lo=lo, thr_hi=hi)
 
 
 def small_members(extra=None):
@@ -62,19 +64,20 @@ def run_together(params, steps, graphs=True, chunks=None):
     return res
 
 
-@pytest.mark.parametrize("graphs", [True, False])
-def test_ensemble_matches_individual_runs_adaptive(graphs):
-    params = small_members(mixed())
+@pytest.mark.parametrize("graphs,monitor", [(True, amps.MONITOR_RATE), (False, amps.MONITOR_RATE),
+                                            (True, amps.MONITOR_TEM)])
+def test_ensemble_matches_individual_runs_adaptive(graphs, monitor):
+    params = small_members(mixed(monitor))
     alone = run_alone(params, 37)
     together = run_together(params, 37, graphs=graphs, chunks=[20, 3, 14])
     for (fa, ta, sa), (fb, tb, sb) in zip(alone, together):
         assert np.array_equal(fa, fb)
         assert np.array_equal(ta, tb)
         assert sa == sb
-    # the thresholds must actually mix tiers for this to test anything (the
-    # FP32 tile path is covered by the plain FP32 case)
-    mix = np.concatenate([t.ravel() for _, t, _ in alone])
-    assert len(np.unique(mix)) >= 2
+    # the thresholds must actually mix tiers during the run for this to test
+    # anything (the FP32 tile path is covered by the plain FP32 case)
+    steps_per_tier = np.sum([st["tile_steps"] for _, _, st in alone], axis=0)
+    assert np.count_nonzero(steps_per_tier) >= 2
 
 
 @pytest.mark.parametrize("tier", [amps.TIER_FP32, amps.TIER_FP64])
