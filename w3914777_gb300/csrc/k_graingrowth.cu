@@ -429,6 +429,12 @@ __global__ void __launch_bounds__(kThreads, 4) gg_step_kernel(StepArgs a)
     __shared__ double red[kThreads / 32];
     __shared__ uint8_t ntier[9];
     float *sm = reinterpret_cast<float *>(smraw);
+    // programmatic dependent launch (gg_launch): the next step's CTAs may be
+    // scheduled into the slots this grid's last wave leaves free; every CTA
+    // waits for the previous grid to complete, its writes visible, before
+    // its first global read (both are no-ops for a plain launch)
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     const int tile = blockIdx.x;
     const int tier = a.tier_out[tile];
     const int tx = tile % a.ntx, ty = tile / a.ntx;
@@ -553,6 +559,24 @@ size_t gg_smem_bytes(int tile, int tier, int nf)
     return (size_t)nf * (tile == 32 ? Stage<float, 32, 1>::FIELD : Stage<float, 16, 1>::FIELD) * sizeof(float);
 }
 
+// A step-kernel launch that may begin while the previous kernel on the
+// stream finishes (programmatic stream serialization; the kernel waits for
+// it with griddepcontrol.wait before reading anything it wrote).
+template <typename K> static cudaError_t launch_pdl(K kernel, int grid, size_t smem, cudaStream_t s, const StepArgs &a)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, a);
+}
+
 cudaError_t gg_launch(int tile, int tier, bool ref, const StepArgs &a, int grid, cudaStream_t s)
 {
     const size_t smem = gg_smem_bytes(tile, tier, a.nf);
@@ -561,15 +585,14 @@ cudaError_t gg_launch(int tile, int tier, bool ref, const StepArgs &a, int grid,
         if (ref) K<TT, true><<<grid, kThreads, smem, s>>>(a);                   \
         else K<TT, false><<<grid, kThreads, smem, s>>>(a);                      \
     } while (0)
-#define AMPS_GGM(TT)                                                                        \
-    do {                                                                                    \
-        if (a.monitor_now) {                                                                \
-            if (ref) gg_step_kernel<TT, true, true><<<grid, kThreads, smem, s>>>(a);        \
-            else gg_step_kernel<TT, false, true><<<grid, kThreads, smem, s>>>(a);           \
-        } else {                                                                            \
-            if (ref) gg_step_kernel<TT, true, false><<<grid, kThreads, smem, s>>>(a);       \
-            else gg_step_kernel<TT, false, false><<<grid, kThreads, smem, s>>>(a);          \
-        }                                                                                   \
+#define AMPS_GGM(TT)                                                                                \
+    do {                                                                                            \
+        if (a.monitor_now) {                                                                        \
+            if (ref) return launch_pdl(gg_step_kernel<TT, true, true>, grid, smem, s, a);          \
+            return launch_pdl(gg_step_kernel<TT, false, true>, grid, smem, s, a);                  \
+        }                                                                                           \
+        if (ref) return launch_pdl(gg_step_kernel<TT, true, false>, grid, smem, s, a);             \
+        return launch_pdl(gg_step_kernel<TT, false, false>, grid, smem, s, a);                     \
     } while (0)
     if (tier == TIER_FP64) {
         if (tile == 32) AMPS_GGL(gg_step_f64_kernel, 32);
