@@ -34,6 +34,7 @@ struct amps_handle {
     bool transition = false;  // next step reads tiles at tier_prev
     uint8_t *d_tier_prev = nullptr, *d_tier_cur = nullptr;
     int *d_lists = nullptr, *d_counts = nullptr;
+    int *d_order = nullptr;  // launch order of the fused grain-growth step (adaptive runs)
     double *d_metric = nullptr, *d_snap = nullptr;
     int nmon = 0;
     unsigned long long *d_stats = nullptr;
@@ -181,7 +182,7 @@ static void free_all(amps_handle *h)
     for (int t = 0; t < 3; ++t)
         for (int q = 0; q < 2; ++q)
             if (h->store[t][q]) cudaFree(h->store[t][q]);
-    void *ps[] = {h->d_tier_prev, h->d_tier_cur, h->d_lists, h->d_counts, h->d_metric, h->d_snap, h->d_stats,
+    void *ps[] = {h->d_tier_prev, h->d_tier_cur, h->d_lists, h->d_order, h->d_counts, h->d_metric, h->d_snap, h->d_stats,
                   h->d_flags, h->d_log, h->d_log_n, h->d_step_base, h->d_stage, h->d_partials, h->d_out,
                   h->d_diag};
     for (void *q : ps)
@@ -239,6 +240,7 @@ extern "C" int amps_create(const amps_params *p, amps_handle **out)
     ALLOC(h->d_tier_prev, h->ntiles, "tier map");
     ALLOC(h->d_tier_cur, h->ntiles, "tier map");
     ALLOC(h->d_lists, sizeof(int) * 3 * h->ntiles, "tile lists");
+    ALLOC(h->d_order, sizeof(int) * h->ntiles, "launch order");
     ALLOC(h->d_counts, sizeof(int) * 4, "tile counts");
     ALLOC(h->d_metric, sizeof(double) * h->ntiles, "monitor metric");
     h->nmon = p->monitor_field < 0 ? h->nf : 1;
@@ -394,6 +396,7 @@ static int reclassify_resting(amps_handle *h)
         c.thr_lo = p.thr_lo; c.thr_hi = p.thr_hi; c.high_tier = p.high_tier; c.use_mid = h->use_mid;
         c.stats = h->d_stats; c.log = h->d_log; c.log_n = h->d_log_n; c.max_log = p.max_log;
         c.step_base = h->d_step_base; c.advance = 0; c.stat_steps = 0;
+        c.order = h->d_order; c.bc = p.bc;
         CK(h, classify(c, h->stream));
         h->transition = true;
     }
@@ -538,6 +541,8 @@ static StepArgs step_args(const amps_handle *h, int parity, bool transition, int
     a.tier_in = transition ? h->d_tier_prev : h->d_tier_cur;
     a.tier_out = h->d_tier_cur;
     a.count = h->d_counts;
+    // adaptive runs: slow tiles first (the classification's launch order)
+    a.order = p.model == AMPS_GRAINGROWTH && p.mode == AMPS_END2END_MIX ? h->d_order : nullptr;
     a.nx = p.nx; a.ny = p.ny; a.ntx = h->ntx; a.nty = h->nty; a.nf = h->nf; a.bc = p.bc; a.stencil = p.stencil;
     a.n = h->n;
     a.monitor_now = monitor_now ? 1 : 0;
@@ -635,6 +640,7 @@ static ClassifyArgs classify_args(const amps_handle *h, int advance, int stat_st
     c.thr_lo = p.thr_lo; c.thr_hi = p.thr_hi; c.high_tier = p.high_tier; c.use_mid = h->use_mid;
     c.stats = h->d_stats; c.log = h->d_log; c.log_n = h->d_log_n; c.max_log = p.max_log;
     c.step_base = h->d_step_base; c.advance = advance; c.stat_steps = stat_steps;
+    c.order = h->d_order; c.bc = p.bc;
     return c;
 }
 

@@ -66,6 +66,7 @@ struct StepArgs {
     const uint8_t *tier_out;  // tier every tile is computed and stored in
     const int *list;          // tiles whose tier_out == this launch's tier
     const int *count;         // count[tier]
+    const int *order;         // fused grain-growth step: tile of each CTA (nullptr: blockIdx.x)
     int nx, ny, ntx, nty, nf, bc, stencil;
     int64_t n;                // nx*ny
     // monitor (active when monitor_now != 0)
@@ -218,7 +219,10 @@ __device__ __forceinline__ void load_neighbour_tiers(const StepArgs &a, int tx, 
 // an interior 8-cell row segment (16-byte vector loads) or one halo cell --
 // whose coordinates, tier and offsets are computed once; the field loop then
 // only adds the field stride, issuing a batch of loads before any store.
-template <typename CT, int T, int R>
+// SKIP32: the FP32-owned slots already hold their values (copied by this
+// same thread: stage_tile_async32 gives every thread the same slots); only
+// the others are loaded and converted.
+template <typename CT, int T, int R, bool SKIP32 = false>
 __device__ __forceinline__ void stage_tile(const StepArgs &a, CT *sm, const uint8_t *nt, int tx, int ty, int f0,
                                            int nfs)
 {
@@ -254,6 +258,7 @@ __device__ __forceinline__ void stage_tile(const StepArgs &a, CT *sm, const uint
             goff[q] = (int64_t)gy * a.nx + gx;
             soff[q] = r * S::P + (k < R ? S::O - R + k : S::O + T + (k - R));
         }
+        if (SKIP32 && tier[q] == TIER_FP32) kind[q] = 0;
     }
     for (int fb = 0; fb < nfs; fb += B) {
         CT v[SLOTS][B][8];
@@ -300,8 +305,9 @@ __device__ __forceinline__ void stage_tile(const StepArgs &a, CT *sm, const uint
 // values are read once from global memory) and 4-byte copies for the halo
 // cells, every field in flight at once, no register round trip.  Same slot
 // layout and the same floats as stage_tile; the caller synchronises after
-// the final wait issued here.
-template <int T, int R>
+// the final wait issued here (WAIT = false: committed, not waited for --
+// cp_async_wait_all before the shared memory is read or reused).
+template <int T, int R, bool WAIT = true>
 __device__ __forceinline__ void stage_tile_async32(const StepArgs &a, float *sm, int tx, int ty, int nfs)
 {
     using S = Stage<float, T, R>;
@@ -338,8 +344,11 @@ __device__ __forceinline__ void stage_tile_async32(const StepArgs &a, float *sm,
         }
     }
     asm volatile("cp.async.commit_group;" ::: "memory");
-    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    if (WAIT) asm volatile("cp.async.wait_group 0;" ::: "memory");
 }
+
+// Wait for this thread's committed asynchronous copies (stage_tile_async32<..., false>).
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
 // ---- block reductions (warp shuffle + one shared slot per warp) ------------------
 __device__ __forceinline__ double warp_max(double v)

@@ -65,6 +65,8 @@ struct ClassifyArgs {
     int64_t *step_base;
     int advance;                // steps to add to *step_base (one period, or 0)
     int stat_steps;             // steps the current counts ran for (tile-step stats)
+    int *order;                 // optional: launch order of the fused grain-growth step
+    int bc;                     // boundary map of the tile neighbourhood (for order)
 };
 cudaError_t classify(const ClassifyArgs &c, cudaStream_t s);
 // Ensembles: classify (or do the period bookkeeping of) count members whose

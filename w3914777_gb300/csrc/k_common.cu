@@ -170,6 +170,56 @@ __device__ void lists_from_tiers(const uint8_t *tier, int ntiles, int *lists, in
     if (threadIdx.x < 3) counts[threadIdx.x] = (int)((base >> (21 * threadIdx.x)) & 0x1FFFFF);
 }
 
+// Launch order of the fused grain-growth step: first the tiles that take
+// its slow paths -- FP64 or half tiles, and FP32 tiles with a neighbour
+// (after the boundary map) at another tier, which stage their neighbourhood
+// with conversions -- then the all-FP32 neighbourhoods, each group in tile
+// order.  Slow tiles then run in the first wave, where their extra time is
+// absorbed, instead of straggling at the end of the step.  Scheduling only:
+// every tile is computed by exactly one CTA either way.
+__device__ void order_slow_first(const ClassifyArgs &c, unsigned long long *ws)
+{
+    __shared__ unsigned long long base;
+    __shared__ int nslow;
+    const int ntiles = c.ntx * c.nty;
+    if (threadIdx.x == 0) base = 0;
+    __syncthreads();  // also: this block's tier_cur writes are visible to it
+    for (int pass = 0; pass < 2; ++pass) {
+        for (int t0 = 0; t0 < ntiles; t0 += blockDim.x) {
+            const int t = t0 + threadIdx.x;
+            bool slow = false;
+            if (t < ntiles) {
+                const int x = t % c.ntx, y = t / c.ntx;
+                for (int dy = -1; dy <= 1; ++dy)
+                    for (int dx = -1; dx <= 1; ++dx) {
+                        int yy = y + dy, xx = x + dx;
+                        if (c.bc == 0) {
+                            yy = yy < 0 ? yy + c.nty : (yy >= c.nty ? yy - c.nty : yy);
+                            xx = xx < 0 ? xx + c.ntx : (xx >= c.ntx ? xx - c.ntx : xx);
+                        } else {
+                            yy = yy < 0 ? 0 : (yy >= c.nty ? c.nty - 1 : yy);
+                            xx = xx < 0 ? 0 : (xx >= c.ntx ? c.ntx - 1 : xx);
+                        }
+                        slow |= c.tier_cur[yy * c.ntx + xx] != TIER_FP32;
+                    }
+            }
+            // pass 0 places the slow tiles, pass 1 (after nslow of them) the others
+            const bool mine = t < ntiles && slow == (pass == 0);
+            const unsigned long long inc = block_scan((unsigned long long)mine, ws);
+            const unsigned long long b = base;
+            if (mine) c.order[(pass ? nslow : 0) + (int)(b + inc - 1)] = t;
+            __syncthreads();
+            if (threadIdx.x == blockDim.x - 1) base = b + inc;
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            if (pass == 0) nslow = (int)base;
+            base = 0;
+        }
+        __syncthreads();
+    }
+}
+
 __device__ void classify_body(const ClassifyArgs &c)
 {
     __shared__ unsigned long long ws[32];
@@ -207,6 +257,7 @@ __device__ void classify_body(const ClassifyArgs &c)
     atomicAdd(&dem, nd);
     __syncthreads();
     lists_from_tiers(c.tier_cur, ntiles, c.lists, c.counts, ws);
+    if (c.order) order_slow_first(c, ws);
     if (threadIdx.x == 0) {
         c.stats[4] += prom;
         c.stats[5] += dem;

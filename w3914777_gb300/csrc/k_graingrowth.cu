@@ -435,17 +435,33 @@ __global__ void __launch_bounds__(kThreads, 4) gg_step_kernel(StepArgs a)
     // its first global read (both are no-ops for a plain launch)
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     asm volatile("griddepcontrol.wait;" ::: "memory");
-    const int tile = blockIdx.x;
-    const int tier = a.tier_out[tile];
+    const int tile = a.order ? a.order[blockIdx.x] : (int)blockIdx.x;
     const int tx = tile % a.ntx, ty = tile / a.ntx;
     load_neighbour_tiers(a, tx, ty, ntier);
+    // the copy of the FP32 neighbourhood (the common case) starts before the
+    // tiers are known, so that its latency overlaps theirs; where the tile
+    // turns out FP64 or its neighbourhood mixed, the copies are drained and
+    // their data (in-bounds reads of the full-size FP32 store) discarded
+    const bool spec = T == 32 && a.in[TIER_FP32] != nullptr;
+    if (spec) stage_tile_async32<T, 1, false>(a, sm, tx, ty, a.nf);
+    const int tier = a.tier_out[tile];
     __syncthreads();
     if (tier == TIER_FP64) {
+        if (spec) cp_async_wait_all();
         gg_tile_fp64<T, REF>(a, ntier, tile, tx, ty, red);
         return;
     }
-    if (all_fp32(ntier)) stage_tile_async32<T, 1>(a, sm, tx, ty, a.nf);
-    else stage_tile<float, T, 1>(a, sm, ntier, tx, ty, 0, a.nf);
+    const bool all32 = all_fp32(ntier);
+    if (spec) {
+        cp_async_wait_all();
+        // mixed neighbourhood: the FP32-owned slots are in place; each thread
+        // overwrites its own other slots with their converted values
+        if (!all32) stage_tile<float, T, 1, true>(a, sm, ntier, tx, ty, 0, a.nf);
+    } else if (all32) {
+        stage_tile_async32<T, 1>(a, sm, tx, ty, a.nf);
+    } else {
+        stage_tile<float, T, 1>(a, sm, ntier, tx, ty, 0, a.nf);
+    }
     __syncthreads();
     if constexpr (T == 32) {
         // the spatial range needs one reduction per field: gg_tile_lo_impl
