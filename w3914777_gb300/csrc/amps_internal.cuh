@@ -260,6 +260,63 @@ __device__ __forceinline__ void stage_tile(const StepArgs &a, CT *sm, const uint
         }
         if (SKIP32 && tier[q] == TIER_FP32) kind[q] = 0;
     }
+    // half-owned slots first: raw halves take half the registers of
+    // converted values, so HB fields (all 8 when a thread has one slot) go
+    // in one round trip -- 16-byte loads of 8 cells, 2-byte loads of halo
+    // cells -- and are converted on the way to shared memory
+    constexpr int HB0 = 8 / SLOTS;
+    constexpr int HB = HB0 < 1 ? 1 : HB0;
+    bool anyh = false;
+#pragma unroll
+    for (int q = 0; q < SLOTS; ++q) anyh |= kind[q] != 0 && tier[q] == TIER_HALF;
+    if (anyh) {
+        const __half *hs = (const __half *)a.in[TIER_HALF];
+        for (int fb = 0; fb < nfs; fb += HB) {
+            uint4 raw[SLOTS][HB];
+#pragma unroll
+            for (int q = 0; q < SLOTS; ++q)
+#pragma unroll
+                for (int b = 0; b < HB; ++b) {
+                    raw[q][b] = make_uint4(0u, 0u, 0u, 0u);
+                    if (kind[q] != 0 && tier[q] == TIER_HALF && fb + b < nfs) {
+                        const __half *src = hs + (int64_t)(f0 + fb + b) * a.n + goff[q];
+                        if (kind[q] == 1) raw[q][b] = __ldg(reinterpret_cast<const uint4 *>(src));
+                        else raw[q][b].x = __ldg(reinterpret_cast<const unsigned short *>(src));
+                    }
+                }
+#pragma unroll
+            for (int q = 0; q < SLOTS; ++q)
+#pragma unroll
+                for (int b = 0; b < HB; ++b) {
+                    if (kind[q] == 0 || tier[q] != TIER_HALF || fb + b >= nfs) continue;
+                    CT *dst = sm + (fb + b) * S::FIELD + soff[q];
+                    if (kind[q] == 2) {
+                        dst[0] = (CT)__half2float(__ushort_as_half((unsigned short)raw[q][b].x));
+                        continue;
+                    }
+                    const __half2 *h2 = reinterpret_cast<const __half2 *>(&raw[q][b]);
+                    float c[8];
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const float2 f = __half22float2(h2[k]);
+                        c[2 * k] = f.x;
+                        c[2 * k + 1] = f.y;
+                    }
+                    if (sizeof(CT) == 4) {
+                        float4 *d4 = reinterpret_cast<float4 *>(dst);
+                        d4[0] = make_float4(c[0], c[1], c[2], c[3]);
+                        d4[1] = make_float4(c[4], c[5], c[6], c[7]);
+                    } else {
+                        double2 *d2 = reinterpret_cast<double2 *>(dst);
+#pragma unroll
+                        for (int k = 0; k < 4; ++k) d2[k] = make_double2((double)c[2 * k], (double)c[2 * k + 1]);
+                    }
+                }
+        }
+#pragma unroll
+        for (int q = 0; q < SLOTS; ++q)
+            if (tier[q] == TIER_HALF) kind[q] = 0;
+    }
     for (int fb = 0; fb < nfs; fb += B) {
         CT v[SLOTS][B][8];
 #pragma unroll
