@@ -412,30 +412,13 @@ __device__ __noinline__ void gg_tile_fp64_call(const StepArgs &a, const uint8_t 
     gg_tile_fp64<T, REF>(a, nt, tile, tx, ty, red);
 }
 
-// Fused all-tier step: at most 64 registers, so that four CTAs share an SM.
-// MON (the monitor steps, one in `cadence`) is a separate instantiation, so
-// the other steps' kernel carries no monitor code.  Half/FP32 tiles stage
-// their neighbourhood in shared memory.  (Reading it directly through L1 --
-// SRC_G32 -- runs 18.5 against 22.5 us per 1024^2 Q=8 step for an all-FP32
-// grid in isolation, but in the full adaptive run, with monitor steps and
-// mixed-tier neighbourhoods, this kernel measured 22.5 us per step staged
-// against 25.2 direct; the ensemble kernel, whose tile order mixes members,
-// gains from it and uses it.)
+// One tile of the fused step (every tier), by the whole CTA: neighbourhood
+// tiers, staging, update (and the monitor on MON steps).  Shared by the
+// single-run step kernel and the ensemble's tile-queue kernel, so that a
+// member of an ensemble gets exactly the results of a single run.
 template <int T, bool REF, bool MON>
-__global__ void __launch_bounds__(kThreads, 4) gg_step_kernel(StepArgs a)
+__device__ __forceinline__ void gg_tile_step(const StepArgs &a, float *sm, uint8_t *ntier, double *red, int tile)
 {
-    using S = Stage<float, T, 1>;
-    extern __shared__ __align__(16) unsigned char smraw[];
-    __shared__ double red[kThreads / 32];
-    __shared__ uint8_t ntier[9];
-    float *sm = reinterpret_cast<float *>(smraw);
-    // programmatic dependent launch (gg_launch): the next step's CTAs may be
-    // scheduled into the slots this grid's last wave leaves free; every CTA
-    // waits for the previous grid to complete, its writes visible, before
-    // its first global read (both are no-ops for a plain launch)
-    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-    asm volatile("griddepcontrol.wait;" ::: "memory");
-    const int tile = a.order ? a.order[blockIdx.x] : (int)blockIdx.x;
     const int tx = tile % a.ntx, ty = tile / a.ntx;
     load_neighbour_tiers(a, tx, ty, ntier);
     // the copy of the FP32 neighbourhood (the common case) starts before the
@@ -483,7 +466,36 @@ __global__ void __launch_bounds__(kThreads, 4) gg_step_kernel(StepArgs a)
     }
     if (tier == TIER_FP32) gg_tile_lo_impl<T, TIER_FP32, SRC_SMEM, MON>(a, sm, ntier, tile, tx, ty, red);
     else gg_tile_lo_impl<T, TIER_HALF, SRC_SMEM, MON>(a, sm, ntier, tile, tx, ty, red);
-    (void)sizeof(S);
+}
+
+// gg_tile_step out of line, for callers whose StepArgs live in shared
+// memory (inlined, their loads are hoisted and spill).
+template <int T, bool REF, bool MON>
+__device__ __noinline__ void gg_tile_step_call(const StepArgs &a, float *sm, uint8_t *ntier, double *red, int tile)
+{
+    gg_tile_step<T, REF, MON>(a, sm, ntier, red, tile);
+}
+
+// Fused all-tier step: at most 64 registers, so that four CTAs share an SM.
+// MON (the monitor steps, one in `cadence`) is a separate instantiation, so
+// the other steps' kernel carries no monitor code.  Half/FP32 tiles stage
+// their neighbourhood in shared memory (reading it directly through L1
+// measured 18.1 against 15.8 us per adaptive 1024^2 Q=8 step).
+template <int T, bool REF, bool MON>
+__global__ void __launch_bounds__(kThreads, 4) gg_step_kernel(StepArgs a)
+{
+    extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ double red[kThreads / 32];
+    __shared__ uint8_t ntier[9];
+    float *sm = reinterpret_cast<float *>(smraw);
+    // programmatic dependent launch (gg_launch): the next step's CTAs may be
+    // scheduled into the slots this grid's last wave leaves free; every CTA
+    // waits for the previous grid to complete, its writes visible, before
+    // its first global read (both are no-ops for a plain launch)
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    const int tile = a.order ? a.order[blockIdx.x] : (int)blockIdx.x;
+    gg_tile_step<T, REF, MON>(a, sm, ntier, red, tile);
 }
 
 // All-FP64 step (plain FP64 mode): the FP64 neighbourhood is staged in
@@ -766,8 +778,8 @@ cudaError_t gg_prepare_tma(bool ref, int nf, int *blocks_per_sm)
 // Ensemble step: persistent CTAs take (member, tile) work items from a
 // global counter; items are ordered by cost (most fields first), so the
 // dynamic queue approximates longest-first scheduling across members of
-// different sizes and field counts.  A tile's arithmetic is the fused
-// kernel's (same per-tile code, same results); the member's arguments are
+// different sizes and field counts.  A tile is gg_tile_step, the fused
+// kernel's per-tile code (same results); the member's arguments are
 // copied into shared memory when the member changes.  No waits: the counter
 // only hands out indices, and the last CTA to finish resets it.
 template <int T, bool REF, bool MON>
@@ -795,26 +807,7 @@ __global__ void __launch_bounds__(kThreads, 2)
             member = it.x;
         }
         __syncthreads();
-        const StepArgs &a = sa;
-        const int t = it.y, tx = t % a.ntx, ty = t / a.ntx;
-        const int tier = a.tier_out[t];
-        load_neighbour_tiers(a, tx, ty, ntier);
-        __syncthreads();
-        if constexpr (T == 32) {
-            if (tier == TIER_FP32 && all_fp32(ntier))
-                gg_tile_lo_impl<T, TIER_FP32, SRC_G32, MON>(a, nullptr, ntier, t, tx, ty, red);
-            else if (tier == TIER_FP64)
-                gg_tile_fp64_call<T, REF>(a, ntier, t, tx, ty, red);
-            else
-                gg_tile_mixed_call<T, MON>(a, ntier, tier, t, tx, ty, red);
-        } else if (tier == TIER_FP64) {
-            gg_tile_fp64<T, REF>(a, ntier, t, tx, ty, red);
-        } else {
-            stage_tile<float, T, 1>(a, sm, ntier, tx, ty, 0, a.nf);
-            __syncthreads();
-            if (tier == TIER_FP32) gg_tile_lo<T, TIER_FP32>(a, sm, ntier, t, tx, ty, red);
-            else gg_tile_lo<T, TIER_HALF>(a, sm, ntier, t, tx, ty, red);
-        }
+        gg_tile_step_call<T, REF, MON>(sa, sm, ntier, red, it.y);
         __syncthreads();
     }
     if (threadIdx.x == 0) {
@@ -827,8 +820,8 @@ __global__ void __launch_bounds__(kThreads, 2)
     }
 }
 
-// 32^2 ensemble tiles read their neighbourhoods directly (no shared memory)
-size_t gg_ens_smem_bytes(int tile, int max_nf) { return tile == 32 ? 0 : gg_smem_bytes(tile, -1, max_nf); }
+// staging for the member with the most fields
+size_t gg_ens_smem_bytes(int tile, int max_nf) { return gg_smem_bytes(tile, -1, max_nf); }
 
 cudaError_t gg_prepare_ens(int tile, bool ref, int max_nf, int *blocks_per_sm)
 {
