@@ -343,6 +343,26 @@ def test_monitor_flags_non_finite_values(monitor):
             assert s.stats()["numeric_error"] == int(poison)
 
 
+@pytest.mark.parametrize("mode", ["purehigh", "end2end_mix"])
+def test_tma_step_kernel_matches_default(mode, monkeypatch):
+    """The opt-in persistent TMA kernel (AMPS_ENABLE_TMA=1: tensor copies of
+    whole FP32 neighbourhoods, double-buffered) gives the default kernel's
+    results bit for bit."""
+    w = amps()
+    extra = dict(high_tier=w.TIER_FP32) if mode == "purehigh" else dict(monitor=w.MONITOR_RATE, monitor_samples=1,
+                                                                          thr_lo=1e-5)
+    p = w.Params.preset("graingrowth", 0, nx=256, ny=256, nfields=8, tile=32, mode=mode, **extra)
+    out = []
+    for tma in ("0", "1"):
+        monkeypatch.setenv("AMPS_ENABLE_TMA", tma)
+        with w.Simulation(p, init=w.INIT_SEEDED) as s:
+            s.run(25)
+            out.append((s.fields(), s.tiers(), s.stats()))
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
+    assert out[0][2] == out[1][2]
+
+
 def test_set_get_roundtrip_and_reduce():
     w = amps()
     p = w.Params.preset("sintering", 1, mode="purehigh", nx=64, ny=64)

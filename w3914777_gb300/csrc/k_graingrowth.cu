@@ -40,91 +40,28 @@ __device__ __forceinline__ void store_cells(const StepArgs &a, int64_t idx, cons
     }
 }
 
-// Where a half/FP32 tile step reads its neighbourhood from:
-//  SRC_SMEM: the staged float neighbourhood `sm` (16^2 tiles, the TMA kernel);
-//  SRC_G32:  the tile and all eight neighbours hold FP32 input -- three rows
-//            and two halo columns per field straight from the FP32 array
-//            through L1 (no staging copy, no barrier, no shared memory);
-//  SRC_GMIX: any mix of input tiers -- each row segment and halo cell read at
-//            its owner tile's tier and converted to float, as staging would.
-// The arithmetic is the same for all three.
-enum { SRC_SMEM = 0, SRC_G32 = 1, SRC_GMIX = 2 };
-
-// Cells [c0-1, c0+4] of one mapped row of field f into w[0..5] as float:
-// the centre four from the tier `tc` (16/8/32-byte aligned vector), the halo
-// cells from tiers tl / tr.
-__device__ __forceinline__ void ld_row6(const StepArgs &a, int64_t base, int gx0, int gxl, int gxr, int tc, int tl,
-                                        int tr, float *w)
-{
-    if (tc == TIER_FP32) {
-        const float4 q = __ldg(reinterpret_cast<const float4 *>((const float *)a.in[TIER_FP32] + base + gx0));
-        w[1] = q.x; w[2] = q.y; w[3] = q.z; w[4] = q.w;
-    } else if (tc == TIER_HALF) {
-        const uint2 u = __ldg(reinterpret_cast<const uint2 *>((const __half *)a.in[TIER_HALF] + base + gx0));
-        const float2 lo = __half22float2(*reinterpret_cast<const __half2 *>(&u.x));
-        const float2 hi = __half22float2(*reinterpret_cast<const __half2 *>(&u.y));
-        w[1] = lo.x; w[2] = lo.y; w[3] = hi.x; w[4] = hi.y;
-    } else {
-        const double2 *d = reinterpret_cast<const double2 *>((const double *)a.in[TIER_FP64] + base + gx0);
-        const double2 d0 = __ldg(d), d1 = __ldg(d + 1);
-        w[1] = (float)d0.x; w[2] = (float)d0.y; w[3] = (float)d1.x; w[4] = (float)d1.y;
-    }
-    w[0] = load_tier<float>(a, tl, base + gxl);
-    w[5] = load_tier<float>(a, tr, base + gxr);
-}
-
 // MON: this step evaluates the monitor (compiled out of the other steps, so
 // their loop carries no monitor state).
-template <int T, int TIER, int SRC, bool MON>
-__device__ __forceinline__ void gg_tile_lo_impl(const StepArgs &a, const float *sm, const uint8_t *nt, int tile,
-                                                int tx, int ty, double *red)
+template <int T, int TIER, bool MON>
+__device__ __forceinline__ void gg_tile_lo_impl(const StepArgs &a, const float *sm, int tile, int tx, int ty,
+                                                double *red)
 {
     using S = Stage<float, T, 1>;
     constexpr int CPT = T * T / kThreads;  // cells per thread, along x
     constexpr int GPR = T / CPT;           // thread groups per row
-    static_assert(SRC == SRC_SMEM || CPT == 4, "direct reads need 4 cells per thread (32^2 tiles)");
     const int row = threadIdx.x / GPR;
     const int c0 = (threadIdx.x % GPR) * CPT;
     const int nf = a.nf;
     const Phys &ph = a.ph;
     float *smm = const_cast<float *>(sm);
-    // direct reads: mapped offsets of rows row-1, row, row+1 and the mapped
-    // halo columns; GMIX: the tier of each row's centre and halo parts
-    int64_t grow[3] = {0, 0, 0};
-    int gxl = 0, gxr = 0, tcs[3] = {0, 0, 0}, tls[3] = {0, 0, 0}, trs[3] = {0, 0, 0};
-    const int gx0 = tx * T + c0;
-    if (SRC != SRC_SMEM) {
-#pragma unroll
-        for (int rr = 0; rr < 3; ++rr) {
-            const int lr = row - 1 + rr;
-            grow[rr] = (int64_t)bc_map(ty * T + lr, a.ny, a.bc) * a.nx;
-            const int rc = (lr < 0 ? 0 : (lr < T ? 3 : 6));
-            tcs[rr] = nt[rc + 1];
-            tls[rr] = nt[rc + (c0 == 0 ? 0 : 1)];
-            trs[rr] = nt[rc + (c0 + CPT == T ? 2 : 1)];
-        }
-        gxl = bc_map(gx0 - 1, a.nx, a.bc);
-        gxr = bc_map(gx0 + CPT, a.nx, a.bc);
-    }
-    const float *g32 = (const float *)a.in[TIER_FP32];
     float ssum[CPT];
 #pragma unroll
     for (int k = 0; k < CPT; ++k) ssum[k] = 0.f;
     for (int f = 0; f < nf; ++f) {
         float c[CPT];
-        if (SRC == SRC_G32) {
-            const float4 q = __ldg(reinterpret_cast<const float4 *>(g32 + f * a.n + grow[1] + gx0));
-            c[0] = q.x; c[1] = q.y; c[2] = q.z; c[3] = q.w;
-        } else if (SRC == SRC_GMIX) {
-            float w6[6];
-            ld_row6(a, f * a.n + grow[1], gx0, gxl, gxr, tcs[1], tls[1], trs[1], w6);
+        const float *ctr = &S::at(smm, f, row + 1, S::O + c0);
 #pragma unroll
-            for (int k = 0; k < CPT; ++k) c[k] = w6[k + 1];
-        } else {
-            const float *ctr = &S::at(smm, f, row + 1, S::O + c0);
-#pragma unroll
-            for (int k = 0; k < CPT; ++k) c[k] = ctr[k];
-        }
+        for (int k = 0; k < CPT; ++k) c[k] = ctr[k];
 #pragma unroll
         for (int k = 0; k < CPT; ++k) ssum[k] = fmaf(c[k], c[k], ssum[k]);
     }
@@ -144,26 +81,16 @@ __device__ __forceinline__ void gg_tile_lo_impl(const StepArgs &a, const float *
         float w[3][CPT + 2];
 #pragma unroll
         for (int rr = 0; rr < 3; ++rr) {
-            if (SRC == SRC_G32) {
-                const float *b = g32 + f * a.n + grow[rr];
-                const float4 q = __ldg(reinterpret_cast<const float4 *>(b + gx0));
+            const float *p = &S::at(smm, f, row + rr, S::O + c0);
+            if (CPT == 4) {
+                const float4 q = *reinterpret_cast<const float4 *>(p);
                 w[rr][1] = q.x; w[rr][2] = q.y; w[rr][3] = q.z; w[rr][4] = q.w;
-                w[rr][0] = __ldg(b + gxl);
-                w[rr][CPT + 1] = __ldg(b + gxr);
-            } else if (SRC == SRC_GMIX) {
-                ld_row6(a, f * a.n + grow[rr], gx0, gxl, gxr, tcs[rr], tls[rr], trs[rr], w[rr]);
             } else {
-                const float *p = &S::at(smm, f, row + rr, S::O + c0);
-                if (CPT == 4) {
-                    const float4 q = *reinterpret_cast<const float4 *>(p);
-                    w[rr][1] = q.x; w[rr][2] = q.y; w[rr][3] = q.z; w[rr][4] = q.w;
-                } else {
 #pragma unroll
-                    for (int k = 0; k < CPT; ++k) w[rr][k + 1] = p[k];
-                }
-                w[rr][0] = p[-1];
-                w[rr][CPT + 1] = p[CPT];
+                for (int k = 0; k < CPT; ++k) w[rr][k + 1] = p[k];
             }
+            w[rr][0] = p[-1];
+            w[rr][CPT + 1] = p[CPT];
         }
         float out[CPT];
 #pragma unroll
@@ -192,12 +119,11 @@ __device__ __forceinline__ void gg_tile_lo_impl(const StepArgs &a, const float *
     if (MON && threadIdx.x == 0) a.metric[tile] = metric;
 }
 
-template <int T, int TIER, int SRC = SRC_SMEM>
-__device__ __forceinline__ void gg_tile_lo(const StepArgs &a, const float *sm, const uint8_t *nt, int tile, int tx,
-                                           int ty, double *red)
+template <int T, int TIER>
+__device__ __forceinline__ void gg_tile_lo(const StepArgs &a, const float *sm, int tile, int tx, int ty, double *red)
 {
-    if (a.monitor_now) gg_tile_lo_impl<T, TIER, SRC, true>(a, sm, nt, tile, tx, ty, red);
-    else gg_tile_lo_impl<T, TIER, SRC, false>(a, sm, nt, tile, tx, ty, red);
+    if (a.monitor_now) gg_tile_lo_impl<T, TIER, true>(a, sm, tile, tx, ty, red);
+    else gg_tile_lo_impl<T, TIER, false>(a, sm, tile, tx, ty, red);
 }
 
 // Half/FP32 tile, 32^2 tiles, from the staged float neighbourhood: each
@@ -394,24 +320,6 @@ __device__ __forceinline__ bool all_fp32(const uint8_t *nt)
     return ok;
 }
 
-// Tiles off the all-FP32 path (mixed-tier neighbourhoods, half tiles, FP64
-// tiles), kept out of line so that their register demand does not spill the
-// hot path.
-template <int T, bool MON>
-__device__ __noinline__ void gg_tile_mixed_call(const StepArgs &a, const uint8_t *nt, int tier, int tile, int tx,
-                                                int ty, double *red)
-{
-    if (tier == TIER_FP32) gg_tile_lo_impl<T, TIER_FP32, SRC_GMIX, MON>(a, nullptr, nt, tile, tx, ty, red);
-    else gg_tile_lo_impl<T, TIER_HALF, SRC_GMIX, MON>(a, nullptr, nt, tile, tx, ty, red);
-}
-
-template <int T, bool REF>
-__device__ __noinline__ void gg_tile_fp64_call(const StepArgs &a, const uint8_t *nt, int tile, int tx, int ty,
-                                               double *red)
-{
-    gg_tile_fp64<T, REF>(a, nt, tile, tx, ty, red);
-}
-
 // One tile of the fused step (every tier), by the whole CTA: neighbourhood
 // tiers, staging, update (and the monitor on MON steps).  Shared by the
 // single-run step kernel and the ensemble's tile-queue kernel, so that a
@@ -464,8 +372,8 @@ __device__ __forceinline__ void gg_tile_step(const StepArgs &a, float *sm, uint8
             return;
         }
     }
-    if (tier == TIER_FP32) gg_tile_lo_impl<T, TIER_FP32, SRC_SMEM, MON>(a, sm, ntier, tile, tx, ty, red);
-    else gg_tile_lo_impl<T, TIER_HALF, SRC_SMEM, MON>(a, sm, ntier, tile, tx, ty, red);
+    if (tier == TIER_FP32) gg_tile_lo_impl<T, TIER_FP32, MON>(a, sm, tile, tx, ty, red);
+    else gg_tile_lo_impl<T, TIER_HALF, MON>(a, sm, tile, tx, ty, red);
 }
 
 // gg_tile_step out of line, for callers whose StepArgs live in shared
@@ -733,8 +641,8 @@ __global__ void __launch_bounds__(kThreads, 2)
                 if (fast_s[b ^ 1]) mbar_wait_bounded(&mbar[b ^ 1], b ? ph0 : ph1);
                 return;
             }
-            if (tier == TIER_FP32) gg_tile_lo<T, TIER_FP32>(a, sm, ntier, t, tx, ty, red);
-            else gg_tile_lo<T, TIER_HALF>(a, sm, ntier, t, tx, ty, red);
+            if (tier == TIER_FP32) gg_tile_lo<T, TIER_FP32>(a, sm, t, tx, ty, red);
+            else gg_tile_lo<T, TIER_HALF>(a, sm, t, tx, ty, red);
         } else {
             load_neighbour_tiers(a, tx, ty, ntier);
             __syncthreads();
@@ -743,8 +651,8 @@ __global__ void __launch_bounds__(kThreads, 2)
             } else {
                 stage_tile<float, T, 1>(a, sm, ntier, tx, ty, 0, a.nf);
                 __syncthreads();
-                if (tier == TIER_FP32) gg_tile_lo<T, TIER_FP32>(a, sm, ntier, t, tx, ty, red);
-                else gg_tile_lo<T, TIER_HALF>(a, sm, ntier, t, tx, ty, red);
+                if (tier == TIER_FP32) gg_tile_lo<T, TIER_FP32>(a, sm, t, tx, ty, red);
+                else gg_tile_lo<T, TIER_HALF>(a, sm, t, tx, ty, red);
             }
         }
         fence_proxy_async_smem();  // this buffer's reads/writes before its next tensor copy
