@@ -616,8 +616,10 @@ static int launch_step(amps_handle *h, int step_off, bool monitor_now)
             const int r = prof_begin(h, ev);
             if (r) return r;
         }
-        if (fused) e = p.model == AMPS_KOBAYASHI ? kob_launch_lo(h->T, a, h->ntiles, st)
-                                                 : sint_launch_lo(h->T, p.mu_lap_fp64 != 0, a, h->ntiles, st);
+        // the FP64 launch (t = 2) came just before: run alongside it
+        const bool after64 = h->used[TIER_FP64] && !h->profiling;
+        if (fused) e = p.model == AMPS_KOBAYASHI ? kob_launch_lo(h->T, a, h->ntiles, st, after64)
+                                                 : sint_launch_lo(h->T, p.mu_lap_fp64 != 0, a, h->ntiles, st, after64);
         else if (p.model == AMPS_KOBAYASHI) e = kob_launch(h->T, t, ref, a, h->ntiles, st);
         else e = sint_launch(h->T, t, ref, p.mu_lap_fp64 != 0, a, h->ntiles, st);
         if (e != cudaSuccess) FAIL(h, AMPS_ERR_CUDA, "step kernel launch: %s", cudaGetErrorString(e));

@@ -121,6 +121,31 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity
     return false;
 }
 
+// ---- launches ----------------------------------------------------------------
+// Launch `kernel` on `s`; pdl: with programmatic stream serialization, so it
+// may begin once every CTA of the previous kernel on the stream has started
+// (that kernel executes griddepcontrol.launch_dependents).  A kernel launched
+// this way reads nothing the previous one writes before its own
+// griddepcontrol.wait.
+template <typename K, typename... Args>
+inline cudaError_t launch_kernel(K kernel, int grid, size_t smem, cudaStream_t s, bool pdl, Args... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // ---- boundary mapping ------------------------------------------------------
 // Periodic wrap (snowflake/function.h:13-18) or mirror (zero flux) about the
 // domain face: -1 -> 0, -2 -> 1, n -> n-1, n+1 -> n-2.

@@ -10,8 +10,9 @@ cudaError_t sint_launch(int tile, int tier, bool ref, bool mu64, const StepArgs 
 size_t gg_smem_bytes(int tile, int tier, int nf);
 // Kobayashi / sintering: the half and FP32 tiles of a step in one launch
 // (grid = all tiles; FP64 tiles are skipped, left to the FP64 tier launch).
-cudaError_t kob_launch_lo(int tile, const StepArgs &a, int grid, cudaStream_t s);
-cudaError_t sint_launch_lo(int tile, bool mu64, const StepArgs &a, int grid, cudaStream_t s);
+// after64: this step's FP64 launch directly precedes (run alongside it)
+cudaError_t kob_launch_lo(int tile, const StepArgs &a, int grid, cudaStream_t s, bool after64);
+cudaError_t sint_launch_lo(int tile, bool mu64, const StepArgs &a, int grid, cudaStream_t s, bool after64);
 cudaError_t kob_prepare_lo(int tile);
 cudaError_t sint_prepare_lo(int tile, bool mu64);
 // Raise the dynamic shared-memory limit of the kernel a launch would use

@@ -400,8 +400,8 @@ __global__ void __launch_bounds__(kThreads, 4) gg_step_kernel(StepArgs a)
     // scheduled into the slots this grid's last wave leaves free; every CTA
     // waits for the previous grid to complete, its writes visible, before
     // its first global read (both are no-ops for a plain launch)
-    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-    asm volatile("griddepcontrol.wait;" ::: "memory");
+    pdl_trigger();
+    pdl_wait();
     const int tile = a.order ? a.order[blockIdx.x] : (int)blockIdx.x;
     gg_tile_step<T, REF, MON>(a, sm, ntier, red, tile);
 }
@@ -495,22 +495,9 @@ size_t gg_smem_bytes(int tile, int tier, int nf)
     return (size_t)nf * (tile == 32 ? Stage<float, 32, 1>::FIELD : Stage<float, 16, 1>::FIELD) * sizeof(float);
 }
 
-// A step-kernel launch that may begin while the previous kernel on the
-// stream finishes (programmatic stream serialization; the kernel waits for
-// it with griddepcontrol.wait before reading anything it wrote).
 template <typename K> static cudaError_t launch_pdl(K kernel, int grid, size_t smem, cudaStream_t s, const StepArgs &a)
 {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(kThreads);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = s;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    at[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, kernel, a);
+    return launch_kernel(kernel, grid, smem, s, true, a);
 }
 
 cudaError_t gg_launch(int tile, int tier, bool ref, const StepArgs &a, int grid, cudaStream_t s)

@@ -209,6 +209,7 @@ __global__ void __launch_bounds__(kThreads) kob_step_kernel(StepArgs a)
     extern __shared__ __align__(16) unsigned char smraw[];
     __shared__ double red[kThreads / 32];
     __shared__ uint8_t ntier[9];
+    pdl_trigger();  // the step's half/FP32 launch may start alongside (FP64 launch first)
     if ((int)blockIdx.x >= a.count[TIER]) return;
     kob_tile<T, TIER, REF>(a, smraw, red, ntier, a.list[blockIdx.x]);
 }
@@ -216,7 +217,10 @@ __global__ void __launch_bounds__(kThreads) kob_step_kernel(StepArgs a)
 // The half and FP32 tiles of a step in one launch (one CTA per tile; FP64
 // tiles are left to the FP64 launch).  Per-tier launches would each cover
 // only part of the grid -- at 512^2 with 32^2 tiles less than one wave apiece
-// -- and run one after the other.
+// -- and run one after the other.  After the step's FP64 launch it is
+// launched to run alongside it (disjoint tiles and output stores; both read
+// the previous step's state only); its last CTA waits for the FP64 grid
+// before it exits, so this grid completes after both.
 template <int T>
 __global__ void __launch_bounds__(kThreads) kob_step_lo_kernel(StepArgs a)
 {
@@ -227,6 +231,7 @@ __global__ void __launch_bounds__(kThreads) kob_step_lo_kernel(StepArgs a)
     const int tier = a.tier_out[tile];
     if (tier == TIER_FP32) kob_tile<T, TIER_FP32, false>(a, smraw, red, ntier, tile);
     else if (tier == TIER_HALF) kob_tile<T, TIER_HALF, false>(a, smraw, red, ntier, tile);
+    if (blockIdx.x == gridDim.x - 1) pdl_wait();
 }
 
 template <int T, int TIER> static size_t kob_smem()
@@ -264,11 +269,10 @@ cudaError_t kob_launch(int tile, int tier, bool ref, const StepArgs &a, int grid
 #undef AMPS_KOB
 }
 
-cudaError_t kob_launch_lo(int tile, const StepArgs &a, int grid, cudaStream_t s)
+cudaError_t kob_launch_lo(int tile, const StepArgs &a, int grid, cudaStream_t s, bool after64)
 {
-    if (tile == 32) kob_step_lo_kernel<32><<<grid, kThreads, kob_smem<32, TIER_FP32>(), s>>>(a);
-    else kob_step_lo_kernel<16><<<grid, kThreads, kob_smem<16, TIER_FP32>(), s>>>(a);
-    return cudaGetLastError();
+    if (tile == 32) return launch_kernel(kob_step_lo_kernel<32>, grid, kob_smem<32, TIER_FP32>(), s, after64, a);
+    return launch_kernel(kob_step_lo_kernel<16>, grid, kob_smem<16, TIER_FP32>(), s, after64, a);
 }
 
 cudaError_t kob_prepare_lo(int tile)

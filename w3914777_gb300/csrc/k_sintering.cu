@@ -179,6 +179,7 @@ __global__ void __launch_bounds__(kThreads) sint_step_kernel(StepArgs a)
     extern __shared__ __align__(16) unsigned char smraw[];
     __shared__ double red[kThreads / 32];
     __shared__ uint8_t ntier[9];
+    pdl_trigger();  // the step's half/FP32 launch may start alongside (FP64 launch first)
     if ((int)blockIdx.x >= a.count[TIER]) return;
     sint_tile<T, TIER, REF, MU64>(a, smraw, red, ntier, a.list[blockIdx.x]);
 }
@@ -186,7 +187,10 @@ __global__ void __launch_bounds__(kThreads) sint_step_kernel(StepArgs a)
 // The half and FP32 tiles of a step in one launch (one CTA per tile; FP64
 // tiles, whose double staging needs more shared memory, are left to the FP64
 // launch).  Separate half and FP32 launches would each cover only part of
-// the grid and run one after the other.
+// the grid and run one after the other.  After the step's FP64 launch it is
+// launched to run alongside it (disjoint tiles and output stores; both read
+// the previous step's state only); its last CTA waits for the FP64 grid
+// before it exits, so this grid completes after both.
 template <int T, bool MU64>
 __global__ void __launch_bounds__(kThreads) sint_step_lo_kernel(StepArgs a)
 {
@@ -197,6 +201,7 @@ __global__ void __launch_bounds__(kThreads) sint_step_lo_kernel(StepArgs a)
     const int tier = a.tier_out[tile];
     if (tier == TIER_FP32) sint_tile<T, TIER_FP32, false, MU64>(a, smraw, red, ntier, tile);
     else if (tier == TIER_HALF) sint_tile<T, TIER_HALF, false, MU64>(a, smraw, red, ntier, tile);
+    if (blockIdx.x == gridDim.x - 1) pdl_wait();
 }
 
 template <int T, int TIER, bool MU64> static size_t sint_smem(int nf)
@@ -244,18 +249,17 @@ cudaError_t sint_launch(int tile, int tier, bool ref, bool mu64, const StepArgs 
 #undef AMPS_SINT
 }
 
-cudaError_t sint_launch_lo(int tile, bool mu64, const StepArgs &a, int grid, cudaStream_t s)
+cudaError_t sint_launch_lo(int tile, bool mu64, const StepArgs &a, int grid, cudaStream_t s, bool after64)
 {
-#define AMPS_SLO(TT, MM) sint_step_lo_kernel<TT, MM><<<grid, kThreads, sint_smem<TT, TIER_FP32, MM>(a.nf), s>>>(a)
+#define AMPS_SLO(TT, MM) \
+    return launch_kernel(sint_step_lo_kernel<TT, MM>, grid, sint_smem<TT, TIER_FP32, MM>(a.nf), s, after64, a)
     if (tile == 32) {
         if (mu64) AMPS_SLO(32, true);
-        else AMPS_SLO(32, false);
-    } else {
-        if (mu64) AMPS_SLO(16, true);
-        else AMPS_SLO(16, false);
+        AMPS_SLO(32, false);
     }
+    if (mu64) AMPS_SLO(16, true);
+    AMPS_SLO(16, false);
 #undef AMPS_SLO
-    return cudaGetLastError();
 }
 
 cudaError_t sint_prepare_lo(int tile, bool mu64)
