@@ -68,13 +68,40 @@ __device__ __forceinline__ void sint_tile(const StepArgs &a, unsigned char *smra
                 __dmul_rn(__dmul_rn(A2, cc), __dmul_rn(__dsub_rn(1.0, cc), __dsub_rn(1.0, cc))));
             m = __dsub_rn(dfdc, __dmul_rn(0.5 * ph.coefm, lap));
         } else {
-            const MT lap = ((MT)C[-1] + (MT)C[1] + (MT)C[-SC::P] + (MT)C[SC::P] - MT(4) * (MT)cc) * kc<MT>(ph, SN_INV);
-            MT s2 = 0, s3 = 0;
-            for (int k = 0; k < np; ++k) {
-                const MT e = SE::at(sme, k, j + 1, i + SE::O);
-                const MT e2 = e * e;
-                s2 += e2;
-                s3 = fma(e2, e, s3);
+            MT lap, s2 = 0, s3 = 0;
+            bool exact = false;
+            if constexpr (sizeof(MT) == 8 && sizeof(CT) == 4) {
+                // double mu from float inputs.  Where c and every eta are 0 or 1
+                // (the bulk), the sums below are small integers, exact in float:
+                // form them there and keep the FP64 pipe for the other cells.
+                // The results are the double path's to the bit.
+                bool bin = (cc == 0.f || cc == 1.f);
+                float s2f = 0.f, s3f = 0.f;
+                for (int k = 0; k < np; ++k) {
+                    const float e = SE::at(sme, k, j + 1, i + SE::O);
+                    bin &= (e == 0.f || e == 1.f);
+                    const float e2 = e * e;
+                    s2f += e2;
+                    s3f = fmaf(e2, e, s3f);
+                }
+                const float cs = C[-1] + C[1] + C[-SC::P] + C[SC::P];
+                bin &= (C[-1] == 0.f || C[-1] == 1.f) && (C[1] == 0.f || C[1] == 1.f) &&
+                       (C[-SC::P] == 0.f || C[-SC::P] == 1.f) && (C[SC::P] == 0.f || C[SC::P] == 1.f);
+                if (bin) {
+                    exact = true;
+                    s2 = s2f;
+                    s3 = s3f;
+                    lap = ((MT)cs - MT(4) * (MT)cc) * kc<MT>(ph, SN_INV);
+                }
+            }
+            if (!exact) {
+                lap = ((MT)C[-1] + (MT)C[1] + (MT)C[-SC::P] + (MT)C[SC::P] - MT(4) * (MT)cc) * kc<MT>(ph, SN_INV);
+                for (int k = 0; k < np; ++k) {
+                    const MT e = SE::at(sme, k, j + 1, i + SE::O);
+                    const MT e2 = e * e;
+                    s2 += e2;
+                    s3 = fma(e2, e, s3);
+                }
             }
             const MT c1 = MT(1) - (MT)cc;
             const MT A2 = kc<MT>(ph, SN_A2);
