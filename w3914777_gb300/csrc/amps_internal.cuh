@@ -143,6 +143,10 @@ inline cudaError_t launch_kernel(K kernel, int grid, size_t smem, cudaStream_t s
     return cudaLaunchKernelEx(&cfg, kernel, args...);
 }
 
+// x is +0 (bit pattern 0): an integer test, no floating-point instruction
+__device__ __forceinline__ bool pos_zero(double x) { return __double_as_longlong(x) == 0; }
+__device__ __forceinline__ bool pos_zero(float x) { return __float_as_uint(x) == 0u; }
+
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 

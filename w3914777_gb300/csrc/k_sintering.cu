@@ -97,7 +97,11 @@ __device__ __forceinline__ void sint_tile(const StepArgs &a, unsigned char *smra
             if (!exact) {
                 lap = ((MT)C[-1] + (MT)C[1] + (MT)C[-SC::P] + (MT)C[SC::P] - MT(4) * (MT)cc) * kc<MT>(ph, SN_INV);
                 for (int k = 0; k < np; ++k) {
-                    const MT e = SE::at(sme, k, j + 1, i + SE::O);
+                    // FP64 tiles: a +0 order parameter adds +0 to either sum, which never
+                    // holds -0 (float tiles: the test costs more than the arithmetic)
+                    const CT ek = SE::at(sme, k, j + 1, i + SE::O);
+                    if (sizeof(CT) == 8 && pos_zero(ek)) continue;
+                    const MT e = ek;
                     const MT e2 = e * e;
                     s2 += e2;
                     s3 = fma(e2, e, s3);
@@ -156,6 +160,7 @@ __device__ __forceinline__ void sint_tile(const StepArgs &a, unsigned char *smra
             CT se = 0;
             for (int k = 0; k < np; ++k) {
                 const CT e = SE::at(sme, k, j + 1, i + SE::O);
+                if (sizeof(CT) == 8 && pos_zero(e)) continue;  // adds +0 to sums that never hold -0
                 se += e;
                 s2f = fma(e, e, s2f);
             }
@@ -184,6 +189,12 @@ __device__ __forceinline__ void sint_tile(const StepArgs &a, unsigned char *smra
                 if (v >= 1) v = 1;
                 else if (v < 0) v = 0;
                 en = v;
+            } else if (sizeof(CT) == 8 && pos_zero(e) && pos_zero(Ep[-1]) && pos_zero(Ep[1]) && pos_zero(Ep[-SE::P]) &&
+                       pos_zero(Ep[SE::P])) {
+                // a particle absent from the whole stencil stays absent: below, lap
+                // is +0, dfd and the inner term signed zeros, and v = -DTL*(+-0) + (+0)
+                // = +0 -- the same bits, without the arithmetic
+                en = CT(0);
             } else {
                 const CT lap = (Ep[-1] + Ep[1] + Ep[-SE::P] + Ep[SE::P] - CT(4) * e) * kc<CT>(ph, SN_INV);
                 const CT dfd = kc<CT>(ph, SN_B12) * e * (s2f + (CT(1) - cn) - e * (CT(2) - cn));
