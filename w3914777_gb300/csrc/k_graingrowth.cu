@@ -213,12 +213,12 @@ __device__ __forceinline__ void gg_tile_lo_2row(const StepArgs &a, const float *
 
 // Half/FP32 tile, 32^2 tiles, non-monitor steps: the sum of squares over
 // fields is formed once per cell into shared memory (ss, 32x32 floats, after
-// the staged fields), then each thread advances 4 rows x 4 cells of a field
-// from 6 staged rows (1.5 row reads per output row against 2 in
-// gg_tile_lo_2row), the CTA's quarters on fields q, q+4, ...  Per cell the
-// arithmetic, and its order, is gg_tile_lo_2row's.
-template <int TIER>
-__device__ __forceinline__ void gg_tile_lo_4row(const StepArgs &a, const float *sm, float *ss, int tx, int ty)
+// the staged fields), then each thread advances RPT rows x 4 cells of a field
+// from RPT + 2 staged rows (RPT = 4: 1.5 row reads per output row, 8: 1.25,
+// against 2 in gg_tile_lo_2row), the CTA's RPT groups on fields g, g+RPT, ...
+// Per cell the arithmetic, and its order, is gg_tile_lo_2row's.
+template <int TIER, int RPT>
+__device__ __forceinline__ void gg_tile_lo_rows(const StepArgs &a, const float *sm, float *ss, int tx, int ty)
 {
     constexpr int T = 32, CPT = 4, GPR = T / CPT;
     using S = Stage<float, T, 1>;
@@ -237,12 +237,13 @@ __device__ __forceinline__ void gg_tile_lo_4row(const StepArgs &a, const float *
         *reinterpret_cast<float4 *>(ss + row * T + c) = acc;
     }
     __syncthreads();
-    const int quarter = threadIdx.x / (kThreads / 4), t = threadIdx.x % (kThreads / 4);
-    const int r0 = 4 * (t / GPR), c0 = (t % GPR) * CPT;  // tile-local rows r0 .. r0+3
+    static_assert(T % RPT == 0 && (T / RPT) * GPR * RPT == kThreads, "RPT groups of T/RPT x GPR threads");
+    const int group = threadIdx.x / (kThreads / RPT), t = threadIdx.x % (kThreads / RPT);
+    const int r0 = RPT * (t / GPR), c0 = (t % GPR) * CPT;  // tile-local rows r0 .. r0+RPT-1
     const Phys &ph = a.ph;
     const float dtm = ph.gg_dtm, g2 = ph.gg_g2, kap = ph.gg_kap, inv = ph.gg_inv;
     const int64_t gbase = (int64_t)(ty * T + r0) * a.nx + tx * T + c0;
-    for (int f = quarter; f < nf; f += 4) {
+    for (int f = group; f < nf; f += RPT) {
         float w[3][CPT + 2];
         auto load_row = [&](int sr, float *d) {
             const float *p = &S::at(smm, f, sr, S::O + c0);
@@ -254,7 +255,7 @@ __device__ __forceinline__ void gg_tile_lo_4row(const StepArgs &a, const float *
         load_row(r0, w[0]);
         load_row(r0 + 1, w[1]);
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
+        for (int i = 0; i < RPT; ++i) {
             float *up = w[i % 3], *md = w[(i + 1) % 3], *dn = w[(i + 2) % 3];
             load_row(r0 + i + 2, dn);
             const float4 sq = *reinterpret_cast<const float4 *>(ss + (r0 + i) * T + c0);
@@ -426,8 +427,14 @@ __device__ __forceinline__ void gg_tile_step(const StepArgs &a, float *sm, uint8
         // the spatial range needs one reduction per field: gg_tile_lo_impl
         if (!MON) {
             float *ss = sm + a.nf * Stage<float, T, 1>::FIELD;  // gg_smem_bytes reserves it
-            if (tier == TIER_FP32) gg_tile_lo_4row<TIER_FP32>(a, sm, ss, tx, ty);
-            else gg_tile_lo_4row<TIER_HALF>(a, sm, ss, tx, ty);
+            // 8 rows a thread when the fields come in eights (one warp a field)
+            if (a.nf % 8 == 0) {
+                if (tier == TIER_FP32) gg_tile_lo_rows<TIER_FP32, 8>(a, sm, ss, tx, ty);
+                else gg_tile_lo_rows<TIER_HALF, 8>(a, sm, ss, tx, ty);
+            } else {
+                if (tier == TIER_FP32) gg_tile_lo_rows<TIER_FP32, 4>(a, sm, ss, tx, ty);
+                else gg_tile_lo_rows<TIER_HALF, 4>(a, sm, ss, tx, ty);
+            }
             return;
         }
         if (a.monitor_kind == 3) {
