@@ -126,99 +126,19 @@ __device__ __forceinline__ void gg_tile_lo(const StepArgs &a, const float *sm, i
     else gg_tile_lo_impl<T, TIER, false>(a, sm, tile, tx, ty, red);
 }
 
-// Half/FP32 tile, 32^2 tiles, from the staged float neighbourhood: each
-// thread advances 2 rows x 4 cells, reading 4 staged rows (instead of 3 per
-// output row), and the CTA's two halves take alternate fields.  Per cell the
-// arithmetic is gg_tile_lo_impl's.  MK, the monitor kind of a monitor step
-// (0: no monitor, 2: temporal, 3: rate; the spatial range takes
-// gg_tile_lo_impl): the tile metric is a maximum over fields and cells, so
-// each thread folds every field it computes into one accumulator and the
-// block reduces once at the end -- the same metric as one reduction per field.
-template <int TIER, int MK>
-__device__ __forceinline__ void gg_tile_lo_2row(const StepArgs &a, const float *sm, int tile, int tx, int ty,
-                                                double *red)
-{
-    constexpr int T = 32, CPT = 4, GPR = T / CPT;
-    using S = Stage<float, T, 1>;
-    float *smm = const_cast<float *>(sm);
-    const int half = threadIdx.x / (kThreads / 2), t = threadIdx.x % (kThreads / 2);
-    const int r0 = 2 * (t / GPR), c0 = (t % GPR) * CPT;  // tile-local rows r0, r0 + 1
-    const int nf = a.nf;
-    const Phys &ph = a.ph;
-    float ssum[2][CPT];
-#pragma unroll
-    for (int r = 0; r < 2; ++r)
-#pragma unroll
-        for (int k = 0; k < CPT; ++k) ssum[r][k] = 0.f;
-    for (int f = 0; f < nf; ++f)
-#pragma unroll
-        for (int r = 0; r < 2; ++r) {
-            const float4 q = *reinterpret_cast<const float4 *>(&S::at(smm, f, r0 + 1 + r, S::O + c0));
-            ssum[r][0] = fmaf(q.x, q.x, ssum[r][0]);
-            ssum[r][1] = fmaf(q.y, q.y, ssum[r][1]);
-            ssum[r][2] = fmaf(q.z, q.z, ssum[r][2]);
-            ssum[r][3] = fmaf(q.w, q.w, ssum[r][3]);
-        }
-    const float dtm = ph.gg_dtm, g2 = ph.gg_g2, kap = ph.gg_kap, inv = ph.gg_inv;
-    const int64_t gbase = (int64_t)(ty * T + r0) * a.nx + tx * T + c0;
-    MonAccF mon;
-    if (MK) mon_reset(a, mon);
-    for (int f = half; f < nf; f += 2) {
-        const bool mon_f = MK && (a.mfield < 0 || a.mfield == f);
-        const int mslot = a.mfield < 0 ? f : 0;
-        float w[4][CPT + 2];
-#pragma unroll
-        for (int rr = 0; rr < 4; ++rr) {
-            const float *p = &S::at(smm, f, r0 + rr, S::O + c0);
-            const float4 q = *reinterpret_cast<const float4 *>(p);
-            w[rr][1] = q.x; w[rr][2] = q.y; w[rr][3] = q.z; w[rr][4] = q.w;
-            w[rr][0] = p[-1];
-            w[rr][CPT + 1] = p[CPT];
-        }
-#pragma unroll
-        for (int r = 0; r < 2; ++r) {
-            float out[CPT];
-#pragma unroll
-            for (int k = 0; k < CPT; ++k) {
-                const float e = w[r + 1][k + 1];
-                float s;
-                if (a.stencil == 0)
-                    s = (w[r][k] + w[r][k + 1] + w[r][k + 2]) + (w[r + 1][k] + w[r + 1][k + 2]) +
-                        (w[r + 2][k] + w[r + 2][k + 1] + w[r + 2][k + 2]) - 8.f * e;
-                else
-                    s = (w[r + 1][k] + w[r + 1][k + 2]) + (w[r][k + 1] + w[r + 2][k + 1]) - 4.f * e;
-                const float lap = s * inv;
-                const float e2 = e * e;
-                const float dfd = e * fmaf(g2, ssum[r][k] - e2, e2 - 1.f);
-                out[k] = fmaf(-dtm, fmaf(-kap, lap, dfd), e);
-            }
-            const int64_t g = (int64_t)f * a.n + gbase + (int64_t)r * a.nx;
-            store_cells<TIER, CPT>(a, g, out);
-            if constexpr (MK != 0) {
-                if (mon_f) {
-                    const int64_t gi = gbase + (int64_t)r * a.nx;
-#pragma unroll
-                    for (int k = 0; k < CPT; ++k)
-                        mon_add_k<T, MK>(a, mon, mslot, tile, r0 + r, c0 + k, gi + k, round_to_tier<TIER>(out[k]),
-                                         w[r + 1][k + 1]);
-                }
-            }
-        }
-    }
-    if constexpr (MK != 0) {
-        const double metric = mon_finish_k<MK>(a, mon, red);
-        if (threadIdx.x == 0) a.metric[tile] = metric;
-    }
-}
-
-// Half/FP32 tile, 32^2 tiles, non-monitor steps: the sum of squares over
-// fields is formed once per cell into shared memory (ss, 32x32 floats, after
-// the staged fields), then each thread advances RPT rows x 4 cells of a field
-// from RPT + 2 staged rows (RPT = 4: 1.5 row reads per output row, 8: 1.25,
-// against 2 in gg_tile_lo_2row), the CTA's RPT groups on fields g, g+RPT, ...
-// Per cell the arithmetic, and its order, is gg_tile_lo_2row's.
-template <int TIER, int RPT>
-__device__ __forceinline__ void gg_tile_lo_rows(const StepArgs &a, const float *sm, float *ss, int tx, int ty)
+// Half/FP32 tile, 32^2 tiles: the sum of squares over fields is formed once
+// per cell into shared memory (ss, 32x32 floats, after the staged fields),
+// then each thread advances RPT rows x 4 cells of a field from RPT + 2 staged
+// rows with a 3-row register window (RPT = 4: 1.5 row reads per output row,
+// 8: 1.25, against 2 for two rows a thread), the CTA's RPT groups on fields
+// g, g+RPT, ...  Per cell the arithmetic, and its order, is
+// gg_tile_lo_impl's.  MK, the monitor kind of a monitor step (0: none, 2:
+// temporal, 3: rate; the spatial range takes gg_tile_lo_impl): the tile
+// metric is a maximum over fields and cells, so each thread folds every
+// field it computes into one accumulator and the block reduces once.
+template <int TIER, int RPT, int MK = 0>
+__device__ __forceinline__ void gg_tile_lo_rows(const StepArgs &a, const float *sm, float *ss, int tile, int tx,
+                                                int ty, double *red)
 {
     constexpr int T = 32, CPT = 4, GPR = T / CPT;
     using S = Stage<float, T, 1>;
@@ -243,7 +163,11 @@ __device__ __forceinline__ void gg_tile_lo_rows(const StepArgs &a, const float *
     const Phys &ph = a.ph;
     const float dtm = ph.gg_dtm, g2 = ph.gg_g2, kap = ph.gg_kap, inv = ph.gg_inv;
     const int64_t gbase = (int64_t)(ty * T + r0) * a.nx + tx * T + c0;
+    MonAccF mon;
+    if (MK) mon_reset(a, mon);
     for (int f = group; f < nf; f += RPT) {
+        const bool mon_f = MK && (a.mfield < 0 || a.mfield == f);
+        const int mslot = a.mfield < 0 ? f : 0;
         float w[3][CPT + 2];
         auto load_row = [&](int sr, float *d) {
             const float *p = &S::at(smm, f, sr, S::O + c0);
@@ -275,8 +199,21 @@ __device__ __forceinline__ void gg_tile_lo_rows(const StepArgs &a, const float *
                 const float dfd = e * fmaf(g2, ssum[k] - e2, e2 - 1.f);
                 out[k] = fmaf(-dtm, fmaf(-kap, lap, dfd), e);
             }
-            store_cells<TIER, CPT>(a, (int64_t)f * a.n + gbase + (int64_t)i * a.nx, out);
+            const int64_t gi = gbase + (int64_t)i * a.nx;
+            store_cells<TIER, CPT>(a, (int64_t)f * a.n + gi, out);
+            if constexpr (MK != 0) {
+                if (mon_f) {
+#pragma unroll
+                    for (int k = 0; k < CPT; ++k)
+                        mon_add_k<T, MK>(a, mon, mslot, tile, r0 + i, c0 + k, gi + k, round_to_tier<TIER>(out[k]),
+                                         md[k + 1]);
+                }
+            }
         }
+    }
+    if constexpr (MK != 0) {
+        const double metric = mon_finish_k<MK>(a, mon, red);
+        if (threadIdx.x == 0) a.metric[tile] = metric;
     }
 }
 
@@ -425,26 +362,26 @@ __device__ __forceinline__ void gg_tile_step(const StepArgs &a, float *sm, uint8
     __syncthreads();
     if constexpr (T == 32) {
         // the spatial range needs one reduction per field: gg_tile_lo_impl
+        float *ss = sm + a.nf * Stage<float, T, 1>::FIELD;  // gg_smem_bytes reserves it
         if (!MON) {
-            float *ss = sm + a.nf * Stage<float, T, 1>::FIELD;  // gg_smem_bytes reserves it
             // 8 rows a thread when the fields come in eights (one warp a field)
             if (a.nf % 8 == 0) {
-                if (tier == TIER_FP32) gg_tile_lo_rows<TIER_FP32, 8>(a, sm, ss, tx, ty);
-                else gg_tile_lo_rows<TIER_HALF, 8>(a, sm, ss, tx, ty);
+                if (tier == TIER_FP32) gg_tile_lo_rows<TIER_FP32, 8>(a, sm, ss, tile, tx, ty, red);
+                else gg_tile_lo_rows<TIER_HALF, 8>(a, sm, ss, tile, tx, ty, red);
             } else {
-                if (tier == TIER_FP32) gg_tile_lo_rows<TIER_FP32, 4>(a, sm, ss, tx, ty);
-                else gg_tile_lo_rows<TIER_HALF, 4>(a, sm, ss, tx, ty);
+                if (tier == TIER_FP32) gg_tile_lo_rows<TIER_FP32, 4>(a, sm, ss, tile, tx, ty, red);
+                else gg_tile_lo_rows<TIER_HALF, 4>(a, sm, ss, tile, tx, ty, red);
             }
             return;
         }
         if (a.monitor_kind == 3) {
-            if (tier == TIER_FP32) gg_tile_lo_2row<TIER_FP32, 3>(a, sm, tile, tx, ty, red);
-            else gg_tile_lo_2row<TIER_HALF, 3>(a, sm, tile, tx, ty, red);
+            if (tier == TIER_FP32) gg_tile_lo_rows<TIER_FP32, 4, 3>(a, sm, ss, tile, tx, ty, red);
+            else gg_tile_lo_rows<TIER_HALF, 4, 3>(a, sm, ss, tile, tx, ty, red);
             return;
         }
         if (a.monitor_kind == 2) {
-            if (tier == TIER_FP32) gg_tile_lo_2row<TIER_FP32, 2>(a, sm, tile, tx, ty, red);
-            else gg_tile_lo_2row<TIER_HALF, 2>(a, sm, tile, tx, ty, red);
+            if (tier == TIER_FP32) gg_tile_lo_rows<TIER_FP32, 4, 2>(a, sm, ss, tile, tx, ty, red);
+            else gg_tile_lo_rows<TIER_HALF, 4, 2>(a, sm, ss, tile, tx, ty, red);
             return;
         }
     }
