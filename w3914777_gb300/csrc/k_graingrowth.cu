@@ -344,8 +344,10 @@ __device__ __forceinline__ void gg_tile_step(const StepArgs &a, float *sm, uint8
     const int tier = a.tier_out[tile];
     __syncthreads();
     if (tier == TIER_FP64) {
-        if (spec) cp_async_wait_all();
+        // the FP64 path reads through L1, not the staging area: the discarded
+        // copies land while it computes, before the CTA exits
         gg_tile_fp64<T, REF>(a, ntier, tile, tx, ty, red);
+        if (spec) cp_async_wait_all();
         return;
     }
     const bool all32 = all_fp32(ntier);
