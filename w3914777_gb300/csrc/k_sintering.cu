@@ -17,6 +17,102 @@
 
 namespace amps {
 
+// ---- per-cell arithmetic (non-reference order), shared by the whole-tile
+// and the row-band paths.  C points at a cell's c with row stride cs; E at the
+// cell's eta_0, field stride es, row stride rs.
+
+// Chemical potential mu at one cell (sintering/function.h:67-71), in MT.
+template <typename CT, typename MT>
+__device__ __forceinline__ MT sint_mu(const CT *C, int cs, const CT *E, int es, int np, const Phys &ph)
+{
+    const CT cc = C[0];
+    MT lap, s2 = 0, s3 = 0;
+    bool exact = false;
+    if constexpr (sizeof(MT) == 8 && sizeof(CT) == 4) {
+        // double mu from float inputs.  Where c and every eta are 0 or 1
+        // (the bulk), the sums below are small integers, exact in float:
+        // form them there and keep the FP64 pipe for the other cells.
+        // The results are the double path's to the bit.
+        bool bin = (cc == 0.f || cc == 1.f);
+        float s2f = 0.f, s3f = 0.f;
+        for (int k = 0; k < np; ++k) {
+            const float e = E[k * es];
+            bin &= (e == 0.f || e == 1.f);
+            const float e2 = e * e;
+            s2f += e2;
+            s3f = fmaf(e2, e, s3f);
+        }
+        const float csum = C[-1] + C[1] + C[-cs] + C[cs];
+        bin &= (C[-1] == 0.f || C[-1] == 1.f) && (C[1] == 0.f || C[1] == 1.f) && (C[-cs] == 0.f || C[-cs] == 1.f) &&
+               (C[cs] == 0.f || C[cs] == 1.f);
+        if (bin) {
+            exact = true;
+            s2 = s2f;
+            s3 = s3f;
+            lap = ((MT)csum - MT(4) * (MT)cc) * kc<MT>(ph, SN_INV);
+        }
+    }
+    if (!exact) {
+        lap = ((MT)C[-1] + (MT)C[1] + (MT)C[-cs] + (MT)C[cs] - MT(4) * (MT)cc) * kc<MT>(ph, SN_INV);
+        for (int k = 0; k < np; ++k) {
+            // FP64 inputs: a +0 order parameter adds +0 to either sum, which
+            // never holds -0 (float inputs: the test costs more than the arithmetic)
+            const CT ek = E[k * es];
+            if (sizeof(CT) == 8 && pos_zero(ek)) continue;
+            const MT e = ek;
+            const MT e2 = e * e;
+            s2 += e2;
+            s3 = fma(e2, e, s3);
+        }
+    }
+    const MT c1 = MT(1) - (MT)cc;
+    const MT A2 = kc<MT>(ph, SN_A2);
+    const MT dfdc = kc<MT>(ph, SN_B) * (MT(2) * (MT)cc + MT(4) * s3 - MT(6) * s2) + A2 * (MT)cc * c1 * (c1 - (MT)cc);
+    return dfdc - kc<MT>(ph, SN_HCM) * lap;
+}
+
+// c' at one cell (sintering/function.h:90-100) from the mu region M (row
+// stride ms, M at the cell) and the old etas; s2f: sum of eta^2 at the cell.
+template <typename CT, typename MT>
+__device__ __forceinline__ CT sint_c_new(CT cc, const MT *M, int ms, const CT *E, int es, int np, const Phys &ph,
+                                         CT &s2f)
+{
+    const MT lapm = (M[-1] + M[1] + M[-ms] + M[ms] - MT(4) * M[0]) * kc<MT>(ph, SN_INV);
+    const CT phi = cc * cc * cc * fma(CT(6) * cc, cc, CT(10) - CT(15) * cc);
+    CT se = 0;
+    s2f = 0;
+    for (int k = 0; k < np; ++k) {
+        const CT e = E[k * es];
+        if (sizeof(CT) == 8 && pos_zero(e)) continue;  // adds +0 to sums that never hold -0
+        se += e;
+        s2f = fma(e, e, s2f);
+    }
+    const CT sum = se * se - s2f;  // sum_{i != j} eta_i eta_j
+    const CT mob = kc<CT>(ph, SN_DVOL) * phi + kc<CT>(ph, SN_DVAP) * (CT(1) - phi) +
+                   kc<CT>(ph, SN_DSUR) * cc * (CT(1) - cc) + kc<CT>(ph, SN_DGRB) * sum;
+    const CT v = (CT)((MT)cc + (MT)(kc<CT>(ph, SN_DT) * mob) * lapm);
+    return v >= CT(1) ? CT(1) : (v < CT(0) ? CT(0) : v);
+}
+
+// eta' of one particle at one cell (sintering/function.h:126-131); Ep at the
+// cell's eta, row stride rs.
+template <typename CT>
+__device__ __forceinline__ CT sint_eta_new(const CT *Ep, int rs, CT cn, CT s2f, const Phys &ph)
+{
+    const CT e = Ep[0];
+    if (sizeof(CT) == 8 && pos_zero(e) && pos_zero(Ep[-1]) && pos_zero(Ep[1]) && pos_zero(Ep[-rs]) &&
+        pos_zero(Ep[rs])) {
+        // a particle absent from the whole stencil stays absent: below, lap
+        // is +0, dfd and the inner term signed zeros, and v = -DTL*(+-0) + (+0)
+        // = +0 -- the same bits, without the arithmetic
+        return CT(0);
+    }
+    const CT lap = (Ep[-1] + Ep[1] + Ep[-rs] + Ep[rs] - CT(4) * e) * kc<CT>(ph, SN_INV);
+    const CT dfd = kc<CT>(ph, SN_B12) * e * (s2f + (CT(1) - cn) - e * (CT(2) - cn));
+    const CT v = fma(-kc<CT>(ph, SN_DTL), fma(-kc<CT>(ph, SN_HCK), lap, dfd), e);
+    return v >= CT(1) ? CT(1) : (v < CT(0) ? CT(0) : v);
+}
+
 // One tile of one step at tier TIER (smraw: the kernel's dynamic shared
 // memory, sint_smem<T, TIER, MU64> bytes; red / ntier: its static scratch).
 template <int T, int TIER, bool REF, bool MU64>
@@ -68,49 +164,7 @@ __device__ __forceinline__ void sint_tile(const StepArgs &a, unsigned char *smra
                 __dmul_rn(__dmul_rn(A2, cc), __dmul_rn(__dsub_rn(1.0, cc), __dsub_rn(1.0, cc))));
             m = __dsub_rn(dfdc, __dmul_rn(0.5 * ph.coefm, lap));
         } else {
-            MT lap, s2 = 0, s3 = 0;
-            bool exact = false;
-            if constexpr (sizeof(MT) == 8 && sizeof(CT) == 4) {
-                // double mu from float inputs.  Where c and every eta are 0 or 1
-                // (the bulk), the sums below are small integers, exact in float:
-                // form them there and keep the FP64 pipe for the other cells.
-                // The results are the double path's to the bit.
-                bool bin = (cc == 0.f || cc == 1.f);
-                float s2f = 0.f, s3f = 0.f;
-                for (int k = 0; k < np; ++k) {
-                    const float e = SE::at(sme, k, j + 1, i + SE::O);
-                    bin &= (e == 0.f || e == 1.f);
-                    const float e2 = e * e;
-                    s2f += e2;
-                    s3f = fmaf(e2, e, s3f);
-                }
-                const float cs = C[-1] + C[1] + C[-SC::P] + C[SC::P];
-                bin &= (C[-1] == 0.f || C[-1] == 1.f) && (C[1] == 0.f || C[1] == 1.f) &&
-                       (C[-SC::P] == 0.f || C[-SC::P] == 1.f) && (C[SC::P] == 0.f || C[SC::P] == 1.f);
-                if (bin) {
-                    exact = true;
-                    s2 = s2f;
-                    s3 = s3f;
-                    lap = ((MT)cs - MT(4) * (MT)cc) * kc<MT>(ph, SN_INV);
-                }
-            }
-            if (!exact) {
-                lap = ((MT)C[-1] + (MT)C[1] + (MT)C[-SC::P] + (MT)C[SC::P] - MT(4) * (MT)cc) * kc<MT>(ph, SN_INV);
-                for (int k = 0; k < np; ++k) {
-                    // FP64 tiles: a +0 order parameter adds +0 to either sum, which never
-                    // holds -0 (float tiles: the test costs more than the arithmetic)
-                    const CT ek = SE::at(sme, k, j + 1, i + SE::O);
-                    if (sizeof(CT) == 8 && pos_zero(ek)) continue;
-                    const MT e = ek;
-                    const MT e2 = e * e;
-                    s2 += e2;
-                    s3 = fma(e2, e, s3);
-                }
-            }
-            const MT c1 = MT(1) - (MT)cc;
-            const MT A2 = kc<MT>(ph, SN_A2);
-            const MT dfdc = kc<MT>(ph, SN_B) * (MT(2) * (MT)cc + MT(4) * s3 - MT(6) * s2) + A2 * (MT)cc * c1 * (c1 - (MT)cc);
-            m = dfdc - kc<MT>(ph, SN_HCM) * lap;
+            m = sint_mu<CT, MT>(C, SC::P, &SE::at(sme, 0, j + 1, i + SE::O), SE::FIELD, np, ph);
         }
         mu[u] = m;
     }
@@ -155,20 +209,7 @@ __device__ __forceinline__ void sint_tile(const StepArgs &a, unsigned char *smra
                 s2ref = __dadd_rn(s2ref, __dmul_rn(e, e));
             }
         } else {
-            const MT lapm = (mu[o - 1] + mu[o + 1] + mu[o - E] + mu[o + E] - MT(4) * mu[o]) * kc<MT>(ph, SN_INV);
-            const CT phi = cc * cc * cc * fma(CT(6) * cc, cc, CT(10) - CT(15) * cc);
-            CT se = 0;
-            for (int k = 0; k < np; ++k) {
-                const CT e = SE::at(sme, k, j + 1, i + SE::O);
-                if (sizeof(CT) == 8 && pos_zero(e)) continue;  // adds +0 to sums that never hold -0
-                se += e;
-                s2f = fma(e, e, s2f);
-            }
-            const CT sum = se * se - s2f;  // sum_{i != j} eta_i eta_j
-            const CT mob = kc<CT>(ph, SN_DVOL) * phi + kc<CT>(ph, SN_DVAP) * (CT(1) - phi) + kc<CT>(ph, SN_DSUR) * cc * (CT(1) - cc)
-                         + kc<CT>(ph, SN_DGRB) * sum;
-            CT v = (CT)((MT)cc + (MT)(kc<CT>(ph, SN_DT) * mob) * lapm);
-            cn = v >= CT(1) ? CT(1) : (v < CT(0) ? CT(0) : v);
+            cn = sint_c_new<CT, MT>(cc, mu + o, E, &SE::at(sme, 0, j + 1, i + SE::O), SE::FIELD, np, ph, s2f);
         }
         store_tier<TIER>(a, g, cn);
         if (mon_on && a.mfield <= 0)
@@ -189,17 +230,8 @@ __device__ __forceinline__ void sint_tile(const StepArgs &a, unsigned char *smra
                 if (v >= 1) v = 1;
                 else if (v < 0) v = 0;
                 en = v;
-            } else if (sizeof(CT) == 8 && pos_zero(e) && pos_zero(Ep[-1]) && pos_zero(Ep[1]) && pos_zero(Ep[-SE::P]) &&
-                       pos_zero(Ep[SE::P])) {
-                // a particle absent from the whole stencil stays absent: below, lap
-                // is +0, dfd and the inner term signed zeros, and v = -DTL*(+-0) + (+0)
-                // = +0 -- the same bits, without the arithmetic
-                en = CT(0);
             } else {
-                const CT lap = (Ep[-1] + Ep[1] + Ep[-SE::P] + Ep[SE::P] - CT(4) * e) * kc<CT>(ph, SN_INV);
-                const CT dfd = kc<CT>(ph, SN_B12) * e * (s2f + (CT(1) - cn) - e * (CT(2) - cn));
-                CT v = fma(-kc<CT>(ph, SN_DTL), fma(-kc<CT>(ph, SN_HCK), lap, dfd), e);
-                en = v >= CT(1) ? CT(1) : (v < CT(0) ? CT(0) : v);
+                en = sint_eta_new<CT>(Ep, SE::P, cn, s2f, ph);
             }
             store_tier<TIER>(a, (int64_t)(k + 1) * a.n + g, en);
         }
