@@ -136,15 +136,19 @@ def test_graingrowth_fp64_vs_oracle_q_general(q, stencil, bc):
     assert e <= 1e-12
 
 
-def test_sintering_fp64_vs_oracle_n_particles():
+@pytest.mark.parametrize("ref_order,bc", [(1, 0), (0, 0), (0, 1)])
+def test_sintering_fp64_vs_oracle_n_particles(ref_order, bc):
+    """ref_order=0: the FMA-form FP64 tiles, computed in 8-row bands on
+    non-monitor steps (zero flux: mirrored rings at the band edges)."""
     w = amps()
     nx = ny = 128
-    p = w.Params.preset("sintering", 0, mode="purehigh", nx=nx, ny=ny, nfields=4, rmin=10, rmax=16, ref_order=1)
+    p = w.Params.preset("sintering", 0, mode="purehigh", nx=nx, ny=ny, nfields=4, rmin=10, rmax=16,
+                        ref_order=ref_order, bc=bc)
     f0 = w.init_host(p, w.INIT_SEEDED)
     with w.Simulation(p, init=w.INIT_SEEDED) as s:
         s.run(20)
         f = s.fields()
-    op = ob.sint_params(nx, ny, n=4, coefm=p.coefm, coefk=p.coefk, coefl=p.coefl, dsur=p.dsur)
+    op = ob.sint_params(nx, ny, n=4, coefm=p.coefm, coefk=p.coefk, coefl=p.coefl, dsur=p.dsur, bc=bc)
     c, e = ob.sint_run(op, f0[0], list(f0[1:]), 20)
     errs = [rel_err(f[0], c)] + [rel_err(f[k + 1], e[k]) for k in range(4)]
     print("sintering N=4:", errs)

@@ -242,6 +242,90 @@ __device__ __forceinline__ void sint_tile(const StepArgs &a, unsigned char *smra
     }
 }
 
+// ---- FP64 tiles in row bands ----------------------------------------------
+// An FP64 tile of a non-monitor step (non-reference order) is split into
+// T / kBandRows row bands, one CTA each: 4x the parallelism on the
+// latency-bound FP64 arithmetic, and ~50 KB of shared memory instead of the
+// whole tile's ~176 KB, so half/FP32 CTAs share the SM.  A band stages its
+// rows of c (2-cell halo) and of every eta (1-cell halo) in double, forms mu on
+// its rows + a 1-cell ring, then c' and every eta' -- the whole-tile path's
+// per-cell arithmetic (sint_mu, sint_c_new, sint_eta_new), so the same bits.
+constexpr int kBandRows = 8;
+
+template <int T> struct SintBand {
+    static constexpr int BR = kBandRows, NB = T / BR;
+    static constexpr int W1 = T + 2, H1 = BR + 2, FE = W1 * H1;  // etas
+    static constexpr int W2 = T + 4, H2 = BR + 4;                // c
+    static constexpr int WM = T + 2, HM = BR + 2;                // mu
+    static size_t smem(int np) { return sizeof(double) * ((size_t)np * FE + W2 * H2 + WM * HM); }
+};
+
+// Rows [ly0, ly0 + H) x columns [-R, T + R) (tile-local) of fields
+// [f0, f0 + nfs), each cell read at its owner tile's input tier and
+// converted to double, into dst[f][H][T + 2R].
+template <int T, int R>
+__device__ __forceinline__ void stage_band(const StepArgs &a, double *dst, const uint8_t *nt, int tx, int ty,
+                                           int ly0, int H, int f0, int nfs)
+{
+    constexpr int W = T + 2 * R;
+    const int x0 = tx * T, y0 = ty * T;
+    for (int u = threadIdx.x; u < H * W; u += kThreads) {
+        const int ly = ly0 + u / W, lx = u % W - R;
+        const int tier = nt[(ly < 0 ? 0 : (ly < T ? 3 : 6)) + (lx < 0 ? 0 : (lx < T ? 1 : 2))];
+        const int64_t off = (int64_t)bc_map(y0 + ly, a.ny, a.bc) * a.nx + bc_map(x0 + lx, a.nx, a.bc);
+#pragma unroll 4
+        for (int f = 0; f < nfs; ++f) dst[f * H * W + u] = load_tier<double>(a, tier, (int64_t)(f0 + f) * a.n + off);
+    }
+}
+
+template <int T>
+__global__ void __launch_bounds__(kThreads) sint_step_f64_band_kernel(StepArgs a)
+{
+    using B = SintBand<T>;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ uint8_t ntier[9];
+    pdl_trigger();  // the step's half/FP32 launch may start alongside (FP64 launch first)
+    const int item = blockIdx.x / B::NB, band = blockIdx.x % B::NB;
+    if (item >= a.count[TIER_FP64]) return;
+    const int tile = a.list[item];
+    const int np = a.nf - 1;
+    double *sme = reinterpret_cast<double *>(smraw);  // [np][H1][W1]
+    double *smc = sme + np * B::FE;                   // [H2][W2]
+    double *mu = smc + B::W2 * B::H2;                 // [HM][WM]
+    const int tx = tile % a.ntx, ty = tile / a.ntx;
+    const int x0 = tx * T, y0 = ty * T, ly0 = band * B::BR;
+    load_neighbour_tiers(a, tx, ty, ntier);
+    __syncthreads();
+    stage_band<T, 2>(a, smc, ntier, tx, ty, ly0 - 2, B::H2, 0, 1);
+    stage_band<T, 1>(a, sme, ntier, tx, ty, ly0 - 1, B::H1, 1, np);
+    __syncthreads();
+    const Phys &ph = a.ph;
+    // mu on the band + ring; with zero flux an out-of-domain ring cell takes
+    // the mu of the cell it mirrors, which lies in the same band
+    for (int u = threadIdx.x; u < B::WM * B::HM; u += kThreads) {
+        int ly = ly0 - 1 + u / B::WM, lx = u % B::WM - 1;
+        if (a.bc != 0) {
+            lx = bc_map(x0 + lx, a.nx, 1) - x0;
+            ly = bc_map(y0 + ly, a.ny, 1) - y0;
+        }
+        const double *C = smc + (ly - (ly0 - 2)) * B::W2 + lx + 2;
+        const double *E = sme + (ly - (ly0 - 1)) * B::W1 + lx + 1;
+        mu[u] = sint_mu<double, double>(C, B::W2, E, B::FE, np, ph);
+    }
+    __syncthreads();
+    for (int u = threadIdx.x; u < B::BR * T; u += kThreads) {
+        const int jb = u / T, i = u % T;
+        const int64_t g = (int64_t)(y0 + ly0 + jb) * a.nx + x0 + i;
+        const double cc = smc[(jb + 2) * B::W2 + i + 2];
+        const double *E = sme + (jb + 1) * B::W1 + i + 1;
+        double s2f;
+        const double cn = sint_c_new<double, double>(cc, mu + (jb + 1) * B::WM + i + 1, B::WM, E, B::FE, np, ph, s2f);
+        store_tier<TIER_FP64>(a, g, cn);
+        for (int k = 0; k < np; ++k)
+            store_tier<TIER_FP64>(a, (int64_t)(k + 1) * a.n + g, sint_eta_new<double>(E + k * B::FE, B::W1, cn, s2f, ph));
+    }
+}
+
 // The tiles of one tier (list / count built by the classification).
 template <int T, int TIER, bool REF, bool MU64>
 __global__ void __launch_bounds__(kThreads) sint_step_kernel(StepArgs a)
@@ -302,6 +386,13 @@ size_t sint_smem_bytes(int tile, int tier, int nf, bool mu64)
 
 cudaError_t sint_launch(int tile, int tier, bool ref, bool mu64, const StepArgs &a, int grid, cudaStream_t s)
 {
+    if (tier == TIER_FP64 && !ref && !a.monitor_now) {  // row bands (the monitor needs whole tiles)
+        const int np = a.nf - 1;
+        if (tile == 32) return launch_kernel(sint_step_f64_band_kernel<32>, grid * SintBand<32>::NB,
+                                             SintBand<32>::smem(np), s, false, a);
+        return launch_kernel(sint_step_f64_band_kernel<16>, grid * SintBand<16>::NB, SintBand<16>::smem(np), s,
+                             false, a);
+    }
 #define AMPS_SINT(TT)                                                                              \
     switch (tier) {                                                                                \
     case TIER_HALF:                                                                                \
@@ -346,6 +437,11 @@ cudaError_t sint_prepare(int tile, int tier, bool ref, bool mu64)
 {
     const int lim = kMaxDynSmem;
     const auto attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    if (tier == TIER_FP64 && !ref) {
+        const cudaError_t e = tile == 32 ? cudaFuncSetAttribute(sint_step_f64_band_kernel<32>, attr, lim)
+                                         : cudaFuncSetAttribute(sint_step_f64_band_kernel<16>, attr, lim);
+        if (e != cudaSuccess) return e;
+    }
 #define AMPS_SP(TT)                                                                                      \
     switch (tier) {                                                                                      \
     case TIER_HALF:                                                                                      \
