@@ -385,6 +385,29 @@ __device__ __forceinline__ void stage_tile(const StepArgs &a, CT *sm, const uint
     }
 }
 
+// Rows per CTA of the band kernels (a tile of a non-monitor step split into
+// T / kBandRows row bands, one CTA each).
+constexpr int kBandRows = 8;
+
+// Rows [ly0, ly0 + H) x columns [-R, T + R) (tile-local) of fields
+// [f0, f0 + nfs) of tile (tx, ty), each cell read at its owner tile's input
+// tier (nt: load_neighbour_tiers) and converted to CT, into dst[f][H][T + 2R]
+// (a row band of a tile, for the band kernels).
+template <typename CT, int T, int R>
+__device__ __forceinline__ void stage_band(const StepArgs &a, CT *dst, const uint8_t *nt, int tx, int ty, int ly0,
+                                           int H, int f0, int nfs)
+{
+    constexpr int W = T + 2 * R;
+    const int x0 = tx * T, y0 = ty * T;
+    for (int u = threadIdx.x; u < H * W; u += kThreads) {
+        const int ly = ly0 + u / W, lx = u % W - R;
+        const int tier = nt[(ly < 0 ? 0 : (ly < T ? 3 : 6)) + (lx < 0 ? 0 : (lx < T ? 1 : 2))];
+        const int64_t off = (int64_t)bc_map(y0 + ly, a.ny, a.bc) * a.nx + bc_map(x0 + lx, a.nx, a.bc);
+#pragma unroll 4
+        for (int f = 0; f < nfs; ++f) dst[f * H * W + u] = load_tier<CT>(a, tier, (int64_t)(f0 + f) * a.n + off);
+    }
+}
+
 // Stage fields [0, nfs) of a tile whose whole 3x3 neighbourhood holds FP32
 // input (no conversion) with an R-cell halo, by asynchronous global->shared
 // copies: 16-byte copies for the interior 8-cell row segments (L2 only, the

@@ -51,6 +51,49 @@ template <typename CT> __device__ __forceinline__ CT k_cos(CT v) { return cos(v)
 template <typename CT> __device__ __forceinline__ CT k_sin(CT v) { return sin(v); }
 template <typename CT> __device__ __forceinline__ CT k_atan(CT v) { return atan(v); }
 
+// ---- per-cell arithmetic (non-reference order).  (Splitting tiles into row
+// bands around these -- 4x the CTAs -- measured no faster at 512^2, where
+// the step is a fixed-latency critical path, and 25-30% slower at 1024^2 and
+// 2048^2, where the bands' shared ring rows cost throughput.)
+
+// Phase A at one cell (snowflake/function.h:30-34): P at the cell's phi,
+// row stride ps.
+template <typename CT>
+__device__ __forceinline__ void kob_aniso(const CT *P, int ps, const Phys &ph, CT &phx, CT &phy, CT &e, CT &ed)
+{
+    const CT pe = P[1], pw = P[-1], pn = P[ps], pso = P[-ps];
+    phx = (pe - pw) * kc<CT>(ph, KB_HX);
+    phy = (pn - pso) * kc<CT>(ph, KB_HY);
+    const CT arg = kc<CT>(ph, KB_ANISO) * (k_atan2<CT>(phy, phx) - kc<CT>(ph, KB_THETA0));
+    e = kc<CT>(ph, KB_EPSB) * fma(kc<CT>(ph, KB_DELTA), k_cos<CT>(arg), CT(1));
+    ed = kc<CT>(ph, KB_ED) * k_sin<CT>(arg);
+}
+
+// Phase B at one cell (snowflake/function.h:54-59): P, Tm at the cell's phi
+// and T (row stride sp); the phase-A arrays at index o, row stride es.
+template <typename CT>
+__device__ __forceinline__ void kob_update(const CT *P, const CT *Tm, int sp, const CT *px, const CT *py,
+                                           const CT *ep, const CT *epd, int o, int es, const Phys &ph, int64_t step,
+                                           int64_t g, CT &pn, CT &tn)
+{
+    const CT p0 = P[0], t0 = Tm[0];
+    const CT inv = kc<CT>(ph, KB_INV);
+    const CT lp = ((P[-1] + P[1]) + (P[-2] + P[2]) + (P[-sp] + P[sp]) + (P[-2 * sp] + P[2 * sp])
+                   - CT(8) * p0) * inv;
+    const CT lt = ((Tm[-1] + Tm[1]) + (Tm[-2] + Tm[2]) + (Tm[-sp] + Tm[sp]) + (Tm[-2 * sp] + Tm[2 * sp])
+                   - CT(8) * t0) * inv;
+    const int on = o + es, os = o - es, oe = o + 1, ow = o - 1;
+    const CT term1 = (ep[on] * epd[on] * px[on] - ep[os] * epd[os] * px[os]) * kc<CT>(ph, KB_HY);
+    const CT term2 = -(ep[oe] * epd[oe] * py[oe] - ep[ow] * epd[ow] * py[ow]) * kc<CT>(ph, KB_HX);
+    const CT m = kc<CT>(ph, KB_M) * k_atan<CT>(kc<CT>(ph, KB_GAMA) * (kc<CT>(ph, KB_TEQ) - t0));
+    CT drive = p0 - CT(0.5) + m;
+    if (nonzero(ph.noise))
+        drive += kc<CT>(ph, KB_NOISE) * (noise_u01_t<CT>(ph.seed, (uint64_t)step, (uint64_t)g) - CT(0.5));
+    const CT inner = term1 + term2 + ep[o] * ep[o] * lp + p0 * (CT(1) - p0) * drive;
+    pn = fma(kc<CT>(ph, KB_DTT), inner, p0);
+    tn = fma(kc<CT>(ph, KB_KAPPA), pn - p0, fma(kc<CT>(ph, KB_DT), lt, t0));
+}
+
 // One tile of one step at tier TIER (smraw: the kernel's dynamic shared
 // memory, kob_smem<T, TIER> bytes; red / ntier: its static scratch).
 template <int T, int TIER, bool REF>
@@ -92,11 +135,7 @@ __device__ __forceinline__ void kob_tile(const StepArgs &a, unsigned char *smraw
             e = __dmul_rn(ph.epsb, __dadd_rn(1.0, __dmul_rn(ph.delta, cos(arg))));
             ed = __dmul_rn(__dmul_rn(__dmul_rn(-ph.epsb, ph.aniso), ph.delta), sin(arg));
         } else {
-            phx = (pe - pw) * kc<CT>(ph, KB_HX);
-            phy = (pn - ps) * kc<CT>(ph, KB_HY);
-            const CT arg = kc<CT>(ph, KB_ANISO) * (k_atan2<CT>(phy, phx) - kc<CT>(ph, KB_THETA0));
-            e = kc<CT>(ph, KB_EPSB) * fma(kc<CT>(ph, KB_DELTA), k_cos<CT>(arg), CT(1));
-            ed = kc<CT>(ph, KB_ED) * k_sin<CT>(arg);
+            kob_aniso<CT>(&S::at(sm, 0, r, cc), S::P, ph, phx, phy, e, ed);
         }
         const int o = u;
         px[o] = phx; py[o] = phy; ep[o] = e; epd[o] = ed;
@@ -156,21 +195,7 @@ __device__ __forceinline__ void kob_tile(const StepArgs &a, unsigned char *smraw
             pn = __dadd_rn(p0, __dmul_rn(ph.dt / ph.tau, inner));
             tn = __dadd_rn(__dadd_rn(t0, __dmul_rn(ph.dt, lt)), __dmul_rn(ph.kappa, __dsub_rn(pn, p0)));
         } else {
-            const CT inv = kc<CT>(ph, KB_INV);
-            const CT lp = ((P[-1] + P[1]) + (P[-2] + P[2]) + (P[-S::P] + P[S::P]) + (P[-2 * S::P] + P[2 * S::P])
-                           - CT(8) * p0) * inv;
-            const CT lt = ((Tm[-1] + Tm[1]) + (Tm[-2] + Tm[2]) + (Tm[-S::P] + Tm[S::P]) + (Tm[-2 * S::P] + Tm[2 * S::P])
-                           - CT(8) * t0) * inv;
-            const int on = o + E, os = o - E, oe = o + 1, ow = o - 1;
-            const CT term1 = (ep[on] * epd[on] * px[on] - ep[os] * epd[os] * px[os]) * kc<CT>(ph, KB_HY);
-            const CT term2 = -(ep[oe] * epd[oe] * py[oe] - ep[ow] * epd[ow] * py[ow]) * kc<CT>(ph, KB_HX);
-            const CT m = kc<CT>(ph, KB_M) * k_atan<CT>(kc<CT>(ph, KB_GAMA) * (kc<CT>(ph, KB_TEQ) - t0));
-            CT drive = p0 - CT(0.5) + m;
-            if (nonzero(ph.noise))
-                drive += kc<CT>(ph, KB_NOISE) * (noise_u01_t<CT>(ph.seed, (uint64_t)step, (uint64_t)g) - CT(0.5));
-            const CT inner = term1 + term2 + ep[o] * ep[o] * lp + p0 * (CT(1) - p0) * drive;
-            pn = fma(kc<CT>(ph, KB_DTT), inner, p0);
-            tn = fma(kc<CT>(ph, KB_KAPPA), pn - p0, fma(kc<CT>(ph, KB_DT), lt, t0));
+            kob_update<CT>(P, Tm, S::P, px, py, ep, epd, o, E, ph, step, g, pn, tn);
         }
         store_tier<TIER>(a, g, pn);
         store_tier<TIER>(a, a.n + g, tn);

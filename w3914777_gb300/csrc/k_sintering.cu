@@ -250,7 +250,6 @@ __device__ __forceinline__ void sint_tile(const StepArgs &a, unsigned char *smra
 // rows of c (2-cell halo) and of every eta (1-cell halo) in double, forms mu on
 // its rows + a 1-cell ring, then c' and every eta' -- the whole-tile path's
 // per-cell arithmetic (sint_mu, sint_c_new, sint_eta_new), so the same bits.
-constexpr int kBandRows = 8;
 
 template <int T> struct SintBand {
     static constexpr int BR = kBandRows, NB = T / BR;
@@ -259,24 +258,6 @@ template <int T> struct SintBand {
     static constexpr int WM = T + 2, HM = BR + 2;                // mu
     static size_t smem(int np) { return sizeof(double) * ((size_t)np * FE + W2 * H2 + WM * HM); }
 };
-
-// Rows [ly0, ly0 + H) x columns [-R, T + R) (tile-local) of fields
-// [f0, f0 + nfs), each cell read at its owner tile's input tier and
-// converted to double, into dst[f][H][T + 2R].
-template <int T, int R>
-__device__ __forceinline__ void stage_band(const StepArgs &a, double *dst, const uint8_t *nt, int tx, int ty,
-                                           int ly0, int H, int f0, int nfs)
-{
-    constexpr int W = T + 2 * R;
-    const int x0 = tx * T, y0 = ty * T;
-    for (int u = threadIdx.x; u < H * W; u += kThreads) {
-        const int ly = ly0 + u / W, lx = u % W - R;
-        const int tier = nt[(ly < 0 ? 0 : (ly < T ? 3 : 6)) + (lx < 0 ? 0 : (lx < T ? 1 : 2))];
-        const int64_t off = (int64_t)bc_map(y0 + ly, a.ny, a.bc) * a.nx + bc_map(x0 + lx, a.nx, a.bc);
-#pragma unroll 4
-        for (int f = 0; f < nfs; ++f) dst[f * H * W + u] = load_tier<double>(a, tier, (int64_t)(f0 + f) * a.n + off);
-    }
-}
 
 template <int T>
 __global__ void __launch_bounds__(kThreads) sint_step_f64_band_kernel(StepArgs a)
@@ -296,8 +277,8 @@ __global__ void __launch_bounds__(kThreads) sint_step_f64_band_kernel(StepArgs a
     const int x0 = tx * T, y0 = ty * T, ly0 = band * B::BR;
     load_neighbour_tiers(a, tx, ty, ntier);
     __syncthreads();
-    stage_band<T, 2>(a, smc, ntier, tx, ty, ly0 - 2, B::H2, 0, 1);
-    stage_band<T, 1>(a, sme, ntier, tx, ty, ly0 - 1, B::H1, 1, np);
+    stage_band<double, T, 2>(a, smc, ntier, tx, ty, ly0 - 2, B::H2, 0, 1);
+    stage_band<double, T, 1>(a, sme, ntier, tx, ty, ly0 - 1, B::H1, 1, np);
     __syncthreads();
     const Phys &ph = a.ph;
     // mu on the band + ring; with zero flux an out-of-domain ring cell takes
