@@ -707,13 +707,20 @@ def run_configs(kob_steps=2000, sint_steps=20000):
 
 
 def run_profile_case(args):
-    """A short, untimed run of the tuned workload at nx^2 for ncu captures
-    (`--profile-case 2048` puts a 256 MiB FP32 state, larger than L2)."""
+    """A short, untimed run of a tuned workload at nx^2 for ncu captures
+    (`--profile-case 2048` puts a 256 MiB FP32 grain-growth state, larger than
+    L2; `--profile-model kobayashi|sintering` the other models' tuned runs)."""
     import torch
     import w3914777_gb300 as w
     torch.cuda.set_device(0)
-    p = w.Params.preset("graingrowth", 0, nx=args.profile_case, ny=args.profile_case)
-    tuned = load_tuned()
+    model = args.profile_model
+    p = w.Params.preset(model, 0, nx=args.profile_case, ny=args.profile_case)
+    if model == "graingrowth":
+        tuned = load_tuned()
+    else:
+        with open(os.path.join(ROOT, "w3914777_gb300", "tuned",
+                               {"kobayashi": "kobayashi_512.json", "sintering": "sintering_1024_n16.json"}[model])) as f:
+            tuned = json.load(f)["best"]
     if tuned:
         p = p.replace(**tuned["overrides"])
     with w.Simulation(p, init=w.INIT_SEEDED) as s:
@@ -737,6 +744,7 @@ def main():
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--no-configs", action="store_true")
     ap.add_argument("--profile-case", type=int, default=0)
+    ap.add_argument("--profile-model", default="graingrowth", choices=["graingrowth", "kobayashi", "sintering"])
     args = ap.parse_args()
     if args.profile_case:
         run_profile_case(args)
