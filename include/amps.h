@@ -51,7 +51,7 @@ enum {
     AMPS_ERR_ALLOC = 3,       /* device or host allocation failed */
     AMPS_ERR_TIMEOUT = 4,     /* a bounded device wait gave up */
     AMPS_ERR_NUMERIC = 5,     /* NaN or Inf seen by the monitor */
-    AMPS_ERR_UNSUPPORTED = 6  /* valid request this build cannot serve */
+    AMPS_ERR_UNSUPPORTED = 6  /* valid request the library cannot serve */
 };
 
 /* models: the reference's three apps */
