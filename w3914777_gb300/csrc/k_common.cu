@@ -272,15 +272,31 @@ __device__ void classify_body(const ClassifyArgs &c)
     }
 }
 
-__global__ void __launch_bounds__(1024) classify_kernel(ClassifyArgs c) { classify_body(c); }
+// Launched with programmatic dependent launch after the period's last step:
+// its launch overlaps that step's tail, and the next step's launch overlaps
+// it; it waits for the step (and its writes) before reading the metric.
+__global__ void __launch_bounds__(1024) classify_kernel(ClassifyArgs c)
+{
+    pdl_trigger();
+    pdl_wait();
+    classify_body(c);
+}
 
 // One CTA per ensemble member; member b's arguments are cs[b].
 __global__ void __launch_bounds__(1024) classify_batch_kernel(const ClassifyArgs *cs) { classify_body(cs[blockIdx.x]); }
 
 cudaError_t classify(const ClassifyArgs &c, cudaStream_t s)
 {
-    classify_kernel<<<1, 1024, 0, s>>>(c);
-    return cudaGetLastError();
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(1);
+    cfg.blockDim = dim3(1024);
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, classify_kernel, c);
 }
 
 cudaError_t classify_batch(const ClassifyArgs *cs, int count, cudaStream_t s)
