@@ -41,6 +41,7 @@
 namespace {
 
 constexpr int kAdjThreads = 256;
+constexpr int kMaxAdjSmem = 226 * 1024;  // dynamic shared memory opt-in limit
 
 struct KobAdj {
     int nx, ny, bc;
@@ -565,6 +566,221 @@ __global__ void __launch_bounds__(kAdjThreads) gg_adj_kernel(GgAdj p, ParamSrc p
     }
 }
 
+// ---- grain growth, periodic grids, 32x32 tiles ----------------------------
+// The forward step and its adjoint for periodic grids whose sides are
+// multiples of 32 (the Laplacian is then its own transpose): every field of a
+// 32x32 tile plus its halo staged by asynchronous copies in a 16-byte-aligned
+// row layout, the per-cell sums (S = sum e^2; the adjoint's P = sum g e)
+// formed once into shared tiles, then each warp advances one field at a
+// time, a lane sweeping 8 rows x 4 cells with a 3-row register window (the
+// grain-growth step kernel's layout).  The neighbour sums keep gg_lap_s's
+// left-to-right order, so the forward results are gg_fwd_kernel's.
+constexpr int kG32Rows = 8;  // rows per lane
+
+template <typename R> struct G32 {
+    static constexpr int T = 32, O = 16 / (int)sizeof(R) >= 1 ? 16 / (int)sizeof(R) : 1;
+    static constexpr int P = T + 2 * O, ROWS = T + 2, FIELD = ROWS * P;
+    static size_t smem(int nfields, int sums) { return sizeof(R) * ((size_t)nfields * FIELD + (size_t)sums * T * T); }
+};
+
+// Stage q fields (periodic) of tile (tx, ty): one warp per staged row.
+template <typename R>
+__device__ __forceinline__ void gg_stage32(R *s, const R *f, int q, int tx, int ty, const GgAdj &p)
+{
+    using L = G32<R>;
+    const int64_t n = (int64_t)p.nx * p.ny;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int x0 = tx * L::T;
+    for (int rr = warp; rr < q * L::ROWS; rr += kAdjThreads / 32) {
+        const int k = rr / L::ROWS, ry = rr - k * L::ROWS;
+        int gy = ty * L::T - 1 + ry;
+        gy = gy < 0 ? gy + p.ny : (gy >= p.ny ? gy - p.ny : gy);
+        const R *row = f + k * n + (int64_t)gy * p.nx;
+        R *dst = s + k * L::FIELD + ry * L::P + L::O;
+        cp_elem(dst + lane, row + x0 + lane);
+        if (lane < 2) {
+            int hx = lane == 0 ? x0 - 1 : x0 + L::T;
+            hx = hx < 0 ? hx + p.nx : (hx >= p.nx ? hx - p.nx : hx);
+            cp_elem(dst + (lane == 0 ? -1 : L::T), row + hx);
+        }
+    }
+}
+
+// Cells [c-1, c+4] of one staged row into w[0..5].
+template <typename R> __device__ __forceinline__ void ld_row6r(const R *p, R *w)
+{
+    if constexpr (sizeof(R) == 4) {
+        const float4 v = *reinterpret_cast<const float4 *>(p);
+        w[1] = v.x; w[2] = v.y; w[3] = v.z; w[4] = v.w;
+    } else {
+        const double2 a = *reinterpret_cast<const double2 *>(p), b = *reinterpret_cast<const double2 *>(p + 2);
+        w[1] = a.x; w[2] = a.y; w[3] = b.x; w[4] = b.y;
+    }
+    w[0] = p[-1];
+    w[5] = p[4];
+}
+
+// gg_lap_s's neighbour sum, from the window rows up / md / dn around column k+1
+template <typename R> __device__ __forceinline__ R lap_w(const R *up, const R *md, const R *dn, int k, int stencil, R inv)
+{
+    R v;
+    if (stencil == 0)
+        v = up[k] + up[k + 1] + up[k + 2] + md[k] + md[k + 2] + dn[k] + dn[k + 1] + dn[k + 2] - R(8) * md[k + 1];
+    else
+        v = md[k] + md[k + 2] + up[k + 1] + dn[k + 1] - R(4) * md[k + 1];
+    return v * inv;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kAdjThreads) gg_fwd32_kernel(GgAdj p, ParamSrc ps, const R *__restrict__ eta,
+                                                               R *__restrict__ out)
+{
+    using L = G32<R>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    R *se = reinterpret_cast<R *>(smem_raw), *sS = se + p.q * L::FIELD;
+    double mobil, grcoef, gamma;
+    int64_t step;
+    load_params(ps, mobil, grcoef, gamma, step);
+    const int ntx = p.nx / L::T, tx = blockIdx.x % ntx, ty = blockIdx.x / ntx;
+    gg_stage32(se, eta, p.q, tx, ty, p);
+    gg_stage_wait();
+    __syncthreads();
+    {
+        const int row = threadIdx.x / 8, c = (threadIdx.x % 8) * 4;
+        R acc[4] = {R(0), R(0), R(0), R(0)};
+        for (int k = 0; k < p.q; ++k) {
+            const R *q = se + k * L::FIELD + (row + 1) * L::P + L::O + c;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc[j] += q[j] * q[j];
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) sS[row * L::T + c + j] = acc[j];
+    }
+    __syncthreads();
+    const int64_t n = (int64_t)p.nx * p.ny;
+    const R dtm = R(p.dt * mobil), g2 = R(2.0 * gamma), kap = R(grcoef), inv = R(1.0 / p.dxdy);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int c0 = (lane & 7) * 4, r0 = (lane >> 3) * kG32Rows;
+    const int64_t gbase = (int64_t)(ty * L::T + r0) * p.nx + tx * L::T + c0;
+    for (int f = warp; f < p.q; f += kAdjThreads / 32) {
+        const R *fs = se + f * L::FIELD + L::O + c0;
+        R w[3][6];
+        ld_row6r(fs + r0 * L::P, w[0]);
+        ld_row6r(fs + (r0 + 1) * L::P, w[1]);
+#pragma unroll
+        for (int i = 0; i < kG32Rows; ++i) {
+            const R *up = w[i % 3], *md = w[(i + 1) % 3];
+            R *dn = w[(i + 2) % 3];
+            ld_row6r(fs + (r0 + i + 2) * L::P, dn);
+            R o4[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const R e = md[k + 1], e2 = e * e, S = sS[(r0 + i) * L::T + c0 + k];
+                const R dfd = e * (e2 - R(1) + g2 * (S - e2));
+                o4[k] = e - dtm * (dfd - kap * lap_w(up, md, dn, k, p.stencil, inv));
+            }
+            R *dst = out + f * n + gbase + (int64_t)i * p.nx;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) dst[k] = o4[k];
+        }
+    }
+}
+
+// Input cotangents of all q fields and dL/d(L, kappa, gamma) into gparams
+// (gg_adj_kernel's arithmetic; the parameter sums are grouped differently).
+template <typename R>
+__global__ void __launch_bounds__(kAdjThreads) gg_adj32_kernel(GgAdj p, ParamSrc ps, const R *__restrict__ eta,
+                                                               const R *__restrict__ gout, R *__restrict__ gin,
+                                                               double *__restrict__ gparams)
+{
+    using L = G32<R>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ double red[kAdjThreads / 32];
+    R *se = reinterpret_cast<R *>(smem_raw), *sg = se + p.q * L::FIELD;
+    R *sS = sg + p.q * L::FIELD, *sP = sS + L::T * L::T;
+    double mobil, grcoef, gamma;
+    int64_t step;
+    load_params(ps, mobil, grcoef, gamma, step);
+    const int ntx = p.nx / L::T, tx = blockIdx.x % ntx, ty = blockIdx.x / ntx;
+    gg_stage32(se, eta, p.q, tx, ty, p);
+    gg_stage32(sg, gout, p.q, tx, ty, p);
+    gg_stage_wait();
+    __syncthreads();
+    {
+        const int row = threadIdx.x / 8, c = (threadIdx.x % 8) * 4;
+        R S[4] = {R(0), R(0), R(0), R(0)}, P[4] = {R(0), R(0), R(0), R(0)};
+        for (int k = 0; k < p.q; ++k) {
+            const int o = k * L::FIELD + (row + 1) * L::P + L::O + c;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const R e = se[o + j];
+                S[j] += e * e;
+                P[j] += sg[o + j] * e;
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            sS[row * L::T + c + j] = S[j];
+            sP[row * L::T + c + j] = P[j];
+        }
+    }
+    __syncthreads();
+    const int64_t n = (int64_t)p.nx * p.ny;
+    const R dt = R(p.dt), dtm = R(p.dt * mobil), gm = R(gamma), kap = R(grcoef), inv = R(1.0 / p.dxdy);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int c0 = (lane & 7) * 4, r0 = (lane >> 3) * kG32Rows;
+    const int64_t gbase = (int64_t)(ty * L::T + r0) * p.nx + tx * L::T + c0;
+    R gl = R(0), gkap = R(0), ggam = R(0);
+    for (int f = warp; f < p.q; f += kAdjThreads / 32) {
+        const R *fe = se + f * L::FIELD + L::O + c0, *fg = sg + f * L::FIELD + L::O + c0;
+        R we[3][6], wg[3][6];
+        ld_row6r(fe + r0 * L::P, we[0]);
+        ld_row6r(fe + (r0 + 1) * L::P, we[1]);
+        ld_row6r(fg + r0 * L::P, wg[0]);
+        ld_row6r(fg + (r0 + 1) * L::P, wg[1]);
+#pragma unroll
+        for (int i = 0; i < kG32Rows; ++i) {
+            const R *eu = we[i % 3], *em = we[(i + 1) % 3], *gu = wg[i % 3], *gmr = wg[(i + 1) % 3];
+            R *ed = we[(i + 2) % 3], *gd = wg[(i + 2) % 3];
+            ld_row6r(fe + (r0 + i + 2) * L::P, ed);
+            ld_row6r(fg + (r0 + i + 2) * L::P, gd);
+            R o4[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int so = (r0 + i) * L::T + c0 + k;
+                const R S = sS[so], P = sP[so];
+                const R e = em[k + 1], e2 = e * e, gk = gmr[k + 1];
+                const R jac = R(3) * e2 - R(1) + R(2) * gm * (S - e2);  // d dfd_k / d eta_k
+                o4[k] = gk - dtm * (gk * jac + R(4) * gm * e * (P - gk * e)) +
+                        dtm * kap * lap_w(gu, gmr, gd, k, p.stencil, inv);
+                const R lap = lap_w(eu, em, ed, k, p.stencil, inv);
+                const R dfd = e * (e2 - R(1) + R(2) * gm * (S - e2));
+                gl += gk * (-dt) * (dfd - kap * lap);
+                gkap += gk * dtm * lap;
+                ggam += gk * (-dtm) * R(2) * e * (S - e2);
+            }
+            R *dst = gin + f * n + gbase + (int64_t)i * p.nx;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) dst[k] = o4[k];
+        }
+    }
+    const double a = block_sum(gl, red);
+    const double b = block_sum(gkap, red);
+    const double c = block_sum(ggam, red);
+    if (threadIdx.x == 0) {
+        atomicAdd(&gparams[0], a);
+        atomicAdd(&gparams[1], b);
+        atomicAdd(&gparams[2], c);
+    }
+}
+
+// The 32x32 periodic path applies (and its staging fits in shared memory)?
+template <typename R> bool gg_use32(const amps_params *p, int sums)
+{
+    return p->bc == AMPS_BC_PERIODIC && p->nx % 32 == 0 && p->ny % 32 == 0 &&
+           G32<R>::smem(sums == 2 ? 2 * p->nfields : p->nfields, sums) <= (size_t)kMaxAdjSmem;
+}
+
 // ------------------------------------------------------------- launches ----
 constexpr int kTX = 32;
 
@@ -589,6 +805,8 @@ template <typename R> cudaError_t kob_prepare()
     if (e == cudaSuccess) e = cudaFuncSetAttribute(kob_adj_kernel<R, kTX, 8>, attr, (int)kob_adj_smem<R, 8>());
     if (e == cudaSuccess) e = cudaFuncSetAttribute(gg_fwd_kernel<R>, attr, (int)(32 * GReg::N * sizeof(R)));
     if (e == cudaSuccess) e = cudaFuncSetAttribute(gg_adj_kernel<R>, attr, (int)(2 * 32 * GReg::N * sizeof(R)));
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(gg_fwd32_kernel<R>, attr, kMaxAdjSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(gg_adj32_kernel<R>, attr, kMaxAdjSmem);
     return e;
 }
 
@@ -653,6 +871,9 @@ void launch_forward(const amps_params *p, const ParamSrc &ps, const void *in, vo
             kob_fwd_kernel<R, kTX, 16><<<grid, kAdjThreads, kob_fwd_smem<R, 16>(), s>>>(kob_args(p), ps,
                                                                                         (const R *)in, (R *)out);
         }
+    } else if (gg_use32<R>(p, 1)) {
+        gg_fwd32_kernel<R><<<(nx / 32) * (ny / 32), kAdjThreads, G32<R>::smem(p->nfields, 1), s>>>(
+            gg_args(p), ps, (const R *)in, (R *)out);
     } else {
         const dim3 grid((nx + kGX - 1) / kGX, (ny + kGY - 1) / kGY);
         gg_fwd_kernel<R><<<grid, kAdjThreads, (size_t)p->nfields * GReg::N * sizeof(R), s>>>(gg_args(p), ps,
@@ -675,6 +896,9 @@ void launch_adjoint(const amps_params *p, const ParamSrc &ps, const void *in, co
             kob_adj_kernel<R, kTX, 16><<<grid, kAdjThreads, kob_adj_smem<R, 16>(), s>>>(
                 kob_args(p), ps, (const R *)in, (const R *)gout, (R *)gin, gparams);
         }
+    } else if (gg_use32<R>(p, 2)) {
+        gg_adj32_kernel<R><<<(nx / 32) * (ny / 32), kAdjThreads, G32<R>::smem(2 * p->nfields, 2), s>>>(
+            gg_args(p), ps, (const R *)in, (const R *)gout, (R *)gin, gparams);
     } else {
         const dim3 grid((nx + kGX - 1) / kGX, (ny + kGY - 1) / kGY);
         gg_adj_kernel<R><<<grid, kAdjThreads, 2 * (size_t)p->nfields * GReg::N * sizeof(R), s>>>(
