@@ -327,12 +327,15 @@ __device__ __forceinline__ bool all_fp32(const uint8_t *nt)
 }
 
 // One tile of the fused step (every tier), by the whole CTA: neighbourhood
-// tiers, staging, update (and the monitor on MON steps).  Shared by the
+// tiers, staging, update (and the monitor on monitor steps).  Shared by the
 // single-run step kernel and the ensemble's tile-queue kernel, so that a
-// member of an ensemble gets exactly the results of a single run.
-template <int T, bool REF, bool MON>
+// member of an ensemble gets exactly the results of a single run.  MK: 0 for
+// a step without the monitor, 1/2/3 a monitor step of that monitor kind
+// (spatial / temporal / rate), -1 a monitor step of the kind in `a`.
+template <int T, bool REF, int MK>
 __device__ __forceinline__ void gg_tile_step(const StepArgs &a, float *sm, uint8_t *ntier, double *red, int tile)
 {
+    constexpr bool MON = MK != 0;
     const int tx = tile % a.ntx, ty = tile / a.ntx;
     load_neighbour_tiers(a, tx, ty, ntier);
     // the copy of the FP32 neighbourhood (the common case) starts before the
@@ -376,12 +379,12 @@ __device__ __forceinline__ void gg_tile_step(const StepArgs &a, float *sm, uint8
             }
             return;
         }
-        if (a.monitor_kind == 3) {
+        if (MK == 3 || (MK == -1 && a.monitor_kind == 3)) {
             if (tier == TIER_FP32) gg_tile_lo_rows<TIER_FP32, 4, 3>(a, sm, ss, tile, tx, ty, red);
             else gg_tile_lo_rows<TIER_HALF, 4, 3>(a, sm, ss, tile, tx, ty, red);
             return;
         }
-        if (a.monitor_kind == 2) {
+        if (MK == 2 || (MK == -1 && a.monitor_kind == 2)) {
             if (tier == TIER_FP32) gg_tile_lo_rows<TIER_FP32, 4, 2>(a, sm, ss, tile, tx, ty, red);
             else gg_tile_lo_rows<TIER_HALF, 4, 2>(a, sm, ss, tile, tx, ty, red);
             return;
@@ -396,15 +399,16 @@ __device__ __forceinline__ void gg_tile_step(const StepArgs &a, float *sm, uint8
 template <int T, bool REF, bool MON>
 __device__ __noinline__ void gg_tile_step_call(const StepArgs &a, float *sm, uint8_t *ntier, double *red, int tile)
 {
-    gg_tile_step<T, REF, MON>(a, sm, ntier, red, tile);
+    gg_tile_step<T, REF, MON ? -1 : 0>(a, sm, ntier, red, tile);
 }
 
 // Fused all-tier step: at most 64 registers, so that four CTAs share an SM.
-// MON (the monitor steps, one in `cadence`) is a separate instantiation, so
-// the other steps' kernel carries no monitor code.  Half/FP32 tiles stage
+// The monitor steps (one in `cadence`) are separate instantiations, one per
+// monitor kind MK, so the other steps' kernel carries no monitor code and
+// each monitor step's kernel only its own kind's.  Half/FP32 tiles stage
 // their neighbourhood in shared memory (reading it directly through L1
 // measured 18.1 against 15.8 us per adaptive 1024^2 Q=8 step).
-template <int T, bool REF, bool MON>
+template <int T, bool REF, int MK>
 __global__ void __launch_bounds__(kThreads, 4) gg_step_kernel(StepArgs a)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
@@ -418,7 +422,7 @@ __global__ void __launch_bounds__(kThreads, 4) gg_step_kernel(StepArgs a)
     pdl_trigger();
     pdl_wait();
     const int tile = a.order ? a.order[blockIdx.x] : (int)blockIdx.x;
-    gg_tile_step<T, REF, MON>(a, sm, ntier, red, tile);
+    gg_tile_step<T, REF, MK>(a, sm, ntier, red, tile);
 }
 
 // All-FP64 step (plain FP64 mode): the FP64 neighbourhood is staged in
@@ -525,14 +529,22 @@ cudaError_t gg_launch(int tile, int tier, bool ref, const StepArgs &a, int grid,
         if (ref) K<TT, true><<<grid, kThreads, smem, s>>>(a);                   \
         else K<TT, false><<<grid, kThreads, smem, s>>>(a);                      \
     } while (0)
-#define AMPS_GGM(TT)                                                                                \
-    do {                                                                                            \
-        if (a.monitor_now) {                                                                        \
-            if (ref) return launch_pdl(gg_step_kernel<TT, true, true>, grid, smem, s, a);          \
-            return launch_pdl(gg_step_kernel<TT, false, true>, grid, smem, s, a);                  \
-        }                                                                                           \
-        if (ref) return launch_pdl(gg_step_kernel<TT, true, false>, grid, smem, s, a);             \
-        return launch_pdl(gg_step_kernel<TT, false, false>, grid, smem, s, a);                     \
+#define AMPS_GGM(TT)                                                                                  \
+    do {                                                                                              \
+        switch (a.monitor_now ? a.monitor_kind : 0) {                                                 \
+        case 0:                                                                                       \
+            if (ref) return launch_pdl(gg_step_kernel<TT, true, 0>, grid, smem, s, a);                \
+            return launch_pdl(gg_step_kernel<TT, false, 0>, grid, smem, s, a);                        \
+        case 1:                                                                                       \
+            if (ref) return launch_pdl(gg_step_kernel<TT, true, 1>, grid, smem, s, a);                \
+            return launch_pdl(gg_step_kernel<TT, false, 1>, grid, smem, s, a);                        \
+        case 2:                                                                                       \
+            if (ref) return launch_pdl(gg_step_kernel<TT, true, 2>, grid, smem, s, a);                \
+            return launch_pdl(gg_step_kernel<TT, false, 2>, grid, smem, s, a);                        \
+        default:                                                                                      \
+            if (ref) return launch_pdl(gg_step_kernel<TT, true, 3>, grid, smem, s, a);                \
+            return launch_pdl(gg_step_kernel<TT, false, 3>, grid, smem, s, a);                        \
+        }                                                                                             \
     } while (0)
     if (tier == TIER_FP64) {
         if (tile == 32) AMPS_GGL(gg_step_f64_kernel, 32);
@@ -556,20 +568,17 @@ cudaError_t gg_prepare(int tile, int tier, bool ref)
         return ref ? cudaFuncSetAttribute(gg_step_f64_kernel<16, true>, attr, lim)
                    : cudaFuncSetAttribute(gg_step_f64_kernel<16, false>, attr, lim);
     }
-    cudaError_t e;
+    cudaError_t e = cudaSuccess;
+#define AMPS_GGP(TT, MK)                                                                                     \
+    if (e == cudaSuccess)                                                                                    \
+        e = ref ? cudaFuncSetAttribute(gg_step_kernel<TT, true, MK>, attr, lim)                              \
+                : cudaFuncSetAttribute(gg_step_kernel<TT, false, MK>, attr, lim)
     if (tile == 32) {
-        e = ref ? cudaFuncSetAttribute(gg_step_kernel<32, true, false>, attr, lim)
-                : cudaFuncSetAttribute(gg_step_kernel<32, false, false>, attr, lim);
-        if (e == cudaSuccess)
-            e = ref ? cudaFuncSetAttribute(gg_step_kernel<32, true, true>, attr, lim)
-                    : cudaFuncSetAttribute(gg_step_kernel<32, false, true>, attr, lim);
-        return e;
+        AMPS_GGP(32, 0); AMPS_GGP(32, 1); AMPS_GGP(32, 2); AMPS_GGP(32, 3);
+    } else {
+        AMPS_GGP(16, 0); AMPS_GGP(16, 1); AMPS_GGP(16, 2); AMPS_GGP(16, 3);
     }
-    e = ref ? cudaFuncSetAttribute(gg_step_kernel<16, true, false>, attr, lim)
-            : cudaFuncSetAttribute(gg_step_kernel<16, false, false>, attr, lim);
-    if (e == cudaSuccess)
-        e = ref ? cudaFuncSetAttribute(gg_step_kernel<16, true, true>, attr, lim)
-                : cudaFuncSetAttribute(gg_step_kernel<16, false, true>, attr, lim);
+#undef AMPS_GGP
     return e;
 }
 
