@@ -220,6 +220,33 @@ AMPS_API int amps_get_decision_log(amps_handle *h, uint8_t *out, int max_entries
 /* Last monitor metric per tile (double [nty][ntx]). */
 AMPS_API int amps_get_tile_metric(amps_handle *h, double *out);
 AMPS_API int amps_get_stats(amps_handle *h, amps_stats *out);
+
+/* ---- tier control for the cost and selection experiments ------------------- */
+/* Adaptive runs (mode END2END_MIX) only: the k-th classification from now on
+ * takes its tier map from maps[min(k, n_maps - 1)] (n_maps maps of ntiles
+ * bytes, e.g. a decision log) instead of the monitor, and no step carries the
+ * monitor epilogue.  Replaying a monitored run's decision log therefore runs
+ * the same tiles at the same tiers, with the same results, minus the
+ * monitor: the compute-only time of the reference's monitor-cost harness
+ * (snowflake/monitor_independent_withoutmonitor.cu:89-126, which times the
+ * update kernels alone against monitor_independent_withmonitor.cu:71-104).
+ * Every amps_init / amps_set_field(s) restarts at maps[0] (the initial
+ * classification).  n_maps = 0 restores the monitor.  Ensembles reject
+ * members with a schedule. */
+AMPS_API int amps_set_tier_schedule(amps_handle *h, const uint8_t *maps, int n_maps);
+/* Static modes (PUREHIGH, PURELOW, GRAM1, GRAM2): replace the tier map with
+ * tiers[ntiles] and store the current state at the new tiers (the host-side
+ * type_new of snowflake/motivation_mix.cu:87-109, then the mixed steps at
+ * :110-115).  Each tier must be one this mode stores (GRAM: half and the
+ * high tier). */
+AMPS_API int amps_set_tile_tiers(amps_handle *h, const uint8_t *tiers);
+/* The monitor metric of the current state, on demand, without touching the
+ * tiers (get_max_diff1 / get_max_diff2 of snowflake/motivation_mix.cu:77-82),
+ * on the params' monitor field and sample lattice.  kind AMPS_MONITOR_SPA:
+ * out[ntiles] = each tile's range.  kind AMPS_MONITOR_TEM: out == NULL stores
+ * the current samples as the temporal reference (motivation_monitor2_datasychr,
+ * :64-67); out != NULL writes max |current - reference| per tile. */
+AMPS_API int amps_measure_tiles(amps_handle *h, int kind, double *out);
 /* FP64 reduction of one field over the grid (deterministic order).  SUM of c
  * is the sintering conserved mass. */
 AMPS_API int amps_reduce(amps_handle *h, int field, int kind, double *out);

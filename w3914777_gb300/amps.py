@@ -122,6 +122,8 @@ def lib():
             "amps_get_fields": ([vp, vp, ip, ip], ip), "amps_run": ([vp, ip], ip), "amps_set_graphs": ([vp, ip], ip),
             "amps_get_tile_tiers": ([vp, vp], ip), "amps_get_decision_log": ([vp, vp, ip, ctypes.POINTER(ip)], ip),
             "amps_get_tile_metric": ([vp, vp], ip), "amps_get_stats": ([vp, ctypes.POINTER(Stats)], ip),
+            "amps_set_tier_schedule": ([vp, vp, ip], ip), "amps_set_tile_tiers": ([vp, vp], ip),
+            "amps_measure_tiles": ([vp, ip, vp], ip),
             "amps_reduce": ([vp, ip, ip, ctypes.POINTER(dp)], ip),
             "amps_compare": ([vp, ip, vp, ip, ctypes.POINTER(dp), ctypes.POINTER(dp)], ip),
             "amps_set_profiling": ([vp, ip], ip),
@@ -266,6 +268,33 @@ class Simulation:
         self._ck(lib().amps_get_decision_log(self.h, out.ctypes.data, max_entries, ctypes.byref(n)),
                  "amps_get_decision_log")
         return out[: n.value]
+
+    def set_tier_schedule(self, maps):
+        """Adaptive runs: take the tier maps of successive classifications from
+        `maps` (e.g. another run's decision_log()) instead of the monitor, with
+        no monitor epilogue; None or an empty array restores the monitor."""
+        if maps is None or len(maps) == 0:
+            self._ck(lib().amps_set_tier_schedule(self.h, None, 0), "amps_set_tier_schedule")
+            return
+        m = np.ascontiguousarray(maps, dtype=np.uint8).reshape((-1,) + self.ntiles)
+        self._ck(lib().amps_set_tier_schedule(self.h, m.ctypes.data, m.shape[0]), "amps_set_tier_schedule")
+
+    def set_tiers(self, tiers):
+        """Static modes (purehigh, purelow, GRAM1, GRAM2): store the state at
+        the tile tiers `tiers` ([nty][ntx], AMPS_TIER_*) from now on."""
+        t = np.ascontiguousarray(tiers, dtype=np.uint8).reshape(self.ntiles)
+        self._ck(lib().amps_set_tile_tiers(self.h, t.ctypes.data), "amps_set_tile_tiers")
+
+    def measure_tiles(self, kind=MONITOR_SPA):
+        """The monitor metric of the current state per tile ([nty][ntx]); for
+        MONITOR_TEM against the state stored by store_temporal_reference()."""
+        out = np.empty(self.ntiles, dtype=np.float64)
+        self._ck(lib().amps_measure_tiles(self.h, int(kind), out.ctypes.data), "amps_measure_tiles")
+        return out
+
+    def store_temporal_reference(self):
+        """Keep the current monitor samples as the reference of measure_tiles(MONITOR_TEM)."""
+        self._ck(lib().amps_measure_tiles(self.h, MONITOR_TEM, None), "amps_measure_tiles")
 
     def stats(self):
         s = Stats()

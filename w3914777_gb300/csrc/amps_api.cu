@@ -37,6 +37,14 @@ struct amps_handle {
     int *d_order = nullptr;  // launch order of the fused grain-growth step (adaptive runs)
     double *d_metric = nullptr, *d_snap = nullptr;
     int nmon = 0;
+    // tier schedule (amps_set_tier_schedule): sched_n maps of ntiles bytes,
+    // the next one to use at *d_sched_i
+    uint8_t *d_sched = nullptr;
+    int sched_n = 0;
+    int *d_sched_i = nullptr;
+    // on-demand monitor (amps_measure_tiles): its own snapshot and metric
+    double *d_msnap = nullptr, *d_mmetric = nullptr;
+    bool msnap_valid = false;
     unsigned long long *d_stats = nullptr;
     int *d_flags = nullptr;
     uint8_t *d_log = nullptr;
@@ -184,7 +192,7 @@ static void free_all(amps_handle *h)
             if (h->store[t][q]) cudaFree(h->store[t][q]);
     void *ps[] = {h->d_tier_prev, h->d_tier_cur, h->d_lists, h->d_order, h->d_counts, h->d_metric, h->d_snap, h->d_stats,
                   h->d_flags, h->d_log, h->d_log_n, h->d_step_base, h->d_stage, h->d_partials, h->d_out,
-                  h->d_diag};
+                  h->d_diag, h->d_sched, h->d_sched_i, h->d_msnap, h->d_mmetric};
     for (void *q : ps)
         if (q) cudaFree(q);
     if (h->h_pinned) cudaFreeHost(h->h_pinned);
@@ -397,6 +405,11 @@ static int reclassify_resting(amps_handle *h)
         c.stats = h->d_stats; c.log = h->d_log; c.log_n = h->d_log_n; c.max_log = p.max_log;
         c.step_base = h->d_step_base; c.advance = 0; c.stat_steps = 0;
         c.order = h->d_order; c.bc = p.bc;
+        if (h->sched_n) {
+            // a schedule restarts with its first map at every new state
+            CK(h, cudaMemsetAsync(h->d_sched_i, 0, sizeof(int), h->stream));
+            c.sched = h->d_sched; c.sched_n = h->sched_n; c.sched_i = h->d_sched_i;
+        }
         CK(h, classify(c, h->stream));
         h->transition = true;
     }
@@ -643,6 +656,7 @@ static ClassifyArgs classify_args(const amps_handle *h, int advance, int stat_st
     c.stats = h->d_stats; c.log = h->d_log; c.log_n = h->d_log_n; c.max_log = p.max_log;
     c.step_base = h->d_step_base; c.advance = advance; c.stat_steps = stat_steps;
     c.order = h->d_order; c.bc = p.bc;
+    if (h->sched_n) { c.sched = h->d_sched; c.sched_n = h->sched_n; c.sched_i = h->d_sched_i; }
     return c;
 }
 
@@ -661,7 +675,8 @@ static int enqueue_chunk(amps_handle *h, int k0, int cnt)
         if (r) return r;
     }
     for (int s = 0; s < cnt; ++s) {
-        const bool mon = h->mixed && period_end && s == cnt - 1;
+        // a tier schedule stands in for the monitor: no epilogue
+        const bool mon = h->mixed && period_end && s == cnt - 1 && h->sched_n == 0;
         int r = launch_step(h, k0 + s, mon);
         if (r) return r;
     }
@@ -755,6 +770,88 @@ extern "C" int amps_get_tile_metric(amps_handle *h, double *out)
     if (!h || !out) return AMPS_ERR_INVALID;
     CK(h, cudaStreamSynchronize(h->stream));
     CK(h, cudaMemcpy(out, h->d_metric, sizeof(double) * h->ntiles, cudaMemcpyDeviceToHost));
+    return AMPS_OK;
+}
+
+// The tiers a map may hold: those with storage in this handle's mode.
+static int check_maps(amps_handle *h, const uint8_t *maps, int n_maps, const char *what)
+{
+    for (int64_t i = 0; i < (int64_t)n_maps * h->ntiles; ++i)
+        if (maps[i] > TIER_FP64 || !h->used[maps[i]])
+            FAIL(h, AMPS_ERR_INVALID, "%s: map %d tile %d: tier %d is not one of this mode's tiers", what,
+                 (int)(i / h->ntiles), (int)(i % h->ntiles), (int)maps[i]);
+    return AMPS_OK;
+}
+
+extern "C" int amps_set_tier_schedule(amps_handle *h, const uint8_t *maps, int n_maps)
+{
+    if (!h || n_maps < 0 || (n_maps > 0 && !maps)) return AMPS_ERR_INVALID;
+    if (!h->mixed) FAIL(h, AMPS_ERR_INVALID, "amps_set_tier_schedule: only adaptive runs classify");
+    int r = check_maps(h, maps, n_maps, "amps_set_tier_schedule");
+    if (r) return r;
+    CK(h, cudaStreamSynchronize(h->stream));
+    if (h->d_sched) cudaFree(h->d_sched);
+    h->d_sched = nullptr;
+    h->sched_n = 0;
+    if (!h->d_sched_i) CK(h, cudaMalloc(&h->d_sched_i, sizeof(int)));
+    if (n_maps) {
+        const size_t bytes = (size_t)n_maps * h->ntiles;
+        CK(h, cudaMalloc(&h->d_sched, bytes));
+        CK(h, cudaMemcpyAsync(h->d_sched, maps, bytes, cudaMemcpyHostToDevice, h->stream));
+    }
+    CK(h, cudaMemsetAsync(h->d_sched_i, 0, sizeof(int), h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    h->sched_n = n_maps;
+    // the captured periods hold the old classification arguments and monitor steps
+    for (auto &kv : h->graph) cudaGraphExecDestroy(kv.second);
+    h->graph.clear();
+    return AMPS_OK;
+}
+
+extern "C" int amps_set_tile_tiers(amps_handle *h, const uint8_t *tiers)
+{
+    if (!h || !tiers) return AMPS_ERR_INVALID;
+    if (h->mixed) FAIL(h, AMPS_ERR_INVALID, "amps_set_tile_tiers: adaptive runs take their tiers from the monitor");
+    int r = check_maps(h, tiers, 1, "amps_set_tile_tiers");
+    if (r) return r;
+    // the state at its current tiers -> FP64 stage -> stored at the new tiers
+    Grid live = grid_view(h, h->parity, live_tiers(h));
+    CK(h, gather_fields(live, h->d_stage, 0, 0, h->nf, h->stream));
+    CK(h, cudaMemcpyAsync(h->d_tier_cur, tiers, h->ntiles, cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaMemcpyAsync(h->d_tier_prev, tiers, h->ntiles, cudaMemcpyHostToDevice, h->stream));
+    CK(h, build_lists(h->d_tier_cur, h->ntiles, h->d_lists, h->d_counts, h->stream));
+    h->transition = false;
+    Grid g = grid_view(h, h->parity, h->d_tier_cur);
+    CK(h, scatter_fields(g, h->d_stage, 0, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    return AMPS_OK;
+}
+
+extern "C" int amps_measure_tiles(amps_handle *h, int kind, double *out)
+{
+    if (!h || (kind != AMPS_MONITOR_SPA && kind != AMPS_MONITOR_TEM) || (kind == AMPS_MONITOR_SPA && !out))
+        return AMPS_ERR_INVALID;
+    const amps_params &p = h->p;
+    if (kind == AMPS_MONITOR_TEM && out && !h->msnap_valid)
+        FAIL(h, AMPS_ERR_INVALID, "amps_measure_tiles: no temporal reference stored yet (call with out == NULL)");
+    CK(h, cudaStreamSynchronize(h->stream));
+    if (!h->d_mmetric) CK(h, cudaMalloc(&h->d_mmetric, sizeof(double) * h->ntiles));
+    if (kind == AMPS_MONITOR_TEM && !h->d_msnap) {
+        const size_t snap = p.monitor_samples ? (size_t)h->nmon * h->n : (size_t)h->nmon * h->ntiles * 16;
+        CK(h, cudaMalloc(&h->d_msnap, sizeof(double) * snap));
+    }
+    Grid g = grid_view(h, h->parity, live_tiers(h));
+    if (kind == AMPS_MONITOR_SPA) {
+        CK(h, monitor_state(g, 1, p.monitor_samples, p.monitor_field, h->d_mmetric, nullptr, 0, h->d_flags, h->stream));
+    } else if (!out) {
+        CK(h, monitor_state(g, 2, p.monitor_samples, p.monitor_field, nullptr, h->d_msnap, 1, h->d_flags, h->stream));
+        h->msnap_valid = true;
+    } else {
+        CK(h, monitor_state(g, 2, p.monitor_samples, p.monitor_field, h->d_mmetric, h->d_msnap, 0, h->d_flags,
+                            h->stream, 1));
+    }
+    CK(h, cudaStreamSynchronize(h->stream));
+    if (out) CK(h, cudaMemcpy(out, h->d_mmetric, sizeof(double) * h->ntiles, cudaMemcpyDeviceToHost));
     return AMPS_OK;
 }
 
@@ -1050,7 +1147,7 @@ extern "C" int amps_ensemble_create(amps_handle *const *members, int count, amps
         amps_handle *h = members[i];
         if (!h || h->p.model != AMPS_GRAINGROWTH || h->T != h0->T || h->p.cadence != h0->p.cadence ||
             h->mixed != h0->mixed || (h->p.ref_order != 0) != (h0->p.ref_order != 0) ||
-            h->step % h->p.cadence != h0->step % h0->p.cadence)
+            h->step % h->p.cadence != h0->step % h0->p.cadence || h->sched_n)
             return AMPS_ERR_INVALID;
         for (int j = 0; j < i; ++j)
             if (members[j] == h) return AMPS_ERR_INVALID;

@@ -48,8 +48,9 @@ struct Grid {
 cudaError_t scatter_fields(const Grid &g, const void *src, int src_f32, cudaStream_t s);
 cudaError_t gather_fields(const Grid &g, void *dst, int dst_f32, int f0, int nfs, cudaStream_t s);
 // Monitor at time 0 (or after a set_field): metric and temporal snapshot from the state.
+// diff != 0 (kind 2): metric = max |state - snap| over the samples instead of the range.
 cudaError_t monitor_state(const Grid &g, int kind, int samples, int mfield, double *metric, double *snap,
-                          int write_snap, int *flags, cudaStream_t s);
+                          int write_snap, int *flags, cudaStream_t s, int diff = 0);
 // get_type (snowflake/tools.h:212-230) on the device, three tiers, plus
 // ordered per-tier tile lists, stats and the decision log.
 struct ClassifyArgs {
@@ -68,6 +69,11 @@ struct ClassifyArgs {
     int stat_steps;             // steps the current counts ran for (tile-step stats)
     int *order;                 // optional: launch order of the fused grain-growth step
     int bc;                     // boundary map of the tile neighbourhood (for order)
+    // optional tier schedule: the k-th classification takes its tier map from
+    // sched[min(k, sched_n - 1)] instead of the metric (*sched_i = k, advanced here)
+    const uint8_t *sched;
+    int sched_n;
+    int *sched_i;
 };
 cudaError_t classify(const ClassifyArgs &c, cudaStream_t s);
 // Ensembles: classify (or do the period bookkeeping of) count members whose

@@ -66,8 +66,10 @@ cudaError_t gather_fields(const Grid &g, void *dst, int dst_f32, int f0, int nfs
 // ------------------------------------------------------ resting monitor ----
 // One CTA per tile: the spatial metric of the current state, and/or the
 // temporal snapshot (same lattice and slots as the fused epilogues).
+// diff: the temporal metric against snap (max |state - snap|, the fused
+// temporal monitor's reduction) in place of the range.
 __global__ void monitor_state_kernel(Grid g, int kind, int samples, int mfield, double *metric, double *snap,
-                                     int write_snap, int *flags)
+                                     int write_snap, int *flags, int diff)
 {
     __shared__ double red[8];
     const int tile = blockIdx.x;
@@ -77,7 +79,7 @@ __global__ void monitor_state_kernel(Grid g, int kind, int samples, int mfield, 
     for (int f = 0; f < g.nf; ++f) {
         if (mfield >= 0 && f != mfield) continue;
         const int slot = mfield < 0 ? f : 0;
-        double mn = samples ? INFINITY : 1.0, mx = samples ? -INFINITY : 0.0;
+        double mn = samples ? INFINITY : 1.0, mx = samples && !diff ? -INFINITY : 0.0;
         int bad = 0;
         for (int u = threadIdx.x; u < T * T; u += blockDim.x) {
             const int i = u % T, j = u / T;
@@ -95,6 +97,12 @@ __global__ void monitor_state_kernel(Grid g, int kind, int samples, int mfield, 
                 si = (ir < 0 || ic < 0) ? -1 : ir * 4 + ic;
             }
             if (si < 0) continue;
+            if (diff) {
+                const double r = samples ? snap[(int64_t)slot * g.n + c]
+                                         : snap[((int64_t)slot * g.ntx * g.nty + tile) * 16 + si];
+                mx = fmax(mx, fabs(r - v));
+                continue;
+            }
             mn = fmin(mn, v);
             mx = fmax(mx, v);
             if (write_snap) {
@@ -104,17 +112,17 @@ __global__ void monitor_state_kernel(Grid g, int kind, int samples, int mfield, 
         }
         const double bmx = block_max(mx, red);
         const double bmn = block_min(mn, red);
-        result = fmax(result, bmx - bmn);
+        result = fmax(result, diff ? bmx : bmx - bmn);
         if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(flags, 1);
     }
     if (threadIdx.x == 0 && metric) metric[tile] = result;
 }
 
 cudaError_t monitor_state(const Grid &g, int kind, int samples, int mfield, double *metric, double *snap,
-                          int write_snap, int *flags, cudaStream_t s)
+                          int write_snap, int *flags, cudaStream_t s, int diff)
 {
     monitor_state_kernel<<<g.ntx * g.nty, kThreads, 0, s>>>(g, kind, samples, mfield, metric, snap, write_snap,
-                                                          flags);
+                                                          flags, diff);
     return cudaGetLastError();
 }
 
@@ -247,6 +255,7 @@ __device__ void classify_body(const ClassifyArgs &c)
         if (nan || m >= c.thr_hi) nt = c.high_tier;
         else if (c.use_mid && m >= c.thr_lo) nt = TIER_FP32;
         else nt = TIER_HALF;
+        if (c.sched) nt = c.sched[(int64_t)min(*c.sched_i, c.sched_n - 1) * ntiles + t];
         const int old = c.tier_cur[t];
         c.tier_prev[t] = (uint8_t)old;
         c.tier_cur[t] = (uint8_t)nt;
@@ -261,6 +270,7 @@ __device__ void classify_body(const ClassifyArgs &c)
     if (threadIdx.x == 0) {
         c.stats[4] += prom;
         c.stats[5] += dem;
+        if (c.sched) *c.sched_i += 1;  // every thread read it before the barriers above
     }
     if (c.log && c.max_log > 0) {
         const int n = *c.log_n;
