@@ -297,6 +297,26 @@ def test_graph_replay_equals_eager():
     assert out[0][2] == out[1][2]
 
 
+@pytest.mark.parametrize("tile,ref_order,monitor", [(32, 0, 3), (32, 1, 2), (16, 0, 3), (16, 1, 2)])
+def test_graingrowth_fp64_tiles_staged_and_fused_agree(tile, ref_order, monitor):
+    """An adaptive run whose tiles all stay FP64 (thresholds 0): its first
+    period (every tile FP64 by construction) runs the staged FP64 kernel, the
+    later ones the fused kernel's FP64 path, monitor steps included; both
+    give the plain FP64 run's results bit for bit."""
+    w = amps()
+    p = w.Params.preset("graingrowth", 0, nx=128, ny=96, nfields=5, tile=tile, ref_order=ref_order, monitor=monitor,
+                        monitor_samples=1, thr_lo=0.0, thr_hi=0.0)
+    out = []
+    for mode in ("end2end_mix", "purehigh"):
+        with w.Simulation(p.replace(mode=mode), init=w.INIT_SEEDED) as s:
+            s.run(7)
+            s.run(28)
+            out.append(s.fields())
+            if mode == "end2end_mix":
+                assert (s.tiers() == w.TIER_FP64).all()
+    assert np.array_equal(out[0], out[1])
+
+
 @pytest.mark.parametrize("model", ["graingrowth", "kobayashi"])
 def test_profiled_run_equals_plain_and_times_every_launch(model):
     """Profiling (whole periods captured with their event records as graph

@@ -32,6 +32,10 @@ struct amps_handle {
     void *store[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};
     int parity = 0;
     bool transition = false;  // next step reads tiles at tier_prev
+    // every tile is at FP64 until the next classification (the first period
+    // of a temporal / rate monitor): grain growth takes the staged FP64 kernel
+    // when it is prepared (stage64: its FP64 staging fits in shared memory)
+    bool all_fp64 = false, stage64 = false;
     uint8_t *d_tier_prev = nullptr, *d_tier_cur = nullptr;
     int *d_lists = nullptr, *d_counts = nullptr;
     int *d_order = nullptr;  // launch order of the fused grain-growth step (adaptive runs)
@@ -56,7 +60,7 @@ struct amps_handle {
 
     int64_t step = 0;
     bool graphs = true;
-    std::map<int, cudaGraphExec_t> graph;  // key: parity | transition<<1
+    std::map<int, cudaGraphExec_t> graph;  // key: parity | transition<<1 | all_fp64<<2
     std::string err;
     // kernel timing
     bool profiling = false;
@@ -297,6 +301,12 @@ extern "C" int amps_create(const amps_params *p, amps_handle **out)
             return AMPS_ERR_CUDA;
         }
     }
+    // adaptive grain growth with an FP64 high tier: the staged FP64 kernel for
+    // periods whose tiles are all FP64 (a refused attribute leaves the fused kernel)
+    if (p->model == AMPS_GRAINGROWTH && h->mixed && high == TIER_FP64 &&
+        kernel_smem(*p, TIER_FP64, h->nf, true) <= (size_t)kMaxDynSmem)
+        h->stage64 = gg_prepare(h->T, TIER_FP64, p->ref_order != 0) == cudaSuccess;
+    cudaGetLastError();
     {
         // persistent TMA kernel (opt-in, AMPS_ENABLE_TMA=1): grain growth, 32x32 tiles, an FP32 tier, few
         // enough fields for two buffers.  Measured slower than the 4-CTA/SM staged kernel on GB300 (two
@@ -392,10 +402,12 @@ static int reclassify_resting(amps_handle *h)
                 CK(h, monitor_state(g, 2, p.monitor_samples, p.monitor_field, nullptr, h->d_snap, 1, h->d_flags,
                                     h->stream));
             // every tile to the high tier for the first period
+            h->all_fp64 = h->stage64 && h->sched_n == 0;
             std::vector<double> big(h->ntiles, 1e300);
             CK(h, cudaMemcpyAsync(h->d_metric, big.data(), sizeof(double) * h->ntiles, cudaMemcpyHostToDevice, h->stream));
             CK(h, cudaStreamSynchronize(h->stream));
         } else {
+            h->all_fp64 = false;
             CK(h, monitor_state(g, 1, p.monitor_samples, p.monitor_field, h->d_metric, nullptr, 0, h->d_flags, h->stream));
         }
         ClassifyArgs c{};
@@ -607,8 +619,9 @@ static int launch_step(amps_handle *h, int step_off, bool monitor_now)
     const bool ref = p.ref_order != 0;
     if (p.model == AMPS_GRAINGROWTH) {
         // one fused launch covers every tier (profiled per chunk by enqueue_chunk)
-        // all-FP64 runs use the staged FP64 kernel, every other mode the fused one
-        const bool only64 = h->used[TIER_FP64] && !h->used[TIER_FP32] && !h->used[TIER_HALF];
+        // all-FP64 runs and steps use the staged FP64 kernel, every other the fused one
+        const bool only64 = (h->used[TIER_FP64] && !h->used[TIER_FP32] && !h->used[TIER_HALF]) ||
+                            (h->all_fp64 && !monitor_now);
         cudaError_t e = h->use_tma ? gg_launch_tma(ref, h->tm[h->parity], a, h->tma_grid, h->stream)
                                    : gg_launch(h->T, only64 ? TIER_FP64 : -1, ref, a, h->ntiles, h->stream);
         if (e != cudaSuccess) FAIL(h, AMPS_ERR_CUDA, "step kernel launch: %s", cudaGetErrorString(e));
@@ -687,6 +700,7 @@ static int enqueue_chunk(amps_handle *h, int k0, int cnt)
     if (h->mixed && period_end) {
         CK(h, classify(classify_args(h, p.cadence, cnt), h->stream));
         h->transition = true;
+        h->all_fp64 = false;
     } else {
         CK(h, advance_period(h->d_step_base, period_end ? p.cadence : 0, cnt, h->d_counts, h->d_stats, h->stream));
     }
@@ -723,11 +737,11 @@ extern "C" int amps_run(amps_handle *h, int nsteps)
             cudaGraphExecDestroy(ex);  // freed once the launch completes
             if (e != cudaSuccess) FAIL(h, AMPS_ERR_CUDA, "graph launch: %s", cudaGetErrorString(e));
         } else if (h->graphs && !h->profiling && k0 == 0 && cnt == cad && h->stream != nullptr) {
-            const int key = h->parity | (h->transition ? 2 : 0);
+            const int key = h->parity | (h->transition ? 2 : 0) | (h->all_fp64 ? 4 : 0);
             auto it = h->graph.find(key);
             if (it == h->graph.end()) {
                 const int par0 = h->parity;
-                const bool tr0 = h->transition;
+                const bool tr0 = h->transition, all0 = h->all_fp64;
                 cudaGraph_t gr;
                 CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
                 int r = enqueue_chunk(h, 0, cad);
@@ -741,11 +755,13 @@ extern "C" int amps_run(amps_handle *h, int nsteps)
                 it = h->graph.emplace(key, ex).first;
                 h->parity = par0;  // capture advanced the host-side state; replay does it for real
                 h->transition = tr0;
+                h->all_fp64 = all0;
             }
             CK(h, cudaGraphLaunch(it->second, h->stream));
             // mirror the period's effect on the host-side state
             if (cad & 1) h->parity ^= 1;
             h->transition = h->mixed;
+            if (h->mixed) h->all_fp64 = false;
         } else {
             int r = enqueue_chunk(h, k0, cnt);
             if (r) return r;
@@ -1266,6 +1282,7 @@ static void ens_advance_host(amps_ensemble *e, int cnt, bool period_end)
     for (amps_handle *h : e->m) {
         if (cnt & 1) h->parity ^= 1;
         if (cnt > 0) h->transition = e->mixed && period_end;
+        if (e->mixed && period_end) h->all_fp64 = false;
         h->step += cnt;
     }
 }

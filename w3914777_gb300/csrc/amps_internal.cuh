@@ -657,10 +657,12 @@ __device__ __forceinline__ void mon_add_k(const StepArgs &a, MonAccF &m, int msl
                                           int64_t gidx, float v, float old)
 {
     static_assert(KIND == 2 || KIND == 3, "temporal or rate monitor");
-    m.chk = fmax_nan(m.chk, fabsf(v));
     if constexpr (KIND == 3) {
-        m.dmaxf = fmaxf(m.dmaxf, fabsf(v - old));
+        // NaN-propagating: a NaN or infinite value (or a step of more than
+        // FLT_MAX) leaves dmaxf non-finite, which mon_finish_k flags
+        m.dmaxf = fmax_nan(m.dmaxf, fabsf(v - old));
     } else {
+        m.chk = fmax_nan(m.chk, fabsf(v));
         const int si = sample_index<T>(2, a.samples, row, col);
         if (si < 0) return;
         double *sp = snap_ptr<T>(a, mslot, tile, gidx, si);
@@ -674,13 +676,15 @@ template <int KIND>
 __device__ __forceinline__ double mon_finish_k(const StepArgs &a, MonAccF &m, double *red)
 {
     double v;
+    const float chk = KIND == 3 ? m.dmaxf : m.chk;
     if constexpr (KIND == 3) {
+        // the reduction drops a thread's NaN (flagged below) as fmaxf would per cell
         const float mx = block_maxf(m.dmaxf, reinterpret_cast<float *>(red));
         v = threadIdx.x == 0 ? fmax(0.0, (double)mx * a.cadence) : 0.0;
     } else {
         v = fmax(0.0, block_max(m.dmax, red));
     }
-    if (__syncthreads_or(!(m.chk <= 3.402823466e38f)) && threadIdx.x == 0) atomicOr(a.flags, 1);
+    if (__syncthreads_or(!(chk <= 3.402823466e38f)) && threadIdx.x == 0) atomicOr(a.flags, 1);
     return v;
 }
 

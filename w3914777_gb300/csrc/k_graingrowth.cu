@@ -379,6 +379,11 @@ __device__ __forceinline__ void gg_tile_step(const StepArgs &a, float *sm, uint8
             }
             return;
         }
+        if (MK == 3 && a.nf % 8 == 0) {
+            if (tier == TIER_FP32) gg_tile_lo_rows<TIER_FP32, 8, 3>(a, sm, ss, tile, tx, ty, red);
+            else gg_tile_lo_rows<TIER_HALF, 8, 3>(a, sm, ss, tile, tx, ty, red);
+            return;
+        }
         if (MK == 3 || (MK == -1 && a.monitor_kind == 3)) {
             if (tier == TIER_FP32) gg_tile_lo_rows<TIER_FP32, 4, 3>(a, sm, ss, tile, tx, ty, red);
             else gg_tile_lo_rows<TIER_HALF, 4, 3>(a, sm, ss, tile, tx, ty, red);
