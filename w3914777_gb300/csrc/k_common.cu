@@ -185,7 +185,7 @@ __device__ void lists_from_tiers(const uint8_t *tier, int ntiles, int *lists, in
 // order.  Slow tiles then run in the first wave, where their extra time is
 // absorbed, instead of straggling at the end of the step.  Scheduling only:
 // every tile is computed by exactly one CTA either way.
-__device__ void order_slow_first(const ClassifyArgs &c, unsigned long long *ws)
+__device__ void order_slow_first(const ClassifyArgs &c, const uint8_t *tier, unsigned long long *ws)
 {
     __shared__ unsigned long long base;
     __shared__ int nslow;
@@ -208,7 +208,7 @@ __device__ void order_slow_first(const ClassifyArgs &c, unsigned long long *ws)
                             yy = yy < 0 ? 0 : (yy >= c.nty ? c.nty - 1 : yy);
                             xx = xx < 0 ? 0 : (xx >= c.ntx ? c.ntx - 1 : xx);
                         }
-                        slow |= c.tier_cur[yy * c.ntx + xx] != TIER_FP32;
+                        slow |= tier[yy * c.ntx + xx] != TIER_FP32;
                     }
             }
             // pass 0 places the slow tiles, pass 1 (after nslow of them) the others
@@ -228,11 +228,18 @@ __device__ void order_slow_first(const ClassifyArgs &c, unsigned long long *ws)
     }
 }
 
+// Tier maps of up to this many tiles are also kept in the classifying CTA's
+// shared memory, so that the lists, the launch order and the log read them
+// there instead of from global memory.
+constexpr int kClassifyShared = 8192;
+
 __device__ void classify_body(const ClassifyArgs &c)
 {
     __shared__ unsigned long long ws[32];
     __shared__ int prom, dem;
+    __shared__ uint8_t s_tier[kClassifyShared];
     const int ntiles = c.ntx * c.nty;
+    const bool in_smem = ntiles <= kClassifyShared;
     if (threadIdx.x == 0) {
         for (int k = 0; k < 3; ++k) c.stats[k] += (unsigned long long)c.counts[k] * (unsigned long long)c.stat_steps;
         c.stats[3] += 1;
@@ -259,14 +266,16 @@ __device__ void classify_body(const ClassifyArgs &c)
         const int old = c.tier_cur[t];
         c.tier_prev[t] = (uint8_t)old;
         c.tier_cur[t] = (uint8_t)nt;
+        if (in_smem) s_tier[t] = (uint8_t)nt;
         np += nt > old;
         nd += nt < old;
     }
     atomicAdd(&prom, np);
     atomicAdd(&dem, nd);
     __syncthreads();
-    lists_from_tiers(c.tier_cur, ntiles, c.lists, c.counts, ws);
-    if (c.order) order_slow_first(c, ws);
+    const uint8_t *tier = in_smem ? s_tier : c.tier_cur;
+    lists_from_tiers(tier, ntiles, c.lists, c.counts, ws);
+    if (c.order) order_slow_first(c, tier, ws);
     if (threadIdx.x == 0) {
         c.stats[4] += prom;
         c.stats[5] += dem;
@@ -276,7 +285,7 @@ __device__ void classify_body(const ClassifyArgs &c)
         const int n = *c.log_n;
         __syncthreads();
         if (n < c.max_log) {
-            for (int t = threadIdx.x; t < ntiles; t += blockDim.x) c.log[(int64_t)n * ntiles + t] = c.tier_cur[t];
+            for (int t = threadIdx.x; t < ntiles; t += blockDim.x) c.log[(int64_t)n * ntiles + t] = tier[t];
             if (threadIdx.x == 0) *c.log_n = n + 1;
         }
     }
