@@ -214,6 +214,11 @@ AMPS_API int amps_get_kernel_times(amps_handle *h, double *ms, int64_t *launches
 /* Current tier of every tile, row-major [nty][ntx] (AMPS_TIER_*).  The
  * reference keeps this as type_curr (1 = half2, 2 = high). */
 AMPS_API int amps_get_tile_tiers(amps_handle *h, uint8_t *out);
+/* The same map in the reference's type_curr encoding (get_type,
+ * snowflake/tools.h:212-230): 1 = half2 tile, 2 = high-precision tile;
+ * the FP32 tiles of a three-tier run, which have no reference counterpart,
+ * are 3. */
+AMPS_API int amps_get_tile_types(amps_handle *h, uint8_t *out);
 /* Decision log: the tier map after each classification, oldest first,
  * up to max_entries maps of ntiles bytes.  *n_out = maps written. */
 AMPS_API int amps_get_decision_log(amps_handle *h, uint8_t *out, int max_entries, int *n_out);

@@ -187,3 +187,15 @@ def test_monitor_cost_and_sweeps_run():
     assert [r["strategy"] for r in rows] == ["PURE", "AMSTENCIL", "AMSTENCIL", "GRAM1", "GRAM2"]
     assert all(r["ms"] > 0 for r in rows) and all(np.isfinite(r["error"]) for r in rows)
     assert len(E.speedup_table(rows)) == 4
+
+
+@pytest.mark.parametrize("high,thr", [(amps.TIER_FP64, (1e-4, 1e-4)), (amps.TIER_FP64, (1e-5, 1e-3)),
+                                      (amps.TIER_FP32, (1e-4, 1e-4))])
+def test_tile_types_use_the_reference_encoding(high, thr):
+    p = amps.Params.preset("graingrowth", 0, nx=128, ny=128, nfields=4, high_tier=high, thr_lo=thr[0],
+                           thr_hi=thr[1])
+    with amps.Simulation(p, init=amps.INIT_SEEDED) as s:
+        s.run(40)
+        t, ty = s.tiers(), s.tile_types()
+    want = np.where(t == amps.TIER_HALF, 1, np.where(t == high, 2, 3))
+    assert np.array_equal(ty, want) and set(np.unique(ty)) <= ({1, 2, 3} if thr[0] < thr[1] else {1, 2})

@@ -121,6 +121,7 @@ def lib():
             "amps_get_field": ([vp, ip, vp, ip, ip], ip), "amps_set_fields": ([vp, vp, ip, ip], ip),
             "amps_get_fields": ([vp, vp, ip, ip], ip), "amps_run": ([vp, ip], ip), "amps_set_graphs": ([vp, ip], ip),
             "amps_get_tile_tiers": ([vp, vp], ip), "amps_get_decision_log": ([vp, vp, ip, ctypes.POINTER(ip)], ip),
+            "amps_get_tile_types": ([vp, vp], ip),
             "amps_get_tile_metric": ([vp, vp], ip), "amps_get_stats": ([vp, ctypes.POINTER(Stats)], ip),
             "amps_set_tier_schedule": ([vp, vp, ip], ip), "amps_set_tile_tiers": ([vp, vp], ip),
             "amps_measure_tiles": ([vp, ip, vp], ip),
@@ -254,6 +255,12 @@ class Simulation:
     def tiers(self):
         out = np.empty(self.ntiles, dtype=np.uint8)
         self._ck(lib().amps_get_tile_tiers(self.h, out.ctypes.data), "amps_get_tile_tiers")
+        return out
+
+    def tile_types(self):
+        """The tier map in the reference's type_curr encoding (1 half2, 2 high, 3 FP32)."""
+        out = np.empty(self.ntiles, dtype=np.uint8)
+        self._ck(lib().amps_get_tile_types(self.h, out.ctypes.data), "amps_get_tile_types")
         return out
 
     def metric(self):

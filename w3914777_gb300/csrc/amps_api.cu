@@ -781,6 +781,15 @@ extern "C" int amps_get_tile_tiers(amps_handle *h, uint8_t *out)
     return AMPS_OK;
 }
 
+extern "C" int amps_get_tile_types(amps_handle *h, uint8_t *out)
+{
+    const int r = amps_get_tile_tiers(h, out);
+    if (r) return r;
+    const int high = h->p.high_tier;
+    for (int t = 0; t < h->ntiles; ++t) out[t] = out[t] == TIER_HALF ? 1 : (out[t] == high ? 2 : 3);
+    return AMPS_OK;
+}
+
 extern "C" int amps_get_tile_metric(amps_handle *h, double *out)
 {
     if (!h || !out) return AMPS_ERR_INVALID;
