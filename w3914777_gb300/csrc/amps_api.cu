@@ -497,16 +497,14 @@ static int set_impl(amps_handle *h, int f0, int nfs, const void *src, int dtype,
     if (dtype == AMPS_F64) {
         CK(h, cudaMemcpyAsync(dst, src, cnt * 8, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->stream));
     } else {
-        // float input: widen through the pinned buffer (host) or in place (device)
+        // float input (a set-up path, not the time loop): widened to double
+        // on the host, through the pinned buffer
+        CK(h, cudaStreamSynchronize(h->stream));
         if (on_device) {
-            Grid g = live;  // reuse the gather kernel's conversion by copying through d_partials is awkward;
-            (void)g;        // convert on the host side instead
-            CK(h, cudaStreamSynchronize(h->stream));
             std::vector<float> tmp(cnt);
             CK(h, cudaMemcpy(tmp.data(), src, cnt * 4, cudaMemcpyDeviceToHost));
             for (size_t i = 0; i < cnt; ++i) h->h_pinned[i] = tmp[i];
         } else {
-            CK(h, cudaStreamSynchronize(h->stream));
             for (size_t i = 0; i < cnt; ++i) h->h_pinned[i] = ((const float *)src)[i];
         }
         CK(h, cudaMemcpyAsync(dst, h->h_pinned, cnt * 8, cudaMemcpyHostToDevice, h->stream));
