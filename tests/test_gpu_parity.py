@@ -136,6 +136,59 @@ def test_graingrowth_fp64_vs_oracle_q_general(q, stencil, bc):
     assert e <= 1e-12
 
 
+@pytest.mark.parametrize("model,nx,ny,tile,bc", [
+    ("graingrowth", 32, 32, 32, 0), ("graingrowth", 32, 32, 32, 1), ("graingrowth", 16, 16, 16, 0),
+    ("graingrowth", 64, 32, 32, 0), ("graingrowth", 16, 48, 16, 1),
+    ("kobayashi", 16, 16, 16, 0), ("kobayashi", 32, 32, 32, 1), ("kobayashi", 32, 64, 32, 0)])
+def test_smallest_grids_fp64_vs_oracle(model, nx, ny, tile, bc):
+    """Grids of one tile, or one tile across: every periodic neighbour of a
+    tile is the tile itself (or its one partner), and the zero-flux mirror
+    folds the halo back into it."""
+    w = amps()
+    steps = 20
+    if model == "graingrowth":
+        p = w.Params.preset("graingrowth", 0, mode="purehigh", nx=nx, ny=ny, tile=tile, nfields=3, bc=bc,
+                            ref_order=1, dt=0.05, init_amp=0.3)
+        f0 = w.init_host(p, w.INIT_SEEDED)
+        with w.Simulation(p, init=w.INIT_SEEDED) as s:
+            s.run(steps)
+            f = s.fields()
+        o = ob.gg_run(ob.gg_params(nx, ny, q=3, bc=bc, dx=1.0, dy=1.0, dt=0.05, mobil=1.0, grcoef=2.0, gamma=1.5),
+                      list(f0), steps)
+        e = max(rel_err(f[k], o[k]) for k in range(3))
+    else:
+        p = w.Params.preset("kobayashi", 4, mode="purehigh", nx=nx, ny=ny, tile=tile, bc=bc, noise=0.01, seed=7,
+                            init_offset=1, init_r2=20.0)
+        f0 = w.init_host(p, w.INIT_REFERENCE)
+        with w.Simulation(p, init=w.INIT_REFERENCE) as s:
+            s.run(steps)
+            f = s.fields()
+        q = ob.kob_params(nx, ny, bc=bc, aniso=p.aniso, theta0=p.theta0, noise=0.01, seed=7)
+        phi, T = ob.kob_run(q, f0[0], f0[1], steps)
+        e = max(rel_err(f[0], phi), rel_err(f[1], T))
+    print(f"{model} {nx}x{ny} tile {tile} bc {bc}: {e:.3e}")
+    assert e <= 1e-12
+
+
+@pytest.mark.parametrize("nx,ny,bc", [(32, 32, 0), (64, 32, 1), (32, 96, 0)])
+def test_smallest_grids_adaptive_decisions_match_oracle(nx, ny, bc):
+    """The fused grain-growth step, its rate monitor and the classification
+    on grids one tile wide or high."""
+    w = amps()
+    p = w.Params.preset("graingrowth", 0, nx=nx, ny=ny, nfields=4, bc=bc, monitor=w.MONITOR_RATE,
+                        monitor_samples=1, thr_lo=1e-5, thr_hi=3e-3, max_log=16)
+    with w.Simulation(p, init=w.INIT_SEEDED) as s:
+        s.run(39)
+        prev = s.fields()
+        s.run(1)
+        now = s.fields()
+        m_gpu, t_gpu, st = s.metric(), s.tiers(), s.stats()
+    m, t = _oracle_decisions(w, s, p, prev, now)
+    assert np.array_equal(m_gpu, m)
+    assert np.array_equal(t_gpu, t)
+    assert sum(st["tile_steps"]) == 40 * t.size
+
+
 @pytest.mark.parametrize("ref_order,bc", [(1, 0), (0, 0), (0, 1)])
 def test_sintering_fp64_vs_oracle_n_particles(ref_order, bc):
     """ref_order=0: the FMA-form FP64 tiles, computed in 8-row bands on
