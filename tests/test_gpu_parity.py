@@ -170,6 +170,45 @@ def test_smallest_grids_fp64_vs_oracle(model, nx, ny, tile, bc):
     assert e <= 1e-12
 
 
+@pytest.mark.parametrize("nx,ny,tile,bc,ref_order", [(32, 32, 32, 0, 1), (32, 32, 32, 1, 0), (32, 32, 32, 0, 0),
+                                                     (32, 64, 16, 0, 1)])
+def test_smallest_grids_sintering_fp64_vs_oracle(nx, ny, tile, bc, ref_order):
+    """Sintering on one tile (or one tile across): the chemical potential's
+    2-cell halo wraps or mirrors into the tile itself."""
+    w = amps()
+    p = w.Params.preset("sintering", 0, mode="purehigh", nx=nx, ny=ny, tile=tile, nfields=2, rmin=3, rmax=5,
+                        ref_order=ref_order, bc=bc)
+    f0 = w.init_host(p, w.INIT_SEEDED)
+    with w.Simulation(p, init=w.INIT_SEEDED) as s:
+        s.run(20)
+        f = s.fields()
+    op = ob.sint_params(nx, ny, n=2, coefm=p.coefm, coefk=p.coefk, coefl=p.coefl, dsur=p.dsur, bc=bc)
+    c, e = ob.sint_run(op, f0[0], list(f0[1:]), 20)
+    errs = [rel_err(f[0], c)] + [rel_err(f[k + 1], e[k]) for k in range(2)]
+    print(f"sintering {nx}x{ny} tile {tile} bc {bc} ref {ref_order}:", errs)
+    assert max(errs) <= 1e-12
+
+
+@pytest.mark.parametrize("nx,ny,tile,monitor", [(32, 32, 32, 1), (32, 32, 16, 2), (64, 32, 32, 3)])
+def test_smallest_grids_kobayashi_decisions_match_oracle(nx, ny, tile, monitor):
+    """Kobayashi's per-tier kernels, monitor and classification on grids of
+    one or two tiles across."""
+    w = amps()
+    thr = (0.3, 0.6) if monitor == 1 else (1e-4, 1e-2)
+    p = w.Params.preset("kobayashi", 2, mode="end2end_mix", nx=nx, ny=ny, tile=tile, monitor=monitor,
+                        monitor_samples=0, thr_lo=thr[0], thr_hi=thr[1], init_r2=40.0, init_offset=1, max_log=16)
+    back = 1 if monitor == 3 else 10
+    with w.Simulation(p, init=w.INIT_REFERENCE) as s:
+        s.run(50 - back)
+        prev = s.fields()
+        s.run(back)
+        now = s.fields()
+        m_gpu, t_gpu = s.metric(), s.tiers()
+    m, t = _oracle_decisions(w, s, p, prev, now)
+    assert np.array_equal(m_gpu, m)
+    assert np.array_equal(t_gpu, t)
+
+
 @pytest.mark.parametrize("nx,ny,bc", [(32, 32, 0), (64, 32, 1), (32, 96, 0)])
 def test_smallest_grids_adaptive_decisions_match_oracle(nx, ny, bc):
     """The fused grain-growth step, its rate monitor and the classification
