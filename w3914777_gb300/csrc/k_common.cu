@@ -153,6 +153,50 @@ __device__ __forceinline__ unsigned long long block_scan(unsigned long long v, u
     return r;
 }
 
+// Inclusive scan of two 64-bit packed counters at once (the barriers of one
+// scan); *ta, *tb: the block's totals.
+__device__ __forceinline__ void block_scan2(unsigned long long &a, unsigned long long &b, unsigned long long *ws,
+                                            unsigned long long *ta, unsigned long long *tb)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (int)(blockDim.x >> 5);
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long ua = __shfl_up_sync(0xffffffffu, a, o);
+        const unsigned long long ub = __shfl_up_sync(0xffffffffu, b, o);
+        if (lane >= o) {
+            a += ua;
+            b += ub;
+        }
+    }
+    if (lane == 31) {
+        ws[w] = a;
+        ws[32 + w] = b;
+    }
+    __syncthreads();
+    if (w == 0) {
+        unsigned long long sa = lane < nw ? ws[lane] : 0ull, sb = lane < nw ? ws[32 + lane] : 0ull;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned long long ua = __shfl_up_sync(0xffffffffu, sa, o);
+            const unsigned long long ub = __shfl_up_sync(0xffffffffu, sb, o);
+            if (lane >= o) {
+                sa += ua;
+                sb += ub;
+            }
+        }
+        ws[lane] = sa;
+        ws[32 + lane] = sb;
+    }
+    __syncthreads();
+    if (w > 0) {
+        a += ws[w - 1];
+        b += ws[32 + w - 1];
+    }
+    *ta = ws[nw - 1];
+    *tb = ws[32 + nw - 1];
+    __syncthreads();
+}
+
 // Ordered compaction of the tiles of each tier (tier maps are small: one
 // 1024-thread CTA loops over them).
 __device__ void lists_from_tiers(const uint8_t *tier, int ntiles, int *lists, int *counts, unsigned long long *ws)
@@ -228,6 +272,44 @@ __device__ void order_slow_first(const ClassifyArgs &c, const uint8_t *tier, uns
     }
 }
 
+// lists_from_tiers and order_slow_first in one pass, for maps of at most one
+// tile per thread: one scan of two packed counters -- the tier ranks, and
+// the slow (low 32 bits) / all-FP32 (high 32 bits) ranks of the launch
+// order.  Same lists, counts and order as the two routines.
+__device__ void lists_and_order(const ClassifyArgs &c, const uint8_t *tier, unsigned long long *ws)
+{
+    const int ntiles = c.ntx * c.nty;
+    const int t = threadIdx.x;
+    int k = -1;
+    bool slow = false;
+    if (t < ntiles) {
+        k = tier[t];
+        const int x = t % c.ntx, y = t / c.ntx;
+        for (int dy = -1; dy <= 1; ++dy)
+            for (int dx = -1; dx <= 1; ++dx) {
+                int yy = y + dy, xx = x + dx;
+                if (c.bc == 0) {
+                    yy = yy < 0 ? yy + c.nty : (yy >= c.nty ? yy - c.nty : yy);
+                    xx = xx < 0 ? xx + c.ntx : (xx >= c.ntx ? xx - c.ntx : xx);
+                } else {
+                    yy = yy < 0 ? 0 : (yy >= c.nty ? c.nty - 1 : yy);
+                    xx = xx < 0 ? 0 : (xx >= c.ntx ? c.ntx - 1 : xx);
+                }
+                slow |= tier[yy * c.ntx + xx] != TIER_FP32;
+            }
+    }
+    const unsigned long long ma = k >= 0 ? (1ull << (21 * k)) : 0ull;
+    const unsigned long long mb = k >= 0 ? (slow ? 1ull : (1ull << 32)) : 0ull;
+    unsigned long long a = ma, b = mb, ta, tb;
+    block_scan2(a, b, ws, &ta, &tb);
+    if (k >= 0) {
+        const unsigned long long ea = a - ma, eb = b - mb;
+        c.lists[k * ntiles + (int)((ea >> (21 * k)) & 0x1FFFFF)] = t;
+        c.order[slow ? (int)(eb & 0xFFFFFFFFull) : (int)(tb & 0xFFFFFFFFull) + (int)(eb >> 32)] = t;
+    }
+    if (t < 3) c.counts[t] = (int)((ta >> (21 * t)) & 0x1FFFFF);
+}
+
 // Tier maps of up to this many tiles are also kept in the classifying CTA's
 // shared memory, so that the lists, the launch order and the log read them
 // there instead of from global memory.
@@ -235,7 +317,7 @@ constexpr int kClassifyShared = 8192;
 
 __device__ void classify_body(const ClassifyArgs &c)
 {
-    __shared__ unsigned long long ws[32];
+    __shared__ unsigned long long ws[64];
     __shared__ int prom, dem;
     __shared__ uint8_t s_tier[kClassifyShared];
     const int ntiles = c.ntx * c.nty;
@@ -274,8 +356,12 @@ __device__ void classify_body(const ClassifyArgs &c)
     atomicAdd(&dem, nd);
     __syncthreads();
     const uint8_t *tier = in_smem ? s_tier : c.tier_cur;
-    lists_from_tiers(tier, ntiles, c.lists, c.counts, ws);
-    if (c.order) order_slow_first(c, tier, ws);
+    if (c.order && ntiles <= (int)blockDim.x) {
+        lists_and_order(c, tier, ws);
+    } else {
+        lists_from_tiers(tier, ntiles, c.lists, c.counts, ws);
+        if (c.order) order_slow_first(c, tier, ws);
+    }
     if (threadIdx.x == 0) {
         c.stats[4] += prom;
         c.stats[5] += dem;
