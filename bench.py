@@ -712,11 +712,27 @@ def run_configs(kob_steps=2000, sint_steps=20000):
 def run_profile_case(args):
     """A short, untimed run of a tuned workload at nx^2 for ncu captures
     (`--profile-case 2048` puts a 256 MiB FP32 grain-growth state, larger than
-    L2; `--profile-model kobayashi|sintering` the other models' tuned runs)."""
+    L2; `--profile-model kobayashi|sintering` the other models' tuned runs;
+    `graingrowth-adjoint`: sim-steps FP32 step + adjoint-step pairs of the
+    Q = 8 grain-growth module from the seeded state)."""
     import torch
     import w3914777_gb300 as w
     torch.cuda.set_device(0)
     model = args.profile_model
+    if model == "graingrowth-adjoint":
+        from w3914777_gb300 import adjoint
+        p = w.Params.preset("graingrowth", 0, nx=args.profile_case, ny=args.profile_case)
+        st = adjoint.Stepper(p, torch.float32)
+        x = torch.tensor(w.init_host(p, w.INIT_SEEDED), dtype=torch.float32, device="cuda")
+        y, g, gi = torch.empty_like(x), torch.ones_like(x), torch.empty_like(x)
+        gp = torch.zeros(3, dtype=torch.float64, device="cuda")
+        for i in range(args.sim_steps):
+            st.forward(x, i, out=y)
+            st.adjoint(x, g, i, gp, grad_in=gi)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": args.profile_case, "steps": args.sim_steps, "model": model,
+                          "grad_in_norm": float(gi.norm())}))
+        return
     p = w.Params.preset(model, 0, nx=args.profile_case, ny=args.profile_case)
     if model == "graingrowth":
         tuned = load_tuned()
@@ -747,7 +763,8 @@ def main():
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--no-configs", action="store_true")
     ap.add_argument("--profile-case", type=int, default=0)
-    ap.add_argument("--profile-model", default="graingrowth", choices=["graingrowth", "kobayashi", "sintering"])
+    ap.add_argument("--profile-model", default="graingrowth",
+                    choices=["graingrowth", "kobayashi", "sintering", "graingrowth-adjoint"])
     args = ap.parse_args()
     if args.profile_case:
         run_profile_case(args)
