@@ -714,11 +714,27 @@ def run_profile_case(args):
     (`--profile-case 2048` puts a 256 MiB FP32 grain-growth state, larger than
     L2; `--profile-model kobayashi|sintering` the other models' tuned runs;
     `graingrowth-adjoint`: sim-steps FP32 step + adjoint-step pairs of the
-    Q = 8 grain-growth module from the seeded state)."""
+    Q = 8 grain-growth module from the seeded state; `ensemble`: the first
+    profile-case members of the 64-member ensemble workload)."""
     import torch
     import w3914777_gb300 as w
     torch.cuda.set_device(0)
     model = args.profile_model
+    if model == "ensemble":
+        from w3914777_gb300 import ensemble
+        tuned = load_tuned()
+        ov = dict(tuned["overrides"]) if tuned else {}
+        ov.pop("tile", None)
+        params = ensemble.member_params(count=64, seed=2024, overrides=ov)[:args.profile_case]
+        sims = [w.Simulation(p, init=w.INIT_SEEDED) for p in params]
+        with w.Ensemble(sims) as ens:
+            ens.run(args.sim_steps)
+            ens.synchronize()
+        for sm in sims:
+            sm.close()
+        print(json.dumps({"profile_case": args.profile_case, "steps": args.sim_steps, "model": model,
+                          "cells_per_step": ensemble.cells(params)}))
+        return
     if model == "graingrowth-adjoint":
         from w3914777_gb300 import adjoint
         p = w.Params.preset("graingrowth", 0, nx=args.profile_case, ny=args.profile_case)
@@ -764,7 +780,7 @@ def main():
     ap.add_argument("--no-configs", action="store_true")
     ap.add_argument("--profile-case", type=int, default=0)
     ap.add_argument("--profile-model", default="graingrowth",
-                    choices=["graingrowth", "kobayashi", "sintering", "graingrowth-adjoint"])
+                    choices=["graingrowth", "kobayashi", "sintering", "graingrowth-adjoint", "ensemble"])
     args = ap.parse_args()
     if args.profile_case:
         run_profile_case(args)
