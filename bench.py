@@ -144,20 +144,41 @@ def cpu_threads():
         return os.cpu_count() or 1
 
 
-def oracle_rate(nx, q, steps, threads):
-    """FP64 oracle grain-growth step on the host cores: Gcell-updates/s."""
+def _oracle(threads):
+    """The oracle's timed build (tests/oracle_bind.py, liboracle_fast.so: -O3,
+    fused multiply-add, OpenMP over rows).  Loads no part of the product."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     os.environ["OMP_NUM_THREADS"] = str(threads)
     import oracle_bind as ob
-    import w3914777_gb300 as w
-    p = w.Params.preset("graingrowth", 0, nx=nx, ny=nx, nfields=q)
-    f0 = w.init_host(p, w.INIT_SEEDED)
+    return ob
+
+
+def oracle_rate(nx, q, steps, threads):
+    """The reference's FP64 grain-growth update (graingrowth/function.h:5-30,
+    Q-general Fan-Chen form) as a host OpenMP loop: Gcell-updates/s over
+    `steps` steps of the seeded nx^2 Q-field start."""
+    ob = _oracle(threads)
+    f0 = ob.gg_init_uniform(nx, nx, q, 1e-3, 1234)
     op = ob.gg_params(nx, nx, q=q, dx=1.0, dy=1.0, dt=0.05, mobil=1.0, grcoef=2.0, gamma=1.5)
-    ob.gg_run(op, list(f0), 1)  # warm the thread pool
+    ob.gg_run(op, f0, 1, fast=True)  # warm the thread pool
     t0 = time.perf_counter()
-    ob.gg_run(op, list(f0), steps)
+    ob.gg_run(op, f0, steps, fast=True)
     dt = time.perf_counter() - t0
     return nx * nx * steps / dt / 1e9, dt
+
+
+def oracle_rate_kobayashi(steps, threads, n=512):
+    """The reference's FP64 Kobayashi update (snowflake/function.h:5-60) as a
+    host OpenMP loop on the 512^2 plain-FP64 dendrite (zero flux, disc r^2 < 25
+    at the centre, seeded noise 0.01): Gcell-updates/s over `steps` steps."""
+    ob = _oracle(threads)
+    phi, T = ob.kob_init_disc(n, n, n // 2, n // 2, 25.0)
+    kp = ob.kob_params(n, n, bc=1, kappa=1.6, theta0=0.2, noise=0.01, seed=1234)
+    ob.kob_run(kp, phi, T, 1, fast=True)
+    t0 = time.perf_counter()
+    ob.kob_run(kp, phi, T, steps, fast=True)
+    dt = time.perf_counter() - t0
+    return n * n * steps / dt / 1e9, dt
 
 
 def run_reference(args):
@@ -173,16 +194,22 @@ def run_reference(args):
             rates.append((r, dt))
     value = statistics.median([r for r, _ in rates])
     ms = statistics.median([dt for _, dt in rates]) * 1e3
+    kob, kdt = oracle_rate_kobayashi(args.ref_sample_steps, threads)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "Gcell-updates/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
         "config": {"workload": WORKLOAD, "nx": 1024, "ny": 1024, "Q": 8,
-                   "sample": f"{sample} FP64 steps of the 1024^2 Q=8 grid per bench step"},
+                   "sample": f"{sample} FP64 steps of the 1024^2 Q=8 grid per bench step (the rate of the "
+                             "update; the GPU arm's run is 10000 adaptive steps)"},
         "cpu_baseline": {"value": value, "unit": "Gcell-updates/s", "cores": threads, "kind": "port",
-                         "sample": f"{sample} steps of 1024x1024 Q=8 FP64 (oracle restatement of "
-                                   "graingrowth/function.h:5-30, OpenMP over rows)"},
+                         "sample": f"{sample} steps of 1024x1024 Q=8 FP64 (the oracle's restatement of "
+                                   "graingrowth/function.h:5-30, built -O3 with fused multiply-add, "
+                                   "OpenMP over rows)"},
         "e2e": {"value": value, "unit": "Gcell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "configs": {"kobayashi_plain_fp64_512": {
+            "value": kob, "unit": "Gcell-updates/s", "cores": threads,
+            "sample": f"{args.ref_sample_steps} FP64 steps of the 512^2 zero-flux dendrite ({kdt:.2f} s)"}},
     }
     print(json.dumps(line), flush=True)
 
@@ -334,7 +361,9 @@ def run_ours(args):
         threads = cpu_threads()
         r, dt = oracle_rate(1024, 8, args.ref_sample_steps, threads)
         cpu = {"value": r, "unit": "Gcell-updates/s", "cores": threads, "kind": "port",
-               "sample": f"{args.ref_sample_steps} FP64 steps of the 1024x1024 Q=8 grid ({dt:.1f} s)"}
+               "sample": f"{args.ref_sample_steps} FP64 steps of the 1024x1024 Q=8 grid ({dt:.1f} s; the "
+                         "oracle's restatement of graingrowth/function.h:5-30 built -O3 with fused "
+                         "multiply-add, OpenMP over rows)"}
 
     per_run_launches = klaunch[3] + S // p.cadence + 4  # update kernels + classifications + set_fields kernels
     ts = stats["tile_steps"]
@@ -772,7 +801,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--sim-steps", type=int, default=10000)
-    ap.add_argument("--ref-sample-steps", type=int, default=100)
+    ap.add_argument("--ref-sample-steps", type=int, default=500)
     ap.add_argument("--tile", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")

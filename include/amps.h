@@ -62,6 +62,11 @@ enum { AMPS_KOBAYASHI = 0, AMPS_GRAINGROWTH = 1, AMPS_SINTERING = 2 };
  * (snowflake/function.h:72-79) */
 enum { AMPS_PUREHIGH = 0, AMPS_PURELOW = 1, AMPS_END2END_MIX = 2, AMPS_GRAM1 = 3, AMPS_GRAM2 = 4 };
 
+/* Largest tile count of one grid: the classification ranks each tier's
+ * tiles in a 21-bit field of a packed 64-bit counter.  amps_check_params
+ * rejects grids with more tiles (e.g. 16x16 tiles beyond about 23000^2). */
+#define AMPS_MAX_TILES 0x1FFFFF
+
 /* storage / arithmetic tiers of a tile */
 enum { AMPS_TIER_HALF = 0, AMPS_TIER_FP32 = 1, AMPS_TIER_FP64 = 2 };
 

@@ -128,6 +128,15 @@ void orc_gg_init_circle(int nx, int ny, double rx, double ry, double r, double *
         }
 }
 
+void orc_gg_init_uniform(int nx, int ny, int q, double amp, uint64_t seed, double *const *eta)
+{
+    /* no reference counterpart: eta_i ~ U[-amp, amp) i.i.d., keyed by
+     * (seed, field, cell) through the counter-based generator above */
+    const int64_t n = (int64_t)nx * ny;
+    for (int f = 0; f < q; ++f)
+        for (int64_t i = 0; i < n; ++i) eta[f][i] = amp * (2.0 * orc_uniform01(seed, (uint64_t)f, (uint64_t)i) - 1.0);
+}
+
 void orc_gg_step(const orc_gg_params *p, double *const *eta_in, double *const *eta_out)
 {
     const int nx = p->nx, ny = p->ny, bc = p->bc, q = p->q;
@@ -160,6 +169,58 @@ void orc_gg_step(const orc_gg_params *p, double *const *eta_in, double *const *e
                 eta_out[a][i] = ea - dtm * (dfd - p->grcoef * lap);
             }
         }
+    }
+}
+
+/* The timed CPU baseline of the same update (not a checker): fields outer,
+ * one row at a time, the per-cell sum of squares S = sum_b eta_b^2 formed
+ * once per row and sum_{b!=a} taken as S - eta_a^2, so the interior loop
+ * over x is branch-free and vectorises.  Agrees with orc_gg_step to rounding
+ * (tests/test_oracle_golden.py). */
+static inline double gg_cell_fast(int stencil, const double *rd, const double *rc, const double *ru, int xs1,
+                                  int x, int xa1, double S, double inv, double dtm, double g2, double kap)
+{
+    const double lap = stencil == 0
+                           ? rd[xs1] + rd[x] + rd[xa1] + rc[xs1] + rc[xa1] + ru[xs1] + ru[x] + ru[xa1] - 8.0 * rc[x]
+                           : rc[xs1] + rc[xa1] + rd[x] + ru[x] - 4.0 * rc[x];
+    const double ea = rc[x];
+    const double dfd = g2 * ea * (S - ea * ea) + ea * ea * ea - ea;
+    return ea - dtm * (dfd - kap * lap * inv);
+}
+
+static void gg_row_fast(const orc_gg_params *p, double *const *eta_in, double *const *eta_out, int y,
+                        double *S)
+{
+    const int nx = p->nx, ny = p->ny, bc = p->bc, q = p->q, st = p->stencil;
+    const double inv = 1.0 / (p->dx * p->dy), dtm = p->dt * p->mobil, g2 = 2.0 * p->gamma, kap = p->grcoef;
+    const int ys1 = nb(y - 1, ny, bc), ya1 = nb(y + 1, ny, bc);
+    for (int x = 0; x < nx; ++x) S[x] = 0.0;
+    for (int b = 0; b < q; ++b) {
+        const double *restrict e = eta_in[b] + (int64_t)y * nx;
+        for (int x = 0; x < nx; ++x) S[x] += e[x] * e[x];
+    }
+    for (int a = 0; a < q; ++a) {
+        const double *restrict rd = eta_in[a] + (int64_t)ys1 * nx;
+        const double *restrict rc = eta_in[a] + (int64_t)y * nx;
+        const double *restrict ru = eta_in[a] + (int64_t)ya1 * nx;
+        double *restrict o = eta_out[a] + (int64_t)y * nx;
+        /* edge columns through the boundary map, the interior branch-free */
+        o[0] = gg_cell_fast(st, rd, rc, ru, nb(-1, nx, bc), 0, nb(1, nx, bc), S[0], inv, dtm, g2, kap);
+        for (int x = 1; x < nx - 1; ++x)
+            o[x] = gg_cell_fast(st, rd, rc, ru, x - 1, x, x + 1, S[x], inv, dtm, g2, kap);
+        if (nx > 1)
+            o[nx - 1] = gg_cell_fast(st, rd, rc, ru, nx - 2, nx - 1, nb(nx, nx, bc), S[nx - 1], inv, dtm, g2, kap);
+    }
+}
+
+void orc_gg_step_fast(const orc_gg_params *p, double *const *eta_in, double *const *eta_out)
+{
+#pragma omp parallel
+    {
+        double *S = (double *)malloc((size_t)p->nx * sizeof(double));
+#pragma omp for schedule(static)
+        for (int y = 0; y < p->ny; ++y) gg_row_fast(p, eta_in, eta_out, y, S);
+        free(S);
     }
 }
 

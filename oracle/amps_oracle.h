@@ -55,8 +55,16 @@ typedef struct {
  * graingrowth/function.h:5-30 generalised to q fields:
  * dfd_i = 1.0*(2.0*gamma*eta_i*sum_{j!=i} pow(eta_j,2) + pow(eta_i,3) - eta_i). */
 void orc_gg_step(const orc_gg_params *p, double *const *eta_in, double *const *eta_out);
+/* The same update restructured for speed (fields outer, a row at a time,
+ * sum_{j!=i} eta_j^2 as S - eta_i^2): the timed CPU baseline, not a checker;
+ * equal to orc_gg_step to rounding. */
+void orc_gg_step_fast(const orc_gg_params *p, double *const *eta_in, double *const *eta_out);
 /* Circle initial state: graingrowth/tools.h:24-38 (eta2=1 inside radius R). */
 void orc_gg_init_circle(int nx, int ny, double rx, double ry, double r, double *eta1, double *eta2);
+
+/* Seeded start of the multi-grain workloads (no reference counterpart):
+ * eta_i ~ U[-amp, amp) i.i.d. from orc_uniform01(seed, i, cell). */
+void orc_gg_init_uniform(int nx, int ny, int q, double amp, uint64_t seed, double *const *eta);
 
 /* ---- sintering (Cahn-Hilliard c + Allen-Cahn eta_i) -------------------- */
 typedef struct {

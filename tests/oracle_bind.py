@@ -47,24 +47,28 @@ def ptr_array(arrs):
     return t
 
 
-_lib = None
+_libs = {}
 
 
-def build_oracle():
-    subprocess.run(["make", "-s", "-C", ORACLE_DIR, "liboracle.so"], check=True)
+def build_oracle(target="liboracle.so"):
+    subprocess.run(["make", "-s", "-C", ORACLE_DIR, target], check=True)
 
 
-def lib():
-    global _lib
-    if _lib is None:
-        path = os.path.join(ORACLE_DIR, "liboracle.so")
+def lib(fast=False):
+    """The oracle library.  fast=False: the checker (-O2, no fused
+    multiply-add: the reference's rounding); fast=True: the same source at -O3
+    with fused multiply-add, the timed CPU baseline (never a checker)."""
+    name = "liboracle_fast.so" if fast else "liboracle.so"
+    if name not in _libs:
+        path = os.path.join(ORACLE_DIR, name)
         if not os.path.exists(path):
-            build_oracle()
+            build_oracle(name)
         L = ctypes.CDLL(path)
         L.orc_kob_step.argtypes = [ctypes.POINTER(KobParams), _dp, _dp, _dp, ctypes.c_int64]
         L.orc_kob_init_disc.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                         ctypes.c_double, _dp, _dp]
         L.orc_gg_step.argtypes = [ctypes.POINTER(GGParams), ctypes.c_void_p, ctypes.c_void_p]
+        L.orc_gg_step_fast.argtypes = [ctypes.POINTER(GGParams), ctypes.c_void_p, ctypes.c_void_p]
         L.orc_gg_init_circle.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                          ctypes.c_double, _dp, _dp]
         L.orc_sint_step.argtypes = [ctypes.POINTER(SintParams), _dp, ctypes.c_void_p, ctypes.c_void_p, _dp]
@@ -78,8 +82,10 @@ def lib():
         L.orc_uniform01.restype = ctypes.c_double
         L.orc_hash3.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64]
         L.orc_hash3.restype = ctypes.c_uint64
-        _lib = L
-    return _lib
+        L.orc_gg_init_uniform.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                          ctypes.c_uint64, ctypes.c_void_p]
+        _libs[name] = L
+    return _libs[name]
 
 
 # ------------------------------------------------------------ Kobayashi ----
@@ -91,12 +97,13 @@ def kob_params(nx, ny, bc=0, **kw):
     return KobParams(nx=nx, ny=ny, bc=bc, **d)
 
 
-def kob_run(p, phi, T, steps, step0=0):
+def kob_run(p, phi, T, steps, step0=0, fast=False):
     phi = np.ascontiguousarray(phi, dtype=np.float64).copy()
     T = np.ascontiguousarray(T, dtype=np.float64).copy()
     s = np.zeros(6 * p.nx * p.ny)
+    L = lib(fast)
     for k in range(steps):
-        lib().orc_kob_step(ctypes.byref(p), ptr(phi), ptr(T), ptr(s), step0 + k)
+        L.orc_kob_step(ctypes.byref(p), ptr(phi), ptr(T), ptr(s), step0 + k)
     return phi, T
 
 
@@ -115,14 +122,24 @@ def gg_params(nx, ny, q=2, bc=0, stencil=0, **kw):
     return GGParams(nx=nx, ny=ny, bc=bc, q=q, stencil=stencil, **d)
 
 
-def gg_run(p, etas, steps):
+def gg_run(p, etas, steps, fast=False):
+    """steps of the grain-growth update; fast=True: the timed baseline's
+    restructured loop in the -O3 build (equal to the checker to rounding)."""
     cur = [np.ascontiguousarray(e, dtype=np.float64).copy() for e in etas]
     nxt = [np.empty_like(e) for e in cur]
+    L = lib(fast)
+    step = L.orc_gg_step_fast if fast else L.orc_gg_step
     for _ in range(steps):
-        lib().orc_gg_step(ctypes.byref(p), ctypes.cast(ptr_array(cur), ctypes.c_void_p),
-                          ctypes.cast(ptr_array(nxt), ctypes.c_void_p))
+        step(ctypes.byref(p), ctypes.cast(ptr_array(cur), ctypes.c_void_p), ctypes.cast(ptr_array(nxt), ctypes.c_void_p))
         cur, nxt = nxt, cur
     return cur
+
+
+def gg_init_uniform(nx, ny, q, amp, seed):
+    """The seeded multi-grain start: eta_i ~ U[-amp, amp) from (seed, i, cell)."""
+    etas = [np.zeros((ny, nx)) for _ in range(q)]
+    lib().orc_gg_init_uniform(nx, ny, q, amp, seed, ctypes.cast(ptr_array(etas), ctypes.c_void_p))
+    return etas
 
 
 def gg_init_circle(nx, ny, rx, ry, r):

@@ -45,6 +45,20 @@ def test_status_strings_and_errors_never_exit():
     assert e.value.status == 1
 
 
+def test_tile_count_limit():
+    """The classification's packed counters hold 21 bits per tier, so a grid
+    of more than 0x1FFFFF tiles is rejected before any allocation."""
+    w = amps()
+    # 16^2 tiles: 23168^2 / 256 = 2,096,704 tiles fits; 23184^2 (2,099,601) does not
+    ok = w.Params.preset("graingrowth", 1, nx=23168, ny=23168, tile=16)
+    assert ok.check()[0] == 0
+    big = w.Params.preset("graingrowth", 1, nx=23184, ny=23184, tile=16)
+    rc, msg = big.check()
+    assert rc == 1 and "too many tiles" in msg
+    # the same grid with 32^2 tiles is a quarter of the count and is accepted
+    assert big.replace(tile=32, nx=23200, ny=23200).check()[0] == 0
+
+
 @pytest.mark.parametrize("k", [1, 2, 3, 4, 5])
 def test_presets_mirror_reference_parameter_files(k):
     w = amps()

@@ -59,7 +59,7 @@ def foreign_binary(path):
 
 def build(verbose=False, force=False, extra_flags=()):
     os.makedirs(OBJ, exist_ok=True)
-    for path in (LIB, os.path.join(ROOT, "oracle", "liboracle.so")):
+    for path in (LIB, os.path.join(ROOT, "oracle", "liboracle.so"), os.path.join(ROOT, "oracle", "liboracle_fast.so")):
         if foreign_binary(path):
             os.remove(path)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]

@@ -158,6 +158,11 @@ extern "C" int amps_check_params(const amps_params *p, char *msg, size_t len)
     if (p->nx < p->tile || p->ny < p->tile || p->nx % p->tile || p->ny % p->tile)
         BAD("nx, ny (%d, %d) must be positive multiples of the tile (%d)", p->nx, p->ny, p->tile);
     if ((int64_t)p->nx * p->ny > (int64_t)1 << 31) BAD("grid too large");
+    // the classification ranks each tier's tiles in a 21-bit field of one
+    // packed 64-bit counter (three tiers per scan)
+    if ((int64_t)(p->nx / p->tile) * (p->ny / p->tile) > AMPS_MAX_TILES)
+        BAD("too many tiles (%lld > %lld): use the larger tile",
+            (long long)(p->nx / p->tile) * (p->ny / p->tile), (long long)AMPS_MAX_TILES);
     if (p->bc != AMPS_BC_PERIODIC && p->bc != AMPS_BC_NOFLUX) BAD("unknown boundary condition %d", p->bc);
     if (p->high_tier != AMPS_TIER_FP64 && p->high_tier != AMPS_TIER_FP32) BAD("high_tier must be FP64 or FP32");
     if (p->model == AMPS_GRAINGROWTH && (p->nfields < 1 || p->nfields > 32)) BAD("grain growth Q must be 1..32");

@@ -1,6 +1,7 @@
 // k_common.cu -- utility kernels of libamps: tiered state <-> row-major
 // arrays, the monitor on a resting state, tile classification with ordered
 // per-tier work lists, and deterministic FP64 reductions.
+#include "../../include/amps.h"
 #include "amps_kernels.h"
 
 namespace amps {
@@ -212,14 +213,14 @@ __device__ void lists_from_tiers(const uint8_t *tier, int ntiles, int *lists, in
         const unsigned long long b = base;
         if (k >= 0) {
             const unsigned long long excl = b + inc - mine;
-            const int rank = (int)((excl >> (21 * k)) & 0x1FFFFF);
+            const int rank = (int)((excl >> (21 * k)) & AMPS_MAX_TILES);
             lists[k * ntiles + rank] = t;
         }
         __syncthreads();
         if (threadIdx.x == blockDim.x - 1) base = b + inc;
         __syncthreads();
     }
-    if (threadIdx.x < 3) counts[threadIdx.x] = (int)((base >> (21 * threadIdx.x)) & 0x1FFFFF);
+    if (threadIdx.x < 3) counts[threadIdx.x] = (int)((base >> (21 * threadIdx.x)) & AMPS_MAX_TILES);
 }
 
 // Launch order of the fused grain-growth step: first the tiles that take
@@ -304,10 +305,10 @@ __device__ void lists_and_order(const ClassifyArgs &c, const uint8_t *tier, unsi
     block_scan2(a, b, ws, &ta, &tb);
     if (k >= 0) {
         const unsigned long long ea = a - ma, eb = b - mb;
-        c.lists[k * ntiles + (int)((ea >> (21 * k)) & 0x1FFFFF)] = t;
+        c.lists[k * ntiles + (int)((ea >> (21 * k)) & AMPS_MAX_TILES)] = t;
         c.order[slow ? (int)(eb & 0xFFFFFFFFull) : (int)(tb & 0xFFFFFFFFull) + (int)(eb >> 32)] = t;
     }
-    if (t < 3) c.counts[t] = (int)((ta >> (21 * t)) & 0x1FFFFF);
+    if (t < 3) c.counts[t] = (int)((ta >> (21 * t)) & AMPS_MAX_TILES);
 }
 
 // Tier maps of up to this many tiles are also kept in the classifying CTA's

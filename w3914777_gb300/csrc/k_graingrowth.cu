@@ -651,12 +651,22 @@ __global__ void __launch_bounds__(kThreads, 2)
         const int tier = a.tier_out[t];
         float *sm = buf0 + b * bufstride;
         if (fast) {
-            const bool ok = mbar_wait_bounded(&mbar[b], b ? ph1 : ph0);
+            const uint32_t par = b ? ph1 : ph0;
+            const bool ok = mbar_wait_bounded(&mbar[b], par);
             if (b) ph1 ^= 1u; else ph0 ^= 1u;
             if (__syncthreads_or(!ok)) {
-                // give up: flag it, let the copy already in flight land (bounded), leave
-                if (threadIdx.x == 0) atomicOr(a.flags, 2);
-                if (fast_s[b ^ 1]) mbar_wait_bounded(&mbar[b ^ 1], b ? ph0 : ph1);
+                // Give up: flag it, then give both copies that may still be in
+                // flight -- this buffer's (the one that timed out) and the
+                // prefetch into the other -- a second bounded wait before the
+                // CTA leaves, so that neither lands in shared memory after it.
+                // A copy that never completes cannot be recovered here: the
+                // flag makes the host report AMPS_ERR_TIMEOUT.
+                // The CTA's shared memory stays allocated while thread 0 waits.
+                if (threadIdx.x == 0) {
+                    atomicOr(a.flags, 2);
+                    if (!ok) mbar_wait_bounded(&mbar[b], par);
+                    if (fast_s[b ^ 1]) mbar_wait_bounded(&mbar[b ^ 1], b ? ph0 : ph1);
+                }
                 return;
             }
             if (tier == TIER_FP32) gg_tile_lo<T, TIER_FP32>(a, sm, t, tx, ty, red);

@@ -115,7 +115,15 @@ extern "C" int amps_reduce_noalloc(const double *data, int64_t n, int kind, doub
     if (partials_for_current_device(&partials) != cudaSuccess) return AMPS_ERR_CUDA;
     const int nblocks = (int)((n + AMPS_REDUCE_NOALLOC_CELLS_PER_BLOCK - 1) / AMPS_REDUCE_NOALLOC_CELLS_PER_BLOCK);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    noalloc_partial_kernel<<<nblocks, kNoAllocThreads, 0, s>>>(data, n, kind, partials);
-    noalloc_final_kernel<<<1, 32, 0, s>>>(partials, nblocks, kind, out);
-    return cudaGetLastError() == cudaSuccess ? AMPS_OK : AMPS_ERR_CUDA;
+    // cudaLaunchKernel returns this launch's own status; an error left
+    // pending on the calling thread by earlier, unrelated work is neither
+    // reported here nor cleared.
+    void *pargs[] = {(void *)&data, (void *)&n, (void *)&kind, (void *)&partials};
+    if (cudaLaunchKernel((const void *)noalloc_partial_kernel, dim3(nblocks), dim3(kNoAllocThreads), pargs, 0, s) !=
+        cudaSuccess)
+        return AMPS_ERR_CUDA;
+    void *fargs[] = {(void *)&partials, (void *)&nblocks, (void *)&kind, (void *)&out};
+    if (cudaLaunchKernel((const void *)noalloc_final_kernel, dim3(1), dim3(32), fargs, 0, s) != cudaSuccess)
+        return AMPS_ERR_CUDA;
+    return AMPS_OK;
 }
