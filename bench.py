@@ -350,10 +350,32 @@ def run_ours(args):
         fp64_ms = a.elapsed_time(b)
         final64 = s64.fields()
         grains64 = s64.grains(threshold=0.5)
-        # the reference's error metric: mean |a - b| over the grid (graingrowth/end2enderror.py:34)
-        mean_abs = max(s64.compare_all(f, final_mixed[f])["mean_abs"] for f in range(nf))
+        # per field: max-abs, RMS (L2 / sqrt(cells)) and the reference's error
+        # metric, mean |a - b| over the grid (graingrowth/end2enderror.py:34)
+        per_field = [s64.compare_all(f, final_mixed[f]) for f in range(nf)]
+    mean_abs = max(e["mean_abs"] for e in per_field)
     plain = cells * S / (fp64_ms * 1e-3) / 1e9
     err = float(np.max(np.abs(final_mixed - final64)))
+
+    # ---- all-FP32 path on the same workload (what the adaptive run is beside) ----
+    p32 = p.replace(mode="purehigh", high_tier=w.TIER_FP32)
+    with w.Simulation(p32) as s32:
+        s32.set_stream(stream.cuda_stream)
+        with torch.cuda.stream(stream):
+            s32.set_fields_device(dev0.data_ptr())
+            s32.run(2 * p.cadence)
+            s32.set_fields_device(dev0.data_ptr())
+            torch.cuda.synchronize()
+            flush.zero_()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            s32.run(S)
+            b.record(stream)
+        torch.cuda.synchronize()
+        fp32_ms = a.elapsed_time(b)
+        err32 = float(np.max(np.abs(s32.fields() - final64)))
+    all_fp32 = cells * S / (fp32_ms * 1e-3) / 1e9
 
     # ---- CPU baseline (oracle port on host cores), rank 0 only ----
     cpu = None
@@ -366,8 +388,14 @@ def run_ours(args):
                          "multiply-add, OpenMP over rows)"}
 
     per_run_launches = klaunch[3] + S // p.cadence + 4  # update kernels + classifications + set_fields kernels
-    ts = stats["tile_steps"]
+    # tile-steps of one run (the profiled one); the warm start (first period,
+    # every tile FP64, for the temporal and rate monitors) separated out
+    ts = ktiles[:3]
     tot = max(sum(ts), 1)
+    ntiles = (p.nx // T) * (p.ny // T)
+    warm = p.cadence * ntiles if p.monitor != w.MONITOR_SPA else 0
+    ts_after = [ts[0], ts[1], ts[2] - warm]
+    tot_after = max(sum(ts_after), 1)
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "Gcell-updates/s", "n_gpus": world, "steps": args.steps,
@@ -385,14 +413,25 @@ def run_ours(args):
                        "parallelism": f"replicas x{world}"},
             "e2e": {"value": e2e, "unit": "Gcell-updates/s", "h2d_bytes_per_step": bytes_io,
                     "d2h_bytes_per_step": bytes_io, "ms_per_step": e2e_total / len(e2e_ms)},
-            "plain_fp64": {"value": plain, "unit": "Gcell-updates/s", "ms_per_run": fp64_ms},
+            "plain_fp64": {"value": plain, "unit": "Gcell-updates/s", "ms_per_run": fp64_ms,
+                           "arithmetic": "FP64 in fused multiply-add form (ref_order=0), equal to the oracle "
+                                         "to <= 1e-12 relative (tests/test_gpu_parity.py)"},
+            "all_fp32": {"value": all_fp32, "unit": "Gcell-updates/s", "ms_per_run": fp32_ms,
+                         "max_abs_err_vs_fp64": err32},
             "speedup_vs_plain_fp64": value / plain,
             "max_abs_err_vs_fp64": err,
             "mean_abs_err_vs_fp64": mean_abs,
+            "errors_vs_fp64_per_field": [{"field": f"eta{k + 1}", **per_field[k]} for k in range(nf)],
             "grains": {"adaptive": grains_mixed, "fp64": grains64,
                        "note": "connected regions of the dominant eta (>= 0.5), periodic"},
             "tier_mix": {"half": ts[0] / tot, "fp32": ts[1] / tot, "fp64": ts[2] / tot},
-            "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak,
+            "tier_mix_after_warm_start": {"half": ts_after[0] / tot_after, "fp32": ts_after[1] / tot_after,
+                                          "fp64": ts_after[2] / tot_after,
+                                          "note": f"the first {p.cadence} steps run every tile in FP64 "
+                                                  "(the reference's warm start); the thresholds "
+                                                  f"[{p.thr_lo:g}, {p.thr_hi:g}] promote no tile to FP64 "
+                                                  "afterwards on this workload" if ts_after[2] == 0 else ""},
+            "roofline": {"bound": "hbm", "l2_resident": True, "kernel": names[dom], "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                          "peak_source": f"{peak_kind} hbm_gbs",
                          "algorithmic_bytes_per_launch": per_launch_bytes,
@@ -407,6 +446,8 @@ def run_ours(args):
         }
         if cpu:
             line["cpu_baseline"] = cpu
+        if world == 1 and not args.no_hbm:
+            line["roofline_hbm"] = run_roofline_hbm(p, peak, peak_kind)
         # single-GPU evidence: measured at N=1 only
         if world == 1 and not args.no_adjoint:
             line["adjoint"] = run_adjoint()
@@ -419,6 +460,43 @@ def run_ours(args):
     sim.close()
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def run_roofline_hbm(p, peak, peak_kind, n=4096, warm=30, steps=200):
+    """The headline step kernel where HBM, not L2, serves the state: the same
+    tuned adaptive workload at 4096^2 (Q = 8: 512 MiB of FP32 state per
+    parity, four times the L2).  After `warm` steps (the all-FP64 warm-start
+    period and two more), `steps` profiled steps: each launch timed with CUDA
+    events on its stream; algorithmic bytes per launch as in the headline."""
+    import w3914777_gb300 as w
+    q = p.replace(nx=n, ny=n)
+    with w.Simulation(q, init=w.INIT_SEEDED) as s:
+        s.run(warm)
+        s.set_profiling(True)
+        s.run(steps)
+        kms, klaunch, ktiles = s.kernel_times()
+        s.set_profiling(False)
+    T, nf = q.tile, q.num_fields
+    algo = sum(ktiles[k] * T * T * nf * 2 * (2, 4, 8)[k] for k in range(3))
+    launches = max(klaunch[3], 1)
+    per_launch_s = kms[3] * 1e-3 / launches
+    achieved = algo / launches / per_launch_s / 1e9 if per_launch_s > 0 else 0.0
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        try:
+            with open(tpath) as f:
+                traffic = json.load(f).get("gg_step_kernel_4096_bytes_per_launch")
+        except Exception:
+            traffic = None
+    tot = max(sum(ktiles[:3]), 1)
+    return {"bound": "hbm", "kernel": "gg_step_kernel", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": traffic, "peak_source": f"{peak_kind} hbm_gbs",
+            "algorithmic_bytes_per_launch": algo / launches, "us_per_launch": per_launch_s * 1e6,
+            "workload": f"the headline's tuned adaptive grain growth at {n}x{n}, Q={nf}: steps {warm + 1}.."
+                        f"{warm + steps} (after the warm start), state {n * n * nf * 4 / 2**20:.0f} MiB per "
+                        "parity in FP32 > L2",
+            "tier_mix": {k: ktiles[i] / tot for i, k in enumerate(("half", "fp32", "fp64"))}}
 
 
 def run_adjoint(steps=1000, segment=32, n=256):
@@ -648,7 +726,16 @@ def run_ensemble(steps=5000, check_steps=1000, count=64, seed=2024):
     }
 
 
-def run_configs(kob_steps=2000, sint_steps=20000):
+def field_errors(a, b, names):
+    """Per field: max |a - b|, RMS (the L2 norm over sqrt(cells)) and mean |a - b|."""
+    out = {}
+    for k, name in enumerate(names):
+        d = np.abs(a[k] - b[k])
+        out[name] = {"max_abs": float(d.max()), "rms": float(np.sqrt(np.mean(d * d))), "mean_abs": float(d.mean())}
+    return out
+
+
+def run_configs(kob_steps=2000, sint_steps=20000, cpu_sample=200):
     """The other two models' seeded workloads at their tuned settings
     (w3914777_gb300/tuned/*.json), each against its plain FP64 run from the
     same initial state: Kobayashi dendrite 512^2 zero-flux with noise, 2000
@@ -702,15 +789,27 @@ def run_configs(kob_steps=2000, sint_steps=20000):
     # plain runs in the FMA form (ref_order=0), as the adaptive run's FP64 tiles
     ms_64, f_64, x_64, _ = run(p.replace(mode=w.PUREHIGH, high_tier=w.TIER_FP64, ref_order=0), init, kob_steps)
     ms_32, f_32, _, _ = run(p.replace(mode=w.PUREHIGH, high_tier=w.TIER_FP32, ref_order=0), init, kob_steps)
+    # the plain FP64 dendrite in the reference's expression order (snowflake/function.h:5-60,
+    # no fused multiply-add): the 512^2, 2000-step FP64 configuration as the reference computes it
+    ms_64r, f_64r, _, _ = run(p.replace(mode=w.PUREHIGH, high_tier=w.TIER_FP64, ref_order=1), init, kob_steps)
+    # ... and on the host cores (the oracle's -O3 build), a bounded sample of the same steps
+    kob_cpu, kob_cpu_s = oracle_rate_kobayashi(cpu_sample, cpu_threads())
     cells = p.nx * p.ny * kob_steps
     out["kobayashi"] = {
         "workload": f"Kobayashi dendrite {p.nx}x{p.ny} zero-flux, seeded noise, disc r^2<{p.init_r2:g} at the centre, "
                     f"{kob_steps} steps, tuned spatial monitor",
         "value": cells / (ms_a * 1e-3) / 1e9, "unit": "Gcell-updates/s",
         "plain_fp64": cells / (ms_64 * 1e-3) / 1e9, "all_fp32": cells / (ms_32 * 1e-3) / 1e9,
+        "plain_fp64_reference_order": {
+            "value": cells / (ms_64r * 1e-3) / 1e9, "unit": "Gcell-updates/s", "ms": ms_64r,
+            "max_abs_vs_fma_form": float(np.abs(f_64r - f_64).max())},
+        "cpu_baseline": {"value": kob_cpu, "unit": "Gcell-updates/s", "cores": cpu_threads(), "kind": "port",
+                         "sample": f"{cpu_sample} FP64 steps of the same 512^2 dendrite ({kob_cpu_s:.2f} s; the "
+                                   "oracle's restatement of snowflake/function.h:5-60 built -O3, OpenMP over rows)"},
         "speedup_vs_plain_fp64": ms_64 / ms_a,
         "max_abs_err_vs_fp64": float(np.abs(f_a - f_64).max()),
         "mean_abs_err_vs_fp64": float(np.abs(f_a - f_64).mean()),
+        "errors_vs_fp64_per_field": field_errors(f_a, f_64, ("phi", "T")),
         "all_fp32_max_abs_err": float(np.abs(f_32 - f_64).max()),
         "interface": {"adaptive": x_a["interface"], "fp64": x_64["interface"]},
         "tier_mix": dict(zip(("half", "fp32", "fp64"), mix)),
@@ -729,6 +828,7 @@ def run_configs(kob_steps=2000, sint_steps=20000):
         "plain_fp64": cells / (ms_64 * 1e-3) / 1e9, "speedup_vs_plain_fp64": ms_64 / ms_a,
         "max_abs_err_vs_fp64": float(np.abs(f_a - f_64).max()),
         "mean_abs_err_vs_fp64": float(np.abs(f_a - f_64).mean()),
+        "errors_vs_fp64_per_field": field_errors(f_a, f_64, ["c"] + [f"eta{k + 1}" for k in range(p.nfields)]),
         "mass_drift": {"adaptive": (x_a["mass"] - m0) / m0, "fp64": (x_64["mass"] - m0) / m0,
                        "note": "relative change of the FP64 sum of c; the reference clamps c to [0,1] after each "
                                "step (sintering/function.h:100-101), which removes mass in both runs"},
@@ -807,6 +907,7 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--no-configs", action="store_true")
+    ap.add_argument("--no-hbm", action="store_true")
     ap.add_argument("--profile-case", type=int, default=0)
     ap.add_argument("--profile-model", default="graingrowth",
                     choices=["graingrowth", "kobayashi", "sintering", "graingrowth-adjoint", "ensemble"])
