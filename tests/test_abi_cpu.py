@@ -29,7 +29,7 @@ def test_library_exports_every_declared_symbol():
     assert len(syms) >= 20
     missing = [s for s in syms if not hasattr(L, s)]
     assert not missing, missing
-    assert L.amps_abi_version() == 1
+    assert L.amps_abi_version() == 2
 
 
 def test_status_strings_and_errors_never_exit():

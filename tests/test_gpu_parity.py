@@ -400,14 +400,17 @@ def test_mixed_error_envelope_kobayashi():
 
 
 def _spread_thresholds(w, p, steps, f0):
-    """Thresholds at the 40th and 85th percentile of the monitor metric seen
-    after `steps` steps of an all-FP64 run of the same workload, so that a
-    run with them populates all three tiers."""
+    """Thresholds from the monitor metric seen after `steps` steps of an
+    all-FP64 run of the same workload: half the smallest positive value (so
+    tiles whose metric is exactly 0 -- the sintering bulk -- go to half) and
+    the 70th percentile of the positive values, so that a run with them
+    populates all three tiers."""
     with w.Simulation(p.replace(thr_lo=0.0, thr_hi=0.0)) as s:
         s.set_fields(f0)
         s.run(steps)
         m = s.metric().ravel()
-    lo, hi = np.quantile(m, 0.40), np.quantile(m, 0.85)
+    pos = m[m > 0]
+    lo, hi = 0.5 * pos.min(), np.quantile(pos, 0.7)
     return float(lo), float(max(hi, lo))
 
 
@@ -436,7 +439,7 @@ def test_sintering_decisions_match_oracle(monitor, samples):
           np.bincount(t.ravel(), minlength=3))
     assert np.array_equal(m_gpu, m)
     assert np.array_equal(t_gpu, t)
-    assert len(np.unique(t)) >= 2
+    assert len(np.unique(t)) == 3
     assert sum(st["tile_steps"]) == 60 * t.size
 
 

@@ -7,6 +7,8 @@ machine without the reference tree) the committed golden fixtures, which were
 generated from those same builds by tests/golden/make_golden.py, pin the
 oracle instead (tests/test_oracle_golden.py).
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -69,3 +71,20 @@ def test_classify_is_non_periodic_five_point_max():
     assert t[3, 0] == 0 and t[0, 3] == 0 and t[1, 1] == 0
     t3 = ob.classify(np.array([[0.0, 0.2], [0.6, 0.0]]), 0.1, 0.5)
     assert t3.tolist() == [[2, 1], [2, 2]]
+
+
+@pytest.mark.parametrize("monitor,thr", [(2, 1e-4), (1, 0.5)])
+def test_reference_mixed_golden_comes_from_the_reference_kernels(monitor, thr):
+    """tests/golden/graingrowth_mix_ref.npz (the reference's AMSTENCIL runs,
+    made by tests/golden/make_golden_mix.py): its first periods' tier maps
+    are what the reference's kernels, compiled here for the CPU, produce."""
+    import importlib.util
+    if not os.path.exists(os.path.join(ob.REF_DIR, f"libref_ggmix_m{monitor}.so")):
+        pytest.skip("oracle/_ref not built (no reference tree)")
+    spec = importlib.util.spec_from_file_location(
+        "make_golden_mix", os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "make_golden_mix.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "graingrowth_mix_ref.npz"))
+    types, _, _ = mg.run_mix(monitor, thr, steps=30)
+    assert np.array_equal(types, g[mg.key(monitor, thr) + "_types"][:3])

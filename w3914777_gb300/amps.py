@@ -24,6 +24,7 @@ PUREHIGH, PURELOW, END2END_MIX, GRAM1, GRAM2 = 0, 1, 2, 3, 4
 TIER_HALF, TIER_FP32, TIER_FP64 = 0, 1, 2
 BC_PERIODIC, BC_NOFLUX = 0, 1
 MONITOR_SPA, MONITOR_TEM, MONITOR_RATE = 1, 2, 3
+HALF_FP32, HALF_REF, HALF_HFMA2 = 0, 1, 2
 F64, F32 = 0, 1
 INIT_REFERENCE, INIT_SEEDED = 0, 1
 REDUCE_SUM, REDUCE_MIN, REDUCE_MAX, REDUCE_SUMSQ = 0, 1, 2, 3
@@ -44,7 +45,8 @@ _DBL_FIELDS = ["thr_lo", "thr_hi", "gram_ratio", "dx", "dy", "dt", "tau", "epsb"
 class Params(ctypes.Structure):
     """amps_params (include/amps.h)."""
     _fields_ = ([(n, ctypes.c_int) for n in _INT_FIELDS] + [(n, ctypes.c_double) for n in _DBL_FIELDS]
-                + [("init_offset", ctypes.c_int), ("seed", ctypes.c_uint64)])
+                + [("init_offset", ctypes.c_int), ("seed", ctypes.c_uint64), ("half_arith", ctypes.c_int),
+                   ("ref_snapshot", ctypes.c_int)])
 
     @classmethod
     def preset(cls, model, preset=0, **overrides):

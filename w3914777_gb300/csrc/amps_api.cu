@@ -41,6 +41,9 @@ struct amps_handle {
     int *d_order = nullptr;  // launch order of the fused grain-growth step (adaptive runs)
     double *d_metric = nullptr, *d_snap = nullptr;
     int nmon = 0;
+    // ref_snapshot (grain growth, Kobayashi; temporal monitor on the lattice):
+    // the snapshot as it stood after the last classification
+    double *d_snap_keep = nullptr;
     // tier schedule (amps_set_tier_schedule): sched_n maps of ntiles bytes,
     // the next one to use at *d_sched_i
     uint8_t *d_sched = nullptr;
@@ -161,6 +164,11 @@ static Phys make_phys(const amps_params &p)
     ph.gg_g2 = (float)(2.0 * ph.gamma);
     ph.gg_kap = (float)ph.grcoef;
     ph.gg_inv = (float)ph.inv_dxdy;
+    {
+        const double gh[8] = {ph.dt, ph.mobil, ph.grcoef, ph.dxdy, ph.gamma, ph.dt * ph.mobil,
+                              ph.grcoef * ph.inv_dxdy, 2.0 * ph.gamma};
+        for (int i = 0; i < 8; ++i) ph.gg_h[i] = __half_as_ushort(__float2half_rn((float)gh[i]));
+    }
     double *k = ph.kd;
     if (p.model == AMPS_KOBAYASHI) {
         k[KB_HX] = 0.5 / ph.dx; k[KB_HY] = 0.5 / ph.dy; k[KB_ANISO] = ph.aniso; k[KB_THETA0] = ph.theta0;
@@ -196,7 +204,7 @@ static void free_all(amps_handle *h)
             if (h->store[t][q]) cudaFree(h->store[t][q]);
     void *ps[] = {h->d_tier_prev, h->d_tier_cur, h->d_lists, h->d_order, h->d_counts, h->d_metric, h->d_snap, h->d_stats,
                   h->d_flags, h->d_log, h->d_log_n, h->d_step_base, h->d_stage, h->d_partials, h->d_out,
-                  h->d_diag, h->d_sched, h->d_sched_i, h->d_msnap, h->d_mmetric};
+                  h->d_diag, h->d_sched, h->d_sched_i, h->d_msnap, h->d_mmetric, h->d_snap_keep};
     for (void *q : ps)
         if (q) cudaFree(q);
     if (h->h_pinned) cudaFreeHost(h->h_pinned);
@@ -258,6 +266,9 @@ extern "C" int amps_create(const amps_params *p, amps_handle **out)
     h->nmon = p->monitor_field < 0 ? h->nf : 1;
     const size_t snap = p->monitor_samples ? (size_t)h->nmon * h->n : (size_t)h->nmon * h->ntiles * 16;
     ALLOC(h->d_snap, sizeof(double) * snap, "monitor snapshot");
+    if (p->ref_snapshot && p->monitor == AMPS_MONITOR_TEM && !p->monitor_samples && p->model != AMPS_SINTERING &&
+        h->mixed)
+        ALLOC(h->d_snap_keep, sizeof(double) * snap, "reference snapshot");
     ALLOC(h->d_stats, sizeof(unsigned long long) * 8, "stats");
     ALLOC(h->d_flags, sizeof(int) * 4, "flags");
     ALLOC(h->d_log_n, sizeof(int), "log count");
@@ -288,7 +299,7 @@ extern "C" int amps_create(const amps_params *p, amps_handle **out)
         cudaError_t pe;
         if (p->model == AMPS_GRAINGROWTH) {
             const bool only64 = h->used[TIER_FP64] && !h->used[TIER_FP32] && !h->used[TIER_HALF];
-            pe = gg_prepare(h->T, only64 ? TIER_FP64 : -1, p->ref_order != 0);
+            pe = gg_prepare(h->T, only64 ? TIER_FP64 : -1, p->ref_order != 0, p->half_arith);
         }
         else if (p->model == AMPS_KOBAYASHI) pe = kob_prepare(h->T, t, p->ref_order != 0);
         else pe = sint_prepare(h->T, t, p->ref_order != 0, p->mu_lap_fp64 != 0);
@@ -305,7 +316,7 @@ extern "C" int amps_create(const amps_params *p, amps_handle **out)
     // periods whose tiles are all FP64 (a refused attribute leaves the fused kernel)
     if (p->model == AMPS_GRAINGROWTH && h->mixed && high == TIER_FP64 &&
         kernel_smem(*p, TIER_FP64, h->nf, true) <= (size_t)kMaxDynSmem)
-        h->stage64 = gg_prepare(h->T, TIER_FP64, p->ref_order != 0) == cudaSuccess;
+        h->stage64 = gg_prepare(h->T, TIER_FP64, p->ref_order != 0, 0) == cudaSuccess;
     cudaGetLastError();
     {
         // persistent TMA kernel (opt-in, AMPS_ENABLE_TMA=1): grain growth, 32x32 tiles, an FP32 tier, few
@@ -314,7 +325,7 @@ extern "C" int amps_create(const amps_params *p, amps_handle **out)
         const bool only64 = h->used[TIER_FP64] && !h->used[TIER_FP32] && !h->used[TIER_HALF];
         const char *on = getenv("AMPS_ENABLE_TMA");
         if (p->model == AMPS_GRAINGROWTH && p->tile == 32 && h->used[TIER_FP32] && !only64 && h->nf <= kTmaMaxFields &&
-            on && on[0] == '1') {
+            p->half_arith == AMPS_HALF_FP32 && on && on[0] == '1') {
             int bps = 0, dev = 0, sms = 0;
             if (encode_field_map(&h->tm[0], h->store[TIER_FP32][0], p->nx, p->ny, h->nf) &&
                 encode_field_map(&h->tm[1], h->store[TIER_FP32][1], p->nx, p->ny, h->nf) &&
@@ -423,6 +434,8 @@ static int reclassify_resting(amps_handle *h)
             c.sched = h->d_sched; c.sched_n = h->sched_n; c.sched_i = h->d_sched_i;
         }
         CK(h, classify(c, h->stream));
+        if (h->d_snap_keep && !h->sched_n)
+            CK(h, snap_ref_fixup(h->d_snap, h->d_snap_keep, h->d_tier_cur, h->ntiles, h->nmon, h->stream));
         h->transition = true;
     }
     return AMPS_OK;
@@ -574,6 +587,7 @@ static StepArgs step_args(const amps_handle *h, int parity, bool transition, int
     a.mfield = p.monitor_field;
     a.mu_lap_fp64 = p.mu_lap_fp64;
     a.cadence = p.cadence;
+    a.half_arith = p.half_arith;
     a.metric = h->d_metric;
     a.snap = h->d_snap;
     a.flags = h->d_flags;
@@ -697,6 +711,8 @@ static int enqueue_chunk(amps_handle *h, int k0, int cnt)
     }
     if (h->mixed && period_end) {
         CK(h, classify(classify_args(h, p.cadence, cnt), h->stream));
+        if (h->d_snap_keep && !h->sched_n)
+            CK(h, snap_ref_fixup(h->d_snap, h->d_snap_keep, h->d_tier_cur, h->ntiles, h->nmon, h->stream));
         h->transition = true;
         h->all_fp64 = false;
     } else {
@@ -1166,6 +1182,12 @@ extern "C" int amps_ensemble_create(amps_handle *const *members, int count, amps
     *out = nullptr;
     if (!members || count < 1) return AMPS_ERR_INVALID;
     amps_handle *h0 = members[0];
+    for (int i = 0; i < count; ++i)
+        if (members[i] && (members[i]->p.half_arith != AMPS_HALF_FP32 || members[i]->d_snap_keep)) {
+            g_create_err = "amps_ensemble_create: members with binary16 arithmetic or the reference's snapshot "
+                           "rule run only through amps_run";
+            return AMPS_ERR_UNSUPPORTED;
+        }
     for (int i = 0; i < count; ++i) {
         amps_handle *h = members[i];
         if (!h || h->p.model != AMPS_GRAINGROWTH || h->T != h0->T || h->p.cadence != h0->p.cadence ||

@@ -175,6 +175,10 @@ extern "C" int amps_check_params(const amps_params *p, char *msg, size_t len)
     if (!(p->dx > 0) || !(p->dy > 0) || !(p->dt > 0)) BAD("dx, dy, dt must be positive");
     if (p->mode == AMPS_GRAM1 || p->mode == AMPS_GRAM2)
         if (!(p->gram_ratio >= 0 && p->gram_ratio <= 1)) BAD("gram_ratio must be in [0,1]");
+    if (p->half_arith < AMPS_HALF_FP32 || p->half_arith > AMPS_HALF_HFMA2) BAD("half_arith must be 0, 1 or 2");
+    if (p->half_arith != AMPS_HALF_FP32 && p->model != AMPS_GRAINGROWTH)
+        BAD("binary16 arithmetic (half_arith %d) is built for grain growth only", p->half_arith);
+    if (p->ref_snapshot != 0 && p->ref_snapshot != 1) BAD("ref_snapshot must be 0 or 1");
     if (msg && len) msg[0] = 0;
     return AMPS_OK;
 #undef BAD

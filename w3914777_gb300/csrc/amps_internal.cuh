@@ -36,6 +36,10 @@ struct Phys {
     // a handful of FP64 conversions per thread and tile cost ~18% of a step):
     // (float)(dt*L), (float)(2*gamma), (float)kappa, (float)(1/dxdy)
     float gg_dtm, gg_g2, gg_kap, gg_inv;
+    // grain growth's binary16 constants (half_arith != 0; enum GgHalf): each
+    // double constant rounded to float, then to half, as the reference's
+    // __float2half2_rn(double) calls do (graingrowth/end2end_mix.cu:59-67)
+    unsigned short gg_h[8];
     // Kobayashi and sintering constants of the non-reference-order tiles,
     // derived on the host in double (kd) and rounded to float (kf), the same
     // values the tiles would derive per thread (index: enum KConst)
@@ -52,6 +56,10 @@ enum KConst {
     SN_INV = 0, SN_B, SN_A2, SN_HCM, SN_DVOL, SN_DVAP, SN_DSUR, SN_DGRB, SN_DT, SN_B12, SN_DTL, SN_HCK,
     KCONST_MAX = 24
 };
+
+// Indices of Phys::gg_h: dt, L, kappa, dx*dy, gamma (the reference's
+// AMPS_HALF_REF expressions) and dt*L, kappa/(dx*dy), 2*gamma (the HFMA2 form).
+enum GgHalf { GH_DT, GH_MOB, GH_KAP, GH_DXDY, GH_GAM, GH_DTM, GH_KINV, GH_G2 };
 
 // Constant i of Phys::kd / Phys::kf at the tile's compute type.
 template <typename CT> __device__ __forceinline__ CT kc(const Phys &ph, int i);
@@ -71,6 +79,7 @@ struct StepArgs {
     int64_t n;                // nx*ny
     // monitor (active when monitor_now != 0)
     int monitor_now, monitor_kind, samples, mfield, mu_lap_fp64, cadence;
+    int half_arith;           // grain growth: AMPS_HALF_FP32 / _REF / _HFMA2 (half tiles' arithmetic)
     double *metric;           // [ntiles]
     double *snap;             // temporal snapshot: [nmon][ntiles][16] or [nmon][n]
     int *flags;               // bit 0: NaN/Inf seen; bit 1: a bounded device wait gave up

@@ -17,7 +17,11 @@ cudaError_t kob_prepare_lo(int tile);
 cudaError_t sint_prepare_lo(int tile, bool mu64);
 // Raise the dynamic shared-memory limit of the kernel a launch would use
 // (must run before any graph capture).
-cudaError_t gg_prepare(int tile, int tier, bool ref);
+cudaError_t gg_prepare(int tile, int tier, bool ref, int half_arith);
+// The fused step with binary16 arithmetic on half tiles (half_arith 1 or 2;
+// k_gg_half.cu), called by gg_launch / gg_prepare.
+cudaError_t gg_launch_half(int tile, bool ref, const StepArgs &a, int grid, size_t smem, cudaStream_t s);
+cudaError_t gg_prepare_half(int tile, bool ref, int half_arith);
 cudaError_t kob_prepare(int tile, int tier, bool ref);
 cudaError_t sint_prepare(int tile, int tier, bool ref, bool mu64);
 // Persistent TMA-pipelined grain-growth step (32x32 tiles, FP32 neighbourhoods by tensor copy).
@@ -82,6 +86,10 @@ cudaError_t classify_batch(const ClassifyArgs *cs, int count, cudaStream_t s);
 cudaError_t advance_batch(const ClassifyArgs *cs, int count, cudaStream_t s);
 // Rebuild lists/counts from tier_cur without reclassifying (static tier maps).
 cudaError_t build_lists(const uint8_t *tier, int ntiles, int *lists, int *counts, cudaStream_t s);
+// The reference's temporal snapshot (amps_params.ref_snapshot), after a
+// classification: on the 4x4 lattice, tiles now at half keep their previous
+// snapshot in the lattice columns of the tile's second half; keep := snap.
+cudaError_t snap_ref_fixup(double *snap, double *keep, const uint8_t *tier, int ntiles, int nmon, cudaStream_t s);
 // Bookkeeping at the end of a period when no classification runs.
 cudaError_t advance_period(int64_t *step_base, int advance, int stat_steps, const int *counts,
                            unsigned long long *stats, cudaStream_t s);

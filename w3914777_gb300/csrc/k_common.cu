@@ -417,6 +417,30 @@ __global__ void __launch_bounds__(1024) build_lists_kernel(const uint8_t *tier, 
     lists_from_tiers(tier, ntiles, lists, counts, ws);
 }
 
+// graingrowth/function.h:38-39,68-73 (and snowflake/function.h:69-70,106-113):
+// at every 10th step the update kernel copies the monitored field into the
+// snapshot, but a low tile's second 8-column block returns before the copy,
+// so its samples in columns 10 and 14 keep the value of the last step at
+// which the tile was high.  Here the monitor step's epilogue has written the
+// whole lattice (the state the classification just judged); this puts the
+// earlier values back where the reference keeps them.  keep holds the
+// snapshot as it stood after the previous classification.
+__global__ void snap_ref_kernel(double *snap, double *keep, const uint8_t *tier, int ntiles, int total)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    const int si = i % 16, t = (i / 16) % ntiles;
+    if (tier[t] == TIER_HALF && (si % 4) >= 2) snap[i] = keep[i];
+    keep[i] = snap[i];
+}
+
+cudaError_t snap_ref_fixup(double *snap, double *keep, const uint8_t *tier, int ntiles, int nmon, cudaStream_t s)
+{
+    const int total = nmon * ntiles * 16;
+    snap_ref_kernel<<<(total + 255) / 256, 256, 0, s>>>(snap, keep, tier, ntiles, total);
+    return cudaGetLastError();
+}
+
 cudaError_t build_lists(const uint8_t *tier, int ntiles, int *lists, int *counts, cudaStream_t s)
 {
     build_lists_kernel<<<1, 1024, 0, s>>>(tier, ntiles, lists, counts);
