@@ -151,6 +151,8 @@ typedef struct amps_stats {
     int64_t promotions, demotions; /* tier changes over all classifications */
     int32_t tiles;                 /* tiles in the grid */
     int32_t numeric_error;         /* 1 if the monitor saw NaN or Inf */
+    int64_t kernel_launches;       /* kernels amps_run has launched (steps, classifications; graph
+                                      replays count the kernels of the graph) */
 } amps_stats;
 
 typedef struct amps_handle amps_handle;

@@ -627,6 +627,35 @@ def test_tma_step_kernel_matches_default(mode, monkeypatch):
     assert out[0][2] == out[1][2]
 
 
+@pytest.mark.parametrize("case", ["adaptive_q8", "adaptive_q5_noflux", "fp32_q8", "adaptive_q8_eager"])
+def test_multi_step_kernel_matches_one_launch_per_step(case, monkeypatch):
+    """The multi-step kernel (the interior steps of a period in one launch, a
+    CTA per (step, tile), each tile starting once its neighbourhood finished
+    the previous step) gives the one-launch-per-step results bit for bit:
+    three tiers with a rate monitor, Q = 5 on the 4-row path with zero flux,
+    the all-FP32 plain mode (whole periods in one launch), graphs off; runs
+    split into partial periods."""
+    w = amps()
+    q = 5 if "q5" in case else 8
+    extra = dict(mode="purehigh", high_tier=w.TIER_FP32) if case.startswith("fp32") else \
+        dict(monitor=w.MONITOR_RATE, monitor_samples=1, thr_lo=1e-5, thr_hi=3e-3)
+    p = w.Params.preset("graingrowth", 0, nx=256, ny=192, nfields=q, tile=32,
+                        bc=1 if "noflux" in case else 0, **extra)
+    out = []
+    for off in ("1", "0"):
+        monkeypatch.setenv("AMPS_DISABLE_FLOW", off)
+        with w.Simulation(p, init=w.INIT_SEEDED, graphs=not case.endswith("eager")) as s:
+            s.run(23)
+            s.run(17)
+            s.run(60)
+            out.append((s.fields(), s.tiers(), s.stats(), s.kernel_launches()))
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
+    assert out[0][2] == out[1][2]
+    assert out[1][3] < out[0][3]  # fewer launches with the multi-step kernel
+    print(case, "launches per 100 steps: one per step", out[0][3], "multi-step", out[1][3])
+
+
 def test_set_get_roundtrip_and_reduce():
     w = amps()
     p = w.Params.preset("sintering", 1, mode="purehigh", nx=64, ny=64)

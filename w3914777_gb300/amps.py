@@ -87,7 +87,7 @@ class Params(ctypes.Structure):
 class Stats(ctypes.Structure):
     _fields_ = [("steps", ctypes.c_int64), ("tile_steps", ctypes.c_int64 * 3), ("monitor_evals", ctypes.c_int64),
                 ("promotions", ctypes.c_int64), ("demotions", ctypes.c_int64), ("tiles", ctypes.c_int32),
-                ("numeric_error", ctypes.c_int32)]
+                ("numeric_error", ctypes.c_int32), ("kernel_launches", ctypes.c_int64)]
 
     def as_dict(self):
         return {"steps": self.steps, "tile_steps": list(self.tile_steps), "monitor_evals": self.monitor_evals,
@@ -309,6 +309,12 @@ class Simulation:
         s = Stats()
         self._ck(lib().amps_get_stats(self.h, ctypes.byref(s)), "amps_get_stats")
         return s.as_dict()
+
+    def kernel_launches(self):
+        """Kernels amps_run has launched on this handle (steps, classifications)."""
+        s = Stats()
+        self._ck(lib().amps_get_stats(self.h, ctypes.byref(s)), "amps_get_stats")
+        return s.kernel_launches
 
     def reduce(self, k, kind=REDUCE_SUM):
         v = ctypes.c_double()

@@ -62,14 +62,20 @@ struct amps_handle {
     cudaStream_t own = nullptr, stream = nullptr;
 
     int64_t step = 0;
+    int64_t launches = 0;  // kernels enqueued by the run loop (graph replays add their graph's count)
     bool graphs = true;
     std::map<int, cudaGraphExec_t> graph;  // key: parity | transition<<1 | all_fp64<<2
+    std::map<int, int64_t> graph_launches;  // kernels in each period graph
     std::string err;
     // kernel timing
     bool profiling = false;
     struct Ev { int tier; cudaEvent_t a, b; int n; };  // n launches between a and b
     std::vector<Ev> evs;
     std::vector<cudaEvent_t> ev_stash;  // created ahead of a captured profiled period
+    // grain growth: persistent multi-step kernel for the interior steps of a
+    // period (d_flow: per-tile step counters, then the item counter)
+    bool use_flow = false;
+    int *d_flow = nullptr;
     // grain growth: persistent TMA kernel over the FP32 ping-pong buffers
     bool use_tma = false;
     int tma_grid = 0;
@@ -204,7 +210,7 @@ static void free_all(amps_handle *h)
             if (h->store[t][q]) cudaFree(h->store[t][q]);
     void *ps[] = {h->d_tier_prev, h->d_tier_cur, h->d_lists, h->d_order, h->d_counts, h->d_metric, h->d_snap, h->d_stats,
                   h->d_flags, h->d_log, h->d_log_n, h->d_step_base, h->d_stage, h->d_partials, h->d_out,
-                  h->d_diag, h->d_sched, h->d_sched_i, h->d_msnap, h->d_mmetric, h->d_snap_keep};
+                  h->d_diag, h->d_sched, h->d_sched_i, h->d_msnap, h->d_mmetric, h->d_snap_keep, h->d_flow};
     for (void *q : ps)
         if (q) cudaFree(q);
     if (h->h_pinned) cudaFreeHost(h->h_pinned);
@@ -338,6 +344,18 @@ extern "C" int amps_create(const amps_params *p, amps_handle **out)
             cudaGetLastError();  // a refused attribute / encode leaves the generic kernel in charge
         }
     }
+    {
+        // multi-step kernel for the interior steps of a period (grain growth,
+        // 32x32 tiles, the fused step's half/FP32 arithmetic);
+        // AMPS_DISABLE_FLOW=1 keeps one launch per step
+        const bool only64 = h->used[TIER_FP64] && !h->used[TIER_FP32] && !h->used[TIER_HALF];
+        const char *off = getenv("AMPS_DISABLE_FLOW");
+        if (p->model == AMPS_GRAINGROWTH && p->tile == 32 && !only64 && p->half_arith == AMPS_HALF_FP32 &&
+            !h->use_tma && !(off && off[0] == '1') && gg_prepare_flow(p->ref_order != 0) == cudaSuccess &&
+            cudaMalloc((void **)&h->d_flow, sizeof(int) * (h->ntiles + 1)) == cudaSuccess)
+            h->use_flow = true;
+        cudaGetLastError();  // a refused attribute or allocation leaves one launch per step
+    }
     const int start = p->mode == AMPS_PURELOW ? TIER_HALF : high;
     cudaMemsetAsync(h->d_tier_cur, start, h->ntiles, h->stream);
     cudaMemsetAsync(h->d_tier_prev, start, h->ntiles, h->stream);
@@ -376,7 +394,8 @@ extern "C" int amps_synchronize(amps_handle *h)
     CK(h, cudaStreamSynchronize(h->stream));
     int flag = 0;
     CK(h, cudaMemcpy(&flag, h->d_flags, sizeof(int), cudaMemcpyDeviceToHost));
-    if (flag & 2) FAIL(h, AMPS_ERR_TIMEOUT, "a bounded device wait gave up (tensor copy did not complete)");
+    if (flag & 2) FAIL(h, AMPS_ERR_TIMEOUT, "a bounded device wait gave up (a tensor copy, or a multi-step "
+                                            "kernel's wait on a neighbouring tile, did not complete)");
     if (flag & 1) FAIL(h, AMPS_ERR_NUMERIC, "NaN or Inf detected by the monitor");
     return AMPS_OK;
 }
@@ -637,6 +656,7 @@ static int launch_step(amps_handle *h, int step_off, bool monitor_now)
         cudaError_t e = h->use_tma ? gg_launch_tma(ref, h->tm[h->parity], a, h->tma_grid, h->stream)
                                    : gg_launch(h->T, only64 ? TIER_FP64 : -1, ref, a, h->ntiles, h->stream);
         if (e != cudaSuccess) FAIL(h, AMPS_ERR_CUDA, "step kernel launch: %s", cudaGetErrorString(e));
+        ++h->launches;
         h->parity ^= 1;
         h->transition = false;
         return AMPS_OK;
@@ -661,6 +681,7 @@ static int launch_step(amps_handle *h, int step_off, bool monitor_now)
         else if (p.model == AMPS_KOBAYASHI) e = kob_launch(h->T, t, ref, a, h->ntiles, st);
         else e = sint_launch(h->T, t, ref, p.mu_lap_fp64 != 0, a, h->ntiles, st);
         if (e != cudaSuccess) FAIL(h, AMPS_ERR_CUDA, "step kernel launch: %s", cudaGetErrorString(e));
+        ++h->launches;
         if (h->profiling) {
             CK(h, prof_record(h, ev.b));
             h->evs.push_back(ev);
@@ -685,6 +706,24 @@ static ClassifyArgs classify_args(const amps_handle *h, int advance, int stat_st
     return c;
 }
 
+// Steps [k0, k0+n) as one multi-step launch (no tier change and no monitor
+// among them).
+static int launch_flow(amps_handle *h, int k0, int n)
+{
+    CK(h, cudaMemsetAsync(h->d_flow, 0, sizeof(int) * (h->ntiles + 1), h->stream));
+    const StepArgs a0 = step_args(h, h->parity, false, k0, false);
+    const StepArgs a1 = step_args(h, h->parity ^ 1, false, k0 + 1, false);
+    FlowArgs fl;
+    fl.done = h->d_flow;
+    fl.queue = h->d_flow + h->ntiles;
+    fl.nsteps = n;
+    const cudaError_t e = gg_launch_flow(h->p.ref_order != 0, a0, a1, fl, h->stream);
+    if (e != cudaSuccess) FAIL(h, AMPS_ERR_CUDA, "multi-step kernel launch: %s", cudaGetErrorString(e));
+    ++h->launches;
+    if (n & 1) h->parity ^= 1;
+    return AMPS_OK;
+}
+
 // Steps [k0, k0+cnt) of a period, then the period's bookkeeping.
 static int enqueue_chunk(amps_handle *h, int k0, int cnt)
 {
@@ -699,11 +738,22 @@ static int enqueue_chunk(amps_handle *h, int k0, int cnt)
         const int r = prof_begin(h, ev);
         if (r) return r;
     }
-    for (int s = 0; s < cnt; ++s) {
+    for (int s = 0; s < cnt;) {
         // a tier schedule stands in for the monitor: no epilogue
         const bool mon = h->mixed && period_end && s == cnt - 1 && h->sched_n == 0;
+        if (h->use_flow && !h->transition && !h->all_fp64 && !mon) {
+            // the run of steps up to the monitor step (or the chunk's end)
+            const int run = (h->mixed && period_end && h->sched_n == 0) ? cnt - 1 - s : cnt - s;
+            if (run >= 2) {
+                int r = launch_flow(h, k0 + s, run);
+                if (r) return r;
+                s += run;
+                continue;
+            }
+        }
         int r = launch_step(h, k0 + s, mon);
         if (r) return r;
+        ++s;
     }
     if (span) {
         CK(h, prof_record(h, ev.b));
@@ -711,12 +761,16 @@ static int enqueue_chunk(amps_handle *h, int k0, int cnt)
     }
     if (h->mixed && period_end) {
         CK(h, classify(classify_args(h, p.cadence, cnt), h->stream));
-        if (h->d_snap_keep && !h->sched_n)
+        ++h->launches;
+        if (h->d_snap_keep && !h->sched_n) {
             CK(h, snap_ref_fixup(h->d_snap, h->d_snap_keep, h->d_tier_cur, h->ntiles, h->nmon, h->stream));
+            ++h->launches;
+        }
         h->transition = true;
         h->all_fp64 = false;
     } else {
         CK(h, advance_period(h->d_step_base, period_end ? p.cadence : 0, cnt, h->d_counts, h->d_stats, h->stream));
+        ++h->launches;
     }
     return AMPS_OK;
 }
@@ -756,6 +810,7 @@ extern "C" int amps_run(amps_handle *h, int nsteps)
             if (it == h->graph.end()) {
                 const int par0 = h->parity;
                 const bool tr0 = h->transition, all0 = h->all_fp64;
+                const int64_t n0 = h->launches;
                 cudaGraph_t gr;
                 CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
                 int r = enqueue_chunk(h, 0, cad);
@@ -767,11 +822,14 @@ extern "C" int amps_run(amps_handle *h, int nsteps)
                 cudaGraphDestroy(gr);
                 if (e != cudaSuccess) FAIL(h, AMPS_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
                 it = h->graph.emplace(key, ex).first;
+                h->graph_launches[key] = h->launches - n0;
                 h->parity = par0;  // capture advanced the host-side state; replay does it for real
                 h->transition = tr0;
                 h->all_fp64 = all0;
+                h->launches = n0;
             }
             CK(h, cudaGraphLaunch(it->second, h->stream));
+            h->launches += h->graph_launches[key];
             // mirror the period's effect on the host-side state
             if (cad & 1) h->parity ^= 1;
             h->transition = h->mixed;
@@ -921,6 +979,7 @@ extern "C" int amps_get_stats(amps_handle *h, amps_stats *out)
     out->demotions = (int64_t)s[5];
     out->tiles = h->ntiles;
     out->numeric_error = flag & 1;
+    out->kernel_launches = h->launches;
     return AMPS_OK;
 }
 

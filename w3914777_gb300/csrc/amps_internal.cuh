@@ -176,14 +176,20 @@ template <typename CT> __device__ __forceinline__ CT load_tier(const StepArgs &a
     return (CT)__half2float(((const __half *)a.in[0])[idx]);
 }
 
+// Load of step input: NC through the read-only (non-coherent) path, for
+// kernels in which the data cannot change; otherwise from L2 (.cg), for a
+// kernel that also writes what it reads (the persistent multi-step kernel).
+template <bool NC, typename V> __device__ __forceinline__ V ldro(const V *p) { return NC ? __ldg(p) : __ldcg(p); }
+
 // 8 consecutive cells from a tier array, 16-byte aligned (idx % 8 == 0).
-template <typename CT> __device__ __forceinline__ void load8_tier(const StepArgs &a, int tier, int64_t idx, CT v[8])
+template <typename CT, bool NC = true>
+__device__ __forceinline__ void load8_tier(const StepArgs &a, int tier, int64_t idx, CT v[8])
 {
     if (tier == TIER_FP64) {
         const double2 *p = (const double2 *)((const double *)a.in[2] + idx);
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            double2 d = __ldg(p + k);
+            double2 d = ldro<NC>(p + k);
             v[2 * k] = (CT)d.x;
             v[2 * k + 1] = (CT)d.y;
         }
@@ -191,11 +197,11 @@ template <typename CT> __device__ __forceinline__ void load8_tier(const StepArgs
         const float4 *p = (const float4 *)((const float *)a.in[1] + idx);
 #pragma unroll
         for (int k = 0; k < 2; ++k) {
-            float4 f = __ldg(p + k);
+            float4 f = ldro<NC>(p + k);
             v[4 * k] = (CT)f.x; v[4 * k + 1] = (CT)f.y; v[4 * k + 2] = (CT)f.z; v[4 * k + 3] = (CT)f.w;
         }
     } else {
-        uint4 u = __ldg((const uint4 *)((const __half *)a.in[0] + idx));
+        uint4 u = ldro<NC>((const uint4 *)((const __half *)a.in[0] + idx));
         const __half2 *h = (const __half2 *)&u;
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
@@ -260,7 +266,7 @@ __device__ __forceinline__ void load_neighbour_tiers(const StepArgs &a, int tx, 
 // SKIP32: the FP32-owned slots already hold their values (copied by this
 // same thread: stage_tile_async32 gives every thread the same slots); only
 // the others are loaded and converted.
-template <typename CT, int T, int R, bool SKIP32 = false>
+template <typename CT, int T, int R, bool SKIP32 = false, bool NC = true>
 __device__ __forceinline__ void stage_tile(const StepArgs &a, CT *sm, const uint8_t *nt, int tx, int ty, int f0,
                                            int nfs)
 {
@@ -318,8 +324,8 @@ __device__ __forceinline__ void stage_tile(const StepArgs &a, CT *sm, const uint
                     raw[q][b] = make_uint4(0u, 0u, 0u, 0u);
                     if (kind[q] != 0 && tier[q] == TIER_HALF && fb + b < nfs) {
                         const __half *src = hs + (int64_t)(f0 + fb + b) * a.n + goff[q];
-                        if (kind[q] == 1) raw[q][b] = __ldg(reinterpret_cast<const uint4 *>(src));
-                        else raw[q][b].x = __ldg(reinterpret_cast<const unsigned short *>(src));
+                        if (kind[q] == 1) raw[q][b] = ldro<NC>(reinterpret_cast<const uint4 *>(src));
+                        else raw[q][b].x = ldro<NC>(reinterpret_cast<const unsigned short *>(src));
                     }
                 }
 #pragma unroll
@@ -364,7 +370,7 @@ __device__ __forceinline__ void stage_tile(const StepArgs &a, CT *sm, const uint
                 const int f = fb + b;
                 if (f < nfs) {
                     const int64_t idx = (int64_t)(f0 + f) * a.n + goff[q];
-                    if (kind[q] == 1) load8_tier<CT>(a, tier[q], idx, v[q][b]);
+                    if (kind[q] == 1) load8_tier<CT, NC>(a, tier[q], idx, v[q][b]);
                     else if (kind[q] == 2) v[q][b][0] = load_tier<CT>(a, tier[q], idx);
                 }
             }

@@ -24,6 +24,18 @@ cudaError_t gg_launch_half(int tile, bool ref, const StepArgs &a, int grid, size
 cudaError_t gg_prepare_half(int tile, bool ref, int half_arith);
 cudaError_t kob_prepare(int tile, int tier, bool ref);
 cudaError_t sint_prepare(int tile, int tier, bool ref, bool mu64);
+// Multi-step grain-growth kernel (32x32 tiles, the fused step's arithmetic):
+// `nsteps` consecutive steps without a tier change or a monitor in one
+// launch, a CTA per (step, tile); a0 the arguments of the first (and every
+// even) step, a1 of the odd ones; done[ntiles] and *queue zero at launch.
+struct FlowArgs {
+    int *done;
+    int *queue;
+    int nsteps;
+};
+size_t gg_flow_smem_bytes(int nf);
+cudaError_t gg_prepare_flow(bool ref);
+cudaError_t gg_launch_flow(bool ref, const StepArgs &a0, const StepArgs &a1, const FlowArgs &fl, cudaStream_t s);
 // Persistent TMA-pipelined grain-growth step (32x32 tiles, FP32 neighbourhoods by tensor copy).
 constexpr int kTmaMaxFields = 16;
 size_t gg_tma_smem_bytes(int nf);

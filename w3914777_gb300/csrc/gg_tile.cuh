@@ -430,7 +430,9 @@ __device__ __forceinline__ bool all_fp32(const uint8_t *nt)
 // member of an ensemble gets exactly the results of a single run.  MK: 0 for
 // a step without the monitor, 1/2/3 a monitor step of that monitor kind
 // (spatial / temporal / rate), -1 a monitor step of the kind in `a`.
-template <int T, bool REF, int MK, int HA = 0>
+// NC = false: no read-only-path loads (the persistent multi-step kernel
+// reads values that other CTAs of the same launch wrote).
+template <int T, bool REF, int MK, int HA = 0, bool NC = true>
 __device__ __forceinline__ void gg_tile_step(const StepArgs &a, float *sm, uint8_t *ntier, double *red, int tile)
 {
     constexpr bool MON = MK != 0;
@@ -456,11 +458,11 @@ __device__ __forceinline__ void gg_tile_step(const StepArgs &a, float *sm, uint8
         cp_async_wait_all();
         // mixed neighbourhood: the FP32-owned slots are in place; each thread
         // overwrites its own other slots with their converted values
-        if (!all32) stage_tile<float, T, 1, true>(a, sm, ntier, tx, ty, 0, a.nf);
+        if (!all32) stage_tile<float, T, 1, true, NC>(a, sm, ntier, tx, ty, 0, a.nf);
     } else if (all32) {
         stage_tile_async32<T, 1>(a, sm, tx, ty, a.nf);
     } else {
-        stage_tile<float, T, 1>(a, sm, ntier, tx, ty, 0, a.nf);
+        stage_tile<float, T, 1, false, NC>(a, sm, ntier, tx, ty, 0, a.nf);
     }
     __syncthreads();
     if constexpr (HA != 0) {

@@ -100,6 +100,112 @@ __global__ void __launch_bounds__(kThreads) gg_step_f64_kernel(StepArgs a)
     }
 }
 
+// ---- multi-step kernel ---------------------------------------------------------
+// The interior steps of a period (no tier change, no monitor) in one launch.
+// Every step launch of the fused kernel pays a start-up and a drain: its
+// first wave of CTAs all stage at once and its last CTAs finish alone, about
+// 2.4 us of a 13.8 us all-FP32 1024^2 Q=8 step (608 tiles take 9.0 us, 1216
+// take 15.6 us).  Here one grid holds a CTA for every (step, tile) item; a
+// CTA takes the next item in step-major, slow-first order from a counter
+// (not its block index), and an item of step s starts as soon as the 3x3
+// tiles of its neighbourhood have finished step s-1 -- the only data it
+// reads, and the only readers of the buffer it overwrites -- so the next
+// step's tiles run while the last ones of this step still compute.
+//
+// Progress needs no co-residency: a CTA claims an item only once it runs,
+// so every earlier item belongs to a CTA that runs or has finished, and an
+// item waits only on earlier ones (the dynamic-index rule of single-pass
+// scans).  Each wait is bounded: past ~1 s it sets the device error flag
+// (bit 1), which every other wait sees and gives up on, and the CTAs return.
+// Visibility follows the grid-barrier pattern: the producing CTA's threads
+// finish their stores, a CTA barrier, then one thread's device-scope fence
+// and the release of the tile's counter; the consumer's polling thread sees
+// the counter and fences, and a CTA barrier precedes every thread's loads.
+// Loads of step data avoid the read-only path (NC = false), which is not
+// kept coherent with writes made during the launch.
+
+// Thread 0: wait until the 3x3 tiles around `tile` (after the boundary map)
+// have completed `need` steps; false if the wait gave up or another did.
+__device__ bool flow_wait(const StepArgs &a, const int *done, int tile, int need)
+{
+    volatile const int *vd = done;
+    volatile const int *vflag = a.flags;
+    const int tx = tile % a.ntx, ty = tile / a.ntx;
+    for (int dy = -1; dy <= 1; ++dy)
+        for (int dx = -1; dx <= 1; ++dx) {
+            int x = tx + dx, y = ty + dy;
+            if (a.bc == 0) {
+                x = x < 0 ? a.ntx - 1 : (x >= a.ntx ? 0 : x);
+                y = y < 0 ? a.nty - 1 : (y >= a.nty ? 0 : y);
+            } else {
+                x = x < 0 ? 0 : (x >= a.ntx ? a.ntx - 1 : x);
+                y = y < 0 ? 0 : (y >= a.nty ? a.nty - 1 : y);
+            }
+            const int nb = y * a.ntx + x;
+            for (int it = 0; vd[nb] < need; ++it) {
+                if ((*vflag & 2) || it >= (1 << 24)) {
+                    atomicOr(a.flags, 2);
+                    return false;
+                }
+                if (it > 32) __nanosleep(64);
+            }
+        }
+    return true;
+}
+
+// One CTA per (step, tile) item; a0: the arguments of even steps (counted
+// from the launch's first), a1: of odd ones.
+template <bool REF>
+__global__ void __launch_bounds__(kThreads, 4) gg_flow_kernel(StepArgs a0, StepArgs a1, FlowArgs fl)
+{
+    extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ double red[kThreads / 32];
+    __shared__ uint8_t ntier[9];
+    __shared__ int item_s, go_s;
+    float *sm = reinterpret_cast<float *>(smraw);
+    const int ntiles = a0.ntx * a0.nty;
+    if (threadIdx.x == 0) {
+        const int item = atomicAdd(fl.queue, 1);
+        int go = 1;
+        if (item >= ntiles) {
+            const int tile = a0.order ? a0.order[item % ntiles] : item % ntiles;
+            go = flow_wait(a0, fl.done, tile, item / ntiles);
+        }
+        __threadfence();
+        item_s = item;
+        go_s = go;
+    }
+    __syncthreads();
+    if (!go_s) return;
+    const int item = item_s, step = item / ntiles;
+    const int tile = a0.order ? a0.order[item % ntiles] : item % ntiles;
+    if (step & 1) gg_tile_step<32, REF, 0, 0, false>(a1, sm, ntier, red, tile);
+    else gg_tile_step<32, REF, 0, 0, false>(a0, sm, ntier, red, tile);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicExch(&fl.done[tile], step + 1);
+    }
+}
+
+size_t gg_flow_smem_bytes(int nf) { return gg_smem_bytes(32, -1, nf); }
+
+cudaError_t gg_prepare_flow(bool ref)
+{
+    const auto attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    return ref ? cudaFuncSetAttribute(gg_flow_kernel<true>, attr, kMaxDynSmem)
+               : cudaFuncSetAttribute(gg_flow_kernel<false>, attr, kMaxDynSmem);
+}
+
+cudaError_t gg_launch_flow(bool ref, const StepArgs &a0, const StepArgs &a1, const FlowArgs &fl, cudaStream_t s)
+{
+    const int grid = fl.nsteps * a0.ntx * a0.nty;
+    const size_t smem = gg_flow_smem_bytes(a0.nf);
+    if (ref) gg_flow_kernel<true><<<grid, kThreads, smem, s>>>(a0, a1, fl);
+    else gg_flow_kernel<false><<<grid, kThreads, smem, s>>>(a0, a1, fl);
+    return cudaGetLastError();
+}
+
 // tier: TIER_FP64 selects the all-FP64 staged kernel; anything else the fused one.
 size_t gg_smem_bytes(int tile, int tier, int nf)
 {
