@@ -629,9 +629,10 @@ def test_tma_step_kernel_matches_default(mode, monkeypatch):
 
 @pytest.mark.parametrize("case", ["adaptive_q8", "adaptive_q5_noflux", "fp32_q8", "adaptive_q8_eager"])
 def test_multi_step_kernel_matches_one_launch_per_step(case, monkeypatch):
-    """The multi-step kernel (the interior steps of a period in one launch, a
-    CTA per (step, tile), each tile starting once its neighbourhood finished
-    the previous step) gives the one-launch-per-step results bit for bit:
+    """The opt-in multi-step kernel (AMPS_ENABLE_FLOW=1: the interior steps of
+    a period in one launch, a CTA per (step, tile), each tile starting once
+    its neighbourhood finished the previous step) gives the default
+    one-launch-per-step results bit for bit:
     three tiers with a rate monitor, Q = 5 on the 4-row path with zero flux,
     the all-FP32 plain mode (whole periods in one launch), graphs off; runs
     split into partial periods."""
@@ -642,8 +643,8 @@ def test_multi_step_kernel_matches_one_launch_per_step(case, monkeypatch):
     p = w.Params.preset("graingrowth", 0, nx=256, ny=192, nfields=q, tile=32,
                         bc=1 if "noflux" in case else 0, **extra)
     out = []
-    for off in ("1", "0"):
-        monkeypatch.setenv("AMPS_DISABLE_FLOW", off)
+    for on in ("0", "1"):
+        monkeypatch.setenv("AMPS_ENABLE_FLOW", on)
         with w.Simulation(p, init=w.INIT_SEEDED, graphs=not case.endswith("eager")) as s:
             s.run(23)
             s.run(17)

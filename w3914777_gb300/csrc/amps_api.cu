@@ -345,13 +345,16 @@ extern "C" int amps_create(const amps_params *p, amps_handle **out)
         }
     }
     {
-        // multi-step kernel for the interior steps of a period (grain growth,
-        // 32x32 tiles, the fused step's half/FP32 arithmetic);
-        // AMPS_DISABLE_FLOW=1 keeps one launch per step
+        // multi-step kernel for the interior steps of a period (opt-in,
+        // AMPS_ENABLE_FLOW=1; grain growth, 32x32 tiles, the fused step's
+        // half/FP32 arithmetic).  Measured slower than one launch per step on
+        // GB300 (1024^2 Q=8 all-FP32: 14.7 against 13.5 us a step; 4096^2:
+        // 241 against 204): each CTA's claim, neighbour wait and release cost
+        // more than the launch tail they remove.
         const bool only64 = h->used[TIER_FP64] && !h->used[TIER_FP32] && !h->used[TIER_HALF];
-        const char *off = getenv("AMPS_DISABLE_FLOW");
+        const char *on = getenv("AMPS_ENABLE_FLOW");
         if (p->model == AMPS_GRAINGROWTH && p->tile == 32 && !only64 && p->half_arith == AMPS_HALF_FP32 &&
-            !h->use_tma && !(off && off[0] == '1') && gg_prepare_flow(p->ref_order != 0) == cudaSuccess &&
+            !h->use_tma && on && on[0] == '1' && gg_prepare_flow(p->ref_order != 0) == cudaSuccess &&
             cudaMalloc((void **)&h->d_flow, sizeof(int) * (h->ntiles + 1)) == cudaSuccess)
             h->use_flow = true;
         cudaGetLastError();  // a refused attribute or allocation leaves one launch per step

@@ -117,39 +117,41 @@ __global__ void __launch_bounds__(kThreads) gg_step_f64_kernel(StepArgs a)
 // item waits only on earlier ones (the dynamic-index rule of single-pass
 // scans).  Each wait is bounded: past ~1 s it sets the device error flag
 // (bit 1), which every other wait sees and gives up on, and the CTAs return.
-// Visibility follows the grid-barrier pattern: the producing CTA's threads
-// finish their stores, a CTA barrier, then one thread's device-scope fence
-// and the release of the tile's counter; the consumer's polling thread sees
-// the counter and fences, and a CTA barrier precedes every thread's loads.
+// Visibility: the producing CTA's threads finish their stores, a CTA
+// barrier, then one thread's device-scope release store of the tile's
+// counter; each of the consumer's nine polling threads sees its counter and
+// issues a device-scope acquire fence, and a CTA barrier precedes every
+// thread's loads.
 // Loads of step data avoid the read-only path (NC = false), which is not
 // kept coherent with writes made during the launch.
 
-// Thread 0: wait until the 3x3 tiles around `tile` (after the boundary map)
-// have completed `need` steps; false if the wait gave up or another did.
+// Threads 0..8, one tile each of the 3x3 neighbourhood of `tile` (after the
+// boundary map): wait until it has completed `need` steps, then an acquire
+// fence; false if the wait gave up or another did.  The nine waits run side
+// by side (one L2 round trip when they are already met).
 __device__ bool flow_wait(const StepArgs &a, const int *done, int tile, int need)
 {
-    volatile const int *vd = done;
-    volatile const int *vflag = a.flags;
     const int tx = tile % a.ntx, ty = tile / a.ntx;
-    for (int dy = -1; dy <= 1; ++dy)
-        for (int dx = -1; dx <= 1; ++dx) {
-            int x = tx + dx, y = ty + dy;
-            if (a.bc == 0) {
-                x = x < 0 ? a.ntx - 1 : (x >= a.ntx ? 0 : x);
-                y = y < 0 ? a.nty - 1 : (y >= a.nty ? 0 : y);
-            } else {
-                x = x < 0 ? 0 : (x >= a.ntx ? a.ntx - 1 : x);
-                y = y < 0 ? 0 : (y >= a.nty ? a.nty - 1 : y);
-            }
-            const int nb = y * a.ntx + x;
-            for (int it = 0; vd[nb] < need; ++it) {
-                if ((*vflag & 2) || it >= (1 << 24)) {
-                    atomicOr(a.flags, 2);
-                    return false;
-                }
-                if (it > 32) __nanosleep(64);
-            }
+    int x = tx + (int)threadIdx.x % 3 - 1, y = ty + (int)threadIdx.x / 3 - 1;
+    if (a.bc == 0) {
+        x = x < 0 ? a.ntx - 1 : (x >= a.ntx ? 0 : x);
+        y = y < 0 ? a.nty - 1 : (y >= a.nty ? 0 : y);
+    } else {
+        x = x < 0 ? 0 : (x >= a.ntx ? a.ntx - 1 : x);
+        y = y < 0 ? 0 : (y >= a.nty ? a.nty - 1 : y);
+    }
+    volatile const int *vd = done + y * a.ntx + x;
+    volatile const int *vflag = a.flags;
+    for (int it = 0; *vd < need; ++it) {
+        if ((*vflag & 2) || it >= (1 << 24)) {
+            atomicOr(a.flags, 2);
+            return false;
         }
+        if (it > 32) __nanosleep(64);
+    }
+    // acquire: the counter seen above, then the CTA barrier, order every
+    // thread's loads after the producer's stores
+    asm volatile("fence.acq_rel.gpu;" ::: "memory");
     return true;
 }
 
@@ -161,30 +163,23 @@ __global__ void __launch_bounds__(kThreads, 4) gg_flow_kernel(StepArgs a0, StepA
     extern __shared__ __align__(16) unsigned char smraw[];
     __shared__ double red[kThreads / 32];
     __shared__ uint8_t ntier[9];
-    __shared__ int item_s, go_s;
+    __shared__ int item_s;
     float *sm = reinterpret_cast<float *>(smraw);
     const int ntiles = a0.ntx * a0.nty;
-    if (threadIdx.x == 0) {
-        const int item = atomicAdd(fl.queue, 1);
-        int go = 1;
-        if (item >= ntiles) {
-            const int tile = a0.order ? a0.order[item % ntiles] : item % ntiles;
-            go = flow_wait(a0, fl.done, tile, item / ntiles);
-        }
-        __threadfence();
-        item_s = item;
-        go_s = go;
-    }
+    if (threadIdx.x == 0) item_s = atomicAdd(fl.queue, 1);
     __syncthreads();
-    if (!go_s) return;
     const int item = item_s, step = item / ntiles;
     const int tile = a0.order ? a0.order[item % ntiles] : item % ntiles;
+    if (step > 0) {
+        const bool ok = threadIdx.x >= 9 || flow_wait(a0, fl.done, tile, step);
+        if (!__syncthreads_and(ok)) return;
+    }
     if (step & 1) gg_tile_step<32, REF, 0, 0, false>(a1, sm, ntier, red, tile);
     else gg_tile_step<32, REF, 0, 0, false>(a0, sm, ntier, red, tile);
     __syncthreads();
     if (threadIdx.x == 0) {
-        __threadfence();
-        atomicExch(&fl.done[tile], step + 1);
+        // release: the CTA's stores (ordered before by the barrier), then the counter
+        asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(fl.done + tile), "r"(step + 1) : "memory");
     }
 }
 
