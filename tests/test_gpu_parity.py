@@ -627,6 +627,37 @@ def test_tma_step_kernel_matches_default(mode, monkeypatch):
     assert out[0][2] == out[1][2]
 
 
+@pytest.mark.parametrize("case", ["adaptive_q8", "adaptive_q5_noflux", "fp32_q8", "ref_half_q2"])
+def test_bulk_tensor_staging_matches_per_thread_copies(case, monkeypatch):
+    """Interior tiles of the fused grain-growth step fetch their FP32
+    neighbourhood by one bulk tensor copy (the default); with
+    AMPS_DISABLE_TMA_STAGE=1 every tile stages by per-thread asynchronous
+    copies.  Bit for bit the same fields, tiers and statistics: three tiers
+    with a rate monitor, Q = 5 with zero flux, all-FP32, and the
+    binary16-arithmetic half tiles."""
+    w = amps()
+    q = 2 if "q2" in case else (5 if "q5" in case else 8)
+    if case.startswith("fp32"):
+        extra = dict(mode="purehigh", high_tier=w.TIER_FP32)
+    elif case.startswith("ref_half"):
+        extra = dict(monitor=w.MONITOR_RATE, monitor_samples=1, thr_lo=1e-4, thr_hi=3e-3, half_arith=w.HALF_REF)
+    else:
+        extra = dict(monitor=w.MONITOR_RATE, monitor_samples=1, thr_lo=1e-5, thr_hi=3e-3)
+    p = w.Params.preset("graingrowth", 0, nx=256, ny=192, nfields=q, tile=32, bc=1 if "noflux" in case else 0,
+                        **extra)
+    out = []
+    for off in ("1", "0"):
+        monkeypatch.setenv("AMPS_DISABLE_TMA_STAGE", off)
+        with w.Simulation(p, init=w.INIT_SEEDED) as s:
+            s.run(23)
+            s.run(57)
+            out.append((s.fields(), s.tiers(), s.stats()))
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
+    assert out[0][2] == out[1][2]
+    print(case, "tile-steps", out[1][2]["tile_steps"])
+
+
 @pytest.mark.parametrize("case", ["adaptive_q8", "adaptive_q5_noflux", "fp32_q8", "adaptive_q8_eager"])
 def test_multi_step_kernel_matches_one_launch_per_step(case, monkeypatch):
     """The opt-in multi-step kernel (AMPS_ENABLE_FLOW=1: the interior steps of

@@ -78,6 +78,7 @@ struct amps_handle {
     int *d_flow = nullptr;
     // grain growth: persistent TMA kernel over the FP32 ping-pong buffers
     bool use_tma = false;
+    bool tma_stage = false;  // tm[] encoded: the fused step stages interior tiles by tensor copy
     int tma_grid = 0;
     alignas(64) CUtensorMap tm[2];
     // diagnostics scratch (allocated on first use): lab, parent (n ints each),
@@ -324,6 +325,17 @@ extern "C" int amps_create(const amps_params *p, amps_handle **out)
         kernel_smem(*p, TIER_FP64, h->nf, true) <= (size_t)kMaxDynSmem)
         h->stage64 = gg_prepare(h->T, TIER_FP64, p->ref_order != 0, 0) == cudaSuccess;
     cudaGetLastError();
+    {
+        // grain growth, 32x32 tiles, an FP32 tier: tensor maps of the two FP32
+        // parities, so that the fused step fetches interior tiles' FP32
+        // neighbourhoods by one bulk tensor copy each (AMPS_DISABLE_TMA_STAGE=1:
+        // per-thread asynchronous copies only)
+        const char *off = getenv("AMPS_DISABLE_TMA_STAGE");
+        if (p->model == AMPS_GRAINGROWTH && p->tile == 32 && h->used[TIER_FP32] && !(off && off[0] == '1'))
+            h->tma_stage = encode_field_map(&h->tm[0], h->store[TIER_FP32][0], p->nx, p->ny, h->nf) &&
+                           encode_field_map(&h->tm[1], h->store[TIER_FP32][1], p->nx, p->ny, h->nf);
+        cudaGetLastError();
+    }
     {
         // persistent TMA kernel (opt-in, AMPS_ENABLE_TMA=1): grain growth, 32x32 tiles, an FP32 tier, few
         // enough fields for two buffers.  Measured slower than the 4-CTA/SM staged kernel on GB300 (two
@@ -610,6 +622,7 @@ static StepArgs step_args(const amps_handle *h, int parity, bool transition, int
     a.mu_lap_fp64 = p.mu_lap_fp64;
     a.cadence = p.cadence;
     a.half_arith = p.half_arith;
+    a.tma_stage = h->tma_stage ? 1 : 0;
     a.metric = h->d_metric;
     a.snap = h->d_snap;
     a.flags = h->d_flags;
@@ -657,7 +670,8 @@ static int launch_step(amps_handle *h, int step_off, bool monitor_now)
         const bool only64 = (h->used[TIER_FP64] && !h->used[TIER_FP32] && !h->used[TIER_HALF]) ||
                             (h->all_fp64 && !monitor_now);
         cudaError_t e = h->use_tma ? gg_launch_tma(ref, h->tm[h->parity], a, h->tma_grid, h->stream)
-                                   : gg_launch(h->T, only64 ? TIER_FP64 : -1, ref, a, h->ntiles, h->stream);
+                                   : gg_launch(h->T, only64 ? TIER_FP64 : -1, ref, a, h->ntiles, h->stream,
+                                               h->tma_stage ? &h->tm[h->parity] : nullptr);
         if (e != cudaSuccess) FAIL(h, AMPS_ERR_CUDA, "step kernel launch: %s", cudaGetErrorString(e));
         ++h->launches;
         h->parity ^= 1;

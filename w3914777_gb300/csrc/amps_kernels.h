@@ -4,7 +4,9 @@
 
 namespace amps {
 
-cudaError_t gg_launch(int tile, int tier, bool ref, const StepArgs &a, int grid, cudaStream_t s);
+// tm (nullable): tensor map of the step's FP32 input, used when a.tma_stage.
+cudaError_t gg_launch(int tile, int tier, bool ref, const StepArgs &a, int grid, cudaStream_t s,
+                      const CUtensorMap *tm = nullptr);
 cudaError_t kob_launch(int tile, int tier, bool ref, const StepArgs &a, int grid, cudaStream_t s);
 cudaError_t sint_launch(int tile, int tier, bool ref, bool mu64, const StepArgs &a, int grid, cudaStream_t s);
 size_t gg_smem_bytes(int tile, int tier, int nf);
@@ -20,7 +22,8 @@ cudaError_t sint_prepare_lo(int tile, bool mu64);
 cudaError_t gg_prepare(int tile, int tier, bool ref, int half_arith);
 // The fused step with binary16 arithmetic on half tiles (half_arith 1 or 2;
 // k_gg_half.cu), called by gg_launch / gg_prepare.
-cudaError_t gg_launch_half(int tile, bool ref, const StepArgs &a, int grid, size_t smem, cudaStream_t s);
+cudaError_t gg_launch_half(int tile, bool ref, const StepArgs &a, int grid, size_t smem, cudaStream_t s,
+                           const CUtensorMap &tm);
 cudaError_t gg_prepare_half(int tile, bool ref, int half_arith);
 cudaError_t kob_prepare(int tile, int tier, bool ref);
 cudaError_t sint_prepare(int tile, int tier, bool ref, bool mu64);

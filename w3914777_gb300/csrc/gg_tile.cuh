@@ -432,8 +432,13 @@ __device__ __forceinline__ bool all_fp32(const uint8_t *nt)
 // (spatial / temporal / rate), -1 a monitor step of the kind in `a`.
 // NC = false: no read-only-path loads (the persistent multi-step kernel
 // reads values that other CTAs of the same launch wrote).
+// tm, bar (T = 32): a tensor map of this step's FP32 input and an mbarrier;
+// tiles whose halo needs no wrap or mirror then fetch the whole FP32
+// neighbourhood -- every field, 34 rows x 40 columns, the staging layout --
+// by one bulk tensor copy issued by one thread (sm 128-byte aligned).
 template <int T, bool REF, int MK, int HA = 0, bool NC = true>
-__device__ __forceinline__ void gg_tile_step(const StepArgs &a, float *sm, uint8_t *ntier, double *red, int tile)
+__device__ __forceinline__ void gg_tile_step(const StepArgs &a, float *sm, uint8_t *ntier, double *red, int tile,
+                                             const CUtensorMap *tm = nullptr, uint64_t *bar = nullptr)
 {
     constexpr bool MON = MK != 0;
     const int tx = tile % a.ntx, ty = tile / a.ntx;
@@ -443,19 +448,46 @@ __device__ __forceinline__ void gg_tile_step(const StepArgs &a, float *sm, uint8
     // turns out FP64 or its neighbourhood mixed, the copies are drained and
     // their data (in-bounds reads of the full-size FP32 store) discarded
     const bool spec = T == 32 && a.in[TIER_FP32] != nullptr;
-    if (spec) stage_tile_async32<T, 1, false>(a, sm, tx, ty, a.nf);
+    const bool bulk = spec && tm != nullptr && tx >= 1 && ty >= 1 && tx <= a.ntx - 2 && ty <= a.nty - 2;
+    if (bulk) {
+        if (threadIdx.x == 0) {
+            mbar_init(bar, 1);
+            fence_mbar_init();
+            mbar_arrive_expect_tx(bar, (uint32_t)(Stage<float, T, 1>::FIELD * a.nf * sizeof(float)));
+            tma_load_3d(sm, tm, tx * T - Stage<float, T, 1>::O, ty * T - 1, 0, bar);
+        }
+    } else if (spec) {
+        stage_tile_async32<T, 1, false>(a, sm, tx, ty, a.nf);
+    }
+    // the staging copies have landed (false: a bounded wait on the tensor
+    // copy gave up -- flagged; the CTA waits once more for it and returns)
+    auto spec_done = [&]() -> bool {
+        if (!bulk) {
+            cp_async_wait_all();
+            return true;
+        }
+        const bool ok = mbar_wait_bounded(bar, 0);
+        if (__syncthreads_or(!ok)) {
+            if (threadIdx.x == 0) {
+                atomicOr(a.flags, 2);
+                if (!ok) mbar_wait_bounded(bar, 0);
+            }
+            return false;
+        }
+        return true;
+    };
     const int tier = a.tier_out[tile];
     __syncthreads();
     if (tier == TIER_FP64) {
         // the FP64 path reads through L1, not the staging area: the discarded
         // copies land while it computes, before the CTA exits
         gg_tile_fp64<T, REF>(a, ntier, tile, tx, ty, red);
-        if (spec) cp_async_wait_all();
+        if (spec) spec_done();
         return;
     }
     const bool all32 = all_fp32(ntier);
     if (spec) {
-        cp_async_wait_all();
+        if (!spec_done()) return;
         // mixed neighbourhood: the FP32-owned slots are in place; each thread
         // overwrites its own other slots with their converted values
         if (!all32) stage_tile<float, T, 1, true, NC>(a, sm, ntier, tx, ty, 0, a.nf);
@@ -519,13 +551,16 @@ __device__ __noinline__ void gg_tile_step_call(const StepArgs &a, float *sm, uin
 // each monitor step's kernel only its own kind's.  Half/FP32 tiles stage
 // their neighbourhood in shared memory (reading it directly through L1
 // measured 18.1 against 15.8 us per adaptive 1024^2 Q=8 step).
+// tm: the tensor map of the step's FP32 input, valid when a.tma_stage.
 template <int T, bool REF, int MK, int HA = 0>
-__global__ void __launch_bounds__(kThreads, 4) gg_step_kernel(StepArgs a)
+__global__ void __launch_bounds__(kThreads, 4) gg_step_kernel(StepArgs a, const __grid_constant__ CUtensorMap tm)
 {
-    extern __shared__ __align__(16) unsigned char smraw[];
+    extern __shared__ __align__(128) unsigned char smraw[];
     __shared__ double red[kThreads / 32];
     __shared__ uint8_t ntier[9];
-    float *sm = reinterpret_cast<float *>(smraw);
+    __shared__ __align__(8) uint64_t bar;
+    // 128-byte aligned staging (gg_smem_bytes adds the slack), as tensor copies need
+    float *sm = reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(smraw) + 127) & ~uintptr_t(127));
     // programmatic dependent launch (gg_launch): the next step's CTAs may be
     // scheduled into the slots this grid's last wave leaves free; every CTA
     // waits for the previous grid to complete, its writes visible, before
@@ -533,7 +568,7 @@ __global__ void __launch_bounds__(kThreads, 4) gg_step_kernel(StepArgs a)
     pdl_trigger();
     pdl_wait();
     const int tile = a.order ? a.order[blockIdx.x] : (int)blockIdx.x;
-    gg_tile_step<T, REF, MK, HA>(a, sm, ntier, red, tile);
+    gg_tile_step<T, REF, MK, HA>(a, sm, ntier, red, tile, a.tma_stage ? &tm : nullptr, &bar);
 }
 
 

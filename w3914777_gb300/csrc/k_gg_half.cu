@@ -10,28 +10,29 @@
 namespace amps {
 
 template <int T, bool REF, int HA>
-static cudaError_t launch_mk(const StepArgs &a, int grid, size_t smem, cudaStream_t s)
+static cudaError_t launch_mk(const StepArgs &a, int grid, size_t smem, cudaStream_t s, const CUtensorMap &tm)
 {
     switch (a.monitor_now ? a.monitor_kind : 0) {
-    case 0: return launch_kernel(gg_step_kernel<T, REF, 0, HA>, grid, smem, s, true, a);
-    case 1: return launch_kernel(gg_step_kernel<T, REF, 1, HA>, grid, smem, s, true, a);
-    case 2: return launch_kernel(gg_step_kernel<T, REF, 2, HA>, grid, smem, s, true, a);
-    default: return launch_kernel(gg_step_kernel<T, REF, 3, HA>, grid, smem, s, true, a);
+    case 0: return launch_kernel(gg_step_kernel<T, REF, 0, HA>, grid, smem, s, true, a, tm);
+    case 1: return launch_kernel(gg_step_kernel<T, REF, 1, HA>, grid, smem, s, true, a, tm);
+    case 2: return launch_kernel(gg_step_kernel<T, REF, 2, HA>, grid, smem, s, true, a, tm);
+    default: return launch_kernel(gg_step_kernel<T, REF, 3, HA>, grid, smem, s, true, a, tm);
     }
 }
 
 template <int T, int HA>
-static cudaError_t launch_ref(bool ref, const StepArgs &a, int grid, size_t smem, cudaStream_t s)
+static cudaError_t launch_ref(bool ref, const StepArgs &a, int grid, size_t smem, cudaStream_t s, const CUtensorMap &tm)
 {
-    return ref ? launch_mk<T, true, HA>(a, grid, smem, s) : launch_mk<T, false, HA>(a, grid, smem, s);
+    return ref ? launch_mk<T, true, HA>(a, grid, smem, s, tm) : launch_mk<T, false, HA>(a, grid, smem, s, tm);
 }
 
-cudaError_t gg_launch_half(int tile, bool ref, const StepArgs &a, int grid, size_t smem, cudaStream_t s)
+cudaError_t gg_launch_half(int tile, bool ref, const StepArgs &a, int grid, size_t smem, cudaStream_t s,
+                           const CUtensorMap &tm)
 {
     if (a.half_arith == 1)
-        return tile == 32 ? launch_ref<32, 1>(ref, a, grid, smem, s) : launch_ref<16, 1>(ref, a, grid, smem, s);
+        return tile == 32 ? launch_ref<32, 1>(ref, a, grid, smem, s, tm) : launch_ref<16, 1>(ref, a, grid, smem, s, tm);
     if (a.half_arith == 2)
-        return tile == 32 ? launch_ref<32, 2>(ref, a, grid, smem, s) : launch_ref<16, 2>(ref, a, grid, smem, s);
+        return tile == 32 ? launch_ref<32, 2>(ref, a, grid, smem, s, tm) : launch_ref<16, 2>(ref, a, grid, smem, s, tm);
     return cudaErrorInvalidValue;
 }
 

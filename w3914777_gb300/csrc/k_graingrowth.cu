@@ -17,6 +17,8 @@
 #include "amps_kernels.h"
 #include "gg_tile.cuh"
 
+#include <string.h>
+
 namespace amps {
 
 // All-FP64 step (plain FP64 mode): the FP64 neighbourhood is staged in
@@ -206,18 +208,23 @@ size_t gg_smem_bytes(int tile, int tier, int nf)
 {
     if (tier == TIER_FP64)
         return (size_t)nf * (tile == 32 ? Stage<double, 32, 1>::FIELD : Stage<double, 16, 1>::FIELD) * sizeof(double);
-    // 32^2: + the sum-of-squares tile of gg_tile_lo_4row
-    if (tile == 32) return ((size_t)nf * Stage<float, 32, 1>::FIELD + 32 * 32) * sizeof(float);
-    return (size_t)nf * Stage<float, 16, 1>::FIELD * sizeof(float);
+    // 32^2: + the sum-of-squares tile of gg_tile_lo_rows; + 128 bytes to align
+    // the staging for tensor copies (gg_step_kernel)
+    if (tile == 32) return ((size_t)nf * Stage<float, 32, 1>::FIELD + 32 * 32) * sizeof(float) + 128;
+    return (size_t)nf * Stage<float, 16, 1>::FIELD * sizeof(float) + 128;
 }
 
-template <typename K> static cudaError_t launch_pdl(K kernel, int grid, size_t smem, cudaStream_t s, const StepArgs &a)
+template <typename K>
+static cudaError_t launch_pdl(K kernel, int grid, size_t smem, cudaStream_t s, const StepArgs &a, const CUtensorMap &tm)
 {
-    return launch_kernel(kernel, grid, smem, s, true, a);
+    return launch_kernel(kernel, grid, smem, s, true, a, tm);
 }
 
-cudaError_t gg_launch(int tile, int tier, bool ref, const StepArgs &a, int grid, cudaStream_t s)
+cudaError_t gg_launch(int tile, int tier, bool ref, const StepArgs &a, int grid, cudaStream_t s, const CUtensorMap *tmp)
 {
+    CUtensorMap none;
+    memset(&none, 0, sizeof none);
+    const CUtensorMap &tm = tmp ? *tmp : none;
     const size_t smem = gg_smem_bytes(tile, tier, a.nf);
 #define AMPS_GGL(K, TT)                                                         \
     do {                                                                        \
@@ -226,8 +233,8 @@ cudaError_t gg_launch(int tile, int tier, bool ref, const StepArgs &a, int grid,
     } while (0)
 #define AMPS_GGK(TT, MK)                                                                              \
     do {                                                                                              \
-        if (ref) return launch_pdl(gg_step_kernel<TT, true, MK>, grid, smem, s, a);                   \
-        return launch_pdl(gg_step_kernel<TT, false, MK>, grid, smem, s, a);                           \
+        if (ref) return launch_pdl(gg_step_kernel<TT, true, MK>, grid, smem, s, a, tm);               \
+        return launch_pdl(gg_step_kernel<TT, false, MK>, grid, smem, s, a, tm);                       \
     } while (0)
 #define AMPS_GGM(TT)                                                                                  \
     do {                                                                                              \
@@ -242,7 +249,7 @@ cudaError_t gg_launch(int tile, int tier, bool ref, const StepArgs &a, int grid,
         if (tile == 32) AMPS_GGL(gg_step_f64_kernel, 32);
         else AMPS_GGL(gg_step_f64_kernel, 16);
     } else if (a.half_arith != 0) {
-        return gg_launch_half(tile, ref, a, grid, smem, s);  // binary16 half tiles (k_gg_half.cu)
+        return gg_launch_half(tile, ref, a, grid, smem, s, tm);  // binary16 half tiles (k_gg_half.cu)
     } else {
         if (tile == 32) AMPS_GGM(32);
         else AMPS_GGM(16);
