@@ -1215,6 +1215,7 @@ struct amps_ensemble {
     ClassifyArgs *d_cls = nullptr;      // whole periods: advance = stat_steps = cadence
     ClassifyArgs *d_cls_tmp = nullptr;  // partial periods (eager)
     StepArgs *d_tmp = nullptr;          // partial periods (eager): cadence x members
+    CUtensorMap *d_tmaps = nullptr;     // members' FP32 tensor maps [member][parity] (bulk staging)
     bool graphs = true;
     struct Period {
         StepArgs *table = nullptr;
@@ -1249,6 +1250,7 @@ static void ens_free(amps_ensemble *e)
     cudaFree(e->d_cls);
     cudaFree(e->d_cls_tmp);
     cudaFree(e->d_tmp);
+    cudaFree(e->d_tmaps);
     if (e->capture) cudaStreamDestroy(e->capture);
 }
 
@@ -1308,6 +1310,19 @@ extern "C" int amps_ensemble_create(amps_handle *const *members, int count, amps
     if (ce == cudaSuccess) ce = cudaMemset(e->d_queue, 0, 2 * sizeof(int));
     if (ce == cudaSuccess) ce = cudaMemcpy(e->d_cls, cls.data(), sizeof(ClassifyArgs) * count, cudaMemcpyHostToDevice);
     if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&e->capture, cudaStreamNonBlocking);
+    if (ce == cudaSuccess && e->T == 32) {
+        // the members' tensor maps, in global memory where the tile-queue kernel reads them
+        std::vector<CUtensorMap> maps((size_t)2 * count);
+        memset(maps.data(), 0, sizeof(CUtensorMap) * maps.size());
+        for (int i = 0; i < count; ++i)
+            if (members[i]->tma_stage) {
+                maps[2 * i] = members[i]->tm[0];
+                maps[2 * i + 1] = members[i]->tm[1];
+            }
+        ce = cudaMalloc(&e->d_tmaps, sizeof(CUtensorMap) * maps.size());
+        if (ce == cudaSuccess)
+            ce = cudaMemcpy(e->d_tmaps, maps.data(), sizeof(CUtensorMap) * maps.size(), cudaMemcpyHostToDevice);
+    }
     if (ce != cudaSuccess) {
         g_create_err = std::string("amps_ensemble_create: ") + cudaGetErrorString(ce);
         cudaGetLastError();
@@ -1361,6 +1376,7 @@ static std::vector<StepArgs> ens_tables(const amps_ensemble *e, int k0, int cnt)
         for (int s = 0; s < cnt; ++s) {
             const bool mon = e->mixed && period_end && s == cnt - 1;
             t[(size_t)s * M + i] = step_args(h, par, tr, k0 + s, mon);
+            if (e->d_tmaps && h->tma_stage) t[(size_t)s * M + i].tmap = e->d_tmaps + 2 * i + par;
             par ^= 1;
             tr = false;
         }

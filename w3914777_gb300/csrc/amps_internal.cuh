@@ -81,6 +81,7 @@ struct StepArgs {
     int monitor_now, monitor_kind, samples, mfield, mu_lap_fp64, cadence;
     int half_arith;           // grain growth: AMPS_HALF_FP32 / _REF / _HFMA2 (half tiles' arithmetic)
     int tma_stage;            // grain growth: the launch carries a tensor map of the FP32 input (bulk staging)
+    const CUtensorMap *tmap;  // ensemble steps: the member's tensor map of its FP32 input in global memory (or null)
     double *metric;           // [ntiles]
     double *snap;             // temporal snapshot: [nmon][ntiles][16] or [nmon][n]
     int *flags;               // bit 0: NaN/Inf seen; bit 1: a bounded device wait gave up

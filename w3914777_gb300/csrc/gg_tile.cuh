@@ -540,9 +540,10 @@ __device__ __forceinline__ void gg_tile_step(const StepArgs &a, float *sm, uint8
 // gg_tile_step out of line, for callers whose StepArgs live in shared
 // memory (inlined, their loads are hoisted and spill).
 template <int T, bool REF, bool MON>
-__device__ __noinline__ void gg_tile_step_call(const StepArgs &a, float *sm, uint8_t *ntier, double *red, int tile)
+__device__ __noinline__ void gg_tile_step_call(const StepArgs &a, float *sm, uint8_t *ntier, double *red, int tile,
+                                               uint64_t *bar)
 {
-    gg_tile_step<T, REF, MON ? -1 : 0>(a, sm, ntier, red, tile);
+    gg_tile_step<T, REF, MON ? -1 : 0>(a, sm, ntier, red, tile, a.tmap, bar);
 }
 
 // Fused all-tier step: at most 64 registers, so that four CTAs share an SM.

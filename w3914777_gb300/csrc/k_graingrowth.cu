@@ -420,12 +420,14 @@ template <int T, bool REF, bool MON>
 __global__ void __launch_bounds__(kThreads, 2)
     gg_ens_kernel(const StepArgs *__restrict__ table, const int2 *__restrict__ items, int nitems, int *queue)
 {
-    extern __shared__ __align__(16) unsigned char smraw[];
+    extern __shared__ __align__(128) unsigned char smraw[];
     __shared__ double red[kThreads / 32];
     __shared__ uint8_t ntier[9];
     __shared__ __align__(16) StepArgs sa;
     __shared__ int sw;
-    float *sm = reinterpret_cast<float *>(smraw);
+    __shared__ __align__(8) uint64_t bar;
+    // 128-byte aligned staging (gg_smem_bytes adds the slack) for the members' tensor copies
+    float *sm = reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(smraw) + 127) & ~uintptr_t(127));
     static_assert(sizeof(StepArgs) % 4 == 0, "StepArgs copied as 32-bit words");
     int member = -1;
     for (;;) {
@@ -441,7 +443,7 @@ __global__ void __launch_bounds__(kThreads, 2)
             member = it.x;
         }
         __syncthreads();
-        gg_tile_step_call<T, REF, MON>(sa, sm, ntier, red, it.y);
+        gg_tile_step_call<T, REF, MON>(sa, sm, ntier, red, it.y, &bar);
         __syncthreads();
     }
     if (threadIdx.x == 0) {
