@@ -647,6 +647,23 @@ def run_adjoint_gg(steps=200, n=1024, q=8):
     return out
 
 
+ENSEMBLE_TUNED = os.path.join(ROOT, "w3914777_gb300", "tuned", "ensemble_64.json")
+
+
+def ensemble_overrides():
+    """Tile, monitor and thresholds of the 64-member ensemble: the autotuner's
+    choice for the ensemble itself (`python -m w3914777_gb300.autotune
+    ensemble`), else the single-run workload's monitor and thresholds."""
+    try:
+        with open(ENSEMBLE_TUNED) as f:
+            return dict(json.load(f)["best"]["overrides"]), "autotune (ensemble)"
+    except Exception:
+        tuned = load_tuned()
+        ov = dict(tuned["overrides"]) if tuned else {}
+        ov.pop("tile", None)
+        return ov, "single-run tuning"
+
+
 def run_ensemble(steps=5000, check_steps=1000, count=64, seed=2024):
     """64 grain-growth runs (sides 128..1024, Q in {4,8,12,16}, kappa ~ U[1,3],
     L ~ U[0.5,2], per-member stable dt) advanced by one persistent launch per
@@ -657,9 +674,7 @@ def run_ensemble(steps=5000, check_steps=1000, count=64, seed=2024):
     import torch
     from w3914777_gb300 import amps, ensemble
 
-    tuned = load_tuned()
-    ov = dict(tuned["overrides"]) if tuned else {}
-    ov.pop("tile", None)
+    ov, tuned_by = ensemble_overrides()
     params = ensemble.member_params(count=count, seed=seed, overrides=ov)
     cells = ensemble.cells(params)
     stream = torch.cuda.Stream()
@@ -723,6 +738,7 @@ def run_ensemble(steps=5000, check_steps=1000, count=64, seed=2024):
         "speedup_vs_plain_fp64": ms_64 / ms_mix,
         "max_abs_err_vs_fp64": err, "err_steps": check_steps,
         "tier_mix": {k: float(v) / float(ts.sum()) for k, v in zip(("half", "fp32", "fp64"), ts)},
+        "tuned_by": tuned_by, "tile": params[0].tile, "thresholds": [params[0].thr_lo, params[0].thr_hi],
     }
 
 
@@ -851,9 +867,7 @@ def run_profile_case(args):
     model = args.profile_model
     if model == "ensemble":
         from w3914777_gb300 import ensemble
-        tuned = load_tuned()
-        ov = dict(tuned["overrides"]) if tuned else {}
-        ov.pop("tile", None)
+        ov, _ = ensemble_overrides()
         params = ensemble.member_params(count=64, seed=2024, overrides=ov)[:args.profile_case]
         sims = [w.Simulation(p, init=w.INIT_SEEDED) for p in params]
         with w.Ensemble(sims) as ens:
