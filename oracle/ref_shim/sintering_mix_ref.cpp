@@ -1,0 +1,148 @@
+/*
+ * sintering_mix_ref.cpp -- the reference's adaptive mixed-precision
+ * sintering (AMSTENCIL: half2 low tier, double high tier) compiled in place
+ * from the read-only reference tree for the CPU: con1_mix, con2_mix,
+ * phi1_mix, phi2_mix (sintering/function.h:161-774), dataprepare,
+ * get_max_diff1/2, get_type, data_sychro_duringcomputation and
+ * data_sychro_aftercomputation (sintering/tools.h), driven by the initial
+ * state and time loop of sintering/main.cu:45-206.  TEST INFRASTRUCTURE
+ * ONLY: it pins the library's reference-faithful mixed sintering on the CPU.
+ *
+ * Header state: function.h as shipped (paras/para5.h, typedef double
+ * highprecision), with AMSTENCIL defined as sintering/end2end_run1.py writes
+ * it on function.h's strategy line; the monitor kernel is chosen by
+ * REF_MONITOR (the shipped Monitor2 line stays defined: con1_mix then also
+ * refreshes the snapshot, which Monitor1 never reads).  The threshold line
+ * the script rewrites per run becomes a run-time value.  Half arithmetic runs through
+ * the host versions of cuda_fp16.h's half2 operators, each operation
+ * rounded on its own.
+ */
+#include "cuda_cpu_shim.h"
+#define AMSTENCIL
+#include REF_TOOLS_H
+
+/* get_type (sintering/tools.h:38-56) at a run-time threshold: the same rule
+ * the reference compiles against its `const threshold` line (5-point tile
+ * maximum, not periodic; < threshold -> 1, >= threshold -> 2), restated
+ * because sintering/tools.h includes function.h itself and leaves no point
+ * at which that constant could be replaced.  The grain-growth build runs
+ * the reference's own get_type, which is the same code. */
+static void get_type_rt(const double *md, int *type_old, int *type_con, double thr)
+{
+    for (int y = 0; y < unitdimY; ++y)
+        for (int x = 0; x < unitdimX; ++x) {
+            const int t = y * unitdimX + x;
+            type_old[t] = type_con[t];
+            double m = md[t];
+            m = y < unitdimY - 1 ? std::max(m, md[t + unitdimX]) : m;
+            m = y > 0 ? std::max(m, md[t - unitdimX]) : m;
+            m = x < unitdimX - 1 ? std::max(m, md[t + 1]) : m;
+            m = x > 0 ? std::max(m, md[t - 1]) : m;
+            if (m < thr) type_con[t] = 1;
+            else if (m >= thr) type_con[t] = 2;
+        }
+}
+
+extern "C" {
+int ref_sintmix_dims(void) { return dimX; }
+int ref_sintmix_tiles(void) { return unitdimX * unitdimY; }
+
+/* sintering/main.cu:45-206 (AMSTENCIL branch) for `steps` steps at `thr`.
+ * types: [ceil(steps/10)][tiles] uint8, type_con after each classification
+ * (1 = half2, 2 = high).  c, e1, e2: the high arrays at the end, low tiles
+ * gathered from their half2 arrays (data_sychro_aftercomputation). */
+void ref_sintmix_run(int steps, double thr, double *c_out, double *e1_out, double *e2_out, unsigned char *types)
+{
+    const size_t n = (size_t)dimX * dimY, nh = (size_t)dimXd2 * dimY, nt = (size_t)unitdimX * unitdimY;
+    double *hi = (double *)calloc(14 * n, sizeof(double));
+    double *con = hi, *eta1 = hi + n, *eta2 = hi + 2 * n, *eta1_out = hi + 3 * n, *eta2_out = hi + 4 * n,
+           *dummy = hi + 5 * n, *con_lap = hi + 6 * n, *eta1_lap = hi + 7 * n, *eta2_lap = hi + 8 * n,
+           *dummy_lap = hi + 9 * n, *dfdcon = hi + 10 * n, *dfdeta1 = hi + 11 * n, *dfdeta2 = hi + 12 * n,
+           *con_old = hi + 13 * n;
+    half2 *lo = (half2 *)calloc(13 * nh, sizeof(half2));
+    half2 *hcon = lo, *heta1 = lo + nh, *heta2 = lo + 2 * nh, *heta1_out = lo + 3 * nh, *heta2_out = lo + 4 * nh,
+          *hdummy = lo + 5 * nh, *hcon_lap = lo + 6 * nh, *heta1_lap = lo + 7 * nh, *heta2_lap = lo + 8 * nh,
+          *hdummy_lap = lo + 9 * nh, *hdfdcon = lo + 10 * nh, *hdfdeta1 = lo + 11 * nh, *hdfdeta2 = lo + 12 * nh;
+    int *type_con = (int *)calloc(nt, sizeof(int)), *type_old = (int *)calloc(nt, sizeof(int));
+    double *max_diff_con = (double *)calloc(nt, sizeof(double));
+    for (int y = 1; y <= dimY; y++)
+        for (int x = 1; x <= dimX; x++) {
+            float dis1 = sqrt(pow(x - Rx1, 2) + pow(y - Ry1, 2));
+            float dis2 = sqrt(pow(x - Rx1, 2) + pow(y - Ry2, 2));
+            if (dis1 <= R1) {
+                con[(y - 1) * dimX + x - 1] = 1;
+                eta1[(y - 1) * dimX + x - 1] = 1;
+            }
+            if (dis2 <= R2) {
+                con[(y - 1) * dimX + x - 1] = 1;
+                eta2[(y - 1) * dimX + x - 1] = 1;
+                eta1[(y - 1) * dimX + x - 1] = 0.0;
+            }
+        }
+    for (size_t i = 0; i < n; i++) con_old[i] = con[i] == 0 ? 1.0 : 0.0;
+    const dim3 blocks_dataprepare(32, 32), grids_dataprepare(dimX / 32 / 2, dimY / 32);
+    shim_launch(grids_dataprepare, blocks_dataprepare, dataprepare, con, hcon);
+    shim_launch(grids_dataprepare, blocks_dataprepare, dataprepare, eta1, heta1);
+    shim_launch(grids_dataprepare, blocks_dataprepare, dataprepare, eta2, heta2);
+    const half2 hcoefm = lowprecision2highprecision(coefm), hcoefk = lowprecision2highprecision(coefk),
+                hcoefl = lowprecision2highprecision(coefl), hdvol = lowprecision2highprecision(dvol),
+                hdvap = lowprecision2highprecision(dvap), hdsur = lowprecision2highprecision(dsur),
+                hdgrb = lowprecision2highprecision(dgrb), hdxdy = lowprecision2highprecision(dxdy),
+                hdtime = lowprecision2highprecision(dtime), hcf = lowprecision2highprecision(4.0),
+                hzpfive = lowprecision2highprecision(0.5), hone = lowprecision2highprecision(1.0),
+                htwo = lowprecision2highprecision(2.0), hfour = lowprecision2highprecision(4.0),
+                hsix = lowprecision2highprecision(6.0), hten = lowprecision2highprecision(10.0),
+                htwelve = lowprecision2highprecision(12.0), hfifteen = lowprecision2highprecision(15.0),
+                hthirtytwo = lowprecision2highprecision(32.0), highbound = lowprecision2highprecision(1),
+                lowbound = lowprecision2highprecision(0.0);
+    const dim3 blocks(uxd2, unity), grids(2, 1, unitdimX * unitdimY);
+    const dim3 blocks_detect(unitdimX > 32 ? 32 : unitdimX, unitdimY > 32 ? 32 : unitdimY);
+    const dim3 grids_detect(unitdimX > 32 ? unitdimX / 32 : 1, unitdimY > 32 ? unitdimY / 32 : 1);
+    const dim3 sync_blocks(uxd2, unity), sync_grids(1, 1, unitdimX * unitdimY);
+    int period = 0;
+    for (int i = 0; i < steps; i++) {
+        if (i % 10 == 0) {
+#if REF_MONITOR == 1
+            shim_launch(grids_detect, blocks_detect, get_max_diff1, con, max_diff_con);
+#else
+            shim_launch(grids_detect, blocks_detect, get_max_diff2, con_old, con, max_diff_con);
+#endif
+            get_type_rt(max_diff_con, type_old, type_con, thr);
+            shim_launch(sync_grids, sync_blocks, data_sychro_duringcomputation, con, eta1, eta2, hcon, heta1, heta2,
+                        type_old, type_con);
+            if (types)
+                for (size_t t = 0; t < nt; ++t) types[(size_t)period * nt + t] = (unsigned char)type_con[t];
+            ++period;
+        }
+        shim_launch(grids, blocks, con1_mix, type_con, con, con_old, con_lap, eta1, eta2, dfdcon, dummy, hcon,
+                    hcon_lap, heta1, heta2, hdfdcon, hdummy, hcf, hdxdy, hsix, hzpfive, hone, htwo, hfour,
+                    hthirtytwo, hcoefm, i);
+        shim_launch(grids, blocks, con2_mix, type_con, dummy, dummy_lap, con, eta1, eta2, hdummy, hdummy_lap, hcon,
+                    heta1, heta2, hcf, hdxdy, hone, htwo, hsix, hten, hfifteen, hdgrb, hdsur, hdtime, hdvap, hdvol,
+                    highbound, lowbound, i);
+        shim_launch(grids, blocks, phi1_mix, type_con, eta1, eta1_out, eta2, eta1_lap, dfdeta1, con, heta1,
+                    heta1_out, heta2, heta1_lap, hdfdeta1, hcon, hcf, hdxdy, hzpfive, hone, htwo, htwelve, hdtime,
+                    hcoefl, hcoefk, highbound, lowbound, i);
+        shim_launch(grids, blocks, phi2_mix, type_con, eta2, eta2_out, eta1, eta2_lap, dfdeta2, con, heta2,
+                    heta2_out, heta1, heta2_lap, hdfdeta2, hcon, hcf, hdxdy, hzpfive, hone, htwo, htwelve, hdtime,
+                    hcoefl, hcoefk, highbound, lowbound, i);
+        std::swap(eta1, eta1_out);
+        std::swap(eta2, eta2_out);
+        std::swap(heta1, heta1_out);
+        std::swap(heta2, heta2_out);
+    }
+    shim_launch(grids_dataprepare, blocks_dataprepare, data_sychro_aftercomputation, con, hcon, type_con);
+    shim_launch(grids_dataprepare, blocks_dataprepare, data_sychro_aftercomputation, eta1, heta1, type_con);
+    shim_launch(grids_dataprepare, blocks_dataprepare, data_sychro_aftercomputation, eta2, heta2, type_con);
+    for (size_t k = 0; k < n; ++k) {
+        c_out[k] = con[k];
+        e1_out[k] = eta1[k];
+        e2_out[k] = eta2[k];
+    }
+    free(hi);
+    free(lo);
+    free(type_con);
+    free(type_old);
+    free(max_diff_con);
+}
+}

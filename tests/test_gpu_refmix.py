@@ -118,3 +118,58 @@ def test_hfma2_half_tiles_rerun_and_error(monitor, thr):
     print(f"{k} HFMA2: mean |d eta2| {d2.mean():.3e} (reference half2 {ref_err[1]:.3e}), max {d2.max():.3e} "
           f"(reference {ref_err[3]:.3e})")
     assert d2.mean() <= 4 * ref_err[1] + 1e-12 and d2.max() <= 4 * ref_err[3] + 1e-12
+
+
+SINT_GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "sintering_mix_ref.npz")
+
+
+def _sint_runs():
+    return [(int(m), float(t)) for m, t in np.load(SINT_GOLD)["runs"]]
+
+
+_sint_pure_cache = {}
+
+
+@pytest.mark.parametrize("monitor,thr", _sint_runs())
+def test_reference_mixed_sintering_decisions_fields_and_error(monitor, thr):
+    """Sintering in the reference's own mixed arithmetic (half_arith =
+    AMPS_HALF_REF: the chemical potential at each cell's owner tier, half
+    tiles in binary16 in the reference's order) against the reference's
+    AMSTENCIL runs on the CPU (tests/golden/sintering_mix_ref.npz; para5,
+    512^2, 16^2 tiles, 500 steps).  Bars: every period's tier map equals the
+    reference's type_con; the final c, eta1, eta2 within 1e-9 of the
+    reference's (FP64 tiles call the device pow(), the reference's CPU build
+    glibc's; the half tiles round those ulps away or keep them); the mean
+    and max |mixed - plain FP64| per field at most the reference's own
+    + 1e-9."""
+    w = amps()
+    g = np.load(SINT_GOLD)
+    k = _key(monitor, thr)
+    steps = int(g["steps"])
+    p = w.Params.preset("sintering", 5, mode="end2end_mix", monitor=monitor, monitor_samples=0, monitor_field=0,
+                        thr_lo=thr, thr_hi=thr, ref_order=1, half_arith=w.HALF_REF, max_log=64)
+    with w.Simulation(p, init=w.INIT_REFERENCE) as s:
+        s.run(steps)
+        f = s.fields()
+        log = s.decision_log()
+        st = s.stats()
+    ref_types = g[k + "_types"]
+    ours = np.where(log.reshape(log.shape[0], -1) == w.TIER_HALF, 1, 2).astype(np.uint8)
+    bad = [i for i in range(ref_types.shape[0]) if not np.array_equal(ours[i], ref_types[i])]
+    print(f"sintering {k}: half tiles first/last period {int((ours[0] == 1).sum())}/"
+          f"{int((ours[ref_types.shape[0] - 1] == 1).sum())}, periods differing: {bad[:5]}, tiles {st['tile_steps']}")
+    assert not bad
+    if k + "_c" in g.files:
+        e = max(float(np.abs(f[i] - g[k + n]).max()) for i, n in enumerate(("_c", "_eta1", "_eta2")))
+        print(f"sintering {k}: fields vs the reference's mixed run: {e:.3e}")
+        assert e <= 1e-9
+    if steps not in _sint_pure_cache:
+        q = w.Params.preset("sintering", 5, mode="purehigh", ref_order=1)
+        with w.Simulation(q, init=w.INIT_REFERENCE) as s:
+            s.run(steps)
+            _sint_pure_cache[steps] = s.fields()
+    pure = _sint_pure_cache[steps]
+    d = [np.abs(f[i] - pure[i]) for i in range(3)]
+    ours_err = np.array([x.mean() for x in d] + [x.max() for x in d])
+    print(f"sintering {k}: error vs plain FP64: ours {ours_err}, reference {g[k + '_err']}")
+    assert np.all(ours_err <= g[k + "_err"] + 1e-9)

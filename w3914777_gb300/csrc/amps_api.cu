@@ -79,6 +79,7 @@ struct amps_handle {
     // grain growth: persistent TMA kernel over the FP32 ping-pong buffers
     bool use_tma = false;
     bool tma_stage = false;  // tm[] encoded: the fused step stages interior tiles by tensor copy
+    double *d_mu = nullptr;  // sintering, AMPS_HALF_REF: the chemical potential of every cell
     int tma_grid = 0;
     alignas(64) CUtensorMap tm[2];
     // diagnostics scratch (allocated on first use): lab, parent (n ints each),
@@ -175,6 +176,9 @@ static Phys make_phys(const amps_params &p)
         const double gh[8] = {ph.dt, ph.mobil, ph.grcoef, ph.dxdy, ph.gamma, ph.dt * ph.mobil,
                               ph.grcoef * ph.inv_dxdy, 2.0 * ph.gamma};
         for (int i = 0; i < 8; ++i) ph.gg_h[i] = __half_as_ushort(__float2half_rn((float)gh[i]));
+        const double sh[11] = {ph.coefm, ph.coefk, ph.coefl, ph.dvol, ph.dvap, ph.dsur, ph.dgrb, ph.dxdy, ph.dt,
+                               2.0 * ph.A, ph.B};
+        for (int i = 0; i < 11; ++i) ph.sn_h[i] = __half_as_ushort(__float2half_rn((float)sh[i]));
     }
     double *k = ph.kd;
     if (p.model == AMPS_KOBAYASHI) {
@@ -211,7 +215,8 @@ static void free_all(amps_handle *h)
             if (h->store[t][q]) cudaFree(h->store[t][q]);
     void *ps[] = {h->d_tier_prev, h->d_tier_cur, h->d_lists, h->d_order, h->d_counts, h->d_metric, h->d_snap, h->d_stats,
                   h->d_flags, h->d_log, h->d_log_n, h->d_step_base, h->d_stage, h->d_partials, h->d_out,
-                  h->d_diag, h->d_sched, h->d_sched_i, h->d_msnap, h->d_mmetric, h->d_snap_keep, h->d_flow};
+                  h->d_diag, h->d_sched, h->d_sched_i, h->d_msnap, h->d_mmetric, h->d_snap_keep, h->d_flow,
+                  h->d_mu};
     for (void *q : ps)
         if (q) cudaFree(q);
     if (h->h_pinned) cudaFreeHost(h->h_pinned);
@@ -281,6 +286,8 @@ extern "C" int amps_create(const amps_params *p, amps_handle **out)
     ALLOC(h->d_log_n, sizeof(int), "log count");
     if (p->max_log > 0) ALLOC(h->d_log, (size_t)p->max_log * h->ntiles, "decision log");
     ALLOC(h->d_step_base, sizeof(int64_t), "step counter");
+    if (p->model == AMPS_SINTERING && p->half_arith == AMPS_HALF_REF)
+        ALLOC(h->d_mu, sizeof(double) * h->n, "chemical potential");
     ALLOC(h->d_stage, sizeof(double) * h->nf * h->n, "staging");
     ALLOC(h->d_partials, sizeof(double) * 2 * 1024, "partials");
     ALLOC(h->d_out, sizeof(double) * 4, "result");
@@ -674,6 +681,25 @@ static int launch_step(amps_handle *h, int step_off, bool monitor_now)
                                                h->tma_stage ? &h->tm[h->parity] : nullptr);
         if (e != cudaSuccess) FAIL(h, AMPS_ERR_CUDA, "step kernel launch: %s", cudaGetErrorString(e));
         ++h->launches;
+        h->parity ^= 1;
+        h->transition = false;
+        return AMPS_OK;
+    }
+    if (h->d_mu) {
+        // sintering in the reference's own mixed arithmetic: the chemical
+        // potential pass, then the update pass, every tier in each (index 3)
+        amps_handle::Ev ev{3, nullptr, nullptr, 1};
+        if (h->profiling) {
+            const int r = prof_begin(h, ev);
+            if (r) return r;
+        }
+        cudaError_t e = sint_ref_launch(h->T, a, h->d_mu, h->ntiles, h->stream);
+        if (e != cudaSuccess) FAIL(h, AMPS_ERR_CUDA, "step kernel launch: %s", cudaGetErrorString(e));
+        h->launches += 2;
+        if (h->profiling) {
+            CK(h, prof_record(h, ev.b));
+            h->evs.push_back(ev);
+        }
         h->parity ^= 1;
         h->transition = false;
         return AMPS_OK;

@@ -176,8 +176,15 @@ extern "C" int amps_check_params(const amps_params *p, char *msg, size_t len)
     if (p->mode == AMPS_GRAM1 || p->mode == AMPS_GRAM2)
         if (!(p->gram_ratio >= 0 && p->gram_ratio <= 1)) BAD("gram_ratio must be in [0,1]");
     if (p->half_arith < AMPS_HALF_FP32 || p->half_arith > AMPS_HALF_HFMA2) BAD("half_arith must be 0, 1 or 2");
-    if (p->half_arith != AMPS_HALF_FP32 && p->model != AMPS_GRAINGROWTH)
-        BAD("binary16 arithmetic (half_arith %d) is built for grain growth only", p->half_arith);
+    if (p->half_arith == AMPS_HALF_HFMA2 && p->model != AMPS_GRAINGROWTH)
+        BAD("the HFMA2 half arithmetic is built for grain growth only");
+    if (p->half_arith == AMPS_HALF_REF && p->model == AMPS_KOBAYASHI)
+        BAD("the reference's half arithmetic is built for grain growth and sintering (Kobayashi's needs "
+            "device-only half transcendentals)");
+    if (p->half_arith == AMPS_HALF_REF && p->model == AMPS_SINTERING &&
+        (p->high_tier != AMPS_TIER_FP64 || (p->mode == AMPS_END2END_MIX && p->thr_lo != p->thr_hi)))
+        BAD("sintering with the reference's half arithmetic has the reference's two tiers: half and FP64 "
+            "(high_tier FP64, thr_lo == thr_hi)");
     if (p->ref_snapshot != 0 && p->ref_snapshot != 1) BAD("ref_snapshot must be 0 or 1");
     if (msg && len) msg[0] = 0;
     return AMPS_OK;

@@ -40,6 +40,10 @@ struct Phys {
     // double constant rounded to float, then to half, as the reference's
     // __float2half2_rn(double) calls do (graingrowth/end2end_mix.cu:59-67)
     unsigned short gg_h[8];
+    // sintering's binary16 constants (half_arith = AMPS_HALF_REF; enum SintHalf),
+    // rounded double -> float -> half as sintering/tools.h's
+    // lowprecision2highprecision(double) rounds them
+    unsigned short sn_h[12];
     // Kobayashi and sintering constants of the non-reference-order tiles,
     // derived on the host in double (kd) and rounded to float (kf), the same
     // values the tiles would derive per thread (index: enum KConst)
@@ -60,6 +64,8 @@ enum KConst {
 // Indices of Phys::gg_h: dt, L, kappa, dx*dy, gamma (the reference's
 // AMPS_HALF_REF expressions) and dt*L, kappa/(dx*dy), 2*gamma (the HFMA2 form).
 enum GgHalf { GH_DT, GH_MOB, GH_KAP, GH_DXDY, GH_GAM, GH_DTM, GH_KINV, GH_G2 };
+// Indices of Phys::sn_h: coefm, coefk, coefl, dvol, dvap, dsur, dgrb, dx*dy, dt, 2A, B.
+enum SintHalf { SH_COEFM, SH_COEFK, SH_COEFL, SH_DVOL, SH_DVAP, SH_DSUR, SH_DGRB, SH_DXDY, SH_DT, SH_A2, SH_B };
 
 // Constant i of Phys::kd / Phys::kf at the tile's compute type.
 template <typename CT> __device__ __forceinline__ CT kc(const Phys &ph, int i);

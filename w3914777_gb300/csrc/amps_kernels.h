@@ -27,6 +27,9 @@ cudaError_t gg_launch_half(int tile, bool ref, const StepArgs &a, int grid, size
 cudaError_t gg_prepare_half(int tile, bool ref, int half_arith);
 cudaError_t kob_prepare(int tile, int tier, bool ref);
 cudaError_t sint_prepare(int tile, int tier, bool ref, bool mu64);
+// Sintering in the reference's own mixed arithmetic (half_arith = AMPS_HALF_REF):
+// mu of every cell at its owner's tier into mu[n], then c' and every eta'.
+cudaError_t sint_ref_launch(int tile, const StepArgs &a, double *mu, int grid, cudaStream_t s);
 // Multi-step grain-growth kernel (32x32 tiles, the fused step's arithmetic):
 // `nsteps` consecutive steps without a tier change or a monitor in one
 // launch, a CTA per (step, tile); a0 the arguments of the first (and every
