@@ -79,12 +79,14 @@ enum { AMPS_BC_PERIODIC = 0, AMPS_BC_NOFLUX = 1 };
  * estimate of Monitor2 that needs no snapshot; no reference counterpart) */
 enum { AMPS_MONITOR_SPA = 1, AMPS_MONITOR_TEM = 2, AMPS_MONITOR_RATE = 3 };
 
-/* arithmetic of half tiles (amps_params.half_arith; grain growth) */
+/* arithmetic of half tiles (amps_params.half_arith; grain growth, sintering) */
 enum {
     AMPS_HALF_FP32 = 0,  /* binary16 storage, FP32 arithmetic (the default) */
-    AMPS_HALF_REF = 1,   /* binary16 arithmetic on adjacent-column pairs, every +, -, *, / rounded in the
-                            reference's expression order (graingrowth/function.h:163-166): the parity
-                            path of the reference's AMSTENCIL mixed mode */
+    AMPS_HALF_REF = 1,   /* binary16 arithmetic, every +, -, *, / rounded in the reference's expression
+                            order: grain growth on adjacent-column pairs (graingrowth/function.h:163-166),
+                            sintering per cell with the chemical potential at each cell's owner tier
+                            (sintering/function.h:245-249,401-411,556-565; FP64 high tier, one
+                            threshold): the parity path of the reference's AMSTENCIL mixed mode */
     AMPS_HALF_HFMA2 = 2  /* binary16 pairs with fused multiply-adds (HFMA2) */
 };
 
@@ -135,7 +137,8 @@ typedef struct amps_params {
     double init_r2, init_r, rmin, rmax, init_amp;
     int init_offset;
     uint64_t seed;
-    int half_arith;       /* AMPS_HALF_FP32 / AMPS_HALF_REF / AMPS_HALF_HFMA2 (grain growth) */
+    int half_arith;       /* AMPS_HALF_FP32 / AMPS_HALF_REF (grain growth, sintering) / AMPS_HALF_HFMA2
+                             (grain growth) */
     int ref_snapshot;     /* 1: the temporal monitor's lattice snapshot as the reference keeps it: a tile
                              computed at half refreshes only the first half of its columns
                              (graingrowth/function.h:38-39,68-73, snowflake/function.h:69-70,106-113,

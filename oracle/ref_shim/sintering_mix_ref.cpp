@@ -15,7 +15,10 @@
  * refreshes the snapshot, which Monitor1 never reads).  The threshold line
  * the script rewrites per run becomes a run-time value.  Half arithmetic runs through
  * the host versions of cuda_fp16.h's half2 operators, each operation
- * rounded on its own.
+ * rounded on its own.  Built with SHIM_CUBE_RN (cuda_cpu_shim.h): the
+ * reference's pow(x, 3) is the correctly rounded cube, as in the library's
+ * reference-order sintering kernels -- this run is chaotic at the ulp level,
+ * so the two sides need one cube to agree bit for bit.
  */
 #include "cuda_cpu_shim.h"
 #define AMSTENCIL

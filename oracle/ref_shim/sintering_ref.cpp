@@ -4,7 +4,10 @@
  * compiled in place from the read-only reference tree for the CPU, in the
  * shipped header state (#define PURE; function.h includes paras/para5.h, whose
  * highprecision is already double).  The step sequence follows
- * sintering/main.cu:136-147.  TEST INFRASTRUCTURE ONLY.
+ * sintering/main.cu:136-147.  Built twice: as shipped (libref_sintering.so)
+ * and with SHIM_CUBE_RN (libref_sintering_rn.so, pow(x, 3) the correctly
+ * rounded cube), the plain run the mixed golden is measured against.
+ * TEST INFRASTRUCTURE ONLY.
  */
 #include "cuda_cpu_shim.h"
 #include REF_FUNCTION_H

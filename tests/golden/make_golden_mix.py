@@ -8,7 +8,12 @@ steps as the scripts set `timesteps`:
   grain growth: graingrowth/end2end_mix.cu with graingrowth/function.h:33-277
     and graingrowth/tools.h, parameter set para1 (512x512, 16x16 tiles);
   sintering: sintering/main.cu:45-206 with sintering/function.h:161-774 and
-    sintering/tools.h, the shipped parameter set para5 (512x512).
+    sintering/tools.h, the shipped parameter set para5 (512x512), built with
+    SHIM_CUBE_RN: pow(x, 3) is the correctly rounded cube, on both sides of
+    every comparison.  This run is chaotic at the ulp level (a one-ulp change
+    grows about 1.5x per step; the two particles dissolve into clamped cells),
+    and the last bit of pow(x, 3) differs between the C library, CUDA and a
+    correctly rounded cube, so a bit-level pin needs one cube everywhere.
 
 Per run (key prefix m<monitor>_<threshold>):
   types   [periods][1024] uint8: type_curr after each classification
@@ -87,7 +92,9 @@ def _sint_job(args):
 
 
 def run_sint_pure(steps=STEPS):
-    R = ob.ref_lib("sintering")
+    """The reference's plain sintering, built like the mixed runs with pow(x, 3)
+    as the correctly rounded cube (libref_sintering_rn.so)."""
+    R = ob.ref_lib("sintering_rn")
     n = R.ref_sint_dims()
     pr = ob.ref_params("sintering", 15)
     c, e1, e2 = ob.sint_init_two(n, n, pr[12], pr[13], pr[10], pr[14], pr[11])
@@ -97,7 +104,8 @@ def run_sint_pure(steps=STEPS):
 
 def make_sintering():
     for m in (1, 2):
-        if not os.path.exists(os.path.join(ob.REF_DIR, f"libref_sintmix_m{m}.so")):
+        if not os.path.exists(os.path.join(ob.REF_DIR, f"libref_sintmix_m{m}.so")) or \
+                not os.path.exists(os.path.join(ob.REF_DIR, "libref_sintering_rn.so")):
             raise SystemExit("oracle/_ref/libref_sintmix_m*.so missing: run `make -C oracle ref`")
     with mp.get_context("spawn").Pool(min(len(RUNS), os.cpu_count() or 1)) as pool:
         results = dict(pool.map(_sint_job, RUNS))

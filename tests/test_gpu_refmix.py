@@ -136,12 +136,13 @@ def test_reference_mixed_sintering_decisions_fields_and_error(monitor, thr):
     AMPS_HALF_REF: the chemical potential at each cell's owner tier, half
     tiles in binary16 in the reference's order) against the reference's
     AMSTENCIL runs on the CPU (tests/golden/sintering_mix_ref.npz; para5,
-    512^2, 16^2 tiles, 500 steps).  Bars: every period's tier map equals the
-    reference's type_con; the final c, eta1, eta2 within 1e-9 of the
-    reference's (FP64 tiles call the device pow(), the reference's CPU build
-    glibc's; the half tiles round those ulps away or keep them); the mean
-    and max |mixed - plain FP64| per field at most the reference's own
-    + 1e-9."""
+    512^2, 16^2 tiles, 500 steps).  Both sides take pow(x, 3) as the
+    correctly rounded cube: this run amplifies a one-ulp difference about
+    1.5x per step, so any other cube (the C library's, CUDA's) moves the
+    decisions within ~100 steps.  Bars: every period's tier map equals the
+    reference's type_con; the final c, eta1, eta2 equal the reference's bit
+    for bit; the max |mixed - plain FP64| per field equals the reference's,
+    the mean agrees to 1e-12 (numpy's summation order on each machine)."""
     w = amps()
     g = np.load(SINT_GOLD)
     k = _key(monitor, thr)
@@ -162,7 +163,7 @@ def test_reference_mixed_sintering_decisions_fields_and_error(monitor, thr):
     if k + "_c" in g.files:
         e = max(float(np.abs(f[i] - g[k + n]).max()) for i, n in enumerate(("_c", "_eta1", "_eta2")))
         print(f"sintering {k}: fields vs the reference's mixed run: {e:.3e}")
-        assert e <= 1e-9
+        assert e == 0.0
     if steps not in _sint_pure_cache:
         q = w.Params.preset("sintering", 5, mode="purehigh", ref_order=1)
         with w.Simulation(q, init=w.INIT_REFERENCE) as s:
@@ -172,4 +173,6 @@ def test_reference_mixed_sintering_decisions_fields_and_error(monitor, thr):
     d = [np.abs(f[i] - pure[i]) for i in range(3)]
     ours_err = np.array([x.mean() for x in d] + [x.max() for x in d])
     print(f"sintering {k}: error vs plain FP64: ours {ours_err}, reference {g[k + '_err']}")
-    assert np.all(ours_err <= g[k + "_err"] + 1e-9)
+    # the maxima bit for bit; the means within numpy's summation order
+    assert np.array_equal(ours_err[3:], g[k + "_err"][3:])
+    np.testing.assert_allclose(ours_err[:3], g[k + "_err"][:3], rtol=1e-12, atol=0)

@@ -164,6 +164,21 @@ inline cudaError_t launch_kernel(K kernel, int grid, size_t smem, cudaStream_t s
 __device__ __forceinline__ bool pos_zero(double x) { return __double_as_longlong(x) == 0; }
 __device__ __forceinline__ bool pos_zero(float x) { return __float_as_uint(x) == 0u; }
 
+// x^3 correctly rounded (to nearest), from error-free products (Dekker's
+// exact product through a fused multiply-add: x*x = p + pe exactly, p*x = hi
+// + he exactly, so x^3 = hi + he + pe*x with pe*x far below hi's last bit).
+// The reference's pow(x, 3) is a library call whose last bit depends on the
+// platform's pow; the reference-order sintering kernels take this cube so
+// that their FP64 tiles can be pinned bit for bit against the reference's
+// kernels built for the CPU with the same cube.  Each operation is rounded
+// on its own, in the order written here (the CPU build runs the same five).
+__device__ __forceinline__ double cube_rn(double x)
+{
+    const double p = __dmul_rn(x, x), pe = __fma_rn(x, x, -p);
+    const double hi = __dmul_rn(p, x), he = __fma_rn(p, x, -hi);
+    return __dadd_rn(hi, __dadd_rn(he, __dmul_rn(pe, x)));
+}
+
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 

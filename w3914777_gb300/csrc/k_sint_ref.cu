@@ -65,11 +65,11 @@ __global__ void __launch_bounds__(kThreads) sint_ref_mu_kernel(StepArgs a, doubl
             const double lap = __ddiv_rn(__dsub_rn(__dadd_rn(__dadd_rn(__dadd_rn(cw, ce), cs), cn), __dmul_rn(4.0, c)),
                                          ph.dxdy);
             const double e0 = cell<T>(a, 1, gx, gy);
-            double s2 = __dmul_rn(e0, e0), s3 = pow(e0, 3.0);
+            double s2 = __dmul_rn(e0, e0), s3 = cube_rn(e0);
             for (int k = 1; k < np; ++k) {
                 const double e = cell<T>(a, 1 + k, gx, gy);
                 s2 = __dadd_rn(s2, __dmul_rn(e, e));
-                s3 = __dadd_rn(s3, pow(e, 3.0));
+                s3 = __dadd_rn(s3, cube_rn(e));
             }
             const double A2 = 2.0 * ph.A;
             const double dfdc = __dadd_rn(
@@ -128,7 +128,7 @@ __global__ void __launch_bounds__(kThreads) sint_ref_update_kernel(StepArgs a, c
             // sintering/function.h:90-101 (con2_pure; the high branch of con2_mix)
             const double lapm = __ddiv_rn(__dsub_rn(__dadd_rn(__dadd_rn(__dadd_rn(mw, me), ms), mn), __dmul_rn(4.0, m0)),
                                           ph.dxdy);
-            const double phi = __dmul_rn(pow(c, 3.0), __dadd_rn(__dsub_rn(10.0, __dmul_rn(15.0, c)), __dmul_rn(6.0, __dmul_rn(c, c))));
+            const double phi = __dmul_rn(cube_rn(c), __dadd_rn(__dsub_rn(10.0, __dmul_rn(15.0, c)), __dmul_rn(6.0, __dmul_rn(c, c))));
             double sum = 0.0;
             for (int p = 0; p < np; ++p)
                 for (int q = p + 1; q < np; ++q)

@@ -151,11 +151,11 @@ __device__ __forceinline__ void sint_tile(const StepArgs &a, unsigned char *smra
             const double lap = __ddiv_rn(__dsub_rn(__dadd_rn(__dadd_rn(__dadd_rn(C[-1], C[1]), C[-SC::P]), C[SC::P]),
                                                    __dmul_rn(4.0, cc)), ph.dxdy);
             double e0 = SE::at(sme, 0, j + 1, i + SE::O);
-            double s2 = __dmul_rn(e0, e0), s3 = pow(e0, 3.0);
+            double s2 = __dmul_rn(e0, e0), s3 = cube_rn(e0);
             for (int k = 1; k < np; ++k) {
                 const double e = SE::at(sme, k, j + 1, i + SE::O);
                 s2 = __dadd_rn(s2, __dmul_rn(e, e));
-                s3 = __dadd_rn(s3, pow(e, 3.0));
+                s3 = __dadd_rn(s3, cube_rn(e));
             }
             const double A2 = 2.0 * ph.A;
             const double dfdc = __dadd_rn(
@@ -189,7 +189,7 @@ __device__ __forceinline__ void sint_tile(const StepArgs &a, unsigned char *smra
         if (REF) {
             const double lapm = __ddiv_rn(__dsub_rn(__dadd_rn(__dadd_rn(__dadd_rn(mu[o - 1], mu[o + 1]), mu[o - E]), mu[o + E]),
                                                     __dmul_rn(4.0, mu[o])), ph.dxdy);
-            const double phi = __dmul_rn(pow((double)cc, 3.0),
+            const double phi = __dmul_rn(cube_rn((double)cc),
                                          __dadd_rn(__dsub_rn(10.0, __dmul_rn(15.0, cc)), __dmul_rn(6.0, __dmul_rn(cc, cc))));
             double sum = 0.0;
             for (int p = 0; p < np; ++p)
