@@ -669,7 +669,7 @@ def ensemble_overrides():
 
 
 def run_ensemble(steps=5000, check_steps=1000, count=64, seed=2024):
-    """64 grain-growth runs (sides 128..1024, Q in {4,8,12,16}, kappa ~ U[1,3],
+    """64 grain-growth runs (any integer sides 128..1024, Q in {4,8,12,16}, kappa ~ U[1,3],
     L ~ U[0.5,2], per-member stable dt) advanced by one persistent launch per
     step, at the autotuned monitor and thresholds.  Times `steps` steps of the
     ensemble; compares, over `check_steps` steps, the same members run one
@@ -732,7 +732,8 @@ def run_ensemble(steps=5000, check_steps=1000, count=64, seed=2024):
         sm.close()
     ts = np.sum([st["tile_steps"] for st in stats], axis=0)
     return {
-        "workload": f"{count} grain-growth runs, sides 128..1024 (multiples of 32), Q in {{4,8,12,16}}, "
+        "workload": f"{count} grain-growth runs, square sides drawn log-uniformly in 128..1024 (any integer: "
+                    f"{sum(p.nx % p.tile != 0 for p in params)} members have partial edge tiles), Q in {{4,8,12,16}}, "
                     f"kappa~U[1,3], L~U[0.5,2], dt=min(0.05, 0.9*2/(12 L kappa)), seeded eta~U[-1e-3,1e-3], "
                     f"{steps} steps, one persistent tile-queue launch per step",
         "members": count, "cells_per_step": cells,

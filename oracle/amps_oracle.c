@@ -331,7 +331,9 @@ void orc_sample_points(int tile, int kind, int *pts4)
 
 void orc_monitor_spa(const double *f, int nx, int ny, int tile, int samples, double *metric)
 {
-    const int ntx = nx / tile, nty = ny / tile;
+    /* a side that is not a multiple of the tile: partial edge tiles, whose
+     * samples past the domain are skipped */
+    const int ntx = (nx + tile - 1) / tile, nty = (ny + tile - 1) / tile;
     int pts[4];
     orc_sample_points(tile, 1, pts);
     for (int ty = 0; ty < nty; ++ty)
@@ -344,6 +346,7 @@ void orc_monitor_spa(const double *f, int nx, int ny, int tile, int samples, dou
                 for (int k = 0; k < cnt; ++k) {
                     const int y = ty * tile + (samples ? j : pts[j]);
                     const int x = tx * tile + (samples ? k : pts[k]);
+                    if (x >= nx || y >= ny) continue;
                     const double v = f[(int64_t)y * nx + x];
                     if (v < mn) mn = v;
                     if (v > mx) mx = v;
@@ -355,7 +358,9 @@ void orc_monitor_spa(const double *f, int nx, int ny, int tile, int samples, dou
 void orc_monitor_tem(const double *f, const double *last, int nx, int ny, int tile, int samples,
                      double *metric)
 {
-    const int ntx = nx / tile, nty = ny / tile;
+    /* a side that is not a multiple of the tile: partial edge tiles, whose
+     * samples past the domain are skipped */
+    const int ntx = (nx + tile - 1) / tile, nty = (ny + tile - 1) / tile;
     int pts[4];
     orc_sample_points(tile, 2, pts);
     for (int ty = 0; ty < nty; ++ty)
@@ -366,6 +371,7 @@ void orc_monitor_tem(const double *f, const double *last, int nx, int ny, int ti
                 for (int k = 0; k < cnt; ++k) {
                     const int y = ty * tile + (samples ? j : pts[j]);
                     const int x = tx * tile + (samples ? k : pts[k]);
+                    if (x >= nx || y >= ny) continue;
                     const double d = fabs(last[(int64_t)y * nx + x] - f[(int64_t)y * nx + x]);
                     if (d > mx) mx = d;
                 }
@@ -377,7 +383,9 @@ void orc_monitor_rate(const double *f, const double *prev, int nx, int ny, int t
                       double *metric)
 {
     /* defined in FP32 arithmetic: max |float(f) - float(prev)|, times the cadence in double */
-    const int ntx = nx / tile, nty = ny / tile;
+    /* a side that is not a multiple of the tile: partial edge tiles, whose
+     * samples past the domain are skipped */
+    const int ntx = (nx + tile - 1) / tile, nty = (ny + tile - 1) / tile;
     int pts[4];
     orc_sample_points(tile, 2, pts);
     for (int ty = 0; ty < nty; ++ty)
@@ -388,6 +396,7 @@ void orc_monitor_rate(const double *f, const double *prev, int nx, int ny, int t
                 for (int k = 0; k < cnt; ++k) {
                     const int y = ty * tile + (samples ? j : pts[j]);
                     const int x = tx * tile + (samples ? k : pts[k]);
+                    if (x >= nx || y >= ny) continue;
                     const int64_t i = (int64_t)y * nx + x;
                     const float d = fabsf((float)f[i] - (float)prev[i]);
                     if (d > mx) mx = d;

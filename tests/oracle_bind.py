@@ -179,27 +179,31 @@ def sint_init_two(nx, ny, rx1, ry1, r1, ry2, r2):
 
 
 # -------------------------------------------------------------- monitor ----
+def _ntiles(nx, ny, tile):
+    return -(-ny // tile), -(-nx // tile)  # partial edge tiles on ragged sides
+
+
 def monitor_spa(f, tile, samples=0):
     ny, nx = f.shape
-    m = np.zeros((ny // tile) * (nx // tile))
+    m = np.zeros(_ntiles(nx, ny, tile))
     lib().orc_monitor_spa(ptr(np.ascontiguousarray(f)), nx, ny, tile, samples, ptr(m))
-    return m.reshape(ny // tile, nx // tile)
+    return m
 
 
 def monitor_tem(f, last, tile, samples=0):
     ny, nx = f.shape
-    m = np.zeros((ny // tile) * (nx // tile))
+    m = np.zeros(_ntiles(nx, ny, tile))
     lib().orc_monitor_tem(ptr(np.ascontiguousarray(f)), ptr(np.ascontiguousarray(last)), nx, ny, tile,
                           samples, ptr(m))
-    return m.reshape(ny // tile, nx // tile)
+    return m
 
 
 def monitor_rate(f, prev, tile, cadence, samples=0):
     ny, nx = f.shape
-    m = np.zeros((ny // tile) * (nx // tile))
+    m = np.zeros(_ntiles(nx, ny, tile))
     lib().orc_monitor_rate(ptr(np.ascontiguousarray(f)), ptr(np.ascontiguousarray(prev)), nx, ny, tile, samples,
                            cadence, ptr(m))
-    return m.reshape(ny // tile, nx // tile)
+    return m
 
 
 def classify(metric, thr_lo, thr_hi):

@@ -37,12 +37,31 @@ def test_status_strings_and_errors_never_exit():
     L = w.lib()
     assert L.amps_status_string(0) == b"ok"
     assert b"invalid" in L.amps_status_string(1)
-    p = w.Params.preset("graingrowth", 1, nx=100)  # not a multiple of the tile
+    p = w.Params.preset("kobayashi", 2, nx=100)  # not a multiple of the tile
     rc, msg = p.check()
     assert rc == 1 and "multiples" in msg
     with pytest.raises(w.AmpsError) as e:
         w.Simulation(p)
     assert e.value.status == 1
+
+
+def test_ragged_sides_grain_growth_only():
+    """Sides that are not multiples of the tile: grain growth computes the
+    partial edge tiles' valid cells; Kobayashi and sintering, the binary16
+    half-tile arithmetic and the reference's snapshot rule need whole tiles."""
+    w = amps()
+    gg = w.Params.preset("graingrowth", 0, nx=100, ny=77, nfields=4)
+    assert gg.check()[0] == 0
+    assert gg.replace(nx=33, ny=33, tile=32).check()[0] == 0
+    assert gg.replace(nx=31).check()[0] == 1                    # below one tile
+    assert gg.replace(half_arith=w.HALF_REF).check()[0] == 1
+    assert gg.replace(half_arith=w.HALF_HFMA2).check()[0] == 1
+    assert gg.replace(ref_snapshot=1).check()[0] == 1
+    assert gg.replace(nx=96, ny=64, half_arith=w.HALF_REF).check()[0] == 0
+    assert w.Params.preset("sintering", 0, nx=100, ny=96).check()[0] == 1
+    # the tile limit counts the partial tiles
+    rc, msg = w.Params.preset("graingrowth", 1, nx=23169, ny=23168, tile=16).check()
+    assert rc == 1 and "too many tiles" in msg
 
 
 def test_tile_count_limit():

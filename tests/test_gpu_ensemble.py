@@ -95,6 +95,31 @@ def test_ensemble_matches_individual_runs_plain(tier):
         assert sa["steps"] == sb["steps"]
 
 
+@pytest.mark.parametrize("monitor", [amps.MONITOR_RATE, amps.MONITOR_TEM])
+def test_ensemble_ragged_members_match_individual_runs(monitor):
+    """Members whose sides are not multiples of the tile (partial edge tiles,
+    storage of whole tiles), mixed with whole-tile members, as the ensemble
+    workload draws them: each member's fields, tiers and statistics equal its
+    run alone."""
+    specs = [(100, 4, 2.0, 1.0), (75, 3, 1.3, 1.7), (64, 8, 2.7, 0.6), (129, 2, 1.1, 1.9), (33, 5, 2.2, 1.2)]
+    params = []
+    for i, (side, q, kap, mob) in enumerate(specs):
+        p = amps.Params.preset(amps.GRAINGROWTH, 0, nx=side, ny=side, nfields=q, grcoef=kap, mobil=mob, tile=32,
+                               seed=300 + i, init_amp=0.3)
+        p.dt = ensemble.stable_dt(mob, kap)
+        for k, v in mixed(monitor).items():
+            setattr(p, k, v)
+        params.append(p)
+    alone = run_alone(params, 33)
+    together = run_together(params, 33, chunks=[13, 20])
+    for (fa, ta, sa), (fb, tb, sb) in zip(alone, together):
+        assert np.array_equal(fa, fb)
+        assert np.array_equal(ta, tb)
+        assert sa == sb
+    steps_per_tier = np.sum([st["tile_steps"] for _, _, st in alone], axis=0)
+    assert np.count_nonzero(steps_per_tier) >= 2
+
+
 def test_ensemble_members_keep_their_own_step_counters_and_stats():
     params = small_members(mixed())
     sims = [amps.Simulation(p, init=amps.INIT_SEEDED) for p in params]

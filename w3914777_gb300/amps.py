@@ -185,7 +185,7 @@ class Simulation:
         self.h = h
         self.nf = params.num_fields
         self.shape = (params.ny, params.nx)
-        self.ntiles = (params.ny // params.tile, params.nx // params.tile)
+        self.ntiles = (-(-params.ny // params.tile), -(-params.nx // params.tile))  # ragged sides: partial edge tiles
         if not graphs:
             lib().amps_set_graphs(self.h, 0)
         if init is not None:

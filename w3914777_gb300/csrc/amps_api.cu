@@ -26,7 +26,12 @@ using namespace amps;
 struct amps_handle {
     amps_params p;
     int nf = 0, T = 0, ntx = 0, nty = 0, ntiles = 0;
-    int64_t n = 0;
+    int64_t n = 0;   // cells of the domain (nx * ny): host and gathered arrays
+    // storage of one field: whole tiles, row pitch px = ntx * T, nty * T rows
+    // (ns = px * nty * T; px == nx and ns == n unless the grid is ragged)
+    int px = 0;
+    int64_t ns = 0;
+    bool ragged = false;
     bool used[3] = {false, false, false};
     bool mixed = false, use_mid = false;
     void *store[3][2] = {{nullptr, nullptr}, {nullptr, nullptr}, {nullptr, nullptr}};
@@ -138,8 +143,9 @@ static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
     return fn;
 }
 
-// [nf][ny][nx] float array -> box {40 columns, 34 rows, nf fields}: a 32x32
-// tile with a 1-cell halo and its columns padded to 16-byte boundaries.
+// [nf][ny][nx] float array (nx: the storage's row pitch, ny: its rows) ->
+// box {40 columns, 34 rows, nf fields}: a 32x32 tile with a 1-cell halo and
+// its columns padded to 16-byte boundaries.
 static bool encode_field_map(CUtensorMap *tm, void *base, int nx, int ny, int nf)
 {
     auto enc = tensor_map_encoder();
@@ -237,10 +243,13 @@ extern "C" int amps_create(const amps_params *p, amps_handle **out)
     h->p = *p;
     h->nf = amps_num_fields(p);
     h->T = p->tile;
-    h->ntx = p->nx / p->tile;
-    h->nty = p->ny / p->tile;
+    h->ntx = (p->nx + p->tile - 1) / p->tile;
+    h->nty = (p->ny + p->tile - 1) / p->tile;
     h->ntiles = h->ntx * h->nty;
     h->n = (int64_t)p->nx * p->ny;
+    h->px = h->ntx * p->tile;
+    h->ns = (int64_t)h->px * h->nty * p->tile;
+    h->ragged = h->ns != h->n;
     const int high = p->high_tier;
     h->mixed = p->mode == AMPS_END2END_MIX;
     h->use_mid = h->mixed && high == TIER_FP64 && p->thr_lo < p->thr_hi;
@@ -268,7 +277,7 @@ extern "C" int amps_create(const amps_params *p, amps_handle **out)
     if (cudaMalloc((void **)&(ptr), (bytes)) != cudaSuccess) return fail(AMPS_ERR_ALLOC, what);
     for (int t = 0; t < 3; ++t)
         if (h->used[t])
-            for (int q = 0; q < 2; ++q) ALLOC(h->store[t][q], (size_t)h->nf * h->n * tier_size(t), "field storage");
+            for (int q = 0; q < 2; ++q) ALLOC(h->store[t][q], (size_t)h->nf * h->ns * tier_size(t), "field storage");
     ALLOC(h->d_tier_prev, h->ntiles, "tier map");
     ALLOC(h->d_tier_cur, h->ntiles, "tier map");
     ALLOC(h->d_lists, sizeof(int) * 3 * h->ntiles, "tile lists");
@@ -276,7 +285,7 @@ extern "C" int amps_create(const amps_params *p, amps_handle **out)
     ALLOC(h->d_counts, sizeof(int) * 4, "tile counts");
     ALLOC(h->d_metric, sizeof(double) * h->ntiles, "monitor metric");
     h->nmon = p->monitor_field < 0 ? h->nf : 1;
-    const size_t snap = p->monitor_samples ? (size_t)h->nmon * h->n : (size_t)h->nmon * h->ntiles * 16;
+    const size_t snap = p->monitor_samples ? (size_t)h->nmon * h->ns : (size_t)h->nmon * h->ntiles * 16;
     ALLOC(h->d_snap, sizeof(double) * snap, "monitor snapshot");
     if (p->ref_snapshot && p->monitor == AMPS_MONITOR_TEM && !p->monitor_samples && p->model != AMPS_SINTERING &&
         h->mixed)
@@ -307,13 +316,13 @@ extern "C" int amps_create(const amps_params *p, amps_handle **out)
     // zero state at the starting tier so that an un-initialised run is defined
     for (int t = 0; t < 3; ++t)
         if (h->used[t])
-            for (int q = 0; q < 2; ++q) cudaMemsetAsync(h->store[t][q], 0, (size_t)h->nf * h->n * tier_size(t), h->stream);
+            for (int q = 0; q < 2; ++q) cudaMemsetAsync(h->store[t][q], 0, (size_t)h->nf * h->ns * tier_size(t), h->stream);
     for (int t = 0; t < 3; ++t) {
         if (!h->used[t]) continue;
         cudaError_t pe;
         if (p->model == AMPS_GRAINGROWTH) {
             const bool only64 = h->used[TIER_FP64] && !h->used[TIER_FP32] && !h->used[TIER_HALF];
-            pe = gg_prepare(h->T, only64 ? TIER_FP64 : -1, p->ref_order != 0, p->half_arith);
+            pe = gg_prepare(h->T, only64 ? TIER_FP64 : -1, p->ref_order != 0, p->half_arith, h->ragged);
         }
         else if (p->model == AMPS_KOBAYASHI) pe = kob_prepare(h->T, t, p->ref_order != 0);
         else pe = sint_prepare(h->T, t, p->ref_order != 0, p->mu_lap_fp64 != 0);
@@ -339,8 +348,8 @@ extern "C" int amps_create(const amps_params *p, amps_handle **out)
         // per-thread asynchronous copies only)
         const char *off = getenv("AMPS_DISABLE_TMA_STAGE");
         if (p->model == AMPS_GRAINGROWTH && p->tile == 32 && h->used[TIER_FP32] && !(off && off[0] == '1'))
-            h->tma_stage = encode_field_map(&h->tm[0], h->store[TIER_FP32][0], p->nx, p->ny, h->nf) &&
-                           encode_field_map(&h->tm[1], h->store[TIER_FP32][1], p->nx, p->ny, h->nf);
+            h->tma_stage = encode_field_map(&h->tm[0], h->store[TIER_FP32][0], h->px, h->nty * h->T, h->nf) &&
+                           encode_field_map(&h->tm[1], h->store[TIER_FP32][1], h->px, h->nty * h->T, h->nf);
         cudaGetLastError();
     }
     {
@@ -350,10 +359,10 @@ extern "C" int amps_create(const amps_params *p, amps_handle **out)
         const bool only64 = h->used[TIER_FP64] && !h->used[TIER_FP32] && !h->used[TIER_HALF];
         const char *on = getenv("AMPS_ENABLE_TMA");
         if (p->model == AMPS_GRAINGROWTH && p->tile == 32 && h->used[TIER_FP32] && !only64 && h->nf <= kTmaMaxFields &&
-            p->half_arith == AMPS_HALF_FP32 && on && on[0] == '1') {
+            p->half_arith == AMPS_HALF_FP32 && !h->ragged && on && on[0] == '1') {
             int bps = 0, dev = 0, sms = 0;
-            if (encode_field_map(&h->tm[0], h->store[TIER_FP32][0], p->nx, p->ny, h->nf) &&
-                encode_field_map(&h->tm[1], h->store[TIER_FP32][1], p->nx, p->ny, h->nf) &&
+            if (encode_field_map(&h->tm[0], h->store[TIER_FP32][0], h->px, h->nty * h->T, h->nf) &&
+                encode_field_map(&h->tm[1], h->store[TIER_FP32][1], h->px, h->nty * h->T, h->nf) &&
                 gg_prepare_tma(p->ref_order != 0, h->nf, &bps) == cudaSuccess && bps > 0 &&
                 cudaGetDevice(&dev) == cudaSuccess &&
                 cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess) {
@@ -373,7 +382,7 @@ extern "C" int amps_create(const amps_params *p, amps_handle **out)
         const bool only64 = h->used[TIER_FP64] && !h->used[TIER_FP32] && !h->used[TIER_HALF];
         const char *on = getenv("AMPS_ENABLE_FLOW");
         if (p->model == AMPS_GRAINGROWTH && p->tile == 32 && !only64 && p->half_arith == AMPS_HALF_FP32 &&
-            !h->use_tma && on && on[0] == '1' && gg_prepare_flow(p->ref_order != 0) == cudaSuccess &&
+            !h->use_tma && !h->ragged && on && on[0] == '1' && gg_prepare_flow(p->ref_order != 0) == cudaSuccess &&
             cudaMalloc((void **)&h->d_flow, sizeof(int) * (h->ntiles + 1)) == cudaSuccess)
             h->use_flow = true;
         cudaGetLastError();  // a refused attribute or allocation leaves one launch per step
@@ -436,6 +445,7 @@ static Grid grid_view(amps_handle *h, int parity, const uint8_t *tier)
     for (int t = 0; t < 3; ++t) g.store[t] = h->store[t][parity];
     g.tier = tier;
     g.nx = h->p.nx; g.ny = h->p.ny; g.ntx = h->ntx; g.nty = h->nty; g.tile = h->T; g.nf = h->nf; g.n = h->n;
+    g.px = h->px; g.fs = h->ns;
     return g;
 }
 
@@ -621,7 +631,8 @@ static StepArgs step_args(const amps_handle *h, int parity, bool transition, int
     // adaptive runs: slow tiles first (the classification's launch order)
     a.order = p.model == AMPS_GRAINGROWTH && p.mode == AMPS_END2END_MIX ? h->d_order : nullptr;
     a.nx = p.nx; a.ny = p.ny; a.ntx = h->ntx; a.nty = h->nty; a.nf = h->nf; a.bc = p.bc; a.stencil = p.stencil;
-    a.n = h->n;
+    a.px = h->px;
+    a.n = h->ns;
     a.monitor_now = monitor_now ? 1 : 0;
     a.monitor_kind = p.monitor;
     a.samples = p.monitor_samples;
@@ -977,7 +988,7 @@ extern "C" int amps_measure_tiles(amps_handle *h, int kind, double *out)
     CK(h, cudaStreamSynchronize(h->stream));
     if (!h->d_mmetric) CK(h, cudaMalloc(&h->d_mmetric, sizeof(double) * h->ntiles));
     if (kind == AMPS_MONITOR_TEM && !h->d_msnap) {
-        const size_t snap = p.monitor_samples ? (size_t)h->nmon * h->n : (size_t)h->nmon * h->ntiles * 16;
+        const size_t snap = p.monitor_samples ? (size_t)h->nmon * h->ns : (size_t)h->nmon * h->ntiles * 16;
         CK(h, cudaMalloc(&h->d_msnap, sizeof(double) * snap));
     }
     Grid g = grid_view(h, h->parity, live_tiers(h));

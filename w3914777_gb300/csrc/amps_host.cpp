@@ -155,14 +155,23 @@ extern "C" int amps_check_params(const amps_params *p, char *msg, size_t len)
     if (p->model < 0 || p->model > 2) BAD("unknown model %d", p->model);
     if (p->mode < 0 || p->mode > 4) BAD("unknown mode %d", p->mode);
     if (p->tile != 16 && p->tile != 32) BAD("tile must be 16 or 32 (got %d)", p->tile);
-    if (p->nx < p->tile || p->ny < p->tile || p->nx % p->tile || p->ny % p->tile)
-        BAD("nx, ny (%d, %d) must be positive multiples of the tile (%d)", p->nx, p->ny, p->tile);
-    if ((int64_t)p->nx * p->ny > (int64_t)1 << 31) BAD("grid too large");
+    if (p->nx < p->tile || p->ny < p->tile)
+        BAD("nx, ny (%d, %d) must be at least the tile (%d)", p->nx, p->ny, p->tile);
+    // ragged grids (a side not a multiple of the tile): grain growth only;
+    // storage keeps whole tiles and the edge tiles compute their valid cells
+    const bool ragged = p->nx % p->tile || p->ny % p->tile;
+    if (ragged && p->model != AMPS_GRAINGROWTH)
+        BAD("nx, ny (%d, %d) must be multiples of the tile (%d) for Kobayashi and sintering "
+            "(grain growth takes any sides)", p->nx, p->ny, p->tile);
+    if (ragged && p->half_arith != AMPS_HALF_FP32)
+        BAD("binary16 half-tile arithmetic needs sides that are multiples of the tile");
+    if (ragged && p->ref_snapshot) BAD("the reference's snapshot rule needs sides that are multiples of the tile");
+    const int64_t ntx = (p->nx + p->tile - 1) / p->tile, nty = (p->ny + p->tile - 1) / p->tile;
+    if (ntx * nty * p->tile * p->tile > (int64_t)1 << 31) BAD("grid too large");
     // the classification ranks each tier's tiles in a 21-bit field of one
     // packed 64-bit counter (three tiers per scan)
-    if ((int64_t)(p->nx / p->tile) * (p->ny / p->tile) > AMPS_MAX_TILES)
-        BAD("too many tiles (%lld > %lld): use the larger tile",
-            (long long)(p->nx / p->tile) * (p->ny / p->tile), (long long)AMPS_MAX_TILES);
+    if (ntx * nty > AMPS_MAX_TILES)
+        BAD("too many tiles (%lld > %lld): use the larger tile", (long long)(ntx * nty), (long long)AMPS_MAX_TILES);
     if (p->bc != AMPS_BC_PERIODIC && p->bc != AMPS_BC_NOFLUX) BAD("unknown boundary condition %d", p->bc);
     if (p->high_tier != AMPS_TIER_FP64 && p->high_tier != AMPS_TIER_FP32) BAD("high_tier must be FP64 or FP32");
     if (p->model == AMPS_GRAINGROWTH && (p->nfields < 1 || p->nfields > 32)) BAD("grain growth Q must be 1..32");

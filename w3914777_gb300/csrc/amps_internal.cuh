@@ -82,7 +82,8 @@ struct StepArgs {
     const int *count;         // count[tier]
     const int *order;         // fused grain-growth step: tile of each CTA (nullptr: blockIdx.x)
     int nx, ny, ntx, nty, nf, bc, stencil;
-    int64_t n;                // nx*ny
+    int px;                   // row pitch of the storage: ntx * tile (== nx unless the grid is ragged)
+    int64_t n;                // field stride of the storage: px * nty * tile (== nx * ny unless ragged)
     // monitor (active when monitor_now != 0)
     int monitor_now, monitor_kind, samples, mfield, mu_lap_fp64, cadence;
     int half_arith;           // grain growth: AMPS_HALF_FP32 / _REF / _HFMA2 (half tiles' arithmetic)
@@ -313,7 +314,7 @@ __device__ __forceinline__ void stage_tile(const StepArgs &a, CT *sm, const uint
             const int gy = bc_map(y0 - R + r, a.ny, a.bc);
             kind[q] = 1;
             tier[q] = nt[(r < R ? 0 : (r < T + R ? 3 : 6)) + 1];
-            goff[q] = (int64_t)gy * a.nx + x0 + 8 * sg;
+            goff[q] = (int64_t)gy * a.px + x0 + 8 * sg;
             soff[q] = r * S::P + S::O + 8 * sg;
         } else if (u < U) {
             const int h = u - UI, k = h % (2 * R), r = h / (2 * R);
@@ -322,7 +323,7 @@ __device__ __forceinline__ void stage_tile(const StepArgs &a, CT *sm, const uint
             const int gx = bc_map(lx, a.nx, a.bc);
             kind[q] = 2;
             tier[q] = nt[(r < R ? 0 : (r < T + R ? 3 : 6)) + (k < R ? 0 : 2)];
-            goff[q] = (int64_t)gy * a.nx + gx;
+            goff[q] = (int64_t)gy * a.px + gx;
             soff[q] = r * S::P + (k < R ? S::O - R + k : S::O + T + (k - R));
         }
         if (SKIP32 && tier[q] == TIER_FP32) kind[q] = 0;
@@ -440,7 +441,7 @@ __device__ __forceinline__ void stage_band(const StepArgs &a, CT *dst, const uin
     for (int u = threadIdx.x; u < H * W; u += kThreads) {
         const int ly = ly0 + u / W, lx = u % W - R;
         const int tier = nt[(ly < 0 ? 0 : (ly < T ? 3 : 6)) + (lx < 0 ? 0 : (lx < T ? 1 : 2))];
-        const int64_t off = (int64_t)bc_map(y0 + ly, a.ny, a.bc) * a.nx + bc_map(x0 + lx, a.nx, a.bc);
+        const int64_t off = (int64_t)bc_map(y0 + ly, a.ny, a.bc) * a.px + bc_map(x0 + lx, a.nx, a.bc);
 #pragma unroll 4
         for (int f = 0; f < nfs; ++f) dst[f * H * W + u] = load_tier<CT>(a, tier, (int64_t)(f0 + f) * a.n + off);
     }
@@ -469,13 +470,13 @@ __device__ __forceinline__ void stage_tile_async32(const StepArgs &a, float *sm,
         bool seg;
         if (u < UI) {
             const int sg = u % SEG, r = u / SEG;
-            goff = (int64_t)bc_map(y0 - R + r, a.ny, a.bc) * a.nx + x0 + 8 * sg;
+            goff = (int64_t)bc_map(y0 - R + r, a.ny, a.bc) * a.px + x0 + 8 * sg;
             soff = r * S::P + S::O + 8 * sg;
             seg = true;
         } else {
             const int h = u - UI, k = h % (2 * R), r = h / (2 * R);
             const int lx = k < R ? x0 - R + k : x0 + T + (k - R);
-            goff = (int64_t)bc_map(y0 - R + r, a.ny, a.bc) * a.nx + bc_map(lx, a.nx, a.bc);
+            goff = (int64_t)bc_map(y0 - R + r, a.ny, a.bc) * a.px + bc_map(lx, a.nx, a.bc);
             soff = r * S::P + (k < R ? S::O - R + k : S::O + T + (k - R));
             seg = false;
         }

@@ -19,12 +19,18 @@ cudaError_t kob_prepare_lo(int tile);
 cudaError_t sint_prepare_lo(int tile, bool mu64);
 // Raise the dynamic shared-memory limit of the kernel a launch would use
 // (must run before any graph capture).
-cudaError_t gg_prepare(int tile, int tier, bool ref, int half_arith);
+// ragged: a side is not a multiple of the tile (the partial-edge-tile kernels).
+cudaError_t gg_prepare(int tile, int tier, bool ref, int half_arith, bool ragged = false);
 // The fused step with binary16 arithmetic on half tiles (half_arith 1 or 2;
 // k_gg_half.cu), called by gg_launch / gg_prepare.
 cudaError_t gg_launch_half(int tile, bool ref, const StepArgs &a, int grid, size_t smem, cudaStream_t s,
                            const CUtensorMap &tm);
 cudaError_t gg_prepare_half(int tile, bool ref, int half_arith);
+// The fused step for ragged grids (a side not a multiple of the tile: partial
+// edge tiles; k_gg_ragged.cu), called by gg_launch / gg_prepare.
+cudaError_t gg_launch_ragged(int tile, bool ref, const StepArgs &a, int grid, size_t smem, cudaStream_t s,
+                             const CUtensorMap &tm);
+cudaError_t gg_prepare_ragged(int tile, bool ref);
 cudaError_t kob_prepare(int tile, int tier, bool ref);
 cudaError_t sint_prepare(int tile, int tier, bool ref, bool mu64);
 // Sintering in the reference's own mixed arithmetic (half_arith = AMPS_HALF_REF):
@@ -63,10 +69,12 @@ struct Grid {
     void *store[3];           // one parity, per tier
     const uint8_t *tier;      // tier of every tile
     int nx, ny, ntx, nty, tile, nf;
-    int64_t n;
+    int64_t n;                // cells of the domain (nx * ny): the row-major arrays these kernels exchange
+    int px;                   // storage row pitch (ntx * tile)
+    int64_t fs;               // storage field stride (px * nty * tile)
 };
 
-// Row-major [nf][n] double/float <-> tiered storage.
+// Row-major [nf][ny][nx] double/float <-> tiered storage (pitch px, field stride fs).
 cudaError_t scatter_fields(const Grid &g, const void *src, int src_f32, cudaStream_t s);
 cudaError_t gather_fields(const Grid &g, void *dst, int dst_f32, int f0, int nfs, cudaStream_t s);
 // Monitor at time 0 (or after a set_field): metric and temporal snapshot from the state.

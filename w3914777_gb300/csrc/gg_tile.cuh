@@ -59,7 +59,7 @@ __device__ __forceinline__ void gg_tile_lo_impl(const StepArgs &a, const float *
         for (int k = 0; k < CPT; ++k) ssum[k] = fmaf(c[k], c[k], ssum[k]);
     }
     const float dtm = ph.gg_dtm, g2 = ph.gg_g2, kap = ph.gg_kap, inv = ph.gg_inv;
-    const int64_t gbase = (int64_t)(ty * T + row) * a.nx + tx * T + c0;
+    const int64_t gbase = (int64_t)(ty * T + row) * a.px + tx * T + c0;
     double metric = 0.0;
     MonAccF mon;
     for (int f = 0; f < nf; ++f) {
@@ -102,10 +102,13 @@ __device__ __forceinline__ void gg_tile_lo_impl(const StepArgs &a, const float *
         }
         store_cells<TIER, CPT>(a, (int64_t)f * a.n + gbase, out);
         if (mon_f) {
+            // a ragged grid's edge tile: cells past the domain are not samples
+            const int vw = min(T, a.nx - tx * T), vh = min(T, a.ny - ty * T);
 #pragma unroll
             for (int k = 0; k < CPT; ++k)
-                mon_add<T>(a, mon, mslot, tile, row, c0 + k, gbase + k, round_to_tier<TIER>(out[k]), w[1][k + 1],
-                           snapv[k]);
+                if (row < vh && c0 + k < vw)
+                    mon_add<T>(a, mon, mslot, tile, row, c0 + k, gbase + k, round_to_tier<TIER>(out[k]), w[1][k + 1],
+                               snapv[k]);
             metric = mon_finish(a, mon, red, metric);
         }
     }
@@ -155,7 +158,7 @@ __device__ __forceinline__ void gg_tile_lo_rows(const StepArgs &a, const float *
     const int r0 = RPT * (t / GPR), c0 = (t % GPR) * CPT;  // tile-local rows r0 .. r0+RPT-1
     const Phys &ph = a.ph;
     const float dtm = ph.gg_dtm, g2 = ph.gg_g2, kap = ph.gg_kap, inv = ph.gg_inv;
-    const int64_t gbase = (int64_t)(ty * T + r0) * a.nx + tx * T + c0;
+    const int64_t gbase = (int64_t)(ty * T + r0) * a.px + tx * T + c0;
     MonAccF mon;
     if (MK) mon_reset(a, mon);
     for (int f = group; f < nf; f += RPT) {
@@ -192,14 +195,17 @@ __device__ __forceinline__ void gg_tile_lo_rows(const StepArgs &a, const float *
                 const float dfd = e * fmaf(g2, ssum[k] - e2, e2 - 1.f);
                 out[k] = fmaf(-dtm, fmaf(-kap, lap, dfd), e);
             }
-            const int64_t gi = gbase + (int64_t)i * a.nx;
+            const int64_t gi = gbase + (int64_t)i * a.px;
             store_cells<TIER, CPT>(a, (int64_t)f * a.n + gi, out);
             if constexpr (MK != 0) {
-                if (mon_f) {
+                // a ragged grid's edge tile: cells past the domain are not samples
+                if (mon_f && r0 + i < min(T, a.ny - ty * T)) {
+                    const int vw = min(T, a.nx - tx * T);
 #pragma unroll
                     for (int k = 0; k < CPT; ++k)
-                        mon_add_k<T, MK>(a, mon, mslot, tile, r0 + i, c0 + k, gi + k, round_to_tier<TIER>(out[k]),
-                                         md[k + 1]);
+                        if (c0 + k < vw)
+                            mon_add_k<T, MK>(a, mon, mslot, tile, r0 + i, c0 + k, gi + k, round_to_tier<TIER>(out[k]),
+                                             md[k + 1]);
                 }
             }
         }
@@ -211,21 +217,26 @@ __device__ __forceinline__ void gg_tile_lo_rows(const StepArgs &a, const float *
 }
 
 // One cell of the FP64 tile's neighbourhood at tile-local (ly, lx), read at
-// its owner tile's input tier.
+// its owner tile's input tier: the tile of the 3x3 neighbourhood at that
+// position, or (own: a ragged grid's edge tile, whose boundary-mapped halo
+// can lie in another tile) the tile that holds the mapped cell.
 template <int T>
-__device__ __forceinline__ double ld_nb64(const StepArgs &a, const uint8_t *nt, int f, int x0, int y0, int ly, int lx)
+__device__ __forceinline__ double ld_nb64(const StepArgs &a, const uint8_t *nt, int f, int x0, int y0, int ly, int lx,
+                                          bool own = false)
 {
     const int gy = bc_map(y0 + ly, a.ny, a.bc), gx = bc_map(x0 + lx, a.nx, a.bc);
     const int cls = (ly < 0 ? 0 : (ly < T ? 3 : 6)) + (lx < 0 ? 0 : (lx < T ? 1 : 2));
-    return load_tier<double>(a, nt[cls], (int64_t)f * a.n + (int64_t)gy * a.nx + gx);
+    const int tier = own ? a.tier_in[(gy / T) * a.ntx + gx / T] : nt[cls];
+    return load_tier<double>(a, tier, (int64_t)f * a.n + (int64_t)gy * a.px + gx);
 }
 
 // FP64 tile: direct loads through L1 with a rolling 3-row window, FP64
 // arithmetic; REF keeps the reference's expression order and rounding
 // (graingrowth/function.h:20-23).
-template <int T, bool REF>
+template <int T, bool REF, bool PARTIAL = false>
 __device__ __forceinline__ void gg_tile_fp64(const StepArgs &a, const uint8_t *nt, int tile, int tx, int ty, double *red)
 {
+    constexpr bool partial = PARTIAL;  // a ragged grid's edge tile: owner-tier loads
     constexpr int RPT = T * T / kThreads;
     const int col = threadIdx.x % T;
     const int r0 = (threadIdx.x / T) * RPT;
@@ -239,10 +250,10 @@ __device__ __forceinline__ void gg_tile_fp64(const StepArgs &a, const uint8_t *n
         for (int f = 0; f < nf; ++f)
 #pragma unroll
             for (int j = 0; j < RPT; ++j) {
-                const double v = ld_nb64<T>(a, nt, f, x0, y0, r0 + j, col);
+                const double v = ld_nb64<T>(a, nt, f, x0, y0, r0 + j, col, partial);
                 ssum[j] = fma(v, v, ssum[j]);
             }
-    const int64_t gbase = (int64_t)(y0 + r0) * a.nx + x0 + col;
+    const int64_t gbase = (int64_t)(y0 + r0) * a.px + x0 + col;
     double metric = 0.0;
     MonAcc mon;
     for (int f = 0; f < nf; ++f) {
@@ -252,14 +263,14 @@ __device__ __forceinline__ void gg_tile_fp64(const StepArgs &a, const uint8_t *n
         double rd[3], rc[3], ru[3];
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            rd[k] = ld_nb64<T>(a, nt, f, x0, y0, r0 - 1, col + k - 1);
-            rc[k] = ld_nb64<T>(a, nt, f, x0, y0, r0, col + k - 1);
+            rd[k] = ld_nb64<T>(a, nt, f, x0, y0, r0 - 1, col + k - 1, partial);
+            rc[k] = ld_nb64<T>(a, nt, f, x0, y0, r0, col + k - 1, partial);
         }
 #pragma unroll 1
         for (int j = 0; j < RPT; ++j) {
 #pragma unroll
-            for (int k = 0; k < 3; ++k) ru[k] = ld_nb64<T>(a, nt, f, x0, y0, r0 + j + 1, col + k - 1);
-            const int64_t g = gbase + (int64_t)j * a.nx;
+            for (int k = 0; k < 3; ++k) ru[k] = ld_nb64<T>(a, nt, f, x0, y0, r0 + j + 1, col + k - 1, partial);
+            const int64_t g = gbase + (int64_t)j * a.px;
             const double snapv = mon_f ? snap_prefetch<T>(a, mslot, tile, r0 + j, col, g) : 0.0;
             const double e = rc[1];
             double out;
@@ -276,7 +287,7 @@ __device__ __forceinline__ void gg_tile_fp64(const StepArgs &a, const uint8_t *n
                 bool first = true;
                 for (int b = 0; b < nf; ++b) {
                     if (b == f) continue;
-                    const double v = ld_nb64<T>(a, nt, b, x0, y0, r0 + j, col);
+                    const double v = ld_nb64<T>(a, nt, b, x0, y0, r0 + j, col, partial);
                     const double s2 = __dmul_rn(v, v);
                     sum = first ? s2 : __dadd_rn(sum, s2);
                     first = false;
@@ -296,7 +307,9 @@ __device__ __forceinline__ void gg_tile_fp64(const StepArgs &a, const uint8_t *n
                 out = fma(-(ph.dt * ph.mobil), fma(-ph.grcoef, lap, dfd), e);
             }
             ((double *)a.out[TIER_FP64])[(int64_t)f * a.n + g] = out;
-            if (mon_f) mon_add<T>(a, mon, mslot, tile, r0 + j, col, g, out, e, snapv);
+            // a ragged grid's edge tile: cells past the domain are not samples
+            if (mon_f && (!PARTIAL || (r0 + j < a.ny - y0 && col < a.nx - x0)))
+                mon_add<T>(a, mon, mslot, tile, r0 + j, col, g, out, e, snapv);
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
                 rd[k] = rc[k];
@@ -306,6 +319,14 @@ __device__ __forceinline__ void gg_tile_fp64(const StepArgs &a, const uint8_t *n
         if (mon_f) metric = mon_finish(a, mon, red, metric);
     }
     if (a.monitor_now && threadIdx.x == 0) a.metric[tile] = metric;
+}
+
+// The FP64 tile of a ragged grid's edge, out of line (off the whole tiles' registers).
+template <int T, bool REF>
+__device__ __noinline__ void gg_tile_fp64_partial(const StepArgs &a, const uint8_t *nt, int tile, int tx, int ty,
+                                                  double *red)
+{
+    gg_tile_fp64<T, REF, true>(a, nt, tile, tx, ty, red);
 }
 
 __device__ __forceinline__ __half2 gg_hconst(const Phys &ph, int i)
@@ -398,7 +419,7 @@ __device__ __forceinline__ void gg_tile_half2(const StepArgs &a, const float *sm
                 const __half2 dfd = __hmul2(ctr, __hfma2(gg_hconst(ph, GH_G2), sum, __hfma2(ctr, ctr, __hneg2(h1))));
                 out = __hfma2(__hneg2(gg_hconst(ph, GH_DTM)), __hfma2(__hneg2(gg_hconst(ph, GH_KINV)), s, dfd), ctr);
             }
-            const int64_t g = (int64_t)(ty * T + row) * a.nx + tx * T + c;
+            const int64_t g = (int64_t)(ty * T + row) * a.px + tx * T + c;
             *reinterpret_cast<__half2 *>((__half *)a.out[TIER_HALF] + (int64_t)f * a.n + g) = out;
             if (mon_f) {
                 const double s0 = snap_prefetch<T>(a, mslot, tile, row, c, g);
@@ -411,6 +432,46 @@ __device__ __forceinline__ void gg_tile_half2(const StepArgs &a, const float *sm
         if (mon_f) metric = mon_finish(a, mon, red, metric);
     }
     if (MK != 0 && threadIdx.x == 0) a.metric[tile] = metric;
+}
+
+// ---- ragged grids ----------------------------------------------------------------
+// A grid whose sides are not multiples of the tile keeps whole tiles in
+// storage (row pitch px = ntx*T, nty*T rows): the last tile column and row
+// reach past the domain into that padding.  Such a partial tile is staged and
+// computed as a whole tile -- its cells past the domain compute from padding
+// and store into padding, which no cell inside the domain ever reads, and
+// the monitor skips them -- with one correction: the staged slots of column
+// w and row h (w x h: the tile's cells inside the domain), the right and
+// lower halo of its last valid cells, held padding and are re-read across
+// the boundary map (periodic: column 0 / row 0 of the domain) at the input
+// tier of the tile that owns them.  Every access stays inside the storage:
+// rows and halo columns are boundary-mapped (nx, ny >= T), interior row
+// segments end at most at the padded pitch.
+__device__ __forceinline__ bool gg_partial_tile(const StepArgs &a, int T, int tx, int ty)
+{
+    return (tx + 1) * T > a.nx || (ty + 1) * T > a.ny;
+}
+
+// The patch of a partial tile's staging (Stage<CT, T, 1> layout, fields
+// [0, nf)); the caller synchronises before and after.
+template <typename CT, int T>
+__device__ __noinline__ void patch_ragged(const StepArgs &a, CT *sm, int tx, int ty)
+{
+    using S = Stage<CT, T, 1>;
+    const int x0 = tx * T, y0 = ty * T;
+    const int w = min(T, a.nx - x0), h = min(T, a.ny - y0);
+    // column w for rows -1..h (when w < T); row h for columns -1..w-1, or
+    // -1..T when the tile is whole in x (the corner (w, h) once)
+    const int nc = w < T ? h + 2 : 0;
+    const int nr = h < T ? (w < T ? w + 1 : w + 2) : 0;
+    for (int u = threadIdx.x; u < nc + nr; u += kThreads) {
+        const int lx = u < nc ? w : u - nc - 1, ly = u < nc ? u - 1 : h;
+        const int gx = bc_map(x0 + lx, a.nx, a.bc), gy = bc_map(y0 + ly, a.ny, a.bc);
+        const int tier = a.tier_in[(gy / T) * a.ntx + gx / T];
+        const int64_t o = (int64_t)gy * a.px + gx;
+        CT *d = &S::at(sm, 0, ly + 1, S::O + lx);
+        for (int f = 0; f < a.nf; ++f) d[f * S::FIELD] = load_tier<CT>(a, tier, (int64_t)f * a.n + o);
+    }
 }
 
 // Fused all-tier step: at most 64 registers, so that four CTAs share an SM
@@ -431,12 +492,14 @@ __device__ __forceinline__ bool all_fp32(const uint8_t *nt)
 // a step without the monitor, 1/2/3 a monitor step of that monitor kind
 // (spatial / temporal / rate), -1 a monitor step of the kind in `a`.
 // NC = false: no read-only-path loads (the persistent multi-step kernel
-// reads values that other CTAs of the same launch wrote).
+// reads values that other CTAs of the same launch wrote).  RG: the grid may
+// be ragged (its edge tiles partial); compiled out of the whole-tile grids'
+// kernels, whose registers it would otherwise spill.
 // tm, bar (T = 32): a tensor map of this step's FP32 input and an mbarrier;
 // tiles whose halo needs no wrap or mirror then fetch the whole FP32
 // neighbourhood -- every field, 34 rows x 40 columns, the staging layout --
 // by one bulk tensor copy issued by one thread (sm 128-byte aligned).
-template <int T, bool REF, int MK, int HA = 0, bool NC = true>
+template <int T, bool REF, int MK, int HA = 0, bool NC = true, bool RG = false>
 __device__ __forceinline__ void gg_tile_step(const StepArgs &a, float *sm, uint8_t *ntier, double *red, int tile,
                                              const CUtensorMap *tm = nullptr, uint64_t *bar = nullptr)
 {
@@ -481,7 +544,8 @@ __device__ __forceinline__ void gg_tile_step(const StepArgs &a, float *sm, uint8
     if (tier == TIER_FP64) {
         // the FP64 path reads through L1, not the staging area: the discarded
         // copies land while it computes, before the CTA exits
-        gg_tile_fp64<T, REF>(a, ntier, tile, tx, ty, red);
+        if (RG && gg_partial_tile(a, T, tx, ty)) gg_tile_fp64_partial<T, REF>(a, ntier, tile, tx, ty, red);
+        else gg_tile_fp64<T, REF>(a, ntier, tile, tx, ty, red);
         if (spec) spec_done();
         return;
     }
@@ -497,6 +561,10 @@ __device__ __forceinline__ void gg_tile_step(const StepArgs &a, float *sm, uint8
         stage_tile<float, T, 1, false, NC>(a, sm, ntier, tx, ty, 0, a.nf);
     }
     __syncthreads();
+    if (RG && gg_partial_tile(a, T, tx, ty)) {  // a ragged grid's edge tile: its wrapped halo
+        patch_ragged<float, T>(a, sm, tx, ty);
+        __syncthreads();
+    }
     if constexpr (HA != 0) {
         if (tier == TIER_HALF) {
             gg_tile_half2<T, MK, HA>(a, sm, tile, tx, ty, red);
@@ -543,7 +611,7 @@ template <int T, bool REF, bool MON>
 __device__ __noinline__ void gg_tile_step_call(const StepArgs &a, float *sm, uint8_t *ntier, double *red, int tile,
                                                uint64_t *bar)
 {
-    gg_tile_step<T, REF, MON ? -1 : 0>(a, sm, ntier, red, tile, a.tmap, bar);
+    gg_tile_step<T, REF, MON ? -1 : 0, 0, true, true>(a, sm, ntier, red, tile, a.tmap, bar);
 }
 
 // Fused all-tier step: at most 64 registers, so that four CTAs share an SM.
@@ -553,7 +621,7 @@ __device__ __noinline__ void gg_tile_step_call(const StepArgs &a, float *sm, uin
 // their neighbourhood in shared memory (reading it directly through L1
 // measured 18.1 against 15.8 us per adaptive 1024^2 Q=8 step).
 // tm: the tensor map of the step's FP32 input, valid when a.tma_stage.
-template <int T, bool REF, int MK, int HA = 0>
+template <int T, bool REF, int MK, int HA = 0, bool RG = false>
 __global__ void __launch_bounds__(kThreads, 4) gg_step_kernel(StepArgs a, const __grid_constant__ CUtensorMap tm)
 {
     extern __shared__ __align__(128) unsigned char smraw[];
@@ -569,7 +637,7 @@ __global__ void __launch_bounds__(kThreads, 4) gg_step_kernel(StepArgs a, const 
     pdl_trigger();
     pdl_wait();
     const int tile = a.order ? a.order[blockIdx.x] : (int)blockIdx.x;
-    gg_tile_step<T, REF, MK, HA>(a, sm, ntier, red, tile, a.tma_stage ? &tm : nullptr, &bar);
+    gg_tile_step<T, REF, MK, HA, true, RG>(a, sm, ntier, red, tile, a.tma_stage ? &tm : nullptr, &bar);
 }
 
 

@@ -12,6 +12,12 @@ __device__ __forceinline__ int tier_of(const Grid &g, int x, int y)
     return g.tier[(y / g.tile) * g.ntx + x / g.tile];
 }
 
+// storage index of domain cell (x, y) of field f
+__device__ __forceinline__ int64_t store_index(const Grid &g, int f, int x, int y)
+{
+    return (int64_t)f * g.fs + (int64_t)y * g.px + x;
+}
+
 __global__ void scatter_kernel(Grid g, const void *src, int src_f32)
 {
     const int64_t total = (int64_t)g.nf * g.n;
@@ -20,17 +26,19 @@ __global__ void scatter_kernel(Grid g, const void *src, int src_f32)
         const int x = (int)(c % g.nx), y = (int)(c / g.nx);
         const double v = src_f32 ? (double)((const float *)src)[k] : ((const double *)src)[k];
         const int t = tier_of(g, x, y);
-        if (t == TIER_FP64) ((double *)g.store[2])[k] = v;
-        else if (t == TIER_FP32) ((float *)g.store[1])[k] = (float)v;
-        else ((__half *)g.store[0])[k] = __float2half_rn((float)v);
+        const int64_t q = store_index(g, (int)(k / g.n), x, y);
+        if (t == TIER_FP64) ((double *)g.store[2])[q] = v;
+        else if (t == TIER_FP32) ((float *)g.store[1])[q] = (float)v;
+        else ((__half *)g.store[0])[q] = __float2half_rn((float)v);
     }
 }
 
+// c: index of the cell in the row-major domain array
 __device__ __forceinline__ double read_cell(const Grid &g, int f, int64_t c)
 {
     const int x = (int)(c % g.nx), y = (int)(c / g.nx);
     const int t = tier_of(g, x, y);
-    const int64_t k = (int64_t)f * g.n + c;
+    const int64_t k = store_index(g, f, x, y);
     if (t == TIER_FP64) return ((const double *)g.store[2])[k];
     if (t == TIER_FP32) return (double)((const float *)g.store[1])[k];
     return (double)__half2float(((const __half *)g.store[0])[k]);
@@ -84,7 +92,10 @@ __global__ void monitor_state_kernel(Grid g, int kind, int samples, int mfield, 
         int bad = 0;
         for (int u = threadIdx.x; u < T * T; u += blockDim.x) {
             const int i = u % T, j = u / T;
+            // a ragged grid's edge tile: only its cells inside the domain
+            if (tx * T + i >= g.nx || ty * T + j >= g.ny) continue;
             const int64_t c = (int64_t)(ty * T + j) * g.nx + tx * T + i;
+            const int64_t sc = (int64_t)(ty * T + j) * g.px + tx * T + i;  // snapshot slot: storage layout
             const double v = read_cell(g, f, c);
             if (!(v == v) || isinf(v)) bad = 1;
             int si = 0;
@@ -99,7 +110,7 @@ __global__ void monitor_state_kernel(Grid g, int kind, int samples, int mfield, 
             }
             if (si < 0) continue;
             if (diff) {
-                const double r = samples ? snap[(int64_t)slot * g.n + c]
+                const double r = samples ? snap[(int64_t)slot * g.fs + sc]
                                          : snap[((int64_t)slot * g.ntx * g.nty + tile) * 16 + si];
                 mx = fmax(mx, fabs(r - v));
                 continue;
@@ -107,7 +118,7 @@ __global__ void monitor_state_kernel(Grid g, int kind, int samples, int mfield, 
             mn = fmin(mn, v);
             mx = fmax(mx, v);
             if (write_snap) {
-                if (samples) snap[(int64_t)slot * g.n + c] = v;
+                if (samples) snap[(int64_t)slot * g.fs + sc] = v;
                 else snap[((int64_t)slot * g.ntx * g.nty + tile) * 16 + si] = v;
             }
         }

@@ -39,6 +39,10 @@ __global__ void __launch_bounds__(kThreads) gg_step_f64_kernel(StepArgs a)
     __syncthreads();
     stage_tile<double, T, 1>(a, sm, ntier, tx, ty, 0, a.nf);
     __syncthreads();
+    if (gg_partial_tile(a, T, tx, ty)) {  // a ragged grid's edge tile: its wrapped halo
+        patch_ragged<double, T>(a, sm, tx, ty);
+        __syncthreads();
+    }
     const int col = threadIdx.x % T;
     const int r0 = (threadIdx.x / T) * RPT;
     const int c = S::O + col;
@@ -54,7 +58,7 @@ __global__ void __launch_bounds__(kThreads) gg_step_f64_kernel(StepArgs a)
                 const double v = S::at(sm, f, r0 + j + 1, c);
                 ssum[j] = fma(v, v, ssum[j]);
             }
-    const int64_t gbase = (int64_t)(ty * T + r0) * a.nx + tx * T + col;
+    const int64_t gbase = (int64_t)(ty * T + r0) * a.px + tx * T + col;
     for (int f = 0; f < nf; ++f) {
         double w[RPT + 2][3];
 #pragma unroll
@@ -97,7 +101,7 @@ __global__ void __launch_bounds__(kThreads) gg_step_f64_kernel(StepArgs a)
                 const double dfd = e * fma(2.0 * ph.gamma, ssum[j] - e2, e2 - 1.0);
                 out = fma(-(ph.dt * ph.mobil), fma(-ph.grcoef, lap, dfd), e);
             }
-            ((double *)a.out[TIER_FP64])[(int64_t)f * a.n + gbase + (int64_t)j * a.nx] = out;
+            ((double *)a.out[TIER_FP64])[(int64_t)f * a.n + gbase + (int64_t)j * a.px] = out;
         }
     }
 }
@@ -248,6 +252,8 @@ cudaError_t gg_launch(int tile, int tier, bool ref, const StepArgs &a, int grid,
     if (tier == TIER_FP64) {
         if (tile == 32) AMPS_GGL(gg_step_f64_kernel, 32);
         else AMPS_GGL(gg_step_f64_kernel, 16);
+    } else if (a.nx % tile || a.ny % tile) {
+        return gg_launch_ragged(tile, ref, a, grid, smem, s, tm);  // partial edge tiles (k_gg_ragged.cu)
     } else if (a.half_arith != 0) {
         return gg_launch_half(tile, ref, a, grid, smem, s, tm);  // binary16 half tiles (k_gg_half.cu)
     } else {
@@ -260,7 +266,7 @@ cudaError_t gg_launch(int tile, int tier, bool ref, const StepArgs &a, int grid,
     return cudaGetLastError();
 }
 
-cudaError_t gg_prepare(int tile, int tier, bool ref, int half_arith)
+cudaError_t gg_prepare(int tile, int tier, bool ref, int half_arith, bool ragged)
 {
     const int lim = kMaxDynSmem;
     const auto attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
@@ -271,6 +277,7 @@ cudaError_t gg_prepare(int tile, int tier, bool ref, int half_arith)
                    : cudaFuncSetAttribute(gg_step_f64_kernel<16, false>, attr, lim);
     }
     if (half_arith != 0) return gg_prepare_half(tile, ref, half_arith);
+    if (ragged) return gg_prepare_ragged(tile, ref);
     cudaError_t e = cudaSuccess;
 #define AMPS_GGP(TT, MK)                                                                                     \
     if (e == cudaSuccess)                                                                                    \

@@ -5,7 +5,8 @@ different sizes, field counts and coefficients advanced together by
 No reference counterpart: the reference runs one grid per process
 (graingrowth/end2end_mix.cu).  Each member is the 1024^2 Q=8 Fan-Chen
 workload's physics (gamma = 1.5, dx = 1, eta ~ U[-1e-3, 1e-3] seeded) with
-  side  = round(exp(U[ln 128, ln 1024])), rounded to a multiple of the tile,
+  side  = round(exp(U[ln 128, ln 1024])) (any integer: the edge tiles of a
+          side that is not a multiple of the tile are partial),
   Q     in {4, 8, 12, 16},
   kappa ~ U[1, 3],  L ~ U[0.5, 2],
   dt    = stable_dt(L, kappa).
@@ -31,13 +32,15 @@ def stable_dt(mobil, grcoef, dx=1.0, dt_max=0.05, safety=0.9):
     return min(dt_max, safety * 2.0 * dx * dx / (12.0 * mobil * grcoef))
 
 
-def member_params(count=64, seed=2024, tile=32, overrides=None):
-    """Parameters of `count` seeded ensemble members (list of amps.Params)."""
+def member_params(count=64, seed=2024, tile=32, overrides=None, round_to_tile=False):
+    """Parameters of `count` seeded ensemble members (list of amps.Params);
+    round_to_tile: sides rounded to multiples of the tile (no partial tiles)."""
     rng = np.random.default_rng(seed)
     out = []
     for i in range(count):
         side = int(round(math.exp(rng.uniform(math.log(128), math.log(1024)))))
-        side = max(tile, int(round(side / tile)) * tile)
+        if round_to_tile:
+            side = max(tile, int(round(side / tile)) * tile)
         q = int(rng.choice([4, 8, 12, 16]))
         kappa = float(rng.uniform(1.0, 3.0))
         mobil = float(rng.uniform(0.5, 2.0))
