@@ -1,0 +1,26 @@
+// graingrowth_pure.cu -- the reference's plain grain-growth kernels
+// (graingrowth/function.h:5-30 kernel1_pure, graingrowth/tools.h:24-38
+// dataprepare_high) built in place from the read-only reference tree into
+// device code for the GB300, with the header settings of
+// graingrowth/end2end_pure.py (typedef double highprecision, PURE, End2end)
+// and the parameter set REF_PARA_H.  The reference's own code, unchanged; no
+// host code is built (baseline/ref_cuda.cpp drives it).
+#include "prelude.cuh"
+#define float double
+#include REF_PARA_H
+#undef float
+#undef AMSTENCIL
+#undef HALF2
+#undef monitor_conversion_independent
+#ifndef PURE
+#define PURE
+#endif
+#ifndef End2end
+#define End2end
+#endif
+#define PARA5_H
+#include REF_FUNCTION_H
+#include REF_TOOLS_H
+
+// the build's compile-time sizes, read by the host driver: dimX, dimY, unitx, unity
+__device__ int ref_dims[4] = {dimX, dimY, unitx, unity};

@@ -460,10 +460,68 @@ def run_ours(args):
             line["ensemble"] = run_ensemble()
         if world == 1 and not args.no_configs:
             line["configs"] = run_configs()
+        if world == 1 and not args.no_refcuda:
+            line["reference_cuda"] = run_reference_cuda()
         print(json.dumps(line), flush=True)
     sim.close()
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def run_reference_cuda(steps=2000):
+    """The reference's own CUDA kernels on this GPU beside the library, at the
+    reference's own configurations (its parameter files: 512^2, 16^2 tiles):
+    grain growth para1 (Q = 2) and the Kobayashi dendrite para2, plain FP64
+    and AMSTENCIL at the sweep scripts' thresholds.  The reference: its device
+    code built from its sources for sm_103a (baseline/_ref/*.cubin), its host
+    loops restated around driver-API launches (baseline/ref_cuda.cpp), timed
+    by its own event window (step 5 to the end; one device synchronisation
+    per step, as its programs do).  The library: amps_run of the same
+    configuration (reference order, the same monitor and threshold), wall
+    clock around run + synchronize.  Rates in Gcell-updates/s."""
+    import time
+    from w3914777_gb300 import amps
+    try:
+        from baseline import refcuda
+    except ImportError as e:
+        return {"unavailable": f"baseline package: {e}"}
+    if not (refcuda.available("graingrowth_pure") and refcuda.available("snowflake_pure")):
+        return {"unavailable": "the reference's cubins (baseline/_ref) are not built: they need the reference tree"}
+    n = 512 * 512
+    total = steps + 5
+    rate = lambda ms: n * steps / (ms * 1e-3) / 1e9  # noqa: E731
+
+    def ours(p):
+        with amps.Simulation(p, init=amps.INIT_REFERENCE) as s:
+            s.run(10)
+            s.synchronize()
+            t0 = time.perf_counter()
+            s.run(steps)
+            s.synchronize()
+            return n * steps / (time.perf_counter() - t0) / 1e9
+
+    out = {"note": "reference: its own kernels and event window; ours: amps_run, wall clock; "
+                   f"{steps} steps at the reference's configurations (512^2, 16^2 tiles)",
+           "steps": steps}
+    gg = {"ref_plain_fp64": rate(refcuda.gg_pure(total)[2]),
+          "ours_plain_fp64_reference_order": ours(amps.Params.preset("graingrowth", 1, mode="purehigh", ref_order=1)),
+          "ours_plain_fp64_fma": ours(amps.Params.preset("graingrowth", 1, mode="purehigh", ref_order=0))}
+    for m, thr in ((2, 1e-4), (1, 0.5)):
+        gg[f"ref_amstencil_monitor{m}_{thr:g}"] = rate(refcuda.gg_mix(total, thr, m)[3])
+        gg[f"ours_mixed_monitor{m}_{thr:g}"] = ours(amps.Params.preset(
+            "graingrowth", 1, mode="end2end_mix", monitor=m, monitor_samples=0, monitor_field=1, thr_lo=thr,
+            thr_hi=thr, ref_order=1, half_arith=amps.HALF_REF, ref_snapshot=1))
+    out["graingrowth_para1"] = gg
+    kob = {"ref_plain_fp64": rate(refcuda.kob_pure(total)[2]),
+           "ours_plain_fp64_reference_order": ours(amps.Params.preset("kobayashi", 2, mode="purehigh", ref_order=1)),
+           "ours_plain_fp64_fma": ours(amps.Params.preset("kobayashi", 2, mode="purehigh", ref_order=0))}
+    for m, thr in ((1, 0.5), (2, 1e-4)):
+        kob[f"ref_amstencil_monitor{m}_{thr:g}"] = rate(refcuda.kob_mix(total, thr, m)[3])
+        kob[f"ours_mixed_monitor{m}_{thr:g}"] = ours(amps.Params.preset(
+            "kobayashi", 2, mode="end2end_mix", monitor=m, monitor_samples=0, monitor_field=0, thr_lo=thr,
+            thr_hi=thr, ref_order=1))
+    out["kobayashi_para2"] = kob
+    return out
 
 
 def run_roofline_hbm(p, peak, peak_kind, n=4096, warm=30, steps=200):
@@ -927,6 +985,7 @@ def main():
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--no-configs", action="store_true")
     ap.add_argument("--no-hbm", action="store_true")
+    ap.add_argument("--no-refcuda", action="store_true")
     ap.add_argument("--profile-case", type=int, default=0)
     ap.add_argument("--profile-model", default="graingrowth",
                     choices=["graingrowth", "kobayashi", "sintering", "graingrowth-adjoint", "ensemble"])

@@ -70,8 +70,13 @@ __device__ __forceinline__ void kob_aniso(const CT *P, int ps, const Phys &ph, C
 }
 
 // Phase B at one cell (snowflake/function.h:54-59): P, Tm at the cell's phi
-// and T (row stride sp); the phase-A arrays at index o, row stride es.
-template <typename CT>
+// and T (row stride sp); the phase-A arrays at index o, row stride es.  The
+// latent heat added to T is kappa times the change of phi as the tile's
+// tier stores it (TIER: the rounding of the stored phi), so that a half
+// tile's T moves with the phi it keeps, as the reference's half2 update does
+// (snowflake/function.h:512-513 reads the new half phi): without it, a phi
+// increment below half an ulp heats T every step while the stored phi stays.
+template <typename CT, int TIER>
 __device__ __forceinline__ void kob_update(const CT *P, const CT *Tm, int sp, const CT *px, const CT *py,
                                            const CT *ep, const CT *epd, int o, int es, const Phys &ph, int64_t step,
                                            int64_t g, CT &pn, CT &tn)
@@ -91,7 +96,7 @@ __device__ __forceinline__ void kob_update(const CT *P, const CT *Tm, int sp, co
         drive += kc<CT>(ph, KB_NOISE) * (noise_u01_t<CT>(ph.seed, (uint64_t)step, (uint64_t)g) - CT(0.5));
     const CT inner = term1 + term2 + ep[o] * ep[o] * lp + p0 * (CT(1) - p0) * drive;
     pn = fma(kc<CT>(ph, KB_DTT), inner, p0);
-    tn = fma(kc<CT>(ph, KB_KAPPA), pn - p0, fma(kc<CT>(ph, KB_DT), lt, t0));
+    tn = fma(kc<CT>(ph, KB_KAPPA), round_to_tier<TIER>(pn) - p0, fma(kc<CT>(ph, KB_DT), lt, t0));
 }
 
 // One tile of one step at tier TIER (smraw: the kernel's dynamic shared
@@ -195,7 +200,7 @@ __device__ __forceinline__ void kob_tile(const StepArgs &a, unsigned char *smraw
             pn = __dadd_rn(p0, __dmul_rn(ph.dt / ph.tau, inner));
             tn = __dadd_rn(__dadd_rn(t0, __dmul_rn(ph.dt, lt)), __dmul_rn(ph.kappa, __dsub_rn(pn, p0)));
         } else {
-            kob_update<CT>(P, Tm, S::P, px, py, ep, epd, o, E, ph, step, g, pn, tn);
+            kob_update<CT, TIER>(P, Tm, S::P, px, py, ep, epd, o, E, ph, step, g, pn, tn);
         }
         store_tier<TIER>(a, g, pn);
         store_tier<TIER>(a, a.n + g, tn);
