@@ -11,6 +11,10 @@
 //   refcuda_gg_mix:   graingrowth/end2end_mix.cu:31-105 (AMSTENCIL)
 //   refcuda_kob_pure: snowflake/purehigh.cu:13-36 (End2end)
 //   refcuda_kob_mix:  snowflake/end2end_mix.cu:30-112 (AMSTENCIL)
+//   refcuda_sint_pure, refcuda_sint_mix: sintering/main.cu:44-206 (PURE,
+//     AMSTENCIL); the initial state (main.cu:45-59, a host loop) comes from
+//     the caller, and the classification at a run-time threshold from the
+//     wrapper's restated get_type (ref_get_type_rt)
 // The reference allocates with cudaMallocManaged, whose pages the first
 // touch zero-fills; here device allocations are zeroed explicitly.  The
 // elapsed time is the reference's own: CUDA events from step 5 to the end.
@@ -60,7 +64,8 @@ CUfunction kernel(RefModule *m, const char *name)
     for (CUfunction f : all) {
         const char *fn = nullptr;
         if (cuFuncGetName(&fn, f) != CUDA_SUCCESS || !fn) continue;
-        if (strncmp(fn, prefix.c_str(), prefix.size()) == 0) {
+        // (or an extern "C" kernel of the wrapper, by its plain name)
+        if (strncmp(fn, prefix.c_str(), prefix.size()) == 0 || strcmp(fn, name) == 0) {
             m->fns[name] = f;
             return f;
         }
@@ -453,6 +458,161 @@ int refcuda_kob_mix(void *h, int steps, double thr, int monitor, double *phi_hos
     if (phi_host && !ck(cuMemcpyDtoH(phi_host, phi, bytes), "copy")) return 1;
     if (t_host && !ck(cuMemcpyDtoH(t_host, tempr, bytes), "copy")) return 1;
     return 0;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+// sintering/main.cu:136-147 (PURE) for `steps` steps from the caller's
+// state: con1_pure, con2_pure, phi1_pure, phi2_pure, each followed by a device
+// synchronisation, then the swap.  c, e1, e2 (host, dimX*dimY): the initial
+// state in, the fields at the end out; ms: the elapsed time from step 5.
+int refcuda_sint_pure(void *h, int steps, double *c_host, double *e1_host, double *e2_host, float *ms)
+{
+    auto *m = static_cast<RefModule *>(h);
+    if (!m || !current(m)) return 1;
+    const int nx = m->dims[0], ny = m->dims[1], ux = m->dims[2], uy = m->dims[3];
+    const size_t bytes = sizeof(double) * nx * ny;
+    const unsigned tiles = (unsigned)((nx / ux) * (ny / uy));
+    Buffers B;
+    CUdeviceptr con, eta1, eta2, eta1_out, eta2_out, con_lap, eta1_lap, eta2_lap, dummy, dummy_lap, dfdcon, dfdeta1,
+        dfdeta2;
+    for (CUdeviceptr *p : {&con, &eta1, &eta2, &eta1_out, &eta2_out, &con_lap, &eta1_lap, &eta2_lap, &dummy, &dummy_lap,
+                           &dfdcon, &dfdeta1, &dfdeta2})
+        if (!B.get(*p, bytes)) return 1;
+    if (!ck(cuMemcpyHtoD(con, c_host, bytes), "copy") || !ck(cuMemcpyHtoD(eta1, e1_host, bytes), "copy") ||
+        !ck(cuMemcpyHtoD(eta2, e2_host, bytes), "copy"))
+        return 1;
+    const Dim blocks{(unsigned)ux, (unsigned)uy, 1}, grids{1, 1, tiles};
+    Timer t;
+    for (int i = 0; i < steps; ++i) {
+        if (i == 5 && !t.start()) return 1;
+        int step = i;
+        if (!launch(m, "con1_pure", grids, blocks, {&con, &con_lap, &eta1, &eta2, &dfdcon, &dummy, &step}) ||
+            !ck(cuCtxSynchronize(), "sync") ||
+            !launch(m, "con2_pure", grids, blocks, {&dummy, &dummy_lap, &con, &eta1, &eta2, &step}) ||
+            !ck(cuCtxSynchronize(), "sync") ||
+            !launch(m, "phi1_pure", grids, blocks, {&eta1, &eta1_out, &eta2, &eta1_lap, &dfdeta1, &con, &step}) ||
+            !ck(cuCtxSynchronize(), "sync") ||
+            !launch(m, "phi2_pure", grids, blocks, {&eta2, &eta2_out, &eta1, &eta2_lap, &dfdeta2, &con, &step}) ||
+            !ck(cuCtxSynchronize(), "sync"))
+            return 1;
+        std::swap(eta1, eta1_out);
+        std::swap(eta2, eta2_out);
+    }
+    if (!t.stop(ms)) return 1;
+    return !(ck(cuMemcpyDtoH(c_host, con, bytes), "copy") && ck(cuMemcpyDtoH(e1_host, eta1, bytes), "copy") &&
+             ck(cuMemcpyDtoH(e2_host, eta2, bytes), "copy"));
+}
+
+// sintering/main.cu:66-206 (AMSTENCIL) for `steps` steps from the caller's
+// state at threshold `thr` (`monitor`: 1 get_max_diff1 on c, 2 get_max_diff2
+// against con_old).  types: [ceil(steps/10)][tiles] uint8 (1 half2, 2 high);
+// c, e1, e2 in/out as in refcuda_sint_pure (the half tiles gathered by
+// data_sychro_aftercomputation); ms: the elapsed time from step 5.
+int refcuda_sint_mix(void *h, int steps, double thr, int monitor, double *c_host, double *e1_host, double *e2_host,
+                     unsigned char *types, float *ms)
+{
+    auto *m = static_cast<RefModule *>(h);
+    if (!m || !current(m) || (monitor != 1 && monitor != 2)) return 1;
+    const int nx = m->dims[0], ny = m->dims[1], ux = m->dims[2], uy = m->dims[3];
+    const int ntx = nx / ux, nty = ny / uy, tiles = ntx * nty, uxd2 = ux / 2;
+    const size_t n = (size_t)nx * ny, bytes = sizeof(double) * n, hbytes = sizeof(__half) * n;
+    Buffers B;
+    CUdeviceptr con, eta1, eta2, eta1_out, eta2_out, con_lap, eta1_lap, eta2_lap, dummy, dummy_lap, dfdcon, dfdeta1,
+        dfdeta2, con_old;
+    for (CUdeviceptr *p : {&con, &eta1, &eta2, &eta1_out, &eta2_out, &con_lap, &eta1_lap, &eta2_lap, &dummy, &dummy_lap,
+                           &dfdcon, &dfdeta1, &dfdeta2, &con_old})
+        if (!B.get(*p, bytes)) return 1;
+    CUdeviceptr hcon, heta1, heta2, heta1_out, heta2_out, hcon_lap, heta1_lap, heta2_lap, hdummy, hdummy_lap, hdfdcon,
+        hdfdeta1, hdfdeta2, type_con, type_old, max_diff;
+    for (CUdeviceptr *p : {&hcon, &heta1, &heta2, &heta1_out, &heta2_out, &hcon_lap, &heta1_lap, &heta2_lap, &hdummy,
+                           &hdummy_lap, &hdfdcon, &hdfdeta1, &hdfdeta2})
+        if (!B.get(*p, hbytes)) return 1;
+    if (!B.get(type_con, sizeof(int) * tiles) || !B.get(type_old, sizeof(int) * tiles) ||
+        !B.get(max_diff, sizeof(double) * tiles))
+        return 1;
+    {
+        std::vector<double> old(n);
+        for (size_t k = 0; k < n; ++k) old[k] = c_host[k] == 0 ? 1.0 : 0.0;  // main.cu:61-64
+        if (!ck(cuMemcpyHtoD(con, c_host, bytes), "copy") || !ck(cuMemcpyHtoD(eta1, e1_host, bytes), "copy") ||
+            !ck(cuMemcpyHtoD(eta2, e2_host, bytes), "copy") || !ck(cuMemcpyHtoD(con_old, old.data(), bytes), "copy"))
+            return 1;
+    }
+    const Dim blocks_dp{32, 32, 1}, grids_dp{(unsigned)(nx / 32 / 2), (unsigned)(ny / 32), 1};
+    if (!launch(m, "dataprepare", grids_dp, blocks_dp, {&con, &hcon}) ||
+        !launch(m, "dataprepare", grids_dp, blocks_dp, {&eta1, &heta1}) ||
+        !launch(m, "dataprepare", grids_dp, blocks_dp, {&eta2, &heta2}) || !ck(cuCtxSynchronize(), "sync"))
+        return 1;
+    double c[9];  // coefm, coefk, coefl, dvol, dvap, dsur, dgrb, dxdy, dtime
+    if (!consts(m, c, 9)) return 1;
+    auto h2 = [](double v) { return __floats2half2_rn(v, v); };  // lowprecision2highprecision, sintering/tools.h:122
+    __half2 hcoefm = h2(c[0]), hcoefk = h2(c[1]), hcoefl = h2(c[2]), hdvol = h2(c[3]), hdvap = h2(c[4]),
+            hdsur = h2(c[5]), hdgrb = h2(c[6]), hdxdy = h2(c[7]), hdtime = h2(c[8]), hcf = h2(4.0), hzpfive = h2(0.5),
+            hone = h2(1.0), htwo = h2(2.0), hfour = h2(4.0), hsix = h2(6.0), hten = h2(10.0), htwelve = h2(12.0),
+            hfifteen = h2(15.0), hthirtytwo = h2(32.0), highbound = h2(1), lowbound = h2(0.0);
+    const Dim blocks{(unsigned)uxd2, (unsigned)uy, 1}, grids{2, 1, (unsigned)tiles};
+    const Dim blocks_detect{(unsigned)(ntx > 32 ? 32 : ntx), (unsigned)(nty > 32 ? 32 : nty), 1};
+    const Dim grids_detect{(unsigned)(ntx > 32 ? ntx / 32 : 1), (unsigned)(nty > 32 ? nty / 32 : 1), 1};
+    const Dim sync_blocks{(unsigned)uxd2, (unsigned)uy, 1}, sync_grids{1, 1, (unsigned)tiles};
+    Timer t;
+    int period = 0;
+    std::vector<int> tc(tiles);
+    for (int i = 0; i < steps; ++i) {
+        if (i == 5 && !t.start()) return 1;
+        if (i % 10 == 0) {
+            const bool ok = monitor == 1 ? launch(m, "get_max_diff1", grids_detect, blocks_detect, {&con, &max_diff})
+                                         : launch(m, "get_max_diff2", grids_detect, blocks_detect,
+                                                  {&con_old, &con, &max_diff});
+            if (!ok ||
+                !launch(m, "ref_get_type_rt", grids_detect, blocks_detect, {&max_diff, &type_old, &type_con, &thr}) ||
+                !ck(cuCtxSynchronize(), "sync") ||
+                !launch(m, "data_sychro_duringcomputation", sync_grids, sync_blocks,
+                        {&con, &eta1, &eta2, &hcon, &heta1, &heta2, &type_old, &type_con}) ||
+                !ck(cuCtxSynchronize(), "sync"))
+                return 1;
+            if (types) {
+                if (!ck(cuMemcpyDtoH(tc.data(), type_con, sizeof(int) * tiles), "copy")) return 1;
+                for (int k = 0; k < tiles; ++k) types[(size_t)period * tiles + k] = (unsigned char)tc[k];
+            }
+            ++period;
+        }
+        int step = i;
+        if (!launch(m, "con1_mix", grids, blocks,
+                    {&type_con, &con, &con_old, &con_lap, &eta1, &eta2, &dfdcon, &dummy, &hcon, &hcon_lap, &heta1,
+                     &heta2, &hdfdcon, &hdummy, &hcf, &hdxdy, &hsix, &hzpfive, &hone, &htwo, &hfour, &hthirtytwo,
+                     &hcoefm, &step}) ||
+            !ck(cuCtxSynchronize(), "sync") ||
+            !launch(m, "con2_mix", grids, blocks,
+                    {&type_con, &dummy, &dummy_lap, &con, &eta1, &eta2, &hdummy, &hdummy_lap, &hcon, &heta1, &heta2,
+                     &hcf, &hdxdy, &hone, &htwo, &hsix, &hten, &hfifteen, &hdgrb, &hdsur, &hdtime, &hdvap, &hdvol,
+                     &highbound, &lowbound, &step}) ||
+            !ck(cuCtxSynchronize(), "sync") ||
+            !launch(m, "phi1_mix", grids, blocks,
+                    {&type_con, &eta1, &eta1_out, &eta2, &eta1_lap, &dfdeta1, &con, &heta1, &heta1_out, &heta2,
+                     &heta1_lap, &hdfdeta1, &hcon, &hcf, &hdxdy, &hzpfive, &hone, &htwo, &htwelve, &hdtime, &hcoefl,
+                     &hcoefk, &highbound, &lowbound, &step}) ||
+            !ck(cuCtxSynchronize(), "sync") ||
+            !launch(m, "phi2_mix", grids, blocks,
+                    {&type_con, &eta2, &eta2_out, &eta1, &eta2_lap, &dfdeta2, &con, &heta2, &heta2_out, &heta1,
+                     &heta2_lap, &hdfdeta2, &hcon, &hcf, &hdxdy, &hzpfive, &hone, &htwo, &htwelve, &hdtime, &hcoefl,
+                     &hcoefk, &highbound, &lowbound, &step}) ||
+            !ck(cuCtxSynchronize(), "sync"))
+            return 1;
+        std::swap(eta1, eta1_out);
+        std::swap(eta2, eta2_out);
+        std::swap(heta1, heta1_out);
+        std::swap(heta2, heta2_out);
+    }
+    if (!t.stop(ms)) return 1;
+    if (!launch(m, "data_sychro_aftercomputation", grids_dp, blocks_dp, {&con, &hcon, &type_con}) ||
+        !launch(m, "data_sychro_aftercomputation", grids_dp, blocks_dp, {&eta1, &heta1, &type_con}) ||
+        !launch(m, "data_sychro_aftercomputation", grids_dp, blocks_dp, {&eta2, &heta2, &type_con}) ||
+        !ck(cuCtxSynchronize(), "sync"))
+        return 1;
+    return !(ck(cuMemcpyDtoH(c_host, con, bytes), "copy") && ck(cuMemcpyDtoH(e1_host, eta1, bytes), "copy") &&
+             ck(cuMemcpyDtoH(e2_host, eta2, bytes), "copy"));
 }
 
 }  // extern "C"

@@ -7,7 +7,9 @@ part of the library.
 Each cubin fixes the reference's compile-time sizes and constants (its
 parameter file): graingrowth_pure / graingrowth_mix_m{1,2} are
 graingrowth/paras/para1.h (512 x 512, 16 x 16 tiles, Q = 2), snowflake_pure /
-snowflake_mix_m{1,2} snowflake/paras/para2.h (512 x 512, 16 x 16 tiles)."""
+snowflake_mix_m{1,2} snowflake/paras/para2.h (512 x 512, 16 x 16 tiles),
+sintering_pure / sintering_mix sintering/paras/para5.h (512 x 512, 16 x 16
+tiles, two particles; the initial state comes from the caller)."""
 import ctypes
 import os
 
@@ -40,6 +42,9 @@ def lib():
         L.refcuda_kob_pure.argtypes = [ctypes.c_void_p, ctypes.c_int, dp, dp, fp]
         L.refcuda_kob_mix.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_int, dp, dp,
                                       ctypes.c_void_p, fp]
+        L.refcuda_sint_pure.argtypes = [ctypes.c_void_p, ctypes.c_int, dp, dp, dp, fp]
+        L.refcuda_sint_mix.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_int, dp, dp, dp,
+                                       ctypes.c_void_p, fp]
         _lib = L
     return _lib
 
@@ -118,3 +123,26 @@ def kob_mix(steps, thr, monitor):
         m._ck(lib().refcuda_kob_mix(m.h, steps, thr, monitor, _p(phi), _p(t), types.ctypes.data, ctypes.byref(ms)),
               "refcuda_kob_mix")
         return phi, t, types, float(ms.value)
+
+
+def sint_pure(steps, c, e1, e2):
+    """sintering/main.cu (PURE) for `steps` steps from (c, e1, e2):
+    (c, e1, e2, ms from step 5)."""
+    with Module("sintering_pure") as m:
+        c, e1, e2 = (np.array(a, dtype=np.float64, copy=True, order="C") for a in (c, e1, e2))
+        ms = ctypes.c_float(0)
+        m._ck(lib().refcuda_sint_pure(m.h, steps, _p(c), _p(e1), _p(e2), ctypes.byref(ms)), "refcuda_sint_pure")
+        return c, e1, e2, float(ms.value)
+
+
+def sint_mix(steps, thr, monitor, c, e1, e2):
+    """sintering/main.cu (AMSTENCIL, Monitor1/2) for `steps` steps from
+    (c, e1, e2) at threshold `thr`: (c, e1, e2, types [periods][tiles]
+    (1 half2, 2 high), ms from step 5)."""
+    with Module("sintering_mix") as m:
+        c, e1, e2 = (np.array(a, dtype=np.float64, copy=True, order="C") for a in (c, e1, e2))
+        types = np.zeros(((steps + 9) // 10, m.tiles), dtype=np.uint8)
+        ms = ctypes.c_float(0)
+        m._ck(lib().refcuda_sint_mix(m.h, steps, thr, monitor, _p(c), _p(e1), _p(e2), types.ctypes.data,
+                                     ctypes.byref(ms)), "refcuda_sint_mix")
+        return c, e1, e2, types, float(ms.value)

@@ -471,8 +471,9 @@ def run_ours(args):
 def run_reference_cuda(steps=2000):
     """The reference's own CUDA kernels on this GPU beside the library, at the
     reference's own configurations (its parameter files: 512^2, 16^2 tiles):
-    grain growth para1 (Q = 2) and the Kobayashi dendrite para2, plain FP64
-    and AMSTENCIL at the sweep scripts' thresholds.  The reference: its device
+    grain growth para1 (Q = 2), the Kobayashi dendrite para2 and sintering
+    para5 (two particles), plain FP64 and AMSTENCIL at the sweep scripts'
+    thresholds.  The reference: its device
     code built from its sources for sm_103a (baseline/_ref/*.cubin), its host
     loops restated around driver-API launches (baseline/ref_cuda.cpp), timed
     by its own event window (step 5 to the end; one device synchronisation
@@ -521,6 +522,18 @@ def run_reference_cuda(steps=2000):
             "kobayashi", 2, mode="end2end_mix", monitor=m, monitor_samples=0, monitor_field=0, thr_lo=thr,
             thr_hi=thr, ref_order=1))
     out["kobayashi_para2"] = kob
+    if refcuda.available("sintering_pure") and refcuda.available("sintering_mix"):
+        f0 = amps.init_host(amps.Params.preset("sintering", 5, mode="purehigh", ref_order=1), amps.INIT_REFERENCE)
+        sint = {"ref_plain_fp64": rate(refcuda.sint_pure(total, f0[0], f0[1], f0[2])[3]),
+                "ours_plain_fp64_reference_order": ours(amps.Params.preset("sintering", 5, mode="purehigh",
+                                                                           ref_order=1)),
+                "ours_plain_fp64_fma": ours(amps.Params.preset("sintering", 5, mode="purehigh", ref_order=0))}
+        for m, thr in ((2, 1e-4), (1, 0.5)):
+            sint[f"ref_amstencil_monitor{m}_{thr:g}"] = rate(refcuda.sint_mix(total, thr, m, f0[0], f0[1], f0[2])[4])
+            sint[f"ours_mixed_monitor{m}_{thr:g}"] = ours(amps.Params.preset(
+                "sintering", 5, mode="end2end_mix", monitor=m, monitor_samples=0, monitor_field=0, thr_lo=thr,
+                thr_hi=thr, ref_order=1, half_arith=amps.HALF_REF))
+        out["sintering_para5"] = sint
     return out
 
 
