@@ -87,7 +87,10 @@ enum {
                             sintering per cell with the chemical potential at each cell's owner tier
                             (sintering/function.h:245-249,401-411,556-565; FP64 high tier, one
                             threshold): the parity path of the reference's AMSTENCIL mixed mode */
-    AMPS_HALF_HFMA2 = 2  /* binary16 pairs with fused multiply-adds (HFMA2) */
+    AMPS_HALF_HFMA2 = 2, /* binary16 pairs with fused multiply-adds (HFMA2) */
+    AMPS_HALF_SR = 3     /* FP32 arithmetic, binary16 storage by stochastic rounding (unbiased; seeded by
+                            amps_params.seed): a change below half an ulp accumulates instead of rounding away
+                            (Kobayashi) */
 };
 
 /* dtypes crossing the ABI */
@@ -138,7 +141,7 @@ typedef struct amps_params {
     int init_offset;
     uint64_t seed;
     int half_arith;       /* AMPS_HALF_FP32 / AMPS_HALF_REF (grain growth, sintering) / AMPS_HALF_HFMA2
-                             (grain growth) */
+                             (grain growth) / AMPS_HALF_SR (Kobayashi) */
     int ref_snapshot;     /* 1: the temporal monitor's lattice snapshot as the reference keeps it: a tile
                              computed at half refreshes only the first half of its columns
                              (graingrowth/function.h:38-39,68-73, snowflake/function.h:69-70,106-113,

@@ -124,3 +124,11 @@ def test_seeded_states():
     assert np.array_equal(g[0], eta.sum(0))                                # c = 1 inside particles
     assert all(eta[k].sum() > 1000 for k in range(16))                     # all 16 placed, r >= 20
     assert np.array_equal(g, w.init_host(s, w.INIT_SEEDED))                # deterministic
+
+
+def test_stochastic_half_rounding_is_a_kobayashi_option():
+    w = amps()
+    assert w.Params.preset("kobayashi", 2, mode="end2end_mix", half_arith=w.HALF_SR).check()[0] == 0
+    assert w.Params.preset("graingrowth", 0, half_arith=w.HALF_SR).check()[0] == 1
+    assert w.Params.preset("sintering", 0, half_arith=w.HALF_SR).check()[0] == 1
+    assert w.Params.preset("kobayashi", 2, half_arith=4).check()[0] == 1

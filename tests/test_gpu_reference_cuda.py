@@ -14,12 +14,14 @@ What is pinned:
     whose half tiles call the device-only h2cos/h2sin) makes the same tier
     decision in every period as the library's mixed mode at the same monitor
     and threshold (the library's half tiles compute in FP32, the reference's
-    in half2).  Mixed-vs-own-FP64 error after 500 steps: the library's mean
-    and max |d phi| are below the reference's at three of the four settings
-    and within 1.9x / 2.7x at Monitor2 1e-2 (bars 2.5x / 3x); its mean |d T|
-    is lower where T < 1, but at the dendrite's centre (T ~ 1.1, where a
-    half's ulp is 2^-10) its max |d T| is ~3x the reference's (printed, not
-    asserted);
+    in half2).  Mixed-vs-own-FP64 error after 500 steps, to-nearest storage:
+    mean and max |d phi| below the reference's at three of the four settings,
+    within 1.9x / 2.7x at Monitor2 1e-2 (bars 2.5x / 3x); at the dendrite's
+    centre (T ~ 1.1, a half's ulp 2^-10) T's small diffusive increments round
+    away and max |d T| is ~3x the reference's.  With stochastic rounding of
+    the half stores (half_arith = AMPS_HALF_SR) the mean |d phi| and |d T| --
+    the reference's error metric -- are below the reference's at every
+    setting (asserted);
   * sintering (sintering/main.cu, para5): the reference's GPU plain run from
     the library's reference initial state equals its CPU build to 1e-7 after
     40 steps, and its GPU AMSTENCIL run makes the library's reference-mode
@@ -89,25 +91,34 @@ def test_reference_gpu_amstencil_kobayashi_decisions_and_envelope(monitor, thr):
     with w.Simulation(q, init=w.INIT_REFERENCE) as s:
         s.run(steps)
         op = s.fields()
-    p = w.Params.preset("kobayashi", 2, mode="end2end_mix", monitor=monitor, monitor_samples=0, monitor_field=0,
-                        thr_lo=thr, thr_hi=thr, ref_order=1, max_log=64)
-    with w.Simulation(p, init=w.INIT_REFERENCE) as s:
-        s.run(steps)
-        f = s.fields()
-        log = s.decision_log()
-    ours = np.where(log.reshape(log.shape[0], -1) == w.TIER_HALF, 1, 2)
-    bad = [i for i in range(types.shape[0]) if not np.array_equal(ours[i], types[i])]
     ref_err = [float(np.abs(mp - rp).mean()), float(np.abs(mp - rp).max()), float(np.abs(mt - rt).mean()),
                float(np.abs(mt - rt).max())]
-    our_err = [float(np.abs(f[0] - op[0]).mean()), float(np.abs(f[0] - op[0]).max()),
-               float(np.abs(f[1] - op[1]).mean()), float(np.abs(f[1] - op[1]).max())]
-    print(f"kobayashi monitor {monitor} {thr:g}: periods differing {bad[:5]}; mixed vs FP64 "
-          f"(mean phi, max phi, mean T, max T) reference {np.array(ref_err)} ours {np.array(our_err)}")
-    assert not bad
     # the plain FP64 runs agree (the reference's seed is symmetric and
     # ill-conditioned: ulps of atan2 grow to ~1e-7 by step 500)
     assert float(np.abs(op[0] - rp).max()) <= 1e-5
-    assert our_err[0] <= ref_err[0] * 2.5 + 1e-12 and our_err[1] <= ref_err[1] * 3.0 + 1e-12
+    errs = {}
+    for name, ha in (("nearest", w.HALF_FP32), ("stochastic", w.HALF_SR)):
+        p = w.Params.preset("kobayashi", 2, mode="end2end_mix", monitor=monitor, monitor_samples=0, monitor_field=0,
+                            thr_lo=thr, thr_hi=thr, ref_order=1, max_log=64, half_arith=ha)
+        with w.Simulation(p, init=w.INIT_REFERENCE) as s:
+            s.run(steps)
+            f = s.fields()
+            log = s.decision_log()
+        ours = np.where(log.reshape(log.shape[0], -1) == w.TIER_HALF, 1, 2)
+        bad = [i for i in range(types.shape[0]) if not np.array_equal(ours[i], types[i])]
+        assert not bad, (name, bad)
+        errs[name] = [float(np.abs(f[0] - op[0]).mean()), float(np.abs(f[0] - op[0]).max()),
+                      float(np.abs(f[1] - op[1]).mean()), float(np.abs(f[1] - op[1]).max())]
+    print(f"kobayashi monitor {monitor} {thr:g}: decisions equal; mixed vs FP64 (mean phi, max phi, mean T, max T) "
+          f"reference {np.array(ref_err)} nearest {np.array(errs['nearest'])} stochastic {np.array(errs['stochastic'])}")
+    rn, sr = errs["nearest"], errs["stochastic"]
+    assert rn[0] <= ref_err[0] * 2.5 and rn[1] <= ref_err[1] * 3.0
+    # the reference's error metric, the mean |d f| over the grid
+    # (snowflake/end2enderror.py): stochastic rounding within the reference's
+    # own envelope for both fields; the max within 3.5x (one ulp of a
+    # stochastically rounded cell)
+    assert sr[0] <= ref_err[0] and sr[2] <= ref_err[2]
+    assert sr[1] <= ref_err[1] * 3.5 and sr[3] <= ref_err[3] * 3.5
 
 
 def test_reference_gpu_plain_sintering_equals_its_cpu_build():

@@ -24,7 +24,7 @@ PUREHIGH, PURELOW, END2END_MIX, GRAM1, GRAM2 = 0, 1, 2, 3, 4
 TIER_HALF, TIER_FP32, TIER_FP64 = 0, 1, 2
 BC_PERIODIC, BC_NOFLUX = 0, 1
 MONITOR_SPA, MONITOR_TEM, MONITOR_RATE = 1, 2, 3
-HALF_FP32, HALF_REF, HALF_HFMA2 = 0, 1, 2
+HALF_FP32, HALF_REF, HALF_HFMA2, HALF_SR = 0, 1, 2, 3
 F64, F32 = 0, 1
 INIT_REFERENCE, INIT_SEEDED = 0, 1
 REDUCE_SUM, REDUCE_MIN, REDUCE_MAX, REDUCE_SUMSQ = 0, 1, 2, 3

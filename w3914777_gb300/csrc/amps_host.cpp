@@ -184,7 +184,9 @@ extern "C" int amps_check_params(const amps_params *p, char *msg, size_t len)
     if (!(p->dx > 0) || !(p->dy > 0) || !(p->dt > 0)) BAD("dx, dy, dt must be positive");
     if (p->mode == AMPS_GRAM1 || p->mode == AMPS_GRAM2)
         if (!(p->gram_ratio >= 0 && p->gram_ratio <= 1)) BAD("gram_ratio must be in [0,1]");
-    if (p->half_arith < AMPS_HALF_FP32 || p->half_arith > AMPS_HALF_HFMA2) BAD("half_arith must be 0, 1 or 2");
+    if (p->half_arith < AMPS_HALF_FP32 || p->half_arith > AMPS_HALF_SR) BAD("half_arith must be 0, 1, 2 or 3");
+    if (p->half_arith == AMPS_HALF_SR && p->model != AMPS_KOBAYASHI)
+        BAD("stochastic rounding of half tiles is built for Kobayashi only");
     if (p->half_arith == AMPS_HALF_HFMA2 && p->model != AMPS_GRAINGROWTH)
         BAD("the HFMA2 half arithmetic is built for grain growth only");
     if (p->half_arith == AMPS_HALF_REF && p->model == AMPS_KOBAYASHI)

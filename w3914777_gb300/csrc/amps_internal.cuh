@@ -244,6 +244,33 @@ template <int TIER, typename CT> __device__ __forceinline__ CT round_to_tier(CT 
     return v;
 }
 
+// Stochastic rounding of a float to binary16 (half_arith = AMPS_HALF_SR):
+// the binary16 neighbours lo <= v <= hi, hi with probability
+// (v - lo) / (hi - lo) for the 24-bit uniform r24.  Unbiased, so a change
+// below half an ulp accumulates in expectation instead of rounding away at
+// every step (Croci & Giles, "Effects of round-to-nearest and stochastic
+// rounding in the numerical solution of the heat equation in low
+// precision", 2020).  NaN stays NaN; exact values are kept.
+__device__ __forceinline__ __half half_sr(float v, uint32_t r24)
+{
+    const __half lo = __float2half_rd(v), hi = __float2half_ru(v);
+    const float flo = __half2float(lo), fhi = __half2float(hi);
+    return (float)r24 * 0x1.0p-24f * (fhi - flo) < v - flo ? hi : lo;
+}
+
+// 24 uniform bits for the stochastic rounding of cell `cell` at step `step`
+// (a SplitMix64 finaliser; a stream of its own, apart from the seeded noise).
+__device__ __forceinline__ uint32_t sr_bits(uint64_t seed, uint64_t step, uint64_t cell)
+{
+    auto mix = [](uint64_t z) {
+        z += 0x9E3779B97F4A7C15ull;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return z ^ (z >> 31);
+    };
+    return (uint32_t)(mix(mix(~seed ^ mix(step)) + cell) >> 40);
+}
+
 template <int TIER, typename CT> __device__ __forceinline__ void store_tier(const StepArgs &a, int64_t idx, CT v)
 {
     if (TIER == TIER_FP64) ((double *)a.out[2])[idx] = (double)v;

@@ -7,6 +7,7 @@
 // computes phi_x, phi_y, eps, eps' on the tile plus a 1-cell ring in shared
 // memory (phase A), then the update on the tile (phase B).  Nothing but phi
 // and T touches HBM.
+#include "../../include/amps.h"
 #include "amps_internal.cuh"
 #include "amps_kernels.h"
 #include <type_traits>
@@ -70,16 +71,15 @@ __device__ __forceinline__ void kob_aniso(const CT *P, int ps, const Phys &ph, C
 }
 
 // Phase B at one cell (snowflake/function.h:54-59): P, Tm at the cell's phi
-// and T (row stride sp); the phase-A arrays at index o, row stride es.  The
-// latent heat added to T is kappa times the change of phi as the tile's
-// tier stores it (TIER: the rounding of the stored phi), so that a half
-// tile's T moves with the phi it keeps, as the reference's half2 update does
-// (snowflake/function.h:512-513 reads the new half phi): without it, a phi
-// increment below half an ulp heats T every step while the stored phi stays.
-template <typename CT, int TIER>
+// and T (row stride sp); the phase-A arrays at index o, row stride es.  pn
+// comes back as the tile's tier stores it (rnd: the storage rounding), and
+// the latent heat added to T is kappa times that stored change of phi, so
+// that a half tile's T moves with the phi it keeps, as the reference's half2
+// update does (snowflake/function.h:512-513 reads the new half phi).
+template <typename CT, typename RND>
 __device__ __forceinline__ void kob_update(const CT *P, const CT *Tm, int sp, const CT *px, const CT *py,
                                            const CT *ep, const CT *epd, int o, int es, const Phys &ph, int64_t step,
-                                           int64_t g, CT &pn, CT &tn)
+                                           int64_t g, RND rnd, CT &pn, CT &tn)
 {
     const CT p0 = P[0], t0 = Tm[0];
     const CT inv = kc<CT>(ph, KB_INV);
@@ -95,8 +95,8 @@ __device__ __forceinline__ void kob_update(const CT *P, const CT *Tm, int sp, co
     if (nonzero(ph.noise))
         drive += kc<CT>(ph, KB_NOISE) * (noise_u01_t<CT>(ph.seed, (uint64_t)step, (uint64_t)g) - CT(0.5));
     const CT inner = term1 + term2 + ep[o] * ep[o] * lp + p0 * (CT(1) - p0) * drive;
-    pn = fma(kc<CT>(ph, KB_DTT), inner, p0);
-    tn = fma(kc<CT>(ph, KB_KAPPA), round_to_tier<TIER>(pn) - p0, fma(kc<CT>(ph, KB_DT), lt, t0));
+    pn = rnd(fma(kc<CT>(ph, KB_DTT), inner, p0));
+    tn = fma(kc<CT>(ph, KB_KAPPA), pn - p0, fma(kc<CT>(ph, KB_DT), lt, t0));
 }
 
 // One tile of one step at tier TIER (smraw: the kernel's dynamic shared
@@ -200,7 +200,15 @@ __device__ __forceinline__ void kob_tile(const StepArgs &a, unsigned char *smraw
             pn = __dadd_rn(p0, __dmul_rn(ph.dt / ph.tau, inner));
             tn = __dadd_rn(__dadd_rn(t0, __dmul_rn(ph.dt, lt)), __dmul_rn(ph.kappa, __dsub_rn(pn, p0)));
         } else {
-            kob_update<CT, TIER>(P, Tm, S::P, px, py, ep, epd, o, E, ph, step, g, pn, tn);
+            // storage rounding: to nearest, or (half tiles, AMPS_HALF_SR) stochastic
+            const bool sr = TIER == TIER_HALF && a.half_arith == AMPS_HALF_SR;
+            auto rnd = [&](CT v) -> CT {
+                if (TIER == TIER_HALF && sr) return (CT)__half2float(half_sr((float)v, sr_bits(ph.seed, step, g)));
+                return round_to_tier<TIER>(v);
+            };
+            kob_update<CT>(P, Tm, S::P, px, py, ep, epd, o, E, ph, step, g, rnd, pn, tn);
+            if (TIER == TIER_HALF && sr)
+                tn = (CT)__half2float(half_sr((float)tn, sr_bits(ph.seed, step, (uint64_t)(a.n + g))));
         }
         store_tier<TIER>(a, g, pn);
         store_tier<TIER>(a, a.n + g, tn);
