@@ -146,11 +146,12 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity
 // this way reads nothing the previous one writes before its own
 // griddepcontrol.wait.
 template <typename K, typename... Args>
-inline cudaError_t launch_kernel(K kernel, int grid, size_t smem, cudaStream_t s, bool pdl, Args... args)
+inline cudaError_t launch_kernel_nt(K kernel, int grid, int threads, size_t smem, cudaStream_t s, bool pdl,
+                                   Args... args)
 {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(kThreads);
+    cfg.blockDim = dim3(threads);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = s;
     cudaLaunchAttribute at[1];
@@ -159,6 +160,12 @@ inline cudaError_t launch_kernel(K kernel, int grid, size_t smem, cudaStream_t s
     cfg.attrs = at;
     cfg.numAttrs = pdl ? 1 : 0;
     return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
+template <typename K, typename... Args>
+inline cudaError_t launch_kernel(K kernel, int grid, size_t smem, cudaStream_t s, bool pdl, Args... args)
+{
+    return launch_kernel_nt(kernel, grid, kThreads, smem, s, pdl, args...);
 }
 
 // x is +0 (bit pattern 0): an integer test, no floating-point instruction
@@ -317,7 +324,7 @@ __device__ __forceinline__ void load_neighbour_tiers(const StepArgs &a, int tx, 
 // SKIP32: the FP32-owned slots already hold their values (copied by this
 // same thread: stage_tile_async32 gives every thread the same slots); only
 // the others are loaded and converted.
-template <typename CT, int T, int R, bool SKIP32 = false, bool NC = true>
+template <typename CT, int T, int R, bool SKIP32 = false, bool NC = true, int NT = kThreads>
 __device__ __forceinline__ void stage_tile(const StepArgs &a, CT *sm, const uint8_t *nt, int tx, int ty, int f0,
                                            int nfs)
 {
@@ -326,7 +333,7 @@ __device__ __forceinline__ void stage_tile(const StepArgs &a, CT *sm, const uint
     constexpr int UI = S::ROWS * SEG;    // interior 8-cell segments per field
     constexpr int UH = S::ROWS * 2 * R;  // halo cells per field
     constexpr int U = UI + UH;
-    constexpr int SLOTS = (U + kThreads - 1) / kThreads;
+    constexpr int SLOTS = (U + NT - 1) / NT;
     constexpr int B0 = (sizeof(CT) == 8 ? 2 : 4) / SLOTS;
     constexpr int B = B0 < 1 ? 1 : B0;   // fields per batch
     const int x0 = tx * T, y0 = ty * T;
@@ -334,7 +341,7 @@ __device__ __forceinline__ void stage_tile(const StepArgs &a, CT *sm, const uint
     int64_t goff[SLOTS];
 #pragma unroll
     for (int q = 0; q < SLOTS; ++q) {
-        const int u = threadIdx.x + q * kThreads;
+        const int u = threadIdx.x + q * NT;
         kind[q] = 0; tier[q] = 0; soff[q] = 0; goff[q] = 0;
         if (u < UI) {
             const int sg = u % SEG, r = u / SEG;
@@ -538,7 +545,9 @@ __device__ __forceinline__ double warp_min(double v)
     for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
     return v;
 }
-// Max over the block; every thread gets the result.  red: >= 8 doubles of shared memory.
+// Max over the block of NT threads; every thread gets the result.  red: >=
+// NT/32 doubles of shared memory.
+template <int NT = kThreads>
 __device__ __forceinline__ double block_max(double v, double *red)
 {
     v = warp_max(v);
@@ -547,9 +556,10 @@ __device__ __forceinline__ double block_max(double v, double *red)
     __syncthreads();
     double r = red[0];
 #pragma unroll
-    for (int w = 1; w < kThreads / 32; ++w) r = fmax(r, red[w]);
+    for (int w = 1; w < NT / 32; ++w) r = fmax(r, red[w]);
     return r;
 }
+template <int NT = kThreads>
 __device__ __forceinline__ double block_min(double v, double *red)
 {
     v = warp_min(v);
@@ -558,7 +568,7 @@ __device__ __forceinline__ double block_min(double v, double *red)
     __syncthreads();
     double r = red[0];
 #pragma unroll
-    for (int w = 1; w < kThreads / 32; ++w) r = fmin(r, red[w]);
+    for (int w = 1; w < NT / 32; ++w) r = fmin(r, red[w]);
     return r;
 }
 
@@ -686,6 +696,7 @@ __device__ __forceinline__ float warp_maxf(float v)
     for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
     return v;
 }
+template <int NT = kThreads>
 __device__ __forceinline__ float block_maxf(float v, float *red)
 {
     v = warp_maxf(v);
@@ -694,22 +705,23 @@ __device__ __forceinline__ float block_maxf(float v, float *red)
     __syncthreads();
     float r = red[0];
 #pragma unroll
-    for (int w = 1; w < kThreads / 32; ++w) r = fmaxf(r, red[w]);
+    for (int w = 1; w < NT / 32; ++w) r = fmaxf(r, red[w]);
     return r;
 }
 
+template <int NT = kThreads>
 __device__ __forceinline__ double mon_finish(const StepArgs &a, MonAccF &m, double *red, double metric)
 {
     float *redf = reinterpret_cast<float *>(red);
     double v;
     if (a.monitor_kind == 1) {
-        const float mx = block_maxf(m.mx, redf);
-        const float mn = -block_maxf(-m.mn, redf);
+        const float mx = block_maxf<NT>(m.mx, redf);
+        const float mn = -block_maxf<NT>(-m.mn, redf);
         v = (double)mx - (double)mn;
     } else if (a.monitor_kind == 2) {
-        v = block_max(m.dmax, red);
+        v = block_max<NT>(m.dmax, red);
     } else {
-        v = (double)block_maxf(m.dmaxf, redf) * a.cadence;
+        v = (double)block_maxf<NT>(m.dmaxf, redf) * a.cadence;
     }
     if (__syncthreads_or(m.bad) && threadIdx.x == 0) atomicOr(a.flags, 1);
     return fmax(metric, v);
@@ -763,16 +775,17 @@ __device__ __forceinline__ void mon_reset(const StepArgs &a, MonAcc &m)
     m.bad = 0;
 }
 
-// Reduce one field's accumulator over the block and fold into the tile metric.
+// Reduce one field's accumulator over the block of NT threads and fold into the tile metric.
+template <int NT = kThreads>
 __device__ __forceinline__ double mon_finish(const StepArgs &a, MonAcc &m, double *red, double metric)
 {
     double v;
     if (a.monitor_kind == 1) {
-        const double mx = block_max(m.mx, red);
-        const double mn = block_min(m.mn, red);
+        const double mx = block_max<NT>(m.mx, red);
+        const double mn = block_min<NT>(m.mn, red);
         v = mx - mn;
     } else {
-        v = block_max(m.dmax, red);
+        v = block_max<NT>(m.dmax, red);
     }
     if (__syncthreads_or(m.bad) && threadIdx.x == 0) atomicOr(a.flags, 1);
     return fmax(metric, v);

@@ -99,9 +99,16 @@ __device__ __forceinline__ void kob_update(const CT *P, const CT *Tm, int sp, co
     tn = fma(kc<CT>(ph, KB_KAPPA), pn - p0, fma(kc<CT>(ph, KB_DT), lt, t0));
 }
 
+// Threads per Kobayashi tile CTA.  A 512^2 grid is 256 tiles of 32^2, so
+// at 256 threads a tile the step ran one partial wave at ~14 warps per SM,
+// latency-bound; 512 threads a tile double the warps in flight (44 registers
+// a thread: two CTAs per SM).
+constexpr int kKobThreads = 512;
+
 // One tile of one step at tier TIER (smraw: the kernel's dynamic shared
-// memory, kob_smem<T, TIER> bytes; red / ntier: its static scratch).
-template <int T, int TIER, bool REF>
+// memory, kob_smem<T, TIER> bytes; red / ntier: its static scratch; NT
+// threads).
+template <int T, int TIER, bool REF, int NT = kKobThreads>
 __device__ __forceinline__ void kob_tile(const StepArgs &a, unsigned char *smraw, double *red, uint8_t *ntier,
                                          int tile)
 {
@@ -115,14 +122,14 @@ __device__ __forceinline__ void kob_tile(const StepArgs &a, unsigned char *smraw
     const int x0 = tx * T, y0 = ty * T;
     load_neighbour_tiers(a, tx, ty, ntier);
     __syncthreads();
-    stage_tile<CT, T, R>(a, sm, ntier, tx, ty, 0, 2);
+    stage_tile<CT, T, R, false, true, NT>(a, sm, ntier, tx, ty, 0, 2);
     __syncthreads();
     const Phys &ph = a.ph;
 
     // phase A: snowflake/function.h:30-34 on the tile + ring.  With zero-flux
     // boundaries a ring cell outside the domain takes the intermediates of
     // the cell it mirrors, as an index-mapped read of the full-size arrays does.
-    for (int u = threadIdx.x; u < E * E; u += kThreads) {
+    for (int u = threadIdx.x; u < E * E; u += NT) {
         int i = u % E - 1, j = u / E - 1;
         if (a.bc != 0) {
             i = bc_map(x0 + i, a.nx, 1) - x0;
@@ -157,7 +164,7 @@ __device__ __forceinline__ void kob_tile(const StepArgs &a, unsigned char *smraw
     const bool mon_on = a.monitor_now != 0;
     if (mon_on) mon_reset(a, mon);
     const int mslot = 0;
-    for (int u = threadIdx.x; u < T * T; u += kThreads) {
+    for (int u = threadIdx.x; u < T * T; u += NT) {
         const int i = u % T, j = u / T;
         const int r = j + R, cc = i + S::O;
         const int o = (j + 1) * E + (i + 1);
@@ -217,13 +224,13 @@ __device__ __forceinline__ void kob_tile(const StepArgs &a, unsigned char *smraw
                        snap_prefetch<T>(a, mslot, tile, j, i, g));
     }
     if (mon_on) {
-        metric = mon_finish(a, mon, red, metric);
+        metric = mon_finish<NT>(a, mon, red, metric);
         if (a.mfield < 0 || a.mfield == 1) {
             // second monitored field (T): a second pass over the stored values
             MA m2;
             mon_reset(a, m2);
             __syncthreads();
-            for (int u = threadIdx.x; u < T * T; u += kThreads) {
+            for (int u = threadIdx.x; u < T * T; u += NT) {
                 const int i = u % T, j = u / T;
                 const int64_t g = (int64_t)(y0 + j) * a.nx + x0 + i;
                 CT v;
@@ -234,7 +241,7 @@ __device__ __forceinline__ void kob_tile(const StepArgs &a, unsigned char *smraw
                 mon_add<T>(a, m2, slot, tile, j, i, g, v, S::at(sm, 1, j + R, i + S::O),
                            snap_prefetch<T>(a, slot, tile, j, i, g));
             }
-            metric = mon_finish(a, m2, red, metric);
+            metric = mon_finish<NT>(a, m2, red, metric);
         }
         if (threadIdx.x == 0) a.metric[tile] = metric;
     }
@@ -242,10 +249,10 @@ __device__ __forceinline__ void kob_tile(const StepArgs &a, unsigned char *smraw
 
 // The tiles of one tier (list / count built by the classification).
 template <int T, int TIER, bool REF>
-__global__ void __launch_bounds__(kThreads) kob_step_kernel(StepArgs a)
+__global__ void __launch_bounds__(kKobThreads) kob_step_kernel(StepArgs a)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
-    __shared__ double red[kThreads / 32];
+    __shared__ double red[kKobThreads / 32];
     __shared__ uint8_t ntier[9];
     pdl_trigger();  // the step's half/FP32 launch may start alongside (FP64 launch first)
     if ((int)blockIdx.x >= a.count[TIER]) return;
@@ -260,10 +267,10 @@ __global__ void __launch_bounds__(kThreads) kob_step_kernel(StepArgs a)
 // the previous step's state only); its last CTA waits for the FP64 grid
 // before it exits, so this grid completes after both.
 template <int T>
-__global__ void __launch_bounds__(kThreads) kob_step_lo_kernel(StepArgs a)
+__global__ void __launch_bounds__(kKobThreads) kob_step_lo_kernel(StepArgs a)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
-    __shared__ double red[kThreads / 32];
+    __shared__ double red[kKobThreads / 32];
     __shared__ uint8_t ntier[9];
     const int tile = blockIdx.x;
     const int tier = a.tier_out[tile];
@@ -282,7 +289,7 @@ template <int T, int TIER, bool REF>
 static cudaError_t kob_launch_t(const StepArgs &a, int grid, cudaStream_t s)
 {
     const size_t smem = kob_smem<T, TIER>();
-    kob_step_kernel<T, TIER, REF><<<grid, kThreads, smem, s>>>(a);
+    kob_step_kernel<T, TIER, REF><<<grid, kKobThreads, smem, s>>>(a);
     return cudaGetLastError();
 }
 
@@ -309,8 +316,9 @@ cudaError_t kob_launch(int tile, int tier, bool ref, const StepArgs &a, int grid
 
 cudaError_t kob_launch_lo(int tile, const StepArgs &a, int grid, cudaStream_t s, bool after64)
 {
-    if (tile == 32) return launch_kernel(kob_step_lo_kernel<32>, grid, kob_smem<32, TIER_FP32>(), s, after64, a);
-    return launch_kernel(kob_step_lo_kernel<16>, grid, kob_smem<16, TIER_FP32>(), s, after64, a);
+    if (tile == 32)
+        return launch_kernel_nt(kob_step_lo_kernel<32>, grid, kKobThreads, kob_smem<32, TIER_FP32>(), s, after64, a);
+    return launch_kernel_nt(kob_step_lo_kernel<16>, grid, kKobThreads, kob_smem<16, TIER_FP32>(), s, after64, a);
 }
 
 cudaError_t kob_prepare_lo(int tile)
