@@ -11,6 +11,8 @@
 //   refcuda_gg_mix:   graingrowth/end2end_mix.cu:31-105 (AMSTENCIL)
 //   refcuda_kob_pure: snowflake/purehigh.cu:13-36 (End2end)
 //   refcuda_kob_mix:  snowflake/end2end_mix.cu:30-112 (AMSTENCIL)
+//   refcuda_gg_purelow:  graingrowth/purelow.cu:3-47 (HALF2)
+//   refcuda_kob_purelow: snowflake/purelow.cu:3-66 (HALF2)
 //   refcuda_sint_pure, refcuda_sint_mix: sintering/main.cu:44-206 (PURE,
 //     AMSTENCIL); the initial state (main.cu:45-59, a host loop) comes from
 //     the caller, and the classification at a run-time threshold from the
@@ -21,6 +23,7 @@
 #include <cuda.h>
 #include <cuda_fp16.h>
 
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -613,6 +616,91 @@ int refcuda_sint_mix(void *h, int steps, double thr, int monitor, double *c_host
         return 1;
     return !(ck(cuMemcpyDtoH(c_host, con, bytes), "copy") && ck(cuMemcpyDtoH(e1_host, eta1, bytes), "copy") &&
              ck(cuMemcpyDtoH(e2_host, eta2, bytes), "copy"));
+}
+
+}  // extern "C"
+
+extern "C" {
+
+// graingrowth/purelow.cu:3-47 (HALF2) for `steps` steps: dataprepare_half2,
+// then per step kernel1_lowpure for eta1 and for eta2, a device
+// synchronisation and the swap.  eta1, eta2 (host, dimX*dimY/2 half2 pairs as
+// 32-bit words): the fields at the end; ms: the elapsed time from step 5.
+int refcuda_gg_purelow(void *h, int steps, uint32_t *eta1_host, uint32_t *eta2_host, float *ms)
+{
+    auto *m = static_cast<RefModule *>(h);
+    if (!m || !current(m)) return 1;
+    const int nx = m->dims[0], ny = m->dims[1], ux = m->dims[2], uy = m->dims[3];
+    const size_t hbytes = sizeof(__half) * nx * ny;
+    const unsigned tiles = (unsigned)((nx / ux) * (ny / uy));
+    Buffers B;
+    CUdeviceptr eta1, eta2, eta1_out, eta2_out, eta1_lap, eta2_lap, dfdeta1, dfdeta2;
+    for (CUdeviceptr *p : {&eta1, &eta2, &eta1_out, &eta2_out, &eta1_lap, &eta2_lap, &dfdeta1, &dfdeta2})
+        if (!B.get(*p, hbytes)) return 1;
+    const Dim blocks{(unsigned)(ux / 2), (unsigned)uy, 1}, grids{1, 1, tiles};
+    if (!launch(m, "dataprepare_half2", grids, blocks, {&eta1, &eta2}) || !ck(cuCtxSynchronize(), "sync")) return 1;
+    double c[4];  // mobil, grcoef, dxdy, dtime
+    if (!consts(m, c, 4)) return 1;
+    __half2 hmobil = __float2half2_rn(c[0]), hgrcoef = __float2half2_rn(c[1]), hdxdy = __float2half2_rn(c[2]),
+            hdtime = __float2half2_rn(c[3]), height = __float2half2_rn(8.0), hone = __float2half2_rn(1.0),
+            htwo = __float2half2_rn(2.0);
+    Timer t;
+    for (int i = 0; i < steps; ++i) {
+        if (i == 5 && !t.start()) return 1;
+        if (!launch(m, "kernel1_lowpure", grids, blocks,
+                    {&eta1, &eta2, &eta1_lap, &dfdeta1, &eta1_out, &hone, &htwo, &height, &hdtime, &hmobil, &hgrcoef,
+                     &hdxdy}) ||
+            !launch(m, "kernel1_lowpure", grids, blocks,
+                    {&eta2, &eta1, &eta2_lap, &dfdeta2, &eta2_out, &hone, &htwo, &height, &hdtime, &hmobil, &hgrcoef,
+                     &hdxdy}) ||
+            !ck(cuCtxSynchronize(), "sync"))
+            return 1;
+        std::swap(eta1, eta1_out);
+        std::swap(eta2, eta2_out);
+    }
+    if (!t.stop(ms)) return 1;
+    return !(ck(cuMemcpyDtoH(eta1_host, eta1, hbytes), "copy") && ck(cuMemcpyDtoH(eta2_host, eta2, hbytes), "copy"));
+}
+
+// snowflake/purelow.cu:3-66 (HALF2) for `steps` steps: dataprepare_half2
+// (phi; T starts at 0), then per step kernel1_purelow, kernel2_purelow (in
+// place) and a device synchronisation.  phi, T (host, half2 pairs as 32-bit
+// words): the fields at the end; ms: the elapsed time from step 5.
+int refcuda_kob_purelow(void *h, int steps, uint32_t *phi_host, uint32_t *t_host, float *ms)
+{
+    auto *m = static_cast<RefModule *>(h);
+    if (!m || !current(m)) return 1;
+    const int nx = m->dims[0], ny = m->dims[1], ux = m->dims[2], uy = m->dims[3];
+    const size_t hbytes = sizeof(__half) * nx * ny;
+    const unsigned tiles = (unsigned)((nx / ux) * (ny / uy));
+    Buffers B;
+    CUdeviceptr phi, phi_lap, tempr, tempr_lap, phidx, phidy, epsilon, epsilon_deri;
+    for (CUdeviceptr *p : {&phi, &phi_lap, &tempr, &tempr_lap, &phidx, &phidy, &epsilon, &epsilon_deri})
+        if (!B.get(*p, hbytes)) return 1;
+    const Dim blocks{(unsigned)(ux / 2), (unsigned)uy, 1}, grids{1, 1, tiles};
+    if (!launch(m, "dataprepare_half2", grids, blocks, {&phi}) || !ck(cuCtxSynchronize(), "sync")) return 1;
+    double c[14];  // dxdy, dy*2, dx*2, theta0, aniso, delta, epsilonb, alpha, pi, gama, kappa, teq, dtime, tau
+    if (!consts(m, c, 14)) return 1;
+    __half2 hdxdy = __float2half2_rn(c[0]), hdym2 = __float2half2_rn(c[1]), hdxm2 = __float2half2_rn(c[2]),
+            height = __float2half2_rn(8.0), htheta0 = __float2half2_rn(c[3]), haniso = __float2half2_rn(c[4]),
+            hdelta = __float2half2_rn(c[5]), hone = __float2half2_rn(1.0), hepsilonb = __float2half2_rn(c[6]),
+            halpha = __float2half2_rn(c[7]), hpi = __float2half2_rn(c[8]), hgama = __float2half2_rn(c[9]),
+            hkappa = __float2half2_rn(c[10]), hzpf = __float2half2_rn(0.5), hteq = __float2half2_rn(c[11]),
+            hdtime = __float2half2_rn(c[12]), htau = __float2half2_rn(c[13]);
+    Timer t;
+    for (int i = 0; i < steps; ++i) {
+        if (i == 5 && !t.start()) return 1;
+        if (!launch(m, "kernel1_purelow", grids, blocks,
+                    {&phi, &phi_lap, &tempr, &tempr_lap, &phidx, &phidy, &epsilon, &epsilon_deri, &hdxdy, &htheta0,
+                     &haniso, &hone, &hdxm2, &hdym2, &hdelta, &hepsilonb, &height}) ||
+            !launch(m, "kernel2_purelow", grids, blocks,
+                    {&phi, &phi_lap, &epsilon, &epsilon_deri, &phidx, &phidy, &tempr, &tempr_lap, &hdym2, &hdxm2,
+                     &hgama, &hteq, &halpha, &hpi, &hone, &hzpf, &hdtime, &htau, &hkappa}) ||
+            !ck(cuCtxSynchronize(), "sync"))
+            return 1;
+    }
+    if (!t.stop(ms)) return 1;
+    return !(ck(cuMemcpyDtoH(phi_host, phi, hbytes), "copy") && ck(cuMemcpyDtoH(t_host, tempr, hbytes), "copy"));
 }
 
 }  // extern "C"

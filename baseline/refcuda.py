@@ -9,7 +9,9 @@ parameter file): graingrowth_pure / graingrowth_mix_m{1,2} are
 graingrowth/paras/para1.h (512 x 512, 16 x 16 tiles, Q = 2), snowflake_pure /
 snowflake_mix_m{1,2} snowflake/paras/para2.h (512 x 512, 16 x 16 tiles),
 sintering_pure / sintering_mix sintering/paras/para5.h (512 x 512, 16 x 16
-tiles, two particles; the initial state comes from the caller)."""
+tiles, two particles; the initial state comes from the caller);
+graingrowth_purelow / snowflake_purelow the shipped header state (HALF2,
+float constants) with para1 / para2."""
 import ctypes
 import os
 
@@ -45,6 +47,9 @@ def lib():
         L.refcuda_sint_pure.argtypes = [ctypes.c_void_p, ctypes.c_int, dp, dp, dp, fp]
         L.refcuda_sint_mix.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_int, dp, dp, dp,
                                        ctypes.c_void_p, fp]
+        up = ctypes.POINTER(ctypes.c_uint32)
+        L.refcuda_gg_purelow.argtypes = [ctypes.c_void_p, ctypes.c_int, up, up, fp]
+        L.refcuda_kob_purelow.argtypes = [ctypes.c_void_p, ctypes.c_int, up, up, fp]
         _lib = L
     return _lib
 
@@ -146,3 +151,27 @@ def sint_mix(steps, thr, monitor, c, e1, e2):
         m._ck(lib().refcuda_sint_mix(m.h, steps, thr, monitor, _p(c), _p(e1), _p(e2), types.ctypes.data,
                                      ctypes.byref(ms)), "refcuda_sint_mix")
         return c, e1, e2, types, float(ms.value)
+
+
+def _u(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))
+
+
+def gg_purelow(steps):
+    """graingrowth/purelow.cu (HALF2) for `steps` steps: (eta1, eta2 as
+    uint32 [ny][nx/2] half2 words, ms from step 5)."""
+    with Module("graingrowth_purelow") as m:
+        e1, e2 = np.zeros((m.ny, m.nx // 2), np.uint32), np.zeros((m.ny, m.nx // 2), np.uint32)
+        ms = ctypes.c_float(0)
+        m._ck(lib().refcuda_gg_purelow(m.h, steps, _u(e1), _u(e2), ctypes.byref(ms)), "refcuda_gg_purelow")
+        return e1, e2, float(ms.value)
+
+
+def kob_purelow(steps):
+    """snowflake/purelow.cu (HALF2) for `steps` steps: (phi, T as uint32
+    [ny][nx/2] half2 words, ms from step 5)."""
+    with Module("snowflake_purelow") as m:
+        phi, t = np.zeros((m.ny, m.nx // 2), np.uint32), np.zeros((m.ny, m.nx // 2), np.uint32)
+        ms = ctypes.c_float(0)
+        m._ck(lib().refcuda_kob_purelow(m.h, steps, _u(phi), _u(t), ctypes.byref(ms)), "refcuda_kob_purelow")
+        return phi, t, float(ms.value)

@@ -17,7 +17,7 @@
  * `stream` (cudaStream_t as void*, NULL = default stream); the calls return
  * an amps status.
  *
- * This is the compatibility path: one thread per cell, intermediates in
+ * This is the compatibility path: one thread per cell (or half2 pair), intermediates in
  * full-size arrays, several launches per step, as in the reference.  The
  * fast path for the same time loop is amps_run (include/amps.h).
  */
@@ -75,6 +75,36 @@ AMPS_API int amps_get_max_diff2(const amps_params *p, const double *test_data_la
  * else 1.  int arrays [nty][ntx]. */
 AMPS_API int amps_get_type(const amps_params *p, const double *max_diff_con, int *type_old, int *type_con,
                            void *stream);
+
+/* ---- binary16 kernels (HALF2) ---------------------------------------------
+ * Arrays of half2 pairs [ny][nx/2] (void *: each 32-bit element a half2 of
+ * columns 2x (low) and 2x+1 (high) of a row), as the reference's purelow
+ * programs keep them; periodic grids (p->bc = AMPS_BC_PERIODIC), even nx.
+ * The half2 constants the reference's drivers pass (__float2half2_rn of its
+ * compile-time constants) are formed from p. */
+
+/* graingrowth/function.h:280-308 -- one order parameter of the all-half2
+ * step: etaa_lap, dfdetaa, etaa_out from etaa and the other one, etab. */
+AMPS_API int amps_graingrowth_kernel1_lowpure(const amps_params *p, const void *etaa, const void *etab,
+                                              void *etaa_lap, void *dfdetaa, void *etaa_out, void *stream);
+/* graingrowth/tools.h:54-81 -- the initial circle (radius p->init_r about
+ * the centre) into two half2 arrays. */
+AMPS_API int amps_graingrowth_dataprepare_half2(const amps_params *p, void *eta1, void *eta2, void *stream);
+/* snowflake/function.h:607-659 -- phi_lap, tempr_lap, phidx, phidy, epsilon,
+ * epsilon_deri of the all-half2 step (atan2 per half in float, h2cos/h2sin). */
+AMPS_API int amps_snowflake_kernel1_purelow(const amps_params *p, const void *phi, void *phi_lap, const void *tempr,
+                                            void *tempr_lap, void *phidx, void *phidy, void *epsilon,
+                                            void *epsilon_deri, void *stream);
+/* snowflake/function.h:660-700 -- advances phi and tempr in place. */
+AMPS_API int amps_snowflake_kernel2_purelow(const amps_params *p, void *phi, const void *phi_lap, const void *epsilon,
+                                            const void *epsilon_deri, const void *phidx, const void *phidy,
+                                            void *tempr, const void *tempr_lap, void *stream);
+/* snowflake/tools.h:43-58 -- the seed disc into a half2 phi: 1 where r^2 <
+ * p->init_r2 about the centre + p->init_offset, 0 elsewhere. */
+AMPS_API int amps_snowflake_dataprepare_half2(const amps_params *p, void *phi, void *stream);
+/* graingrowth/tools.h:133-155, snowflake/tools.h:108-130 -- half2 pairs to
+ * a float array [ny][nx]. */
+AMPS_API int amps_purelow2high_aftercomputing(const amps_params *p, const void *hdata, float *fdata, void *stream);
 
 #ifdef __cplusplus
 }

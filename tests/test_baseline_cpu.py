@@ -15,5 +15,6 @@ def test_host_driver_builds_and_exports_its_entry_points():
     out = subprocess.run(["nm", "-D", "--defined-only", LIB], check=True, capture_output=True, text=True).stdout
     names = {line.split()[-1] for line in out.splitlines() if line.strip()}
     for name in ("refcuda_error", "refcuda_open", "refcuda_close", "refcuda_dims", "refcuda_gg_pure",
-                 "refcuda_gg_mix", "refcuda_kob_pure", "refcuda_kob_mix", "refcuda_sint_pure", "refcuda_sint_mix"):
+                 "refcuda_gg_mix", "refcuda_kob_pure", "refcuda_kob_mix", "refcuda_sint_pure", "refcuda_sint_mix",
+                 "refcuda_gg_purelow", "refcuda_kob_purelow"):
         assert name in names, name
