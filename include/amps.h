@@ -385,11 +385,13 @@ AMPS_API int amps_adjoint_backward(amps_adjoint *a, const void *grad_final, void
 
 /* ---- ensembles of grain-growth runs --------------------------------------
  * No counterpart in the reference (one run per process there).  Advances
- * `count` grain-growth handles in lockstep: each step is one persistent
- * launch whose CTAs take (member, tile) work items from a queue ordered by
- * cost, so members of different sizes, field counts, parameters and tier
- * maps share the GPU; the members' period-end classifications are one
- * batched launch, and each cadence period is replayed from a CUDA graph.
+ * `count` grain-growth handles in lockstep.  Members are grouped by the
+ * occupancy their field count allows (at most 40 a group); a step is one
+ * launch per group, one CTA per (member, tile), the group's step arguments
+ * passed by value, so members of different sizes, field counts, parameters
+ * and tier maps share the GPU.  Each cadence period is replayed from a CUDA
+ * graph whose groups run as parallel branches; the members' period-end
+ * classifications are one batched launch.
  * Every member keeps its own parameters (dt, mobil, grcoef, gamma,
  * thresholds...), tier maps, statistics and step counter, and gives the same
  * results as amps_run on it alone.  Members must share tile, cadence, mode

@@ -372,8 +372,8 @@ class Simulation:
 
 
 class Ensemble:
-    """Grain-growth `Simulation`s advanced in lockstep by one persistent
-    kernel per step (amps_ensemble_*).  The members stay usable for reads
+    """Grain-growth `Simulation`s advanced in lockstep, one launch per group
+    of members a step (amps_ensemble_*).  The members stay usable for reads
     (fields, tiers, stats) and must outlive the ensemble."""
 
     def __init__(self, members, graphs=True):

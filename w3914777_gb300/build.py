@@ -22,7 +22,7 @@ OBJ = os.path.join(OUT, "obj-" + platform.machine())
 _ELF_MACHINE = {"x86_64": 62, "aarch64": 183}
 
 SOURCES = ["amps_api.cu", "amps_host.cpp", "k_common.cu", "k_graingrowth.cu", "k_gg_half.cu", "k_gg_ragged.cu",
-           "k_kobayashi.cu",
+           "k_gg_ensemble.cu", "k_kobayashi.cu",
            "k_sintering.cu", "k_sint_ref.cu", "k_noalloc.cu", "k_adjoint.cu", "k_diag.cu", "compat.cu",
            "compat_half.cu"]
 # per-file flags: the reference-named kernels keep the reference's rounding (no fused multiply-add)

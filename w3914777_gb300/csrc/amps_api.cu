@@ -17,6 +17,7 @@
 
 #include <algorithm>
 #include <map>
+#include <memory>
 #include <new>
 #include <string>
 #include <vector>
@@ -1245,20 +1246,22 @@ struct amps_ensemble {
     int T = 0, cad = 0, maxnf = 0;
     bool ref = false, mixed = false;
     cudaStream_t stream = nullptr, capture = nullptr;
-    int2 *d_items = nullptr;
-    int nitems = 0, grid = 0;
-    size_t smem = 0;
-    int *d_queue = nullptr;
+    // members launched together: same occupancy class, at most kEnsCap
+    struct Group {
+        std::vector<int> members;  // indices into m
+        std::vector<int> first;    // first work item (CTA) of each member, + the total
+        size_t smem = 0;
+        cudaStream_t s = nullptr;  // its branch of a period graph
+        cudaEvent_t done = nullptr;
+    };
+    std::vector<Group> groups;
+    cudaEvent_t fork = nullptr;
     ClassifyArgs *d_cls = nullptr;      // whole periods: advance = stat_steps = cadence
     ClassifyArgs *d_cls_tmp = nullptr;  // partial periods (eager)
-    StepArgs *d_tmp = nullptr;          // partial periods (eager): cadence x members
     CUtensorMap *d_tmaps = nullptr;     // members' FP32 tensor maps [member][parity] (bulk staging)
     bool graphs = true;
-    struct Period {
-        StepArgs *table = nullptr;
-        cudaGraphExec_t exec = nullptr;
-    };
-    std::map<std::vector<uint8_t>, Period> periods;
+    std::map<std::vector<uint8_t>, cudaGraphExec_t> periods;
+    std::unique_ptr<EnsLaunch> launch;  // host staging of one launch's parameters
     std::string err;
 };
 
@@ -1277,16 +1280,17 @@ struct amps_ensemble {
 
 static void ens_free(amps_ensemble *e)
 {
-    for (auto &kv : e->periods) {
-        if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
-        if (kv.second.table) cudaFree(kv.second.table);
-    }
+    for (auto &kv : e->periods)
+        if (kv.second) cudaGraphExecDestroy(kv.second);
     e->periods.clear();
-    cudaFree(e->d_items);
-    cudaFree(e->d_queue);
+    for (auto &g : e->groups) {
+        if (g.s) cudaStreamDestroy(g.s);
+        if (g.done) cudaEventDestroy(g.done);
+    }
+    e->groups.clear();
+    if (e->fork) cudaEventDestroy(e->fork);
     cudaFree(e->d_cls);
     cudaFree(e->d_cls_tmp);
-    cudaFree(e->d_tmp);
     cudaFree(e->d_tmaps);
     if (e->capture) cudaStreamDestroy(e->capture);
 }
@@ -1314,41 +1318,58 @@ extern "C" int amps_ensemble_create(amps_handle *const *members, int count, amps
     }
     amps_ensemble *e = new (std::nothrow) amps_ensemble;
     if (!e) return AMPS_ERR_ALLOC;
+    e->launch.reset(new (std::nothrow) EnsLaunch);
+    if (!e->launch) {
+        delete e;
+        return AMPS_ERR_ALLOC;
+    }
     e->m.assign(members, members + count);
     e->T = h0->T;
     e->cad = h0->p.cadence;
     e->mixed = h0->mixed;
     e->ref = h0->p.ref_order != 0;
-    // work items: members with more fields first (costliest tiles first)
+    for (int i = 0; i < count; ++i) e->maxnf = std::max(e->maxnf, members[i]->nf);
+    // groups: members with more fields first; a group closes where the
+    // occupancy its largest member's staging allows would change, or at kEnsCap
     std::vector<int> order(count);
     for (int i = 0; i < count; ++i) order[i] = i;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return members[a]->nf > members[b]->nf; });
-    std::vector<int2> items;
-    for (int i : order) {
-        e->maxnf = std::max(e->maxnf, members[i]->nf);
-        for (int t = 0; t < members[i]->ntiles; ++t) items.push_back(make_int2(i, t));
-    }
-    e->nitems = (int)items.size();
     std::vector<ClassifyArgs> cls(count);
     for (int i = 0; i < count; ++i) cls[i] = classify_args(members[i], e->cad, e->cad);
-    int bps = 0, sms = 0, dev = 0;
-    e->smem = gg_ens_smem_bytes(e->T, e->maxnf);
-    cudaError_t ce = gg_prepare_ens(e->T, e->ref, e->maxnf, &bps);
-    if (ce == cudaSuccess) ce = cudaGetDevice(&dev);
-    if (ce == cudaSuccess) ce = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (ce == cudaSuccess && bps < 1) ce = cudaErrorInvalidConfiguration;
-    e->grid = std::max(1, std::min(e->nitems, bps * sms));
-    if (ce == cudaSuccess) ce = cudaMalloc(&e->d_items, sizeof(int2) * items.size());
-    if (ce == cudaSuccess) ce = cudaMalloc(&e->d_queue, 2 * sizeof(int));
+    cudaError_t ce = gg_prepare_ens(e->T, e->ref, gg_ens_smem_bytes(e->T, e->maxnf));
+    std::map<int, int> occ;  // field count -> CTAs an SM
+    for (int i = 0; ce == cudaSuccess && i < count; ++i) {
+        const int nf = members[order[i]]->nf;
+        if (!occ.count(nf)) {
+            int bps = 0;
+            ce = gg_ens_occupancy(e->T, e->ref, gg_ens_smem_bytes(e->T, nf), &bps);
+            if (ce == cudaSuccess && bps < 1) ce = cudaErrorInvalidConfiguration;
+            occ[nf] = bps;
+        }
+    }
+    for (int i = 0; ce == cudaSuccess && i < count; ++i) {
+        amps_handle *h = members[order[i]];
+        if (e->groups.empty() || (int)e->groups.back().members.size() == kEnsCap ||
+            occ[e->m[e->groups.back().members[0]]->nf] != occ[h->nf]) {
+            e->groups.emplace_back();
+            e->groups.back().smem = gg_ens_smem_bytes(e->T, h->nf);
+            e->groups.back().first.push_back(0);
+        }
+        auto &g = e->groups.back();
+        g.members.push_back(order[i]);
+        g.first.push_back(g.first.back() + h->ntiles);
+    }
+    for (auto &g : e->groups) {
+        if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&g.s, cudaStreamNonBlocking);
+        if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&g.done, cudaEventDisableTiming);
+    }
+    if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming);
     if (ce == cudaSuccess) ce = cudaMalloc(&e->d_cls, sizeof(ClassifyArgs) * count);
     if (ce == cudaSuccess) ce = cudaMalloc(&e->d_cls_tmp, sizeof(ClassifyArgs) * count);
-    if (ce == cudaSuccess) ce = cudaMalloc(&e->d_tmp, sizeof(StepArgs) * (size_t)count * e->cad);
-    if (ce == cudaSuccess) ce = cudaMemcpy(e->d_items, items.data(), sizeof(int2) * items.size(), cudaMemcpyHostToDevice);
-    if (ce == cudaSuccess) ce = cudaMemset(e->d_queue, 0, 2 * sizeof(int));
     if (ce == cudaSuccess) ce = cudaMemcpy(e->d_cls, cls.data(), sizeof(ClassifyArgs) * count, cudaMemcpyHostToDevice);
     if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&e->capture, cudaStreamNonBlocking);
     if (ce == cudaSuccess && e->T == 32) {
-        // the members' tensor maps, in global memory where the tile-queue kernel reads them
+        // the members' tensor maps, in global memory where the ensemble kernel reads them
         std::vector<CUtensorMap> maps((size_t)2 * count);
         memset(maps.data(), 0, sizeof(CUtensorMap) * maps.size());
         for (int i = 0; i < count; ++i)
@@ -1399,7 +1420,7 @@ extern "C" const char *amps_ensemble_last_error(const amps_ensemble *e)
     return e ? e->err.c_str() : g_create_err.c_str();
 }
 
-// Step tables of steps [k0, k0+cnt) of a period for every member, from the
+// Step arguments of steps [k0, k0+cnt) of a period for every member, from the
 // members' current host-side parity/transition (table[s * M + i]).
 static std::vector<StepArgs> ens_tables(const amps_ensemble *e, int k0, int cnt)
 {
@@ -1421,14 +1442,41 @@ static std::vector<StepArgs> ens_tables(const amps_ensemble *e, int k0, int cnt)
     return t;
 }
 
-static int ens_enqueue(amps_ensemble *e, const StepArgs *table, const ClassifyArgs *cls, int cnt, bool period_end,
-                       cudaStream_t s)
+// Step k of group g (its members' arguments by value in the launch).
+static int ens_launch(amps_ensemble *e, const amps_ensemble::Group &g, const std::vector<StepArgs> &tab, int k,
+                      bool mon, cudaStream_t s)
 {
     const int M = (int)e->m.size();
-    for (int k = 0; k < cnt; ++k) {
-        const bool mon = e->mixed && period_end && k == cnt - 1;  // as in ens_tables
-        ECK(e, gg_launch_ens(e->T, e->ref, mon, table + (size_t)k * M, e->d_items, e->nitems, e->d_queue, e->grid,
-                             e->smem, s));
+    EnsLaunch &L = *e->launch;
+    L.count = (int)g.members.size();
+    for (int j = 0; j < L.count; ++j) {
+        L.first[j] = g.first[j];
+        L.m[j] = tab[(size_t)k * M + g.members[j]];
+    }
+    L.first[L.count] = g.first[L.count];
+    ECK(e, gg_launch_ens(e->T, e->ref, mon, L, g.smem, s));
+    return AMPS_OK;
+}
+
+// cnt steps of every group, then the period-end classification (or the tier
+// maps' advance).  branches: each group's steps on its own stream, forked
+// from and joined back into s (a period graph's parallel branches).
+static int ens_enqueue(amps_ensemble *e, const std::vector<StepArgs> &tab, const ClassifyArgs *cls, int cnt,
+                       bool period_end, cudaStream_t s, bool branches)
+{
+    const int M = (int)e->m.size();
+    if (branches) ECK(e, cudaEventRecord(e->fork, s));
+    for (auto &g : e->groups) {
+        cudaStream_t gs = branches ? g.s : s;
+        if (branches) ECK(e, cudaStreamWaitEvent(gs, e->fork, 0));
+        for (int k = 0; k < cnt; ++k) {
+            const bool mon = e->mixed && period_end && k == cnt - 1;  // as in ens_tables
+            if (int r = ens_launch(e, g, tab, k, mon, gs)) return r;
+        }
+        if (branches) {
+            ECK(e, cudaEventRecord(g.done, gs));
+            ECK(e, cudaStreamWaitEvent(s, g.done, 0));
+        }
     }
     if (e->mixed && period_end) ECK(e, classify_batch(cls, M, s));
     else ECK(e, advance_batch(cls, M, s));
@@ -1463,34 +1511,35 @@ extern "C" int amps_ensemble_run(amps_ensemble *e, int nsteps)
             for (int i = 0; i < M; ++i) key[i] = (uint8_t)(e->m[i]->parity | (e->m[i]->transition ? 2 : 0));
             auto it = e->periods.find(key);
             if (it == e->periods.end()) {
-                amps_ensemble::Period per;
-                std::vector<StepArgs> tab = ens_tables(e, 0, cnt);
-                ECK(e, cudaMalloc(&per.table, sizeof(StepArgs) * tab.size()));
-                it = e->periods.emplace(key, per).first;
-                ECK(e, cudaMemcpy(it->second.table, tab.data(), sizeof(StepArgs) * tab.size(), cudaMemcpyHostToDevice));
+                const std::vector<StepArgs> tab = ens_tables(e, 0, cnt);
+                it = e->periods.emplace(key, nullptr).first;
                 cudaGraph_t gr = nullptr;
                 ECK(e, cudaStreamBeginCapture(e->capture, cudaStreamCaptureModeThreadLocal));
-                const int r = ens_enqueue(e, it->second.table, e->d_cls, cnt, true, e->capture);
+                const int r = ens_enqueue(e, tab, e->d_cls, cnt, true, e->capture, true);
                 const cudaError_t ce = cudaStreamEndCapture(e->capture, &gr);
-                if (r) return r;
+                if (r) {
+                    if (gr) cudaGraphDestroy(gr);
+                    return r;
+                }
                 if (ce != cudaSuccess) EFAIL(e, AMPS_ERR_CUDA, "ensemble graph capture: %s", cudaGetErrorString(ce));
-                const cudaError_t ci = cudaGraphInstantiate(&it->second.exec, gr, 0);
+                const cudaError_t ci = cudaGraphInstantiate(&it->second, gr, 0);
                 cudaGraphDestroy(gr);
                 if (ci != cudaSuccess) {
-                    it->second.exec = nullptr;
+                    it->second = nullptr;
+                    e->periods.erase(it);
                     EFAIL(e, AMPS_ERR_CUDA, "ensemble graph instantiate: %s", cudaGetErrorString(ci));
                 }
             }
-            ECK(e, cudaGraphLaunch(it->second.exec, e->stream));
+            ECK(e, cudaGraphLaunch(it->second, e->stream));
         } else {
-            // partial period: upload this chunk's tables into the scratch slots once they are free
-            std::vector<StepArgs> tab = ens_tables(e, k0, cnt);
+            // partial period, eager: the step arguments travel in the launches;
+            // the classification's arguments go to their scratch slots once free
+            const std::vector<StepArgs> tab = ens_tables(e, k0, cnt);
             std::vector<ClassifyArgs> cls(M);
             for (int i = 0; i < M; ++i) cls[i] = classify_args(e->m[i], period_end ? e->cad : 0, cnt);
             ECK(e, cudaStreamSynchronize(e->stream));
-            ECK(e, cudaMemcpy(e->d_tmp, tab.data(), sizeof(StepArgs) * tab.size(), cudaMemcpyHostToDevice));
             ECK(e, cudaMemcpy(e->d_cls_tmp, cls.data(), sizeof(ClassifyArgs) * M, cudaMemcpyHostToDevice));
-            if (int r = ens_enqueue(e, e->d_tmp, e->d_cls_tmp, cnt, period_end, e->stream)) return r;
+            if (int r = ens_enqueue(e, tab, e->d_cls_tmp, cnt, period_end, e->stream, false)) return r;
         }
         ens_advance_host(e, cnt, period_end);
         nsteps -= cnt;

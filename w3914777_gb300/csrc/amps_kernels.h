@@ -53,14 +53,21 @@ constexpr int kTmaMaxFields = 16;
 size_t gg_tma_smem_bytes(int nf);
 cudaError_t gg_prepare_tma(bool ref, int nf, int *blocks_per_sm);
 cudaError_t gg_launch_tma(bool ref, const CUtensorMap &tm, const StepArgs &a, int grid, cudaStream_t s);
-// Ensemble step: a persistent kernel over the (member, tile) work items
-// items[nitems] (.x member, .y tile), member m's arguments table[m]; work is
-// taken from the counter queue[0] (queue[1] counts finished CTAs; the last
-// CTA resets both to 0 for the next launch).
+// Ensemble step: one launch per group of members, one CTA per (member, tile)
+// work item; the group's step arguments travel by value in the kernel's
+// parameter space (up to kEnsCap members), read through the constant cache.
+constexpr int kEnsCap = 40;
+struct EnsLaunch {
+    int count;               // members in this launch
+    int first[kEnsCap + 1];  // first CTA of each member; first[count] = the grid
+    StepArgs m[kEnsCap];
+};
+static_assert(sizeof(EnsLaunch) <= 32764, "kernel parameter space");
 size_t gg_ens_smem_bytes(int tile, int max_nf);
-cudaError_t gg_prepare_ens(int tile, bool ref, int max_nf, int *blocks_per_sm);
-cudaError_t gg_launch_ens(int tile, bool ref, bool monitor, const StepArgs *table, const int2 *items, int nitems,
-                          int *queue, int grid, size_t smem, cudaStream_t s);
+// sets the kernels' dynamic shared-memory limit to max_smem
+cudaError_t gg_prepare_ens(int tile, bool ref, size_t max_smem);
+cudaError_t gg_ens_occupancy(int tile, bool ref, size_t smem, int *blocks_per_sm);
+cudaError_t gg_launch_ens(int tile, bool ref, bool monitor, const EnsLaunch &L, size_t smem, cudaStream_t s);
 size_t kob_smem_bytes(int tile, int tier);
 size_t sint_smem_bytes(int tile, int tier, int nf, bool mu64);
 

@@ -416,94 +416,4 @@ cudaError_t gg_prepare_tma(bool ref, int nf, int *blocks_per_sm)
                : cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, gg_step_tma_kernel<false>, kThreads, smem);
 }
 
-// Ensemble step: persistent CTAs take (member, tile) work items from a
-// global counter; items are ordered by cost (most fields first), so the
-// dynamic queue approximates longest-first scheduling across members of
-// different sizes and field counts.  A tile is gg_tile_step, the fused
-// kernel's per-tile code (same results); the member's arguments are
-// copied into shared memory when the member changes.  No waits: the counter
-// only hands out indices, and the last CTA to finish resets it.
-template <int T, bool REF, bool MON>
-__global__ void __launch_bounds__(kThreads, 2)
-    gg_ens_kernel(const StepArgs *__restrict__ table, const int2 *__restrict__ items, int nitems, int *queue)
-{
-    extern __shared__ __align__(128) unsigned char smraw[];
-    __shared__ double red[kThreads / 32];
-    __shared__ uint8_t ntier[9];
-    __shared__ __align__(16) StepArgs sa;
-    __shared__ int sw;
-    __shared__ __align__(8) uint64_t bar;
-    // 128-byte aligned staging (gg_smem_bytes adds the slack) for the members' tensor copies
-    float *sm = reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(smraw) + 127) & ~uintptr_t(127));
-    static_assert(sizeof(StepArgs) % 4 == 0, "StepArgs copied as 32-bit words");
-    int member = -1;
-    for (;;) {
-        if (threadIdx.x == 0) sw = atomicAdd(&queue[0], 1);
-        __syncthreads();
-        const int w = sw;
-        if (w >= nitems) break;
-        const int2 it = items[w];
-        if (it.x != member) {
-            const int *src = reinterpret_cast<const int *>(table + it.x);
-            int *dst = reinterpret_cast<int *>(&sa);
-            for (int k = threadIdx.x; k < (int)(sizeof(StepArgs) / 4); k += kThreads) dst[k] = src[k];
-            member = it.x;
-        }
-        __syncthreads();
-        gg_tile_step_call<T, REF, MON>(sa, sm, ntier, red, it.y, &bar);
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-        __threadfence();
-        if (atomicAdd(&queue[1], 1) == (int)gridDim.x - 1) {
-            queue[0] = 0;
-            queue[1] = 0;
-            __threadfence();
-        }
-    }
-}
-
-// staging for the member with the most fields
-size_t gg_ens_smem_bytes(int tile, int max_nf) { return gg_smem_bytes(tile, -1, max_nf); }
-
-cudaError_t gg_prepare_ens(int tile, bool ref, int max_nf, int *blocks_per_sm)
-{
-    const size_t smem = gg_ens_smem_bytes(tile, max_nf);
-    const auto attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
-    cudaError_t e = cudaSuccess;
-#define AMPS_GGE(TT, RR)                                                                                   \
-    do {                                                                                                   \
-        e = cudaFuncSetAttribute(gg_ens_kernel<TT, RR, false>, attr, (int)smem);                           \
-        if (e == cudaSuccess) e = cudaFuncSetAttribute(gg_ens_kernel<TT, RR, true>, attr, (int)smem);      \
-        if (e != cudaSuccess) return e;                                                                    \
-        return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, gg_ens_kernel<TT, RR, false>, kThreads, smem); \
-    } while (0)
-    if (tile == 32) {
-        if (ref) AMPS_GGE(32, true);
-        AMPS_GGE(32, false);
-    }
-    if (ref) AMPS_GGE(16, true);
-    AMPS_GGE(16, false);
-#undef AMPS_GGE
-}
-
-cudaError_t gg_launch_ens(int tile, bool ref, bool monitor, const StepArgs *table, const int2 *items, int nitems,
-                          int *queue, int grid, size_t smem, cudaStream_t s)
-{
-#define AMPS_GGEL(TT, RR)                                                                                      \
-    do {                                                                                                       \
-        if (monitor) gg_ens_kernel<TT, RR, true><<<grid, kThreads, smem, s>>>(table, items, nitems, queue);    \
-        else gg_ens_kernel<TT, RR, false><<<grid, kThreads, smem, s>>>(table, items, nitems, queue);           \
-    } while (0)
-    if (tile == 32) {
-        if (ref) AMPS_GGEL(32, true);
-        else AMPS_GGEL(32, false);
-    } else {
-        if (ref) AMPS_GGEL(16, true);
-        else AMPS_GGEL(16, false);
-    }
-#undef AMPS_GGEL
-    return cudaGetLastError();
-}
-
 }  // namespace amps

@@ -1,6 +1,7 @@
 """The grain-growth ensemble workload: many independent Fan-Chen runs of
 different sizes, field counts and coefficients advanced together by
-`amps.Ensemble` (one persistent kernel launch per step for all of them).
+`amps.Ensemble` (one launch per group of members a step, the groups as
+parallel branches of each period's CUDA graph).
 
 No reference counterpart: the reference runs one grid per process
 (graingrowth/end2end_mix.cu).  Each member is the 1024^2 Q=8 Fan-Chen
