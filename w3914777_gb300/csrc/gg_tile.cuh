@@ -605,15 +605,6 @@ __device__ __forceinline__ void gg_tile_step(const StepArgs &a, float *sm, uint8
     else gg_tile_lo_impl<T, TIER_HALF, MON>(a, sm, tile, tx, ty, red);
 }
 
-// gg_tile_step out of line, for callers whose StepArgs live in shared
-// memory (inlined, their loads are hoisted and spill).
-template <int T, bool REF, bool MON>
-__device__ __noinline__ void gg_tile_step_call(const StepArgs &a, float *sm, uint8_t *ntier, double *red, int tile,
-                                               uint64_t *bar)
-{
-    gg_tile_step<T, REF, MON ? -1 : 0, 0, true, true>(a, sm, ntier, red, tile, a.tmap, bar);
-}
-
 // Fused all-tier step: at most 64 registers, so that four CTAs share an SM.
 // The monitor steps (one in `cadence`) are separate instantiations, one per
 // monitor kind MK, so the other steps' kernel carries no monitor code and
