@@ -106,6 +106,49 @@ AMPS_API int amps_snowflake_dataprepare_half2(const amps_params *p, void *phi, v
  * a float array [ny][nx]. */
 AMPS_API int amps_purelow2high_aftercomputing(const amps_params *p, const void *hdata, float *fdata, void *stream);
 
+/* ---- the adaptive grain-growth step (AMSTENCIL) ----------------------------
+ * Dual storage as the reference's end2end_mix program keeps it: FP64 arrays
+ * [ny][nx] and half2 arrays [ny][nx/2] of every field, and the tile types
+ * type_curr [ny/tile][nx/tile] (1: half2, 2: FP64).  Square tiles of
+ * p->tile (even, at most 32, dividing both sides); periodic grids, even nx.
+ * The monitor step cadence is p->cadence (the reference's 10). */
+
+/* graingrowth/function.h:33-277 -- one order parameter of the adaptive step:
+ * a type-2 tile computes etaa_lap, dfdetaa, etaa_out in FP64 from the FP64
+ * arrays; a type-1 tile computes hetaa_lap, hdfdetaa, hetaa_out in half2,
+ * taking cells of type-2 neighbour tiles from etaa, and converts its edge
+ * cells (all its cells when (i + 1) % cadence == 0) into etaa_out.  With
+ * p->monitor == AMPS_MONITOR_TEM (the reference's Monitor2 build), step i
+ * with i % cadence == 0 and etai == 2 first copies etaa into etaa_last: every
+ * cell of a type-2 tile, the left half of a type-1 tile, as the reference's
+ * kernel does. */
+AMPS_API int amps_graingrowth_kernel1_mix(const amps_params *p, const double *etaa, double *etaa_last,
+                                          const double *etab, double *etaa_lap, double *dfdetaa, double *etaa_out,
+                                          const void *hetaa, const void *hetab, void *hetaa_lap, void *hdfdetaa,
+                                          void *hetaa_out, const int *type_curr, int i, int etai, void *stream);
+/* graingrowth/tools.h:24-38 -- the initial circle (radius p->init_r about
+ * the centre) into two FP64 arrays. */
+AMPS_API int amps_graingrowth_dataprepare_high(const amps_params *p, double *eta1, double *eta2, void *stream);
+/* graingrowth/tools.h:256-271 -- tiles whose type went 2 -> 1 (old_con ->
+ * new_con) take their half2 pairs of both fields from the FP64 arrays. */
+AMPS_API int amps_graingrowth_data_sychro_duringcomputation(const amps_params *p, const double *eta1,
+                                                            const double *eta2, void *heta1, void *heta2,
+                                                            const int *old_con, const int *new_con, void *stream);
+/* graingrowth/tools.h:172-200 -- type-1 tiles' half2 pairs into the FP64 array. */
+AMPS_API int amps_graingrowth_data_sychro_aftercomputation(const amps_params *p, double *highdata,
+                                                           const void *lowdata, const int *typedata, void *stream);
+/* graingrowth/tools.h:158-171 -- every half2 pair from the FP64 array. */
+AMPS_API int amps_graingrowth_highdata_to_low(const amps_params *p, const double *highdata, void *lowdata,
+                                              void *stream);
+/* graingrowth/function.h:323-341 -- kernel1_mix's conversion of type-1
+ * tiles' cells into etaa_out as its own launch (the reference's
+ * monitor_conversion_independent build). */
+AMPS_API int amps_graingrowth_kernel1_conversion(const amps_params *p, double *etaa_out, const void *hetaa_out,
+                                                 const int *type_curr, int i, void *stream);
+/* graingrowth/function.h:311-321 -- every cell of etaa into etaa_last. */
+AMPS_API int amps_graingrowth_monitor2_lastdata_store(const amps_params *p, const double *etaa, double *etaa_last,
+                                                      void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -110,3 +110,118 @@ def test_half2_wrappers_reject_what_the_reference_cannot_run():
     assert L.amps_graingrowth_kernel1_lowpure(ctypes.byref(bad), *[ptr(t) for t in z], None) != 0
     odd = w().Params.preset("graingrowth", 1, nx=511)
     assert L.amps_graingrowth_kernel1_lowpure(ctypes.byref(odd), *[ptr(t) for t in z], None) != 0
+
+
+def mix_lib():
+    L = lib()
+    dp = ctypes.POINTER(w().Params)
+    I = ctypes.c_int
+    sig = {
+        "amps_graingrowth_kernel1_mix": [P] * 11 + [P, I, I],
+        "amps_graingrowth_dataprepare_high": [P, P],
+        "amps_graingrowth_data_sychro_duringcomputation": [P] * 6,
+        "amps_graingrowth_data_sychro_aftercomputation": [P] * 3,
+        "amps_graingrowth_highdata_to_low": [P, P],
+        "amps_graingrowth_kernel1_conversion": [P, P, P, I],
+        "amps_graingrowth_monitor2_lastdata_store": [P, P],
+        "amps_get_max_diff1": [P, P],
+        "amps_get_max_diff2": [P, P, P],
+        "amps_get_type": [P, P, P],
+    }
+    for name, args in sig.items():
+        f = getattr(L, name)
+        f.argtypes = [dp] + args + [P]
+        f.restype = ctypes.c_int
+    return L
+
+
+@pytest.mark.parametrize("monitor,thr,steps", [(1, 0.5, 200), (2, 1e-4, 200), (2, 1e-2, 120), (1, 0.1, 120)])
+def test_graingrowth_mixed_loop_equals_the_reference_kernels(monitor, thr, steps):
+    """graingrowth/end2end_mix.cu's loop (AMSTENCIL, Monitor1/2) through the
+    reference-named wrappers: the initial circle, per period get_max_diff /
+    get_type / data_sychro_duringcomputation, two kernel1_mix a step, the
+    final data_sychro_aftercomputation -- against the reference's own
+    kernels driven the same way: the tile types of every period and the
+    final fields, bit for bit."""
+    need(f"graingrowth_mix_m{monitor}")
+    L = mix_lib()
+    p = w().Params.preset("graingrowth", 1, mode="end2end_mix", monitor=monitor, thr_lo=thr, thr_hi=thr)
+    with refcuda.Module(f"graingrowth_mix_m{monitor}") as m:
+        assert (m.nx, m.ny, m.ux, m.uy) == (p.nx, p.ny, p.tile, p.tile)
+    pp = ctypes.byref(p)
+    nx, ny, T = p.nx, p.ny, p.tile
+    tiles = (nx // T) * (ny // T)
+    f64 = lambda: torch.zeros((ny, nx), dtype=torch.float64, device="cuda")
+    e1, e2, o1, o2, l1, l2, d1, d2, last = (f64() for _ in range(9))
+    h1, h2, ho1, ho2, hl1, hl2, hd1, hd2 = half2s(p, 8)
+    tcur = torch.zeros(tiles, dtype=torch.int32, device="cuda")
+    told = torch.zeros(tiles, dtype=torch.int32, device="cuda")
+    md = torch.zeros(tiles, dtype=torch.float64, device="cuda")
+    assert L.amps_graingrowth_dataprepare_high(pp, ptr(e1), ptr(e2), None) == 0
+    assert L.amps_graingrowth_dataprepare_half2(pp, ptr(h1), ptr(h2), None) == 0
+    if monitor == 2:  # end2end_mix.cu:43-47
+        last.copy_((e2 == 0).double())
+    types = []
+    for i in range(steps):
+        if i % 10 == 0:
+            if monitor == 1:
+                assert L.amps_get_max_diff1(pp, ptr(e2), ptr(md), None) == 0
+            else:
+                assert L.amps_get_max_diff2(pp, ptr(last), ptr(e2), ptr(md), None) == 0
+            assert L.amps_get_type(pp, ptr(md), ptr(told), ptr(tcur), None) == 0
+            assert L.amps_graingrowth_data_sychro_duringcomputation(pp, ptr(e1), ptr(e2), ptr(h1), ptr(h2),
+                                                                    ptr(told), ptr(tcur), None) == 0
+            types.append(tcur.cpu().numpy().astype(np.uint8))
+        assert L.amps_graingrowth_kernel1_mix(pp, ptr(e1), ptr(last), ptr(e2), ptr(l1), ptr(d1), ptr(o1), ptr(h1),
+                                              ptr(h2), ptr(hl1), ptr(hd1), ptr(ho1), ptr(tcur), i, 1, None) == 0
+        assert L.amps_graingrowth_kernel1_mix(pp, ptr(e2), ptr(last), ptr(e1), ptr(l2), ptr(d2), ptr(o2), ptr(h2),
+                                              ptr(h1), ptr(hl2), ptr(hd2), ptr(ho2), ptr(tcur), i, 2, None) == 0
+        e1, o1, e2, o2 = o1, e1, o2, e2
+        h1, ho1, h2, ho2 = ho1, h1, ho2, h2
+    assert L.amps_graingrowth_data_sychro_aftercomputation(pp, ptr(e1), ptr(h1), ptr(tcur), None) == 0
+    assert L.amps_graingrowth_data_sychro_aftercomputation(pp, ptr(e2), ptr(h2), ptr(tcur), None) == 0
+    torch.cuda.synchronize()
+    r1, r2, rtypes, _ = refcuda.gg_mix(steps, thr, monitor)
+    ours = np.stack(types)
+    both = ours.ravel()
+    mix = np.bincount(both, minlength=3)[1:] / both.size
+    bad = [k for k in range(rtypes.shape[0]) if not np.array_equal(ours[k], rtypes[k])]
+    f1, f2 = e1.cpu().numpy(), e2.cpu().numpy()
+    d = max(float(np.abs(f1 - r1).max()), float(np.abs(f2 - r2).max()))
+    print(f"grain growth mixed loop, monitor {monitor} {thr:g}, {steps} steps: tile types half/FP64 {mix}, "
+          f"periods differing {bad[:5]}, fields max |diff| {d:.3e}")
+    assert not bad
+    assert np.array_equal(f1, r1) and np.array_equal(f2, r2)
+
+
+def test_graingrowth_mix_tools():
+    """highdata_to_low, kernel1_conversion and monitor2_lastdata_store
+    against numpy statements of graingrowth/tools.h:158-171 and
+    function.h:311-341 on random data and types."""
+    L = mix_lib()
+    p = w().Params.preset("graingrowth", 1, mode="end2end_mix")
+    pp = ctypes.byref(p)
+    nx, ny, T = p.nx, p.ny, p.tile
+    rng = np.random.default_rng(3)
+    hi = rng.uniform(-1, 1, (ny, nx))
+    dh = torch.tensor(hi, device="cuda")
+    lo, = half2s(p, 1)
+    assert L.amps_graingrowth_highdata_to_low(pp, ptr(dh), ptr(lo), None) == 0
+    want = hi.astype(np.float32).astype(np.float16)
+    assert np.array_equal(lo.cpu().numpy().view(np.float16), want)
+    last = torch.zeros_like(dh)
+    assert L.amps_graingrowth_monitor2_lastdata_store(pp, ptr(dh), ptr(last), None) == 0
+    assert np.array_equal(last.cpu().numpy(), hi)
+    ty = rng.integers(1, 3, (ny // T, nx // T)).astype(np.int32)
+    dty = torch.tensor(ty, device="cuda")
+    for step in (3, 9):
+        out = torch.full_like(dh, 7.0)
+        assert L.amps_graingrowth_kernel1_conversion(pp, ptr(out), ptr(lo), ptr(dty), step, None) == 0
+        exp = np.full((ny, nx), 7.0)
+        cell = want.astype(np.float64)
+        yy, xx = np.mgrid[0:ny, 0:nx]
+        low_tile = ty[yy // T, xx // T] == 1
+        yo, xo = yy % T, xx % T
+        conv = low_tile & ((yo == 0) | (yo == T - 1) | ((step + 1) % 10 == 0) | (xo == 0) | (xo == T - 1))
+        exp[conv] = cell[conv]
+        assert np.array_equal(out.cpu().numpy(), exp), step

@@ -155,6 +155,256 @@ __global__ void kob_prep_half2(GeoH g, double r2, int off, __half2 *phi)
     phi[(int64_t)y * g.np + x] = __floats2half2_rn(p1, p2);
 }
 
+// ---- the adaptive (AMSTENCIL) grain-growth step, graingrowth/function.h:33-277 ----
+// Dual storage as the reference keeps it: FP64 arrays [ny][nx] (every tile's
+// cells where the tile is high, type 2; a low tile's edge cells, converted
+// each step, and all its cells after a period's last step) and half2 arrays
+// [ny][nx/2] (low tiles, type 1).  One CTA per tile, one thread per half2
+// pair: (T/2) x T threads.  A low tile's thread computes its pair in half2
+// from the half2 array, taking the cells of a high neighbour tile from the
+// FP64 array (graingrowth/function.h:81-170); a high tile's thread computes
+// its two cells in FP64 from the FP64 array (:232-271).
+struct GeoM {
+    int nx, ny, T, ntx, nty;
+};
+
+__device__ __forceinline__ void tile_of(const GeoM &g, int &tx, int &ty)
+{
+    tx = (int)blockIdx.x % g.ntx;
+    ty = (int)blockIdx.x / g.ntx;
+}
+
+struct MixPtrs {
+    const double *a;   // etaa
+    double *last;      // etaa_last (Monitor2 snapshot) or null
+    const double *b;   // etab
+    double *lap, *dfd, *out;
+    const __half2 *ha, *hb;
+    __half2 *hlap, *hdfd, *hout;
+    const int *type;   // type_curr [nty][ntx]
+};
+
+// low half := v (float of an FP64 cell), high half kept
+__device__ __forceinline__ __half2 set_lo(__half2 p, double v) { return __halves2half2(__float2half(v), __high2half(p)); }
+// high half := v, low half kept
+__device__ __forceinline__ __half2 set_hi(__half2 p, double v) { return __halves2half2(__low2half(p), __float2half(v)); }
+
+__global__ void gg_mix_k(GeoM g, GgH c, double dxdy, double dtm, double grcoef, MixPtrs m, int step, int etai,
+                         int cadence, bool snap)
+{
+    int tx, ty;
+    tile_of(g, tx, ty);
+    const int th = g.T / 2, np = g.nx / 2;
+    const int xo = threadIdx.x, yo = threadIdx.y;
+    const int y = ty * g.T + yo;
+    const int ys1 = y > 0 ? y - 1 : g.ny - 1, ya1 = y < g.ny - 1 ? y + 1 : 0;
+    const int tys1 = ty == 0 ? g.nty - 1 : ty - 1, tya1 = ty == g.nty - 1 ? 0 : ty + 1;
+    const int txs1 = tx == 0 ? g.ntx - 1 : tx - 1, txa1 = tx == g.ntx - 1 ? 0 : tx + 1;
+    auto type = [&](int yy, int xx) { return m.type[yy * g.ntx + xx]; };
+    const int own = type(ty, tx);
+    const int64_t row = (int64_t)y * g.nx;
+    const int c0 = tx * g.T + xo;  // this thread's cell; a high tile's thread also has c0 + th
+    // Monitor2 (End2end): the snapshot at the period's first step, of every
+    // cell of a high tile and of the left half of a low tile (whose second
+    // block returned before the snapshot there)
+    if (snap && step % cadence == 0 && etai == 2) {
+        m.last[row + c0] = m.a[row + c0];
+        if (own != 1) m.last[row + c0 + th] = m.a[row + c0 + th];
+    }
+    if (own == 1) {
+        const int x = tx * th + xo;  // pair index
+        const int xs1 = x > 0 ? x - 1 : np - 1, xa1 = x < np - 1 ? x + 1 : 0;
+        auto H = [&](int yy, int xx) { return m.ha[(int64_t)yy * np + xx]; };
+        auto F = [&](int yy, int cx) { return m.a[(int64_t)yy * g.nx + cx]; };
+        // the eight neighbour pairs: W (cells 2x-1, 2x), C (2x, 2x+1), E (2x+1, 2x+2) of rows ys1 / ya1, W / E of y
+        __half2 w_u = shift(H(ys1, xs1), H(ys1, x)), c_u = H(ys1, x), e_u = shift(H(ys1, x), H(ys1, xa1));
+        __half2 w_m = shift(H(y, xs1), H(y, x)), e_m = shift(H(y, x), H(y, xa1));
+        __half2 w_d = shift(H(ya1, xs1), H(ya1, x)), c_d = H(ya1, x), e_d = shift(H(ya1, x), H(ya1, xa1));
+        // cells of high neighbour tiles come from the FP64 array (function.h:91-170)
+        const bool lef = xo == 0, rig = xo == th - 1, top = yo == 0, bot = yo == g.T - 1;
+        const int xl = 2 * xs1 + 1, xc = 2 * x, xr = 2 * xa1;  // columns 2x-1, 2x, 2x+2
+        if (lef && top) {
+            if (type(ty, txs1) == 2) {
+                w_m = set_lo(w_m, F(y, xl));
+                w_d = set_lo(w_d, F(ya1, xl));
+            }
+            if (type(tys1, tx) == 2) {
+                w_u = set_hi(w_u, F(ys1, xc));
+                c_u = __floats2half2_rn(F(ys1, xc), F(ys1, xc + 1));
+                e_u = __floats2half2_rn(F(ys1, xc + 1), F(ys1, xr));
+            }
+            if (type(tys1, txs1) == 2) w_u = set_lo(w_u, F(ys1, xl));
+        } else if (lef && bot) {
+            if (type(ty, txs1) == 2) {
+                w_m = set_lo(w_m, F(y, xl));
+                w_u = set_lo(w_u, F(ys1, xl));
+            }
+            if (type(tya1, tx) == 2) {
+                w_d = set_hi(w_d, F(ya1, xc));
+                c_d = __floats2half2_rn(F(ya1, xc), F(ya1, xc + 1));
+                e_d = __floats2half2_rn(F(ya1, xc + 1), F(ya1, xr));
+            }
+            if (type(tya1, txs1) == 2) w_d = set_lo(w_d, F(ya1, xl));
+        } else if (rig && top) {
+            if (type(ty, txa1) == 2) {
+                e_m = set_hi(e_m, F(y, xr));
+                e_d = set_hi(e_d, F(ya1, xr));
+            }
+            if (type(tys1, tx) == 2) {
+                w_u = __floats2half2_rn(F(ys1, xl), F(ys1, xc));
+                c_u = __floats2half2_rn(F(ys1, xc), F(ys1, xc + 1));
+                e_u = set_lo(e_u, F(ys1, xc + 1));
+            }
+            if (type(tys1, txa1) == 2) e_u = set_hi(e_u, F(ys1, xr));
+        } else if (rig && bot) {
+            if (type(ty, txa1) == 2) {
+                e_u = set_hi(e_u, F(ys1, xr));
+                e_m = set_hi(e_m, F(y, xr));
+            }
+            if (type(tya1, tx) == 2) {
+                w_d = __floats2half2_rn(F(ya1, xl), F(ya1, xc));
+                c_d = __floats2half2_rn(F(ya1, xc), F(ya1, xc + 1));
+                e_d = set_lo(e_d, F(ya1, xc + 1));
+            }
+            if (type(tya1, txa1) == 2) e_d = set_hi(e_d, F(ya1, xr));
+        } else if (lef && type(ty, txs1) == 2) {
+            w_u = set_lo(w_u, F(ys1, xl));
+            w_m = set_lo(w_m, F(y, xl));
+            w_d = set_lo(w_d, F(ya1, xl));
+        } else if (rig && type(ty, txa1) == 2) {
+            e_u = set_hi(e_u, F(ys1, xr));
+            e_m = set_hi(e_m, F(y, xr));
+            e_d = set_hi(e_d, F(ya1, xr));
+        } else if (top && type(tys1, tx) == 2) {
+            w_u = __floats2half2_rn(F(ys1, xl), F(ys1, xc));
+            c_u = __floats2half2_rn(F(ys1, xc), F(ys1, xc + 1));
+            e_u = __floats2half2_rn(F(ys1, xc + 1), F(ys1, xr));
+        } else if (bot && type(tya1, tx) == 2) {
+            w_d = __floats2half2_rn(F(ya1, xl), F(ya1, xc));
+            c_d = __floats2half2_rn(F(ya1, xc), F(ya1, xc + 1));
+            e_d = __floats2half2_rn(F(ya1, xc + 1), F(ya1, xr));
+        }
+        // function.h:163-166, term by term
+        const int64_t i = (int64_t)y * np + x;
+        const __half2 e = m.ha[i];
+        const __half2 l = (w_u + c_u + e_u + w_m + e_m + w_d + c_d + e_d - c.eight * e) / c.dxdy;
+        m.hlap[i] = l;
+        const __half2 sum = m.hb[i] * m.hb[i];
+        const __half2 f = c.one * (c.two * c.one * e * sum + (e * e * e) - e);
+        m.hdfd[i] = f;
+        const __half2 o = e - c.dt * c.mobil * (f - c.grcoef * l);
+        m.hout[i] = o;
+        // function.h:168-176: the tile's edge cells into the FP64 output
+        // (all its cells at a period's last step)
+        if (yo == 0 || yo == g.T - 1 || (step + 1) % cadence == 0) {
+            m.out[row + xc] = __low2float(o);
+            m.out[row + xc + 1] = __high2float(o);
+        } else if (lef) {
+            m.out[row + xc] = __low2float(o);
+        } else if (rig) {
+            m.out[row + xc + 1] = __high2float(o);
+        }
+        return;
+    }
+    // a high tile: two cells, FP64, function.h:232-271
+    for (int k = 0; k < 2; ++k) {
+        const int x = c0 + k * th;
+        const int xs1 = x > 0 ? x - 1 : g.nx - 1, xa1 = x < g.nx - 1 ? x + 1 : 0;
+        auto A = [&](int yy, int xx) { return m.a[(int64_t)yy * g.nx + xx]; };
+        const int64_t i = row + x;
+        const double lap = (A(ys1, xs1) + A(ys1, x) + A(ys1, xa1) + A(y, xs1) + A(y, xa1) + A(ya1, xs1) + A(ya1, x) +
+                            A(ya1, xa1) - 8.0 * A(y, x)) /
+                           dxdy;
+        m.lap[i] = lap;
+        const double sum = pow(m.b[i], 2);
+        const double e = m.a[i];
+        const double f = 1.0 * (2.0 * 1.0 * e * sum + pow(e, 3) - e);
+        m.dfd[i] = f;
+        m.out[i] = e - dtm * (f - grcoef * lap);
+    }
+}
+
+// graingrowth/tools.h:24-38 -- the initial circle in FP64 arrays, one cell a thread
+__global__ void gg_prep_high(int nx, int ny, float rx, float ry, float r, double *e1, double *e2)
+{
+    const int x = blockIdx.x * kBX + threadIdx.x, y = blockIdx.y * kBY + threadIdx.y;
+    if (x >= nx || y >= ny) return;
+    const float d = sqrt(pow(x - rx, 2) + pow(y - ry, 2));
+    const int64_t i = (int64_t)y * nx + x;
+    e1[i] = d <= r ? 0 : 1;
+    e2[i] = d <= r ? 1 : 0;
+}
+
+// per-pair tools over tiles (one CTA per tile, (T/2) x T threads): the pair
+// index and row of this thread, and its tile's type
+struct PairAt {
+    int x, y, tile;
+};
+__device__ __forceinline__ PairAt pair_at(const GeoM &g)
+{
+    int tx, ty;
+    tile_of(g, tx, ty);
+    return PairAt{tx * (g.T / 2) + (int)threadIdx.x, ty * g.T + (int)threadIdx.y, ty * g.ntx + tx};
+}
+
+// graingrowth/tools.h:256-271: tiles turning high -> low take their half2 pairs from the FP64 arrays
+__global__ void gg_sync_during(GeoM g, const double *e1, const double *e2, __half2 *h1, __half2 *h2p,
+                               const int *old_t, const int *new_t)
+{
+    const PairAt q = pair_at(g);
+    if (!(old_t[q.tile] == 2 && new_t[q.tile] == 1)) return;
+    const int64_t i = (int64_t)q.y * (g.nx / 2) + q.x, c = (int64_t)q.y * g.nx + 2 * q.x;
+    h1[i] = __floats2half2_rn(e1[c], e1[c + 1]);
+    h2p[i] = __floats2half2_rn(e2[c], e2[c + 1]);
+}
+
+// graingrowth/tools.h:172-200 (AMSTENCIL): low tiles' pairs into the FP64 array
+__global__ void gg_sync_after(GeoM g, double *hi, const __half2 *lo, const int *type)
+{
+    const PairAt q = pair_at(g);
+    if (type[q.tile] != 1) return;
+    const __half2 v = lo[(int64_t)q.y * (g.nx / 2) + q.x];
+    const int64_t c = (int64_t)q.y * g.nx + 2 * q.x;
+    hi[c] = __low2float(v);
+    hi[c + 1] = __high2float(v);
+}
+
+// graingrowth/tools.h:158-171 (AMSTENCIL): every pair from the FP64 array
+__global__ void gg_high_to_low(GeoM g, const double *hi, __half2 *lo)
+{
+    const PairAt q = pair_at(g);
+    const int64_t c = (int64_t)q.y * g.nx + 2 * q.x;
+    lo[(int64_t)q.y * (g.nx / 2) + q.x] = __floats2half2_rn(hi[c], hi[c + 1]);
+}
+
+// graingrowth/function.h:323-341: kernel1_mix's conversion as its own launch
+__global__ void gg_conversion(GeoM g, double *out, const __half2 *hout, const int *type, int step, int cadence)
+{
+    const PairAt q = pair_at(g);
+    if (type[q.tile] != 1) return;
+    const int xo = threadIdx.x, yo = threadIdx.y, th = g.T / 2;
+    const __half2 o = hout[(int64_t)q.y * (g.nx / 2) + q.x];
+    const int64_t c = (int64_t)q.y * g.nx + 2 * q.x;
+    if (yo == 0 || yo == g.T - 1 || (step + 1) % cadence == 0) {
+        out[c] = __low2float(o);
+        out[c + 1] = __high2float(o);
+    } else if (xo == 0) {
+        out[c] = __low2float(o);
+    } else if (xo == th - 1) {
+        out[c + 1] = __high2float(o);
+    }
+}
+
+// graingrowth/function.h:311-321: every cell into the snapshot
+__global__ void gg_last_store(GeoM g, const double *a, double *last)
+{
+    int tx, ty;
+    tile_of(g, tx, ty);
+    const int64_t c = (int64_t)(ty * g.T + (int)threadIdx.y) * g.nx + tx * g.T + (int)threadIdx.x;
+    last[c] = a[c];
+    last[c + g.T / 2] = a[c + g.T / 2];
+}
+
 int check_half2(const amps_params *p)
 {
     if (!p || p->nx < 4 || p->ny < 5 || p->nx % 2 || p->bc != AMPS_BC_PERIODIC) return AMPS_ERR_INVALID;
@@ -162,6 +412,22 @@ int check_half2(const amps_params *p)
 }
 
 GeoH geoh(const amps_params *p) { return GeoH{p->nx / 2, p->ny}; }
+
+// the tiled half2 kernels: square tiles of an even side dividing both sides, at most 32
+int check_mix(const amps_params *p)
+{
+    if (check_half2(p)) return AMPS_ERR_INVALID;
+    const int T = p->tile;
+    if (T < 2 || T > 32 || T % 2 || p->nx % T || p->ny % T) return AMPS_ERR_INVALID;
+    return AMPS_OK;
+}
+GeoM geom(const amps_params *p) { return GeoM{p->nx, p->ny, p->tile, p->nx / p->tile, p->ny / p->tile}; }
+dim3 tiles_grid(const amps_params *p) { return dim3((unsigned)((p->nx / p->tile) * (p->ny / p->tile))); }
+dim3 pair_block(const amps_params *p) { return dim3((unsigned)(p->tile / 2), (unsigned)p->tile); }
+GgH ggh(const amps_params *p)
+{
+    return GgH{h2(1.0), h2(2.0), h2(8.0), h2(p->dt), h2(p->mobil), h2(p->grcoef), h2(p->dx * p->dy)};
+}
 dim3 gridh(const amps_params *p) { return dim3((p->nx / 2 + kBX - 1) / kBX, (p->ny + kBY - 1) / kBY); }
 
 KobH kobh(const amps_params *p)
@@ -182,7 +448,7 @@ extern "C" int amps_graingrowth_kernel1_lowpure(const amps_params *p, const void
 {
     if (check_half2(p) || !etaa || !etab || !etaa_lap || !dfdetaa || !etaa_out || etaa == etaa_out)
         return AMPS_ERR_INVALID;
-    const GgH c{h2(1.0), h2(2.0), h2(8.0), h2(p->dt), h2(p->mobil), h2(p->grcoef), h2(p->dx * p->dy)};
+    const GgH c = ggh(p);
     gg_lowpure<<<gridh(p), dim3(kBX, kBY), 0, S_>>>(geoh(p), c, (const __half2 *)etaa, (const __half2 *)etab,
                                                     (__half2 *)etaa_lap, (__half2 *)dfdetaa, (__half2 *)etaa_out);
     return launched();
@@ -232,5 +498,74 @@ extern "C" int amps_snowflake_dataprepare_half2(const amps_params *p, void *phi,
 {
     if (check_half2(p) || !phi) return AMPS_ERR_INVALID;
     kob_prep_half2<<<gridh(p), dim3(kBX, kBY), 0, S_>>>(geoh(p), p->init_r2, p->init_offset, (__half2 *)phi);
+    return launched();
+}
+
+extern "C" int amps_graingrowth_kernel1_mix(const amps_params *p, const double *etaa, double *etaa_last,
+                                            const double *etab, double *etaa_lap, double *dfdetaa, double *etaa_out,
+                                            const void *hetaa, const void *hetab, void *hetaa_lap, void *hdfdetaa,
+                                            void *hetaa_out, const int *type_curr, int i, int etai, void *stream)
+{
+    if (check_mix(p) || !etaa || !etab || !etaa_lap || !dfdetaa || !etaa_out || !hetaa || !hetab || !hetaa_lap ||
+        !hdfdetaa || !hetaa_out || !type_curr || etaa == etaa_out || hetaa == hetaa_out || p->cadence < 1)
+        return AMPS_ERR_INVALID;
+    const bool snap = p->monitor == AMPS_MONITOR_TEM;
+    if (snap && !etaa_last) return AMPS_ERR_INVALID;
+    const MixPtrs m{etaa, etaa_last, etab, etaa_lap, dfdetaa, etaa_out, (const __half2 *)hetaa, (const __half2 *)hetab,
+                    (__half2 *)hetaa_lap, (__half2 *)hdfdetaa, (__half2 *)hetaa_out, type_curr};
+    gg_mix_k<<<tiles_grid(p), pair_block(p), 0, S_>>>(geom(p), ggh(p), p->dx * p->dy, p->dt * p->mobil, p->grcoef,
+                                                      m, i, etai, p->cadence, snap);
+    return launched();
+}
+
+extern "C" int amps_graingrowth_dataprepare_high(const amps_params *p, double *eta1, double *eta2, void *stream)
+{
+    if (!p || p->nx < 1 || p->ny < 1 || !eta1 || !eta2) return AMPS_ERR_INVALID;
+    const dim3 grid((p->nx + kBX - 1) / kBX, (p->ny + kBY - 1) / kBY);
+    gg_prep_high<<<grid, dim3(kBX, kBY), 0, S_>>>(p->nx, p->ny, (float)(p->nx / 2), (float)(p->ny / 2),
+                                                  (float)p->init_r, eta1, eta2);
+    return launched();
+}
+
+extern "C" int amps_graingrowth_data_sychro_duringcomputation(const amps_params *p, const double *eta1,
+                                                              const double *eta2, void *heta1, void *heta2,
+                                                              const int *old_con, const int *new_con, void *stream)
+{
+    if (check_mix(p) || !eta1 || !eta2 || !heta1 || !heta2 || !old_con || !new_con) return AMPS_ERR_INVALID;
+    gg_sync_during<<<tiles_grid(p), pair_block(p), 0, S_>>>(geom(p), eta1, eta2, (__half2 *)heta1,
+                                                            (__half2 *)heta2, old_con, new_con);
+    return launched();
+}
+
+extern "C" int amps_graingrowth_data_sychro_aftercomputation(const amps_params *p, double *highdata,
+                                                             const void *lowdata, const int *typedata, void *stream)
+{
+    if (check_mix(p) || !highdata || !lowdata || !typedata) return AMPS_ERR_INVALID;
+    gg_sync_after<<<tiles_grid(p), pair_block(p), 0, S_>>>(geom(p), highdata, (const __half2 *)lowdata, typedata);
+    return launched();
+}
+
+extern "C" int amps_graingrowth_highdata_to_low(const amps_params *p, const double *highdata, void *lowdata,
+                                                void *stream)
+{
+    if (check_mix(p) || !highdata || !lowdata) return AMPS_ERR_INVALID;
+    gg_high_to_low<<<tiles_grid(p), pair_block(p), 0, S_>>>(geom(p), highdata, (__half2 *)lowdata);
+    return launched();
+}
+
+extern "C" int amps_graingrowth_kernel1_conversion(const amps_params *p, double *etaa_out, const void *hetaa_out,
+                                                   const int *type_curr, int i, void *stream)
+{
+    if (check_mix(p) || !etaa_out || !hetaa_out || !type_curr || p->cadence < 1) return AMPS_ERR_INVALID;
+    gg_conversion<<<tiles_grid(p), pair_block(p), 0, S_>>>(geom(p), etaa_out, (const __half2 *)hetaa_out,
+                                                           type_curr, i, p->cadence);
+    return launched();
+}
+
+extern "C" int amps_graingrowth_monitor2_lastdata_store(const amps_params *p, const double *etaa, double *etaa_last,
+                                                        void *stream)
+{
+    if (check_mix(p) || !etaa || !etaa_last) return AMPS_ERR_INVALID;
+    gg_last_store<<<tiles_grid(p), pair_block(p), 0, S_>>>(geom(p), etaa, etaa_last);
     return launched();
 }
