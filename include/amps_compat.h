@@ -149,6 +149,52 @@ AMPS_API int amps_graingrowth_kernel1_conversion(const amps_params *p, double *e
 AMPS_API int amps_graingrowth_monitor2_lastdata_store(const amps_params *p, const double *etaa, double *etaa_last,
                                                       void *stream);
 
+/* ---- the adaptive Kobayashi step (AMSTENCIL) -------------------------------
+ * The same dual storage for phi, tempr and the step's intermediates; tiles
+ * of at least 4 cells a side. */
+
+/* snowflake/function.h:63-375 -- Laplacians, gradients, epsilon and its
+ * derivative: a type-2 tile in FP64 from the FP64 arrays; a type-1 tile in
+ * half2, taking the cells of type-2 neighbour tiles (two cells deep, left,
+ * right, up, down) from phi / tempr, and converting its edge cells of phidx,
+ * phidy, epsilon, epsilon_deri into the FP64 arrays.  With p->monitor ==
+ * AMPS_MONITOR_TEM, step i with i % cadence == 0 first copies phi into
+ * phi_last as the reference's Monitor2 build does (a type-1 tile's left half). */
+AMPS_API int amps_snowflake_kernel1_mix(const amps_params *p, const double *phi, double *phi_last, double *phi_lap,
+                                        double *epsilon, double *epsilon_deri, double *phidx, double *phidy,
+                                        const double *tempr, double *tempr_lap, const void *hphi, void *hphi_lap,
+                                        const void *htempr, void *htempr_lap, void *hphidx, void *hphidy,
+                                        void *hepsilon, void *hepsilon_deri, const int *type_curr, int i,
+                                        void *stream);
+/* snowflake/function.h:376-604 -- phi and tempr advanced in place, each
+ * tile at its type; a type-1 tile converts its two-cell edge band (all its
+ * cells when (i + 1) % cadence == 0) into phi / tempr. */
+AMPS_API int amps_snowflake_mix_kernel2(const amps_params *p, double *phi, const double *phi_lap,
+                                        const double *epsilon, const double *epsilon_deri, const double *phidx,
+                                        const double *phidy, double *tempr, const double *tempr_lap, void *hphi,
+                                        const void *hphi_lap, const void *hepsilon, const void *hepsilon_deri,
+                                        const void *hphidx, const void *hphidy, void *htempr, const void *htempr_lap,
+                                        const int *type_curr, int i, void *stream);
+/* snowflake/function.h:715-759 -- kernel1_mix's conversion as its own launch. */
+AMPS_API int amps_snowflake_kernel1_conversion(const amps_params *p, double *epsilon, double *epsilon_deri,
+                                               double *phidx, double *phidy, const void *hphidx, const void *hphidy,
+                                               const void *hepsilon, const void *hepsilon_deri, const int *type_curr,
+                                               int i, void *stream);
+/* snowflake/function.h:760-790 -- mix_kernel2's conversion as its own launch. */
+AMPS_API int amps_snowflake_kernel2_conversion(const amps_params *p, double *phi, double *tempr, const void *hphi,
+                                               const void *htempr, const int *type_curr, int i, void *stream);
+/* snowflake/function.h:704-714, snowflake/tools.h:133-176 and 231-246 --
+ * the same tools as grain growth's, for phi and tempr. */
+AMPS_API int amps_snowflake_monitor2_lastdata_store(const amps_params *p, const double *phi, double *phi_last,
+                                                    void *stream);
+AMPS_API int amps_snowflake_data_sychro_duringcomputation(const amps_params *p, const double *phi,
+                                                          const double *tempr, void *hphi, void *htempr,
+                                                          const int *old_con, const int *new_con, void *stream);
+AMPS_API int amps_snowflake_data_sychro_aftercomputation(const amps_params *p, double *highdata, const void *lowdata,
+                                                         const int *typedata, void *stream);
+AMPS_API int amps_snowflake_highdata_to_low(const amps_params *p, const double *highdata, void *lowdata,
+                                            void *stream);
+
 #ifdef __cplusplus
 }
 #endif

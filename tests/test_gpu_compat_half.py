@@ -225,3 +225,110 @@ def test_graingrowth_mix_tools():
         conv = low_tile & ((yo == 0) | (yo == T - 1) | ((step + 1) % 10 == 0) | (xo == 0) | (xo == T - 1))
         exp[conv] = cell[conv]
         assert np.array_equal(out.cpu().numpy(), exp), step
+
+
+def kob_mix_lib():
+    L = mix_lib()
+    dp = ctypes.POINTER(w().Params)
+    I = ctypes.c_int
+    sig = {
+        "amps_snowflake_kernel1_mix": [P] * 18 + [I],
+        "amps_snowflake_mix_kernel2": [P] * 17 + [I],
+        "amps_snowflake_dataprepare_high": [P],
+        "amps_snowflake_data_sychro_duringcomputation": [P] * 6,
+        "amps_snowflake_data_sychro_aftercomputation": [P] * 3,
+        "amps_snowflake_kernel2_conversion": [P] * 5 + [I],
+    }
+    for name, args in sig.items():
+        f = getattr(L, name)
+        f.argtypes = [dp] + args + [P]
+        f.restype = ctypes.c_int
+    return L
+
+
+@pytest.mark.parametrize("monitor,thr,steps", [(1, 0.5, 200), (1, 0.1, 120), (2, 1e-4, 200), (2, 1e-2, 120)])
+def test_kobayashi_mixed_loop_equals_the_reference_kernels(monitor, thr, steps):
+    """snowflake/end2end_mix.cu's loop (AMSTENCIL, Monitor1/2) through the
+    reference-named wrappers -- the seed disc, per period get_max_diff /
+    get_type / data_sychro_duringcomputation, kernel1_mix and mix_kernel2 a
+    step, the final data_sychro_aftercomputation -- against the reference's
+    own kernels driven the same way: tile types of every period and the
+    final phi and tempr, bit for bit."""
+    need(f"snowflake_mix_m{monitor}")
+    L = kob_mix_lib()
+    p = w().Params.preset("kobayashi", 2, mode="end2end_mix", monitor=monitor, thr_lo=thr, thr_hi=thr)
+    with refcuda.Module(f"snowflake_mix_m{monitor}") as m:
+        assert (m.nx, m.ny, m.ux, m.uy) == (p.nx, p.ny, p.tile, p.tile)
+    pp = ctypes.byref(p)
+    nx, ny, T = p.nx, p.ny, p.tile
+    tiles = (nx // T) * (ny // T)
+    f64 = lambda: torch.zeros((ny, nx), dtype=torch.float64, device="cuda")
+    phi, plap, eps, epsd, pdx, pdy, tem, tlap, last = (f64() for _ in range(9))
+    hphi, hplap, htem, htlap, hpdx, hpdy, heps, hepsd = half2s(p, 8)
+    tcur = torch.zeros(tiles, dtype=torch.int32, device="cuda")
+    told = torch.zeros(tiles, dtype=torch.int32, device="cuda")
+    md = torch.zeros(tiles, dtype=torch.float64, device="cuda")
+    assert L.amps_snowflake_dataprepare_high(pp, ptr(phi), None) == 0
+    assert L.amps_snowflake_dataprepare_half2(pp, ptr(hphi), None) == 0
+    if monitor == 2:  # end2end_mix.cu:42-46
+        last.copy_((phi == 0).double())
+    types = []
+    for i in range(steps):
+        if i % 10 == 0:
+            if monitor == 1:
+                assert L.amps_get_max_diff1(pp, ptr(phi), ptr(md), None) == 0
+            else:
+                assert L.amps_get_max_diff2(pp, ptr(last), ptr(phi), ptr(md), None) == 0
+            assert L.amps_get_type(pp, ptr(md), ptr(told), ptr(tcur), None) == 0
+            assert L.amps_snowflake_data_sychro_duringcomputation(pp, ptr(phi), ptr(tem), ptr(hphi), ptr(htem),
+                                                                  ptr(told), ptr(tcur), None) == 0
+            types.append(tcur.cpu().numpy().astype(np.uint8))
+        assert L.amps_snowflake_kernel1_mix(pp, ptr(phi), ptr(last), ptr(plap), ptr(eps), ptr(epsd), ptr(pdx),
+                                            ptr(pdy), ptr(tem), ptr(tlap), ptr(hphi), ptr(hplap), ptr(htem),
+                                            ptr(htlap), ptr(hpdx), ptr(hpdy), ptr(heps), ptr(hepsd), ptr(tcur), i,
+                                            None) == 0
+        assert L.amps_snowflake_mix_kernel2(pp, ptr(phi), ptr(plap), ptr(eps), ptr(epsd), ptr(pdx), ptr(pdy),
+                                            ptr(tem), ptr(tlap), ptr(hphi), ptr(hplap), ptr(heps), ptr(hepsd),
+                                            ptr(hpdx), ptr(hpdy), ptr(htem), ptr(htlap), ptr(tcur), i, None) == 0
+    assert L.amps_snowflake_data_sychro_aftercomputation(pp, ptr(phi), ptr(hphi), ptr(tcur), None) == 0
+    assert L.amps_snowflake_data_sychro_aftercomputation(pp, ptr(tem), ptr(htem), ptr(tcur), None) == 0
+    torch.cuda.synchronize()
+    rp, rt, rtypes, _ = refcuda.kob_mix(steps, thr, monitor)
+    ours = np.stack(types)
+    mix = np.bincount(ours.ravel(), minlength=3)[1:] / ours.size
+    bad = [k for k in range(rtypes.shape[0]) if not np.array_equal(ours[k], rtypes[k])]
+    fp, ft = phi.cpu().numpy(), tem.cpu().numpy()
+    d = max(float(np.abs(fp - rp).max()), float(np.abs(ft - rt).max()))
+    print(f"kobayashi mixed loop, monitor {monitor} {thr:g}, {steps} steps: tile types half/FP64 {mix}, "
+          f"periods differing {bad[:5]}, fields max |diff| {d:.3e}")
+    assert not bad
+    assert np.array_equal(fp, rp) and np.array_equal(ft, rt)
+
+
+def test_kobayashi_kernel2_conversion():
+    """kernel2_conversion against a numpy statement of
+    snowflake/function.h:760-790 on random half2 data and tile types."""
+    L = kob_mix_lib()
+    p = w().Params.preset("kobayashi", 2, mode="end2end_mix")
+    pp = ctypes.byref(p)
+    nx, ny, T = p.nx, p.ny, p.tile
+    rng = np.random.default_rng(4)
+    hp = rng.uniform(-1, 1, (ny, nx)).astype(np.float16)
+    ht = rng.uniform(-1, 1, (ny, nx)).astype(np.float16)
+    dhp = torch.tensor(hp.view(np.int32), device="cuda")
+    dht = torch.tensor(ht.view(np.int32), device="cuda")
+    ty = rng.integers(1, 3, (ny // T, nx // T)).astype(np.int32)
+    dty = torch.tensor(ty, device="cuda")
+    for step in (3, 9):
+        fp = torch.full((ny, nx), 7.0, dtype=torch.float64, device="cuda")
+        ft = torch.full((ny, nx), 7.0, dtype=torch.float64, device="cuda")
+        assert L.amps_snowflake_kernel2_conversion(pp, ptr(fp), ptr(ft), ptr(dhp), ptr(dht), ptr(dty), step,
+                                                   None) == 0
+        yy, xx = np.mgrid[0:ny, 0:nx]
+        yo, xo = yy % T, (xx % T) // 2
+        band = (ty[yy // T, xx // T] == 1) & ((yo < 2) | (yo + 2 > T - 1) | (xo == 0) | (xo == T // 2 - 1) |
+                                              ((step + 1) % 10 == 0))
+        for got, src in ((fp, hp), (ft, ht)):
+            exp = np.full((ny, nx), 7.0)
+            exp[band] = src.astype(np.float64)[band]
+            assert np.array_equal(got.cpu().numpy(), exp), step

@@ -324,6 +324,315 @@ __global__ void gg_mix_k(GeoM g, GgH c, double dxdy, double dtm, double grcoef, 
     }
 }
 
+// ---- the adaptive (AMSTENCIL) Kobayashi step, snowflake/function.h:63-604 ----
+// The same dual storage and launch shape as gg_mix_k: phi, tempr and the
+// step's intermediates (phi_lap, tempr_lap, phidx, phidy, epsilon,
+// epsilon_deri) each as an FP64 array and a half2 array.  The stencils reach
+// two cells (the reference's cross Laplacian): a low tile takes the cells of a
+// high neighbour tile (left, right, up, down) from the FP64 arrays, and its
+// edge band is converted into them after each kernel.
+struct KobMixPtrs {
+    double *phi, *last, *phi_lap, *eps, *epsd, *phidx, *phidy, *tempr, *tempr_lap;
+    __half2 *hphi, *hphi_lap, *htempr, *htempr_lap, *hphidx, *hphidy, *heps, *hepsd;
+    const int *type;
+};
+
+// the FP64 constants of a high tile as the reference's compile-time
+// expressions fold them: dx*dy, 2*dx, 2*dy, -epsilonb*aniso*delta,
+// alpha/pi, dtime/tau
+struct KobD {
+    double dxdy, dx2, dy2, epsb, delta, aniso, theta0, nead, apk, gama, teq, dtt, dt, kappa;
+};
+
+struct TileAt {
+    int tx, ty, txs1, txa1, tys1, tya1, xo, yo, th, y, c0;
+};
+__device__ __forceinline__ TileAt tile_at(const GeoM &g)
+{
+    TileAt t;
+    tile_of(g, t.tx, t.ty);
+    t.txs1 = t.tx == 0 ? g.ntx - 1 : t.tx - 1;
+    t.txa1 = t.tx == g.ntx - 1 ? 0 : t.tx + 1;
+    t.tys1 = t.ty == 0 ? g.nty - 1 : t.ty - 1;
+    t.tya1 = t.ty == g.nty - 1 ? 0 : t.ty + 1;
+    t.xo = threadIdx.x;
+    t.yo = threadIdx.y;
+    t.th = g.T / 2;
+    t.y = t.ty * g.T + t.yo;
+    t.c0 = t.tx * g.T + t.xo;
+    return t;
+}
+
+__device__ __forceinline__ int wrapn(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+
+// snowflake/function.h:63-375: Laplacians, gradients and the anisotropy
+__global__ void kob_mix_k1(GeoM g, KobH c, KobD d, KobMixPtrs m, int step, int cadence, bool snap)
+{
+    const TileAt t = tile_at(g);
+    auto type = [&](int yy, int xx) { return m.type[yy * g.ntx + xx]; };
+    const int own = type(t.ty, t.tx);
+    const int y = t.y, nx = g.nx, np = g.nx / 2;
+    const int ys1 = wrapn(y - 1, g.ny), ya1 = wrapn(y + 1, g.ny), ys2 = wrapn(y - 2, g.ny), ya2 = wrapn(y + 2, g.ny);
+    const int64_t row = (int64_t)y * nx;
+    // Monitor2: the snapshot at the period's first step (a low tile's left half only)
+    if (snap && step % cadence == 0) {
+        m.last[row + t.c0] = m.phi[row + t.c0];
+        if (own != 1) m.last[row + t.c0 + t.th] = m.phi[row + t.c0 + t.th];
+    }
+    if (own == 1) {
+        const int x = t.tx * t.th + t.xo;
+        const int xs1 = x > 0 ? x - 1 : np - 1, xa1 = x < np - 1 ? x + 1 : 0;
+        auto HP = [&](int yy, int xx) { return m.hphi[(int64_t)yy * np + xx]; };
+        auto HT = [&](int yy, int xx) { return m.htempr[(int64_t)yy * np + xx]; };
+        auto FP = [&](int yy, int cx) { return m.phi[(int64_t)yy * nx + cx]; };
+        auto FT = [&](int yy, int cx) { return m.tempr[(int64_t)yy * nx + cx]; };
+        __half2 p_xs1 = shift(HP(y, xs1), HP(y, x)), p_xs2 = HP(y, xs1), p_xa1 = shift(HP(y, x), HP(y, xa1)),
+                p_xa2 = HP(y, xa1), p_ys1 = HP(ys1, x), p_ys2 = HP(ys2, x), p_ya1 = HP(ya1, x), p_ya2 = HP(ya2, x);
+        __half2 t_xs1 = shift(HT(y, xs1), HT(y, x)), t_xs2 = HT(y, xs1), t_xa1 = shift(HT(y, x), HT(y, xa1)),
+                t_xa2 = HT(y, xa1), t_ys1 = HT(ys1, x), t_ys2 = HT(ys2, x), t_ya1 = HT(ya1, x), t_ya2 = HT(ya2, x);
+        const int xl = 2 * xs1, xr = 2 * xa1;
+        // function.h:137-158, the x chain
+        if (t.xo == 0 && type(t.ty, t.txs1) == 2) {
+            p_xs1 = set_lo(p_xs1, FP(y, xl + 1));
+            t_xs1 = set_lo(t_xs1, FT(y, xl + 1));
+            p_xs2 = __halves2half2(__float2half(FP(y, xl)), __float2half(FP(y, xl + 1)));
+            t_xs2 = __halves2half2(__float2half(FT(y, xl)), __float2half(FT(y, xl + 1)));
+        } else if (t.xo == 1 && type(t.ty, t.txs1) == 2) {
+            p_xs2 = __halves2half2(__float2half(FP(y, xl)), __float2half(FP(y, xl + 1)));
+            t_xs2 = __halves2half2(__float2half(FT(y, xl)), __float2half(FT(y, xl + 1)));
+        } else if (t.xo == t.th - 1 && type(t.ty, t.txa1) == 2) {
+            p_xa1 = set_hi(p_xa1, FP(y, xr));
+            t_xa1 = set_hi(t_xa1, FT(y, xr));
+            p_xa2 = __halves2half2(__float2half(FP(y, xr)), __float2half(FP(y, xr + 1)));
+            t_xa2 = __halves2half2(__float2half(FT(y, xr)), __float2half(FT(y, xr + 1)));
+        } else if (t.xo == t.th - 2 && type(t.ty, t.txa1) == 2) {
+            p_xa2 = __halves2half2(__float2half(FP(y, xr)), __float2half(FP(y, xr + 1)));
+            t_xa2 = __halves2half2(__float2half(FT(y, xr)), __float2half(FT(y, xr + 1)));
+        }
+        // function.h:160-180, the y chain
+        const int xc = 2 * x;
+        if (t.yo == 0 && type(t.tys1, t.tx) == 2) {
+            p_ys1 = __floats2half2_rn(FP(ys1, xc), FP(ys1, xc + 1));
+            t_ys1 = __floats2half2_rn(FT(ys1, xc), FT(ys1, xc + 1));
+            p_ys2 = __floats2half2_rn(FP(ys2, xc), FP(ys2, xc + 1));
+            t_ys2 = __floats2half2_rn(FT(ys2, xc), FT(ys2, xc + 1));
+        } else if (t.yo == 1 && type(t.tys1, t.tx) == 2) {
+            p_ys2 = __floats2half2_rn(FP(ys2, xc), FP(ys2, xc + 1));
+            t_ys2 = __floats2half2_rn(FT(ys2, xc), FT(ys2, xc + 1));
+        } else if (t.yo == g.T - 1 && type(t.tya1, t.tx) == 2) {
+            p_ya1 = __floats2half2_rn(FP(ya1, xc), FP(ya1, xc + 1));
+            t_ya1 = __floats2half2_rn(FT(ya1, xc), FT(ya1, xc + 1));
+            p_ya2 = __floats2half2_rn(FP(ya2, xc), FP(ya2, xc + 1));
+            t_ya2 = __floats2half2_rn(FT(ya2, xc), FT(ya2, xc + 1));
+        } else if (t.yo == g.T - 2 && type(t.tya1, t.tx) == 2) {
+            p_ya2 = __floats2half2_rn(FP(ya2, xc), FP(ya2, xc + 1));
+            t_ya2 = __floats2half2_rn(FT(ya2, xc), FT(ya2, xc + 1));
+        }
+        // function.h:204-220, term by term
+        const int64_t i = (int64_t)y * np + x;
+        const __half2 dd = c.dxdy;
+        m.hphi_lap[i] = p_xs1 / dd + p_xs2 / dd + p_xa1 / dd + p_xa2 / dd + p_ys1 / dd + p_ys2 / dd + p_ya1 / dd +
+                        p_ya2 / dd - c.eight * HP(y, x) / dd;
+        m.htempr_lap[i] = t_xs1 / dd + t_xs2 / dd + t_xa1 / dd + t_xa2 / dd + t_ys1 / dd + t_ys2 / dd + t_ya1 / dd +
+                          t_ya2 / dd - c.eight * HT(y, x) / dd;
+        const __half2 px = (p_xa1 - p_xs1) / c.dxm2;
+        m.hphidx[i] = px;
+        const __half2 py = (p_ya1 - p_ys1) / c.dym2;
+        m.hphidy[i] = py;
+        const __half2 theta =
+            __floats2half2_rn(atan2(__low2float(py), __low2float(px)), atan2(__high2float(py), __high2float(px)));
+        const __half2 tmp = c.aniso * (theta - c.theta0);
+        const __half2 t1 = h2cos(tmp), t2 = h2sin(tmp);
+        const __half2 e = c.epsb * (c.one + c.delta * t1);
+        m.heps[i] = e;
+        const __half2 ed = -c.epsb * c.aniso * c.delta * t2;
+        m.hepsd[i] = ed;
+        // function.h:221-245: the tile's edge cells into the FP64 arrays
+        if (t.yo == 0 || t.yo == g.T - 1) {
+            m.phidx[row + xc] = __low2float(px);
+            m.phidx[row + xc + 1] = __high2float(px);
+            m.phidy[row + xc] = __low2float(py);
+            m.phidy[row + xc + 1] = __high2float(py);
+            m.eps[row + xc] = __low2float(e);
+            m.eps[row + xc + 1] = __high2float(e);
+            m.epsd[row + xc] = __low2float(ed);
+            m.epsd[row + xc + 1] = __high2float(ed);
+        } else if (t.xo == 0) {
+            m.phidx[row + xc] = __low2float(px);
+            m.phidy[row + xc] = __low2float(py);
+            m.eps[row + xc] = __low2float(e);
+            m.epsd[row + xc] = __low2float(ed);
+        } else if (t.xo == t.th - 1) {
+            m.phidx[row + xc + 1] = __high2float(px);
+            m.phidy[row + xc + 1] = __high2float(py);
+            m.eps[row + xc + 1] = __high2float(e);
+            m.epsd[row + xc + 1] = __high2float(ed);
+        }
+        return;
+    }
+    // a high tile: two cells in FP64, function.h:266-352
+    for (int k = 0; k < 2; ++k) {
+        const int x = t.c0 + k * t.th;
+        const int xs1 = x > 0 ? x - 1 : nx - 1, xa1 = x < nx - 1 ? x + 1 : 0;
+        const int xs2 = x - 2 < 0 ? x - 2 + nx : x - 2, xa2 = x + 2 > nx - 1 ? x + 2 - nx : x + 2;
+        auto P = [&](int yy, int xx) { return m.phi[(int64_t)yy * nx + xx]; };
+        auto T = [&](int yy, int xx) { return m.tempr[(int64_t)yy * nx + xx]; };
+        const int64_t i = row + x;
+        m.phi_lap[i] = P(y, xs1) / d.dxdy + P(y, xs2) / d.dxdy + P(y, xa1) / d.dxdy + P(y, xa2) / d.dxdy +
+                       P(ys1, x) / d.dxdy + P(ys2, x) / d.dxdy + P(ya1, x) / d.dxdy + P(ya2, x) / d.dxdy -
+                       8.0 * P(y, x) / d.dxdy;
+        m.tempr_lap[i] = T(y, xs1) / d.dxdy + T(y, xs2) / d.dxdy + T(y, xa1) / d.dxdy + T(y, xa2) / d.dxdy +
+                         T(ys1, x) / d.dxdy + T(ys2, x) / d.dxdy + T(ya1, x) / d.dxdy + T(ya2, x) / d.dxdy -
+                         8.0 * T(y, x) / d.dxdy;
+        const double px = (P(y, xa1) - P(y, xs1)) / d.dx2;
+        m.phidx[i] = px;
+        const double py = (P(ya1, x) - P(ys1, x)) / d.dy2;
+        m.phidy[i] = py;
+        const double theta = atan2(py, px);
+        m.eps[i] = d.epsb * (1.0 + d.delta * cos(d.aniso * (theta - d.theta0)));
+        m.epsd[i] = d.nead * sin(d.aniso * (theta - d.theta0));
+    }
+}
+
+// snowflake/function.h:376-604: phi and tempr advanced in place
+__global__ void kob_mix_k2(GeoM g, KobH c, KobD d, KobMixPtrs m, int step, int cadence)
+{
+    const TileAt t = tile_at(g);
+    auto type = [&](int yy, int xx) { return m.type[yy * g.ntx + xx]; };
+    const int own = type(t.ty, t.tx);
+    const int y = t.y, nx = g.nx, np = g.nx / 2;
+    const int ys1 = wrapn(y - 1, g.ny), ya1 = wrapn(y + 1, g.ny);
+    const int64_t row = (int64_t)y * nx;
+    if (own == 1) {
+        const int x = t.tx * t.th + t.xo;
+        const int xs1 = x > 0 ? x - 1 : np - 1, xa1 = x < np - 1 ? x + 1 : 0;
+        auto at = [&](int yy, int xx) { return (int64_t)yy * np + xx; };
+        auto F = [&](const double *a, int yy, int cx) { return a[(int64_t)yy * nx + cx]; };
+        const int64_t i = at(y, x);
+        const int xc = 2 * x;
+        const __half2 phi_old = m.hphi[i];
+        __half2 pdx_ya1, e_ya1, ed_ya1, pdx_ys1, e_ys1, ed_ys1, e_xs1, ed_xs1, pdy_xs1, e_xa1, ed_xa1, pdy_xa1;
+        // function.h:429-471: neighbours of a high tile from the FP64 arrays
+        if (t.yo < g.T - 1 || type(t.tya1, t.tx) == 1) {
+            pdx_ya1 = m.hphidx[at(ya1, x)];
+            e_ya1 = m.heps[at(ya1, x)];
+            ed_ya1 = m.hepsd[at(ya1, x)];
+        } else {
+            pdx_ya1 = __floats2half2_rn(F(m.phidx, ya1, xc), F(m.phidx, ya1, xc + 1));
+            e_ya1 = __floats2half2_rn(F(m.eps, ya1, xc), F(m.eps, ya1, xc + 1));
+            ed_ya1 = __floats2half2_rn(F(m.epsd, ya1, xc), F(m.epsd, ya1, xc + 1));
+        }
+        if (t.yo > 0 || type(t.tys1, t.tx) == 1) {
+            pdx_ys1 = m.hphidx[at(ys1, x)];
+            ed_ys1 = m.hepsd[at(ys1, x)];
+            e_ys1 = m.heps[at(ys1, x)];
+        } else {
+            pdx_ys1 = __floats2half2_rn(F(m.phidx, ys1, xc), F(m.phidx, ys1, xc + 1));
+            ed_ys1 = __floats2half2_rn(F(m.epsd, ys1, xc), F(m.epsd, ys1, xc + 1));
+            e_ys1 = __floats2half2_rn(F(m.eps, ys1, xc), F(m.eps, ys1, xc + 1));
+        }
+        if (t.xo > 0 || type(t.ty, t.txs1) == 1) {
+            e_xs1 = shift(m.heps[at(y, xs1)], m.heps[i]);
+            ed_xs1 = shift(m.hepsd[at(y, xs1)], m.hepsd[i]);
+            pdy_xs1 = shift(m.hphidy[at(y, xs1)], m.hphidy[i]);
+        } else {
+            e_xs1 = __halves2half2(__float2half(F(m.eps, y, 2 * xs1 + 1)), __low2half(m.heps[i]));
+            ed_xs1 = __halves2half2(__float2half(F(m.epsd, y, 2 * xs1 + 1)), __low2half(m.hepsd[i]));
+            pdy_xs1 = __halves2half2(__float2half(F(m.phidy, y, 2 * xs1 + 1)), __low2half(m.hphidy[i]));
+        }
+        if (t.xo < t.th - 1 || type(t.ty, t.txa1) == 1) {
+            e_xa1 = shift(m.heps[i], m.heps[at(y, xa1)]);
+            ed_xa1 = shift(m.hepsd[i], m.hepsd[at(y, xa1)]);
+            pdy_xa1 = shift(m.hphidy[i], m.hphidy[at(y, xa1)]);
+        } else {
+            e_xa1 = __halves2half2(__high2half(m.heps[i]), __float2half(F(m.eps, y, 2 * xa1)));
+            ed_xa1 = __halves2half2(__high2half(m.hepsd[i]), __float2half(F(m.epsd, y, 2 * xa1)));
+            pdy_xa1 = __halves2half2(__high2half(m.hphidy[i]), __float2half(F(m.phidy, y, 2 * xa1)));
+        }
+        // function.h:478-489, term by term
+        const __half2 term1 = (e_ya1 * ed_ya1 * pdx_ya1 - e_ys1 * ed_ys1 * pdx_ys1) / c.dym2;
+        const __half2 term2 = -(e_xa1 * ed_xa1 * pdy_xa1 - e_xs1 * ed_xs1 * pdy_xs1) / c.dxm2;
+        __half2 tmp = c.gama * (c.teq - m.htempr[i]);
+        tmp = __floats2half2_rn(atan(__low2float(tmp)), atan(__high2float(tmp)));
+        const __half2 mm = c.alpha / c.pi * tmp;
+        const __half2 pn = m.hphi[i] + (c.dt / c.tau) * (term1 + term2 + (m.heps[i] * m.heps[i]) * m.hphi_lap[i] +
+                                                          phi_old * (c.one - phi_old) * (phi_old - c.zpf + mm));
+        m.hphi[i] = pn;
+        const __half2 tn = m.htempr[i] + c.dt * m.htempr_lap[i] + c.kappa * (pn - phi_old);
+        m.htempr[i] = tn;
+        // function.h:490-499: the two-cell edge band (every cell at a period's last step)
+        if (t.yo < 2 || t.yo + 2 > g.T - 1 || t.xo == 0 || t.xo == t.th - 1 || (step + 1) % cadence == 0) {
+            m.phi[row + xc] = __low2float(pn);
+            m.phi[row + xc + 1] = __high2float(pn);
+            m.tempr[row + xc] = __low2float(tn);
+            m.tempr[row + xc + 1] = __high2float(tn);
+        }
+        return;
+    }
+    // a high tile: two cells in FP64, function.h:511-600
+    for (int k = 0; k < 2; ++k) {
+        const int x = t.c0 + k * t.th;
+        const int xs1 = x > 0 ? x - 1 : nx - 1, xa1 = x < nx - 1 ? x + 1 : 0;
+        auto A = [&](const double *a, int yy, int xx) { return a[(int64_t)yy * nx + xx]; };
+        const int64_t i = row + x;
+        const double phi_old = m.phi[i];
+        const double term1 = (A(m.eps, ya1, x) * A(m.epsd, ya1, x) * A(m.phidx, ya1, x) -
+                              A(m.eps, ys1, x) * A(m.epsd, ys1, x) * A(m.phidx, ys1, x)) /
+                             d.dy2;
+        const double term2 = -(A(m.eps, y, xa1) * A(m.epsd, y, xa1) * A(m.phidy, y, xa1) -
+                               A(m.eps, y, xs1) * A(m.epsd, y, xs1) * A(m.phidy, y, xs1)) /
+                             d.dx2;
+        const double mm = d.apk * atan(d.gama * (d.teq - m.tempr[i]));
+        m.phi[i] = m.phi[i] + d.dtt * (term1 + term2 + pow(m.eps[i], 2) * m.phi_lap[i] +
+                                       phi_old * (1.0 - phi_old) * (phi_old - 0.5 + mm));
+        m.tempr[i] = m.tempr[i] + d.dt * m.tempr_lap[i] + d.kappa * (m.phi[i] - phi_old);
+    }
+}
+
+// snowflake/function.h:715-759: kernel1_mix's conversion as its own launch
+__global__ void kob_conv1(GeoM g, KobMixPtrs m)
+{
+    const TileAt t = tile_at(g);
+    if (m.type[t.ty * g.ntx + t.tx] != 1) return;
+    const int64_t i = (int64_t)t.y * (g.nx / 2) + t.tx * t.th + t.xo;
+    const int64_t c = (int64_t)t.y * g.nx + 2 * (t.tx * t.th + t.xo);
+    const __half2 px = m.hphidx[i], py = m.hphidy[i], e = m.heps[i], ed = m.hepsd[i];
+    if (t.yo == 0 || t.yo == g.T - 1) {
+        m.phidx[c] = __low2float(px);
+        m.phidx[c + 1] = __high2float(px);
+        m.phidy[c] = __low2float(py);
+        m.phidy[c + 1] = __high2float(py);
+        m.eps[c] = __low2float(e);
+        m.eps[c + 1] = __high2float(e);
+        m.epsd[c] = __low2float(ed);
+        m.epsd[c + 1] = __high2float(ed);
+    } else if (t.xo == 0) {
+        m.phidx[c] = __low2float(px);
+        m.phidy[c] = __low2float(py);
+        m.eps[c] = __low2float(e);
+        m.epsd[c] = __low2float(ed);
+    } else if (t.xo == t.th - 1) {
+        m.phidx[c + 1] = __high2float(px);
+        m.phidy[c + 1] = __high2float(py);
+        m.eps[c + 1] = __high2float(e);
+        m.epsd[c + 1] = __high2float(ed);
+    }
+}
+
+// snowflake/function.h:760-790: mix_kernel2's conversion as its own launch
+__global__ void kob_conv2(GeoM g, KobMixPtrs m, int step, int cadence)
+{
+    const TileAt t = tile_at(g);
+    if (m.type[t.ty * g.ntx + t.tx] != 1) return;
+    if (!(t.yo < 2 || t.yo + 2 > g.T - 1 || t.xo == 0 || t.xo == t.th - 1 || (step + 1) % cadence == 0)) return;
+    const int64_t i = (int64_t)t.y * (g.nx / 2) + t.tx * t.th + t.xo;
+    const int64_t c = (int64_t)t.y * g.nx + 2 * (t.tx * t.th + t.xo);
+    m.phi[c] = __low2float(m.hphi[i]);
+    m.phi[c + 1] = __high2float(m.hphi[i]);
+    m.tempr[c] = __low2float(m.htempr[i]);
+    m.tempr[c + 1] = __high2float(m.htempr[i]);
+}
+
 // graingrowth/tools.h:24-38 -- the initial circle in FP64 arrays, one cell a thread
 __global__ void gg_prep_high(int nx, int ny, float rx, float ry, float r, double *e1, double *e2)
 {
@@ -424,6 +733,11 @@ int check_mix(const amps_params *p)
 GeoM geom(const amps_params *p) { return GeoM{p->nx, p->ny, p->tile, p->nx / p->tile, p->ny / p->tile}; }
 dim3 tiles_grid(const amps_params *p) { return dim3((unsigned)((p->nx / p->tile) * (p->ny / p->tile))); }
 dim3 pair_block(const amps_params *p) { return dim3((unsigned)(p->tile / 2), (unsigned)p->tile); }
+KobD kobd(const amps_params *p)
+{
+    return KobD{p->dx * p->dy, 2.0 * p->dx, 2.0 * p->dy, p->epsb, p->delta, p->aniso, p->theta0,
+                -p->epsb * p->aniso * p->delta, p->alpha / p->pi, p->gama, p->teq, p->dt / p->tau, p->dt, p->kappa};
+}
 GgH ggh(const amps_params *p)
 {
     return GgH{h2(1.0), h2(2.0), h2(8.0), h2(p->dt), h2(p->mobil), h2(p->grcoef), h2(p->dx * p->dy)};
@@ -568,4 +882,107 @@ extern "C" int amps_graingrowth_monitor2_lastdata_store(const amps_params *p, co
     if (check_mix(p) || !etaa || !etaa_last) return AMPS_ERR_INVALID;
     gg_last_store<<<tiles_grid(p), pair_block(p), 0, S_>>>(geom(p), etaa, etaa_last);
     return launched();
+}
+
+// the Kobayashi step's arrays, reference order (snowflake/function.h:63, 376)
+static KobMixPtrs kob_ptrs(double *phi, double *phi_last, double *phi_lap, double *epsilon, double *epsilon_deri,
+                           double *phidx, double *phidy, double *tempr, double *tempr_lap, void *hphi, void *hphi_lap,
+                           void *htempr, void *htempr_lap, void *hphidx, void *hphidy, void *hepsilon,
+                           void *hepsilon_deri, const int *type_curr)
+{
+    return KobMixPtrs{phi,  phi_last, phi_lap, epsilon, epsilon_deri, phidx, phidy, tempr, tempr_lap,
+                      (__half2 *)hphi, (__half2 *)hphi_lap, (__half2 *)htempr, (__half2 *)htempr_lap,
+                      (__half2 *)hphidx, (__half2 *)hphidy, (__half2 *)hepsilon, (__half2 *)hepsilon_deri, type_curr};
+}
+
+extern "C" int amps_snowflake_kernel1_mix(const amps_params *p, const double *phi, double *phi_last, double *phi_lap,
+                                          double *epsilon, double *epsilon_deri, double *phidx, double *phidy,
+                                          const double *tempr, double *tempr_lap, const void *hphi, void *hphi_lap,
+                                          const void *htempr, void *htempr_lap, void *hphidx, void *hphidy,
+                                          void *hepsilon, void *hepsilon_deri, const int *type_curr, int i,
+                                          void *stream)
+{
+    if (check_mix(p) || p->tile < 4 || !phi || !phi_lap || !epsilon || !epsilon_deri || !phidx || !phidy || !tempr ||
+        !tempr_lap || !hphi || !hphi_lap || !htempr || !htempr_lap || !hphidx || !hphidy || !hepsilon ||
+        !hepsilon_deri || !type_curr || p->cadence < 1)
+        return AMPS_ERR_INVALID;
+    const bool snap = p->monitor == AMPS_MONITOR_TEM;
+    if (snap && !phi_last) return AMPS_ERR_INVALID;
+    const KobMixPtrs m = kob_ptrs((double *)phi, phi_last, phi_lap, epsilon, epsilon_deri, phidx, phidy,
+                                  (double *)tempr, tempr_lap, (void *)hphi, hphi_lap, (void *)htempr, htempr_lap,
+                                  hphidx, hphidy, hepsilon, hepsilon_deri, type_curr);
+    kob_mix_k1<<<tiles_grid(p), pair_block(p), 0, S_>>>(geom(p), kobh(p), kobd(p), m, i, p->cadence, snap);
+    return launched();
+}
+
+extern "C" int amps_snowflake_mix_kernel2(const amps_params *p, double *phi, const double *phi_lap,
+                                          const double *epsilon, const double *epsilon_deri, const double *phidx,
+                                          const double *phidy, double *tempr, const double *tempr_lap, void *hphi,
+                                          const void *hphi_lap, const void *hepsilon, const void *hepsilon_deri,
+                                          const void *hphidx, const void *hphidy, void *htempr,
+                                          const void *htempr_lap, const int *type_curr, int i, void *stream)
+{
+    if (check_mix(p) || p->tile < 4 || !phi || !phi_lap || !epsilon || !epsilon_deri || !phidx || !phidy || !tempr ||
+        !tempr_lap || !hphi || !hphi_lap || !hepsilon || !hepsilon_deri || !hphidx || !hphidy || !htempr ||
+        !htempr_lap || !type_curr || p->cadence < 1)
+        return AMPS_ERR_INVALID;
+    const KobMixPtrs m = kob_ptrs(phi, nullptr, (double *)phi_lap, (double *)epsilon, (double *)epsilon_deri,
+                                  (double *)phidx, (double *)phidy, tempr, (double *)tempr_lap, hphi, (void *)hphi_lap,
+                                  htempr, (void *)htempr_lap, (void *)hphidx, (void *)hphidy, (void *)hepsilon,
+                                  (void *)hepsilon_deri, type_curr);
+    kob_mix_k2<<<tiles_grid(p), pair_block(p), 0, S_>>>(geom(p), kobh(p), kobd(p), m, i, p->cadence);
+    return launched();
+}
+
+extern "C" int amps_snowflake_kernel1_conversion(const amps_params *p, double *epsilon, double *epsilon_deri,
+                                                 double *phidx, double *phidy, const void *hphidx, const void *hphidy,
+                                                 const void *hepsilon, const void *hepsilon_deri,
+                                                 const int *type_curr, int i, void *stream)
+{
+    (void)i;  // the reference's conversion takes the step and does not use it
+    if (check_mix(p) || !epsilon || !epsilon_deri || !phidx || !phidy || !hphidx || !hphidy || !hepsilon ||
+        !hepsilon_deri || !type_curr)
+        return AMPS_ERR_INVALID;
+    const KobMixPtrs m = kob_ptrs(nullptr, nullptr, nullptr, epsilon, epsilon_deri, phidx, phidy, nullptr, nullptr,
+                                  nullptr, nullptr, nullptr, nullptr, (void *)hphidx, (void *)hphidy,
+                                  (void *)hepsilon, (void *)hepsilon_deri, type_curr);
+    kob_conv1<<<tiles_grid(p), pair_block(p), 0, S_>>>(geom(p), m);
+    return launched();
+}
+
+extern "C" int amps_snowflake_kernel2_conversion(const amps_params *p, double *phi, double *tempr, const void *hphi,
+                                                 const void *htempr, const int *type_curr, int i, void *stream)
+{
+    if (check_mix(p) || p->tile < 4 || !phi || !tempr || !hphi || !htempr || !type_curr || p->cadence < 1)
+        return AMPS_ERR_INVALID;
+    const KobMixPtrs m = kob_ptrs(phi, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, tempr, nullptr,
+                                  (void *)hphi, nullptr, (void *)htempr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                                  type_curr);
+    kob_conv2<<<tiles_grid(p), pair_block(p), 0, S_>>>(geom(p), m, i, p->cadence);
+    return launched();
+}
+
+extern "C" int amps_snowflake_monitor2_lastdata_store(const amps_params *p, const double *phi, double *phi_last,
+                                                      void *stream)
+{
+    return amps_graingrowth_monitor2_lastdata_store(p, phi, phi_last, stream);
+}
+
+extern "C" int amps_snowflake_data_sychro_duringcomputation(const amps_params *p, const double *phi,
+                                                            const double *tempr, void *hphi, void *htempr,
+                                                            const int *old_con, const int *new_con, void *stream)
+{
+    return amps_graingrowth_data_sychro_duringcomputation(p, phi, tempr, hphi, htempr, old_con, new_con, stream);
+}
+
+extern "C" int amps_snowflake_data_sychro_aftercomputation(const amps_params *p, double *highdata, const void *lowdata,
+                                                           const int *typedata, void *stream)
+{
+    return amps_graingrowth_data_sychro_aftercomputation(p, highdata, lowdata, typedata, stream);
+}
+
+extern "C" int amps_snowflake_highdata_to_low(const amps_params *p, const double *highdata, void *lowdata,
+                                              void *stream)
+{
+    return amps_graingrowth_highdata_to_low(p, highdata, lowdata, stream);
 }
