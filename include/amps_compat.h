@@ -195,6 +195,62 @@ AMPS_API int amps_snowflake_data_sychro_aftercomputation(const amps_params *p, d
 AMPS_API int amps_snowflake_highdata_to_low(const amps_params *p, const double *highdata, void *lowdata,
                                             void *stream);
 
+/* ---- the adaptive sintering step (AMSTENCIL) -------------------------------
+ * The same dual storage for con, eta1, eta2 and the intermediates, but a
+ * half2 word of sintering holds a tile's two halves: pair xo of tile tx (in
+ * row y) holds cells tx*tile + xo (low) and tx*tile + xo + tile/2 (high),
+ * as the reference packs them.  A type-2 tile keeps its first and last
+ * columns in the half2 output arrays, where type-1 neighbours read them. */
+
+/* sintering/function.h:161-330 -- con_lap, dfdcon and the chemical potential
+ * dummy.  With p->monitor == AMPS_MONITOR_TEM, step i with i % cadence == 0
+ * first copies every cell of con into con_last (the reference's Monitor2). */
+AMPS_API int amps_sintering_con1_mix(const amps_params *p, const int *type_curr, const double *con, double *con_last,
+                                     double *con_lap, const double *eta1, const double *eta2, double *dfdcon,
+                                     double *dummy, const void *hcon, void *hcon_lap, const void *heta1,
+                                     const void *heta2, void *hdfdcon, void *hdummy, int i, void *stream);
+/* sintering/function.h:331-482 -- con advanced in place (clamped to [0, 1]). */
+AMPS_API int amps_sintering_con2_mix(const amps_params *p, const int *type_curr, const double *dummy,
+                                     double *dummy_lap, double *con, const double *eta1, const double *eta2,
+                                     const void *hdummy, void *hdummy_lap, void *hcon, const void *heta1,
+                                     const void *heta2, int i, void *stream);
+/* sintering/function.h:483-628, 629-774 -- one particle's order parameter
+ * into eta_out (clamped to [0, 1]). */
+AMPS_API int amps_sintering_phi1_mix(const amps_params *p, const int *type_curr, const double *eta1, double *eta1_out,
+                                     const double *eta2, double *eta1_lap, double *dfdeta1, const double *con,
+                                     const void *heta1, void *heta1_out, const void *heta2, void *heta1_lap,
+                                     void *hdfdeta1, const void *hcon, int i, void *stream);
+AMPS_API int amps_sintering_phi2_mix(const amps_params *p, const int *type_curr, const double *eta2, double *eta2_out,
+                                     const double *eta1, double *eta2_lap, double *dfdeta2, const double *con,
+                                     const void *heta2, void *heta2_out, const void *heta1, void *heta2_lap,
+                                     void *hdfdeta2, const void *hcon, int i, void *stream);
+/* sintering/function.h:792-900 -- the four kernels' conversions as their own
+ * launches: type-1 tiles' edge cells (all cells when (i + 1) % cadence == 0,
+ * except for dummy) into the FP64 array, type-2 tiles' first and last
+ * columns into the half2 array. */
+AMPS_API int amps_sintering_con1_conversion(const amps_params *p, const int *type_curr, double *dummy, void *hdummy,
+                                            void *stream);
+AMPS_API int amps_sintering_con2_conversion(const amps_params *p, const int *type_curr, double *con, void *hcon,
+                                            int i, void *stream);
+AMPS_API int amps_sintering_phi1_conversion(const amps_params *p, const int *type_curr, double *eta1_out,
+                                            void *heta1_out, int i, void *stream);
+AMPS_API int amps_sintering_phi2_conversion(const amps_params *p, const int *type_curr, double *eta2_out,
+                                            void *heta2_out, int i, void *stream);
+/* sintering/function.h:778-790 -- con into con_last when i % cadence == 0. */
+AMPS_API int amps_sintering_monitor2_lastdata_store(const amps_params *p, const double *con, double *con_last, int i,
+                                                    void *stream);
+/* sintering/tools.h:57-79 -- tiles whose type went 2 -> 1 take their pairs
+ * of con, eta1, eta2 from the FP64 arrays. */
+AMPS_API int amps_sintering_data_sychro_duringcomputation(const amps_params *p, const double *con,
+                                                          const double *eta1, const double *eta2, void *hcon,
+                                                          void *heta1, void *heta2, const int *old_con,
+                                                          const int *new_con, void *stream);
+/* sintering/tools.h:80-94 -- every pair from the FP64 array. */
+AMPS_API int amps_sintering_dataprepare(const amps_params *p, const double *highdata, void *lowdata, void *stream);
+/* sintering/tools.h:95-121 -- type-1 tiles' pairs into the FP64 array. */
+AMPS_API int amps_sintering_data_sychro_aftercomputation(const amps_params *p, double *highdata, const void *lowdata,
+                                                         const int *typedata, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -332,3 +332,126 @@ def test_kobayashi_kernel2_conversion():
             exp = np.full((ny, nx), 7.0)
             exp[band] = src.astype(np.float64)[band]
             assert np.array_equal(got.cpu().numpy(), exp), step
+
+
+def sint_mix_lib():
+    L = mix_lib()
+    dp = ctypes.POINTER(w().Params)
+    I = ctypes.c_int
+    sig = {
+        "amps_sintering_con1_mix": [P] * 14 + [I],
+        "amps_sintering_con2_mix": [P] * 11 + [I],
+        "amps_sintering_phi1_mix": [P] * 13 + [I],
+        "amps_sintering_phi2_mix": [P] * 13 + [I],
+        "amps_sintering_data_sychro_duringcomputation": [P] * 8,
+        "amps_sintering_dataprepare": [P, P],
+        "amps_sintering_data_sychro_aftercomputation": [P] * 3,
+        "amps_sintering_con2_conversion": [P, P, P, I],
+    }
+    for name, args in sig.items():
+        f = getattr(L, name)
+        f.argtypes = [dp] + args + [P]
+        f.restype = ctypes.c_int
+    return L
+
+
+@pytest.mark.parametrize("monitor,thr,steps", [(1, 0.5, 200), (2, 1e-4, 200), (2, 1e-2, 120), (1, 0.1, 120)])
+def test_sintering_mixed_loop_equals_the_reference_kernels(monitor, thr, steps):
+    """sintering/main.cu's AMSTENCIL loop (Monitor1/2) through the
+    reference-named wrappers -- dataprepare of the two-particle start, per
+    period get_max_diff / get_type / data_sychro_duringcomputation,
+    con1/con2/phi1/phi2_mix a step, the final data_sychro_aftercomputation
+    -- against the reference's own kernels driven the same way: tile types
+    of every period and the final con, eta1, eta2, bit for bit."""
+    need("sintering_mix")
+    L = sint_mix_lib()
+    p = w().Params.preset("sintering", 5, mode="end2end_mix", monitor=monitor, thr_lo=thr, thr_hi=thr)
+    with refcuda.Module("sintering_mix") as m:
+        assert (m.nx, m.ny, m.ux, m.uy) == (p.nx, p.ny, p.tile, p.tile)
+    f0 = w().init_host(p.replace(ref_order=1), w().INIT_REFERENCE)
+    pp = ctypes.byref(p)
+    nx, ny, T = p.nx, p.ny, p.tile
+    tiles = (nx // T) * (ny // T)
+    f64 = lambda: torch.zeros((ny, nx), dtype=torch.float64, device="cuda")
+    con, e1, e2 = (torch.tensor(np.ascontiguousarray(f0[k]), dtype=torch.float64, device="cuda") for k in range(3))
+    last = (con == 0).double()  # main.cu:61-64
+    e1o, e2o, clap, l1, l2, mu, mulap, dfc, d1, d2 = (f64() for _ in range(10))
+    hc, h1, h2, h1o, h2o, hclap, hl1, hl2, hmu, hmulap, hdfc, hd1, hd2 = half2s(p, 13)
+    tcur = torch.zeros(tiles, dtype=torch.int32, device="cuda")
+    told = torch.zeros(tiles, dtype=torch.int32, device="cuda")
+    md = torch.zeros(tiles, dtype=torch.float64, device="cuda")
+    for f, h in ((con, hc), (e1, h1), (e2, h2)):
+        assert L.amps_sintering_dataprepare(pp, ptr(f), ptr(h), None) == 0
+    types = []
+    for i in range(steps):
+        if i % 10 == 0:
+            if monitor == 1:
+                assert L.amps_get_max_diff1(pp, ptr(con), ptr(md), None) == 0
+            else:
+                assert L.amps_get_max_diff2(pp, ptr(last), ptr(con), ptr(md), None) == 0
+            assert L.amps_get_type(pp, ptr(md), ptr(told), ptr(tcur), None) == 0
+            assert L.amps_sintering_data_sychro_duringcomputation(pp, ptr(con), ptr(e1), ptr(e2), ptr(hc), ptr(h1),
+                                                                  ptr(h2), ptr(told), ptr(tcur), None) == 0
+            types.append(tcur.cpu().numpy().astype(np.uint8))
+        assert L.amps_sintering_con1_mix(pp, ptr(tcur), ptr(con), ptr(last), ptr(clap), ptr(e1), ptr(e2), ptr(dfc),
+                                         ptr(mu), ptr(hc), ptr(hclap), ptr(h1), ptr(h2), ptr(hdfc), ptr(hmu), i,
+                                         None) == 0
+        assert L.amps_sintering_con2_mix(pp, ptr(tcur), ptr(mu), ptr(mulap), ptr(con), ptr(e1), ptr(e2), ptr(hmu),
+                                         ptr(hmulap), ptr(hc), ptr(h1), ptr(h2), i, None) == 0
+        assert L.amps_sintering_phi1_mix(pp, ptr(tcur), ptr(e1), ptr(e1o), ptr(e2), ptr(l1), ptr(d1), ptr(con),
+                                         ptr(h1), ptr(h1o), ptr(h2), ptr(hl1), ptr(hd1), ptr(hc), i, None) == 0
+        assert L.amps_sintering_phi2_mix(pp, ptr(tcur), ptr(e2), ptr(e2o), ptr(e1), ptr(l2), ptr(d2), ptr(con),
+                                         ptr(h2), ptr(h2o), ptr(h1), ptr(hl2), ptr(hd2), ptr(hc), i, None) == 0
+        e1, e1o, e2, e2o = e1o, e1, e2o, e2
+        h1, h1o, h2, h2o = h1o, h1, h2o, h2
+    for f, h in ((con, hc), (e1, h1), (e2, h2)):
+        assert L.amps_sintering_data_sychro_aftercomputation(pp, ptr(f), ptr(h), ptr(tcur), None) == 0
+    torch.cuda.synchronize()
+    rc, r1, r2, rtypes, _ = refcuda.sint_mix(steps, thr, monitor, f0[0], f0[1], f0[2])
+    ours = np.stack(types)
+    mix = np.bincount(ours.ravel(), minlength=3)[1:] / ours.size
+    bad = [k for k in range(rtypes.shape[0]) if not np.array_equal(ours[k], rtypes[k])]
+    fc, f1, f2 = con.cpu().numpy(), e1.cpu().numpy(), e2.cpu().numpy()
+    d = max(float(np.abs(a - b).max()) for a, b in ((fc, rc), (f1, r1), (f2, r2)))
+    print(f"sintering mixed loop, monitor {monitor} {thr:g}, {steps} steps: tile types half/FP64 {mix}, "
+          f"periods differing {bad[:5]}, fields max |diff| {d:.3e}")
+    assert not bad
+    assert np.array_equal(fc, rc) and np.array_equal(f1, r1) and np.array_equal(f2, r2)
+
+
+def test_sintering_con2_conversion():
+    """con2_conversion against a numpy statement of
+    sintering/function.h:824-853: type-1 tiles' edge cells (all of them at a
+    period's last step) into the FP64 array, type-2 tiles' first and last
+    columns into the half2 array, in sintering's tile-halves packing."""
+    L = sint_mix_lib()
+    p = w().Params.preset("sintering", 5, mode="end2end_mix")
+    pp = ctypes.byref(p)
+    nx, ny, T = p.nx, p.ny, p.tile
+    th = T // 2
+    rng = np.random.default_rng(6)
+    hv = rng.uniform(0, 1, (ny, nx)).astype(np.float16)  # pair-major: [y][pair][low, high]
+    fv = rng.uniform(0, 1, (ny, nx))
+    ty = rng.integers(1, 3, (ny // T, nx // T)).astype(np.int32)
+    dty = torch.tensor(ty, device="cuda")
+    yy, pp_ = np.mgrid[0:ny, 0:nx // 2]
+    tx, xo = pp_ // th, pp_ % th
+    lo_cell, hi_cell = tx * T + xo, tx * T + xo + th
+    for step in (3, 9):
+        dh = torch.tensor(hv.view(np.int32).copy(), device="cuda")
+        df = torch.tensor(fv, device="cuda")
+        assert L.amps_sintering_con2_conversion(pp, ptr(dty), ptr(df), ptr(dh), step, None) == 0
+        ef, eh = fv.copy(), hv.copy().reshape(ny, nx // 2, 2)
+        low = ty[yy // T, tx] == 1
+        yo = yy % T
+        full = low & ((yo == 0) | (yo == T - 1) | ((step + 1) % 10 == 0))
+        pairs = hv.reshape(ny, nx // 2, 2).astype(np.float64)
+        for mask, cell, half in ((full | (low & (xo == 0)), lo_cell, 0), (full | (low & (xo == th - 1)), hi_cell, 1)):
+            ef[yy[mask], cell[mask]] = pairs[..., half][mask]
+        high = ~low
+        first = high & (xo == 0)
+        eh[yy[first], pp_[first], 0] = fv[yy[first], lo_cell[first]].astype(np.float32).astype(np.float16)
+        last = high & (xo == th - 1)
+        eh[yy[last], pp_[last], 1] = fv[yy[last], hi_cell[last]].astype(np.float32).astype(np.float16)
+        assert np.array_equal(df.cpu().numpy(), ef), step
+        assert np.array_equal(dh.cpu().numpy().view(np.float16).reshape(ny, nx // 2, 2), eh), step

@@ -633,6 +633,299 @@ __global__ void kob_conv2(GeoM g, KobMixPtrs m, int step, int cadence)
     m.tempr[c + 1] = __high2float(m.htempr[i]);
 }
 
+// ---- the adaptive (AMSTENCIL) sintering step, sintering/function.h:161-774 ----
+// Sintering packs a tile's two halves into its half2 words: pair xo of tile
+// tx holds cells x0 + xo (low) and x0 + xo + T/2 (high), x0 = tx * T.  A low
+// tile reads its x neighbours from the half2 arrays only (high tiles keep
+// their first and last columns there, written after each update) and its y
+// neighbours from the FP64 arrays where the tile above / below is high.
+struct SintH {
+    __half2 cf, dxdy, zpfive, one, two, four, six, ten, twelve, fifteen, thirtytwo, coefm, coefk, coefl, dvol, dvap,
+        dsur, dgrb, dt, hi, lo;
+};
+// the FP64 constants the reference's compile-time expressions fold:
+// 0.5 * coefm, 0.5 * coefk, dtime * coefl
+struct SintD {
+    double dxdy, hcoefm, hcoefk, dtcoefl, dt, dvol, dvap, dsur, dgrb;
+};
+
+// the x and y neighbour pairs of a low tile's pair (sintering/function.h:213-216)
+struct NbH {
+    __half2 xs1, xa1, ys1, ya1;
+};
+__device__ __forceinline__ NbH nb_low(const GeoM &g, const TileAt &t, const int *type, const __half2 *h,
+                                      const double *f)
+{
+    const int np = g.nx / 2, th = t.th;
+    const int x = t.tx * th + t.xo, y = t.y;
+    const int xs1 = x > 0 ? x - 1 : np - 1, xa1 = x < np - 1 ? x + 1 : 0;
+    const int ys1 = y > 0 ? y - 1 : g.ny - 1, ya1 = y < g.ny - 1 ? y + 1 : 0;
+    auto H = [&](int yy, int xx) { return h[(int64_t)yy * np + xx]; };
+    const int cl = t.tx * g.T + t.xo;  // the pair's low cell
+    NbH n;
+    n.xs1 = t.xo > 0 ? H(y, xs1) : __halves2half2(__high2half(H(y, xs1)), __low2half(H(y, x + th - 1)));
+    n.xa1 = t.xo < th - 1 ? H(y, xa1) : __halves2half2(__high2half(H(y, x - th + 1)), __low2half(H(y, xa1)));
+    n.ys1 = (t.yo == 0 && type[t.tys1 * g.ntx + t.tx] == 2)
+                ? __floats2half2_rn(f[(int64_t)ys1 * g.nx + cl], f[(int64_t)ys1 * g.nx + cl + th])
+                : H(ys1, x);
+    n.ya1 = (t.yo == g.T - 1 && type[t.tya1 * g.ntx + t.tx] == 2)
+                ? __floats2half2_rn(f[(int64_t)ya1 * g.nx + cl], f[(int64_t)ya1 * g.nx + cl + th])
+                : H(ya1, x);
+    return n;
+}
+
+// a low tile's pair into the FP64 array: both cells on the tile's first and
+// last rows (and, with `all`, everywhere), else the first / last column's cell
+__device__ __forceinline__ void low_to_f64(const GeoM &g, const TileAt &t, __half2 v, double *f, bool all)
+{
+    const int64_t c = (int64_t)t.y * g.nx + t.tx * g.T + t.xo;
+    if (t.yo == 0 || t.yo == g.T - 1 || all) {
+        f[c] = __low2float(v);
+        f[c + t.th] = __high2float(v);
+    } else if (t.xo == 0) {
+        f[c] = __low2float(v);
+    } else if (t.xo == t.th - 1) {
+        f[c + t.th] = __high2float(v);
+    }
+}
+
+// a high tile's first / last column cell into the half2 array (the low half
+// of the tile's first pair, the high half of its last pair)
+__device__ __forceinline__ void high_edge_to_h2(const GeoM &g, const TileAt &t, int cx, double v, __half2 *h)
+{
+    const int64_t row = (int64_t)t.y * (g.nx / 2);
+    if (cx == 0) {
+        __half2 &w = h[row + t.tx * t.th];
+        w = __halves2half2(__float2half(v), __high2half(w));
+    }
+    if (cx == g.T - 1) {
+        __half2 &w = h[row + t.tx * t.th + t.th - 1];
+        w = __halves2half2(__low2half(w), __float2half(v));
+    }
+}
+
+struct SintPtrs {
+    double *con, *last, *con_lap, *eta1, *eta2, *dfd, *dummy, *dummy_lap;
+    __half2 *hcon, *hcon_lap, *heta1, *heta2, *hdfd, *hdummy, *hdummy_lap;
+    const int *type;
+};
+
+// sintering/function.h:161-330: con_lap, dfdcon and the chemical potential (dummy)
+__global__ void sint_con1_k(GeoM g, SintH c, SintD d, SintPtrs m, int step, int cadence, bool snap)
+{
+    const TileAt t = tile_at(g);
+    const int own = m.type[t.ty * g.ntx + t.tx];
+    const int y = t.y, nx = g.nx, np = g.nx / 2;
+    const int64_t row = (int64_t)y * nx;
+    // Monitor2: every cell of con at the period's first step
+    if (snap && step % cadence == 0) {
+        m.last[row + t.c0] = m.con[row + t.c0];
+        m.last[row + t.c0 + t.th] = m.con[row + t.c0 + t.th];
+    }
+    if (own == 1) {
+        const int64_t i = (int64_t)y * np + t.tx * t.th + t.xo;
+        const NbH n = nb_low(g, t, m.type, m.hcon, m.con);
+        const __half2 cc = m.hcon[i], e1 = m.heta1[i], e2 = m.heta2[i];
+        const __half2 lap = (n.xs1 + n.xa1 + n.ys1 + n.ya1 - c.cf * cc) / c.dxdy;
+        m.hcon_lap[i] = lap;
+        const __half2 sum2 = e1 * e1 + e2 * e2;
+        const __half2 sum3 = e1 * e1 * e1 + e2 * e2 * e2;
+        const __half2 f = (c.two * cc + c.four * sum3 - c.six * sum2) - c.thirtytwo * (cc * cc) * (c.one - cc) +
+                          c.thirtytwo * cc * ((c.one - cc) * (c.one - cc));
+        m.hdfd[i] = f;
+        const __half2 mu = f - c.zpfive * c.coefm * lap;
+        m.hdummy[i] = mu;
+        low_to_f64(g, t, mu, m.dummy, false);
+        return;
+    }
+    for (int k = 0; k < 2; ++k) {
+        const int cx = t.xo + k * t.th, x = t.tx * g.T + cx;
+        const int xs1 = x > 0 ? x - 1 : nx - 1, xa1 = x < nx - 1 ? x + 1 : 0;
+        const int ys1 = y > 0 ? y - 1 : g.ny - 1, ya1 = y < g.ny - 1 ? y + 1 : 0;
+        auto C = [&](int yy, int xx) { return m.con[(int64_t)yy * nx + xx]; };
+        const int64_t i = row + x;
+        const double lap = (C(y, xs1) + C(y, xa1) + C(ys1, x) + C(ya1, x) - 4.0 * C(y, x)) / d.dxdy;
+        m.con_lap[i] = lap;
+        const double e1 = m.eta1[i], e2 = m.eta2[i], cc = m.con[i];
+        const double sum2 = pow(e1, 2) + pow(e2, 2);
+        const double sum3 = pow(e1, 3) + pow(e2, 3);
+        const double f = 1.0 * (2.0 * cc + 4.0 * sum3 - 6.0 * sum2) - 2.0 * 16.0 * pow(cc, 2) * (1.0 - cc) +
+                         2.0 * 16.0 * cc * pow(1.0 - cc, 2);
+        m.dfd[i] = f;
+        const double mu = f - d.hcoefm * lap;
+        m.dummy[i] = mu;
+        high_edge_to_h2(g, t, cx, mu, m.hdummy);
+    }
+}
+
+// sintering/function.h:331-482: con advanced by the mobility times the potential's Laplacian, clamped to [0, 1]
+__global__ void sint_con2_k(GeoM g, SintH c, SintD d, SintPtrs m, int step, int cadence)
+{
+    const TileAt t = tile_at(g);
+    const int own = m.type[t.ty * g.ntx + t.tx];
+    const int y = t.y, nx = g.nx, np = g.nx / 2;
+    const int64_t row = (int64_t)y * nx;
+    if (own == 1) {
+        const int64_t i = (int64_t)y * np + t.tx * t.th + t.xo;
+        const NbH n = nb_low(g, t, m.type, m.hdummy, m.dummy);
+        const __half2 lap = (n.xs1 + n.xa1 + n.ys1 + n.ya1 - c.cf * m.hdummy[i]) / c.dxdy;
+        m.hdummy_lap[i] = lap;
+        const __half2 cc = m.hcon[i];
+        const __half2 phi = cc * cc * cc * (c.ten - c.fifteen * cc + c.six * (cc * cc));
+        const __half2 sum = m.heta1[i] * m.heta2[i] * c.two;
+        const __half2 mob = c.dvol * phi + c.dvap * (c.one - phi) + c.dsur * cc * (c.one - cc) + c.dgrb * sum;
+        __half2 v = cc + c.dt * mob * lap;
+        v = __hmin2(c.hi, v);
+        v = __hmax2(c.lo, v);
+        m.hcon[i] = v;
+        low_to_f64(g, t, v, m.con, (step + 1) % cadence == 0);
+        return;
+    }
+    for (int k = 0; k < 2; ++k) {
+        const int cx = t.xo + k * t.th, x = t.tx * g.T + cx;
+        const int xs1 = x > 0 ? x - 1 : nx - 1, xa1 = x < nx - 1 ? x + 1 : 0;
+        const int ys1 = y > 0 ? y - 1 : g.ny - 1, ya1 = y < g.ny - 1 ? y + 1 : 0;
+        auto D = [&](int yy, int xx) { return m.dummy[(int64_t)yy * nx + xx]; };
+        const int64_t i = row + x;
+        const double lap = (D(y, xs1) + D(y, xa1) + D(ys1, x) + D(ya1, x) - 4.0 * D(y, x)) / d.dxdy;
+        m.dummy_lap[i] = lap;
+        const double cc = m.con[i];
+        const double phi = pow(cc, 3) * (10.0 - 15.0 * cc + 6.0 * pow(cc, 2));
+        const double sum = m.eta1[i] * m.eta2[i] * 2;
+        const double mob = d.dvol * phi + d.dvap * (1.0 - phi) + d.dsur * cc * (1.0 - cc) + d.dgrb * sum;
+        double v = cc + d.dt * mob * lap;
+        if (v >= 1) v = 1;
+        else if (v < 0) v = 0;
+        m.con[i] = v;
+        high_edge_to_h2(g, t, cx, v, m.hcon);
+    }
+}
+
+struct SintPhiPtrs {
+    const double *a, *b, *con;  // this order parameter, the other one, con
+    double *out, *lap, *dfd;
+    const __half2 *ha, *hb, *hcon;
+    __half2 *hout, *hlap, *hdfd;
+    const int *type;
+};
+
+// sintering/function.h:483-774 (phi1_mix, and phi2_mix with the fields
+// swapped): one order parameter's update, clamped to [0, 1].  The sum of
+// squares keeps the reference's operand order, eta1's term first (SECOND:
+// this is eta2), in two kernels as the reference has them: the compiler
+// canonicalises a run-time choice between the two orders into one, and the
+// two orders can round differently once a product is fused.
+template <bool SECOND>
+__global__ void sint_phi_k(GeoM g, SintH c, SintD d, SintPhiPtrs m, int step, int cadence)
+{
+    const TileAt t = tile_at(g);
+    const int own = m.type[t.ty * g.ntx + t.tx];
+    const int y = t.y, nx = g.nx, np = g.nx / 2;
+    const int64_t row = (int64_t)y * nx;
+    if (own == 1) {
+        const int64_t i = (int64_t)y * np + t.tx * t.th + t.xo;
+        const NbH n = nb_low(g, t, m.type, m.ha, m.a);
+        const __half2 e = m.ha[i], o = m.hb[i], cc = m.hcon[i];
+        const __half2 lap = (n.xs1 + n.xa1 + n.ys1 + n.ya1 - c.cf * e) / c.dxdy;
+        m.hlap[i] = lap;
+        __half2 sum2;
+        if constexpr (SECOND) sum2 = (o * o) + (e * e);
+        else sum2 = (e * e) + (o * o);
+        const __half2 f = c.one * (-c.twelve * (e * e) * (c.two - cc) + c.twelve * e * (c.one - cc) + c.twelve * e * sum2);
+        m.hdfd[i] = f;
+        __half2 v = e - c.dt * c.coefl * (f - c.zpfive * c.coefk * lap);
+        v = __hmin2(c.hi, v);
+        v = __hmax2(c.lo, v);
+        m.hout[i] = v;
+        low_to_f64(g, t, v, m.out, (step + 1) % cadence == 0);
+        return;
+    }
+    for (int k = 0; k < 2; ++k) {
+        const int cx = t.xo + k * t.th, x = t.tx * g.T + cx;
+        const int xs1 = x > 0 ? x - 1 : nx - 1, xa1 = x < nx - 1 ? x + 1 : 0;
+        const int ys1 = y > 0 ? y - 1 : g.ny - 1, ya1 = y < g.ny - 1 ? y + 1 : 0;
+        auto A = [&](int yy, int xx) { return m.a[(int64_t)yy * nx + xx]; };
+        const int64_t i = row + x;
+        const double lap = (A(y, xs1) + A(y, xa1) + A(ys1, x) + A(ya1, x) - 4.0 * A(y, x)) / d.dxdy;
+        m.lap[i] = lap;
+        const double e = m.a[i], cc = m.con[i];
+        double sum2;
+        if constexpr (SECOND) sum2 = pow(m.b[i], 2) + pow(e, 2);
+        else sum2 = pow(e, 2) + pow(m.b[i], 2);
+        // the reference's expression with its multiply-adds fused as its
+        // build fuses them (each sum takes the product on its left; the
+        // update, e - dtime*coefl*(...), one fused step), stated with
+        // explicit roundings: inlined in this kernel the compiler left the
+        // last one unfused
+        const double m12 = __dmul_rn(12.0, e);
+        const double s12 = __fma_rn(__dmul_rn(-12.0, pow(e, 2)), 2.0 - cc, __dmul_rn(m12, 1.0 - cc));
+        const double f = __fma_rn(m12, sum2, s12);
+        m.dfd[i] = f;
+        double v = __fma_rn(-d.dtcoefl, __fma_rn(-d.hcoefk, lap, f), e);
+        if (v >= 1) v = 1;
+        else if (v < 0) v = 0;
+        m.out[i] = v;
+        high_edge_to_h2(g, t, cx, v, (__half2 *)m.hout);
+    }
+}
+
+// sintering/function.h:792-900: the conversions of con1/con2/phi1/phi2_mix as
+// their own launches (`all`: every low-tile cell at a period's last step,
+// when the field's conversion has that clause)
+__global__ void sint_conv_k(GeoM g, const int *type, double *f, __half2 *h, int step, int cadence, bool period_clause)
+{
+    const TileAt t = tile_at(g);
+    if (type[t.ty * g.ntx + t.tx] == 1) {
+        const __half2 v = h[(int64_t)t.y * (g.nx / 2) + t.tx * t.th + t.xo];
+        low_to_f64(g, t, v, f, period_clause && (step + 1) % cadence == 0);
+        return;
+    }
+    for (int k = 0; k < 2; ++k) {
+        const int cx = t.xo + k * t.th;
+        high_edge_to_h2(g, t, cx, f[(int64_t)t.y * g.nx + t.tx * g.T + cx], h);
+    }
+}
+
+// sintering/tools.h:57-79: tiles turning high -> low take their pairs of con, eta1, eta2 from the FP64 arrays
+__global__ void sint_sync_during(GeoM g, const double *c, const double *e1, const double *e2, __half2 *hc,
+                                 __half2 *h1, __half2 *h2p, const int *old_t, const int *new_t)
+{
+    const TileAt t = tile_at(g);
+    const int tile = t.ty * g.ntx + t.tx;
+    if (!(old_t[tile] == 2 && new_t[tile] == 1)) return;
+    const int64_t i = (int64_t)t.y * (g.nx / 2) + t.tx * t.th + t.xo, f = (int64_t)t.y * g.nx + t.c0;
+    hc[i] = __floats2half2_rn(c[f], c[f + t.th]);
+    h1[i] = __floats2half2_rn(e1[f], e1[f + t.th]);
+    h2p[i] = __floats2half2_rn(e2[f], e2[f + t.th]);
+}
+
+// sintering/tools.h:80-94 and 95-121: every pair from the FP64 array / low tiles' pairs into it
+__global__ void sint_to_low(GeoM g, const double *f, __half2 *h)
+{
+    const TileAt t = tile_at(g);
+    const int64_t c = (int64_t)t.y * g.nx + t.c0;
+    h[(int64_t)t.y * (g.nx / 2) + t.tx * t.th + t.xo] = __floats2half2_rn(f[c], f[c + t.th]);
+}
+__global__ void sint_sync_after(GeoM g, double *f, const __half2 *h, const int *type)
+{
+    const TileAt t = tile_at(g);
+    if (type[t.ty * g.ntx + t.tx] != 1) return;
+    const __half2 v = h[(int64_t)t.y * (g.nx / 2) + t.tx * t.th + t.xo];
+    const int64_t c = (int64_t)t.y * g.nx + t.c0;
+    f[c] = __low2float(v);
+    f[c + t.th] = __high2float(v);
+}
+
+// sintering/function.h:778-790: con into con_last at a period's first step
+__global__ void sint_last_k(GeoM g, const double *con, double *last, int step, int cadence)
+{
+    if (step % cadence) return;
+    const TileAt t = tile_at(g);
+    const int64_t c = (int64_t)t.y * g.nx + t.c0;
+    last[c] = con[c];
+    last[c + t.th] = con[c + t.th];
+}
+
 // graingrowth/tools.h:24-38 -- the initial circle in FP64 arrays, one cell a thread
 __global__ void gg_prep_high(int nx, int ny, float rx, float ry, float r, double *e1, double *e2)
 {
@@ -733,6 +1026,19 @@ int check_mix(const amps_params *p)
 GeoM geom(const amps_params *p) { return GeoM{p->nx, p->ny, p->tile, p->nx / p->tile, p->ny / p->tile}; }
 dim3 tiles_grid(const amps_params *p) { return dim3((unsigned)((p->nx / p->tile) * (p->ny / p->tile))); }
 dim3 pair_block(const amps_params *p) { return dim3((unsigned)(p->tile / 2), (unsigned)p->tile); }
+// sintering/tools.h:122-127: each constant as __floats2half2_rn(v, v)
+SintH sinth(const amps_params *p)
+{
+    return SintH{h2(4.0),      h2(p->dx * p->dy), h2(0.5),      h2(1.0),      h2(2.0),      h2(4.0),
+                 h2(6.0),      h2(10.0),          h2(12.0),     h2(15.0),     h2(32.0),     h2(p->coefm),
+                 h2(p->coefk), h2(p->coefl),      h2(p->dvol),  h2(p->dvap),  h2(p->dsur),  h2(p->dgrb),
+                 h2(p->dt),    h2(1.0),           h2(0.0)};
+}
+SintD sintd(const amps_params *p)
+{
+    return SintD{p->dx * p->dy, 0.5 * p->coefm, 0.5 * p->coefk, p->dt * p->coefl, p->dt,
+                 p->dvol,       p->dvap,        p->dsur,        p->dgrb};
+}
 KobD kobd(const amps_params *p)
 {
     return KobD{p->dx * p->dy, 2.0 * p->dx, 2.0 * p->dy, p->epsb, p->delta, p->aniso, p->theta0,
@@ -985,4 +1291,138 @@ extern "C" int amps_snowflake_highdata_to_low(const amps_params *p, const double
                                               void *stream)
 {
     return amps_graingrowth_highdata_to_low(p, highdata, lowdata, stream);
+}
+
+extern "C" int amps_sintering_con1_mix(const amps_params *p, const int *type_curr, const double *con, double *con_last,
+                                       double *con_lap, const double *eta1, const double *eta2, double *dfdcon,
+                                       double *dummy, const void *hcon, void *hcon_lap, const void *heta1,
+                                       const void *heta2, void *hdfdcon, void *hdummy, int i, void *stream)
+{
+    if (check_mix(p) || !type_curr || !con || !con_lap || !eta1 || !eta2 || !dfdcon || !dummy || !hcon ||
+        !hcon_lap || !heta1 || !heta2 || !hdfdcon || !hdummy || p->cadence < 1)
+        return AMPS_ERR_INVALID;
+    const bool snap = p->monitor == AMPS_MONITOR_TEM;
+    if (snap && !con_last) return AMPS_ERR_INVALID;
+    const SintPtrs m{(double *)con, con_last, con_lap, (double *)eta1, (double *)eta2, dfdcon, dummy, nullptr,
+                     (__half2 *)hcon, (__half2 *)hcon_lap, (__half2 *)heta1, (__half2 *)heta2, (__half2 *)hdfdcon,
+                     (__half2 *)hdummy, nullptr, type_curr};
+    sint_con1_k<<<tiles_grid(p), pair_block(p), 0, S_>>>(geom(p), sinth(p), sintd(p), m, i, p->cadence, snap);
+    return launched();
+}
+
+extern "C" int amps_sintering_con2_mix(const amps_params *p, const int *type_curr, const double *dummy,
+                                       double *dummy_lap, double *con, const double *eta1, const double *eta2,
+                                       const void *hdummy, void *hdummy_lap, void *hcon, const void *heta1,
+                                       const void *heta2, int i, void *stream)
+{
+    if (check_mix(p) || !type_curr || !dummy || !dummy_lap || !con || !eta1 || !eta2 || !hdummy || !hdummy_lap ||
+        !hcon || !heta1 || !heta2 || p->cadence < 1)
+        return AMPS_ERR_INVALID;
+    const SintPtrs m{con, nullptr, nullptr, (double *)eta1, (double *)eta2, nullptr, (double *)dummy, dummy_lap,
+                     (__half2 *)hcon, nullptr, (__half2 *)heta1, (__half2 *)heta2, nullptr, (__half2 *)hdummy,
+                     (__half2 *)hdummy_lap, type_curr};
+    sint_con2_k<<<tiles_grid(p), pair_block(p), 0, S_>>>(geom(p), sinth(p), sintd(p), m, i, p->cadence);
+    return launched();
+}
+
+static int sint_phi(const amps_params *p, const int *type_curr, const double *eta, double *eta_out,
+                    const double *other, double *eta_lap, double *dfdeta, const double *con, const void *heta,
+                    void *heta_out, const void *hother, void *heta_lap, void *hdfdeta, const void *hcon, int i,
+                    bool second, void *stream)
+{
+    if (check_mix(p) || !type_curr || !eta || !eta_out || !other || !eta_lap || !dfdeta || !con || !heta ||
+        !heta_out || !hother || !heta_lap || !hdfdeta || !hcon || eta == eta_out || heta == heta_out ||
+        p->cadence < 1)
+        return AMPS_ERR_INVALID;
+    const SintPhiPtrs m{eta, other, con, eta_out, eta_lap, dfdeta, (const __half2 *)heta, (const __half2 *)hother,
+                        (const __half2 *)hcon, (__half2 *)heta_out, (__half2 *)heta_lap, (__half2 *)hdfdeta,
+                        type_curr};
+    if (second) sint_phi_k<true><<<tiles_grid(p), pair_block(p), 0, S_>>>(geom(p), sinth(p), sintd(p), m, i, p->cadence);
+    else sint_phi_k<false><<<tiles_grid(p), pair_block(p), 0, S_>>>(geom(p), sinth(p), sintd(p), m, i, p->cadence);
+    return launched();
+}
+
+extern "C" int amps_sintering_phi1_mix(const amps_params *p, const int *type_curr, const double *eta1,
+                                       double *eta1_out, const double *eta2, double *eta1_lap, double *dfdeta1,
+                                       const double *con, const void *heta1, void *heta1_out, const void *heta2,
+                                       void *heta1_lap, void *hdfdeta1, const void *hcon, int i, void *stream)
+{
+    return sint_phi(p, type_curr, eta1, eta1_out, eta2, eta1_lap, dfdeta1, con, heta1, heta1_out, heta2, heta1_lap,
+                    hdfdeta1, hcon, i, false, stream);
+}
+
+extern "C" int amps_sintering_phi2_mix(const amps_params *p, const int *type_curr, const double *eta2,
+                                       double *eta2_out, const double *eta1, double *eta2_lap, double *dfdeta2,
+                                       const double *con, const void *heta2, void *heta2_out, const void *heta1,
+                                       void *heta2_lap, void *hdfdeta2, const void *hcon, int i, void *stream)
+{
+    return sint_phi(p, type_curr, eta2, eta2_out, eta1, eta2_lap, dfdeta2, con, heta2, heta2_out, heta1, heta2_lap,
+                    hdfdeta2, hcon, i, true, stream);
+}
+
+static int sint_conv(const amps_params *p, const int *type_curr, double *f, void *h, int i, bool clause,
+                     void *stream)
+{
+    if (check_mix(p) || !type_curr || !f || !h || p->cadence < 1) return AMPS_ERR_INVALID;
+    sint_conv_k<<<tiles_grid(p), pair_block(p), 0, S_>>>(geom(p), type_curr, f, (__half2 *)h, i, p->cadence, clause);
+    return launched();
+}
+
+extern "C" int amps_sintering_con1_conversion(const amps_params *p, const int *type_curr, double *dummy,
+                                              void *hdummy, void *stream)
+{
+    return sint_conv(p, type_curr, dummy, hdummy, 0, false, stream);
+}
+
+extern "C" int amps_sintering_con2_conversion(const amps_params *p, const int *type_curr, double *con, void *hcon,
+                                              int i, void *stream)
+{
+    return sint_conv(p, type_curr, con, hcon, i, true, stream);
+}
+
+extern "C" int amps_sintering_phi1_conversion(const amps_params *p, const int *type_curr, double *eta1_out,
+                                              void *heta1_out, int i, void *stream)
+{
+    return sint_conv(p, type_curr, eta1_out, heta1_out, i, true, stream);
+}
+
+extern "C" int amps_sintering_phi2_conversion(const amps_params *p, const int *type_curr, double *eta2_out,
+                                              void *heta2_out, int i, void *stream)
+{
+    return sint_conv(p, type_curr, eta2_out, heta2_out, i, true, stream);
+}
+
+extern "C" int amps_sintering_monitor2_lastdata_store(const amps_params *p, const double *con, double *con_last,
+                                                      int i, void *stream)
+{
+    if (check_mix(p) || !con || !con_last || p->cadence < 1) return AMPS_ERR_INVALID;
+    sint_last_k<<<tiles_grid(p), pair_block(p), 0, S_>>>(geom(p), con, con_last, i, p->cadence);
+    return launched();
+}
+
+extern "C" int amps_sintering_data_sychro_duringcomputation(const amps_params *p, const double *con,
+                                                            const double *eta1, const double *eta2, void *hcon,
+                                                            void *heta1, void *heta2, const int *old_con,
+                                                            const int *new_con, void *stream)
+{
+    if (check_mix(p) || !con || !eta1 || !eta2 || !hcon || !heta1 || !heta2 || !old_con || !new_con)
+        return AMPS_ERR_INVALID;
+    sint_sync_during<<<tiles_grid(p), pair_block(p), 0, S_>>>(geom(p), con, eta1, eta2, (__half2 *)hcon,
+                                                              (__half2 *)heta1, (__half2 *)heta2, old_con, new_con);
+    return launched();
+}
+
+extern "C" int amps_sintering_dataprepare(const amps_params *p, const double *highdata, void *lowdata, void *stream)
+{
+    if (check_mix(p) || !highdata || !lowdata) return AMPS_ERR_INVALID;
+    sint_to_low<<<tiles_grid(p), pair_block(p), 0, S_>>>(geom(p), highdata, (__half2 *)lowdata);
+    return launched();
+}
+
+extern "C" int amps_sintering_data_sychro_aftercomputation(const amps_params *p, double *highdata, const void *lowdata,
+                                                           const int *typedata, void *stream)
+{
+    if (check_mix(p) || !highdata || !lowdata || !typedata) return AMPS_ERR_INVALID;
+    sint_sync_after<<<tiles_grid(p), pair_block(p), 0, S_>>>(geom(p), highdata, (const __half2 *)lowdata, typedata);
+    return launched();
 }
