@@ -733,8 +733,8 @@ static int launch_step(amps_handle *h, int step_off, bool monitor_now)
         const bool after64 = h->used[TIER_FP64] && !h->profiling;
         if (fused) e = p.model == AMPS_KOBAYASHI ? kob_launch_lo(h->T, a, h->ntiles, st, after64)
                                                  : sint_launch_lo(h->T, p.mu_lap_fp64 != 0, a, h->ntiles, st, after64);
-        else if (p.model == AMPS_KOBAYASHI) e = kob_launch(h->T, t, ref, a, h->ntiles, st);
-        else e = sint_launch(h->T, t, ref, p.mu_lap_fp64 != 0, a, h->ntiles, st);
+        else if (p.model == AMPS_KOBAYASHI) e = kob_launch(h->T, t, ref, a, h->ntiles, st, !h->profiling);
+        else e = sint_launch(h->T, t, ref, p.mu_lap_fp64 != 0, a, h->ntiles, st, !h->profiling);
         if (e != cudaSuccess) FAIL(h, AMPS_ERR_CUDA, "step kernel launch: %s", cudaGetErrorString(e));
         ++h->launches;
         if (h->profiling) {

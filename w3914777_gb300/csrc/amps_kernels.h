@@ -7,8 +7,10 @@ namespace amps {
 // tm (nullable): tensor map of the step's FP32 input, used when a.tma_stage.
 cudaError_t gg_launch(int tile, int tier, bool ref, const StepArgs &a, int grid, cudaStream_t s,
                       const CUtensorMap *tm = nullptr);
-cudaError_t kob_launch(int tile, int tier, bool ref, const StepArgs &a, int grid, cudaStream_t s);
-cudaError_t sint_launch(int tile, int tier, bool ref, bool mu64, const StepArgs &a, int grid, cudaStream_t s);
+// pdl: launched programmatically after the stream's previous grid (the kernel waits for it first)
+cudaError_t kob_launch(int tile, int tier, bool ref, const StepArgs &a, int grid, cudaStream_t s, bool pdl = false);
+cudaError_t sint_launch(int tile, int tier, bool ref, bool mu64, const StepArgs &a, int grid, cudaStream_t s,
+                        bool pdl = false);
 size_t gg_smem_bytes(int tile, int tier, int nf);
 // Kobayashi / sintering: the half and FP32 tiles of a step in one launch
 // (grid = all tiles; FP64 tiles are skipped, left to the FP64 tier launch).

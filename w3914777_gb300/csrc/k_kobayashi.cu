@@ -266,13 +266,19 @@ __device__ __forceinline__ void kob_tile(const StepArgs &a, unsigned char *smraw
 }
 
 // The tiles of one tier (list / count built by the classification).
+// Launched programmatically after the previous step's last grid (kob_launch):
+// its CTAs wait for that grid to complete, its writes visible, and only then
+// release the step's half/FP32 launch, which runs alongside (FP64 launch
+// first) -- so no grid of this step reads before the previous one has
+// written, and the launch itself overlaps the previous step.
 template <int T, int TIER, bool REF>
 __global__ void __launch_bounds__(kKobThreads) kob_step_kernel(StepArgs a)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
     __shared__ double red[kKobThreads / 32];
     __shared__ uint8_t ntier[9];
-    pdl_trigger();  // the step's half/FP32 launch may start alongside (FP64 launch first)
+    pdl_wait();
+    pdl_trigger();
     if ((int)blockIdx.x >= a.count[TIER]) return;
     kob_tile<T, TIER, REF>(a, smraw, red, ntier, a.list[blockIdx.x]);
 }
@@ -303,11 +309,9 @@ template <int T, int TIER> static size_t kob_smem()
 }
 
 template <int T, int TIER, bool REF>
-static cudaError_t kob_launch_t(const StepArgs &a, int grid, cudaStream_t s)
+static cudaError_t kob_launch_t(const StepArgs &a, int grid, cudaStream_t s, bool pdl)
 {
-    const size_t smem = kob_smem<T, TIER>();
-    kob_step_kernel<T, TIER, REF><<<grid, kKobThreads, smem, s>>>(a);
-    return cudaGetLastError();
+    return launch_kernel_nt(kob_step_kernel<T, TIER, REF>, grid, kKobThreads, kob_smem<T, TIER>(), s, pdl, a);
 }
 
 size_t kob_smem_bytes(int tile, int tier)
@@ -316,15 +320,15 @@ size_t kob_smem_bytes(int tile, int tier)
     return tier == TIER_FP64 ? kob_smem<16, TIER_FP64>() : kob_smem<16, TIER_FP32>();
 }
 
-cudaError_t kob_launch(int tile, int tier, bool ref, const StepArgs &a, int grid, cudaStream_t s)
+cudaError_t kob_launch(int tile, int tier, bool ref, const StepArgs &a, int grid, cudaStream_t s, bool pdl)
 {
 #define AMPS_KOB(TT)                                                                \
     switch (tier) {                                                                 \
-    case TIER_HALF: return kob_launch_t<TT, TIER_HALF, false>(a, grid, s);          \
-    case TIER_FP32: return kob_launch_t<TT, TIER_FP32, false>(a, grid, s);          \
+    case TIER_HALF: return kob_launch_t<TT, TIER_HALF, false>(a, grid, s, pdl);     \
+    case TIER_FP32: return kob_launch_t<TT, TIER_FP32, false>(a, grid, s, pdl);     \
     default:                                                                        \
-        return ref ? kob_launch_t<TT, TIER_FP64, true>(a, grid, s)                  \
-                   : kob_launch_t<TT, TIER_FP64, false>(a, grid, s);                \
+        return ref ? kob_launch_t<TT, TIER_FP64, true>(a, grid, s, pdl)             \
+                   : kob_launch_t<TT, TIER_FP64, false>(a, grid, s, pdl);           \
     }
     if (tile == 32) { AMPS_KOB(32) }
     AMPS_KOB(16)

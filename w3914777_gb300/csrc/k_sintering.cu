@@ -265,7 +265,10 @@ __global__ void __launch_bounds__(kThreads) sint_step_f64_band_kernel(StepArgs a
     using B = SintBand<T>;
     extern __shared__ __align__(16) unsigned char smraw[];
     __shared__ uint8_t ntier[9];
-    pdl_trigger();  // the step's half/FP32 launch may start alongside (FP64 launch first)
+    // launched programmatically after the previous step's last grid: wait
+    // for it, then release the step's half/FP32 launch (FP64 launch first)
+    pdl_wait();
+    pdl_trigger();
     const int item = blockIdx.x / B::NB, band = blockIdx.x % B::NB;
     if (item >= a.count[TIER_FP64]) return;
     const int tile = a.list[item];
@@ -308,13 +311,17 @@ __global__ void __launch_bounds__(kThreads) sint_step_f64_band_kernel(StepArgs a
 }
 
 // The tiles of one tier (list / count built by the classification).
+// Launched programmatically after the previous step's last grid: its CTAs
+// wait for that grid, then release the step's half/FP32 launch, which runs
+// alongside (FP64 launch first).
 template <int T, int TIER, bool REF, bool MU64>
 __global__ void __launch_bounds__(kThreads) sint_step_kernel(StepArgs a)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
     __shared__ double red[kThreads / 32];
     __shared__ uint8_t ntier[9];
-    pdl_trigger();  // the step's half/FP32 launch may start alongside (FP64 launch first)
+    pdl_wait();
+    pdl_trigger();
     if ((int)blockIdx.x >= a.count[TIER]) return;
     sint_tile<T, TIER, REF, MU64>(a, smraw, red, ntier, a.list[blockIdx.x]);
 }
@@ -348,11 +355,9 @@ template <int T, int TIER, bool MU64> static size_t sint_smem(int nf)
 }
 
 template <int T, int TIER, bool REF, bool MU64>
-static cudaError_t sint_launch_t(const StepArgs &a, int grid, cudaStream_t s)
+static cudaError_t sint_launch_t(const StepArgs &a, int grid, cudaStream_t s, bool pdl)
 {
-    const size_t smem = sint_smem<T, TIER, MU64>(a.nf);
-    sint_step_kernel<T, TIER, REF, MU64><<<grid, kThreads, smem, s>>>(a);
-    return cudaGetLastError();
+    return launch_kernel(sint_step_kernel<T, TIER, REF, MU64>, grid, sint_smem<T, TIER, MU64>(a.nf), s, pdl, a);
 }
 
 size_t sint_smem_bytes(int tile, int tier, int nf, bool mu64)
@@ -365,26 +370,27 @@ size_t sint_smem_bytes(int tile, int tier, int nf, bool mu64)
     return mu64 ? sint_smem<16, TIER_FP32, true>(nf) : sint_smem<16, TIER_FP32, false>(nf);
 }
 
-cudaError_t sint_launch(int tile, int tier, bool ref, bool mu64, const StepArgs &a, int grid, cudaStream_t s)
+cudaError_t sint_launch(int tile, int tier, bool ref, bool mu64, const StepArgs &a, int grid, cudaStream_t s,
+                        bool pdl)
 {
     if (tier == TIER_FP64 && !ref && !a.monitor_now) {  // row bands (the monitor needs whole tiles)
         const int np = a.nf - 1;
         if (tile == 32) return launch_kernel(sint_step_f64_band_kernel<32>, grid * SintBand<32>::NB,
-                                             SintBand<32>::smem(np), s, false, a);
+                                             SintBand<32>::smem(np), s, pdl, a);
         return launch_kernel(sint_step_f64_band_kernel<16>, grid * SintBand<16>::NB, SintBand<16>::smem(np), s,
-                             false, a);
+                             pdl, a);
     }
 #define AMPS_SINT(TT)                                                                              \
     switch (tier) {                                                                                \
     case TIER_HALF:                                                                                \
-        return mu64 ? sint_launch_t<TT, TIER_HALF, false, true>(a, grid, s)                        \
-                    : sint_launch_t<TT, TIER_HALF, false, false>(a, grid, s);                      \
+        return mu64 ? sint_launch_t<TT, TIER_HALF, false, true>(a, grid, s, pdl)                        \
+                    : sint_launch_t<TT, TIER_HALF, false, false>(a, grid, s, pdl);                      \
     case TIER_FP32:                                                                                \
-        return mu64 ? sint_launch_t<TT, TIER_FP32, false, true>(a, grid, s)                        \
-                    : sint_launch_t<TT, TIER_FP32, false, false>(a, grid, s);                      \
+        return mu64 ? sint_launch_t<TT, TIER_FP32, false, true>(a, grid, s, pdl)                        \
+                    : sint_launch_t<TT, TIER_FP32, false, false>(a, grid, s, pdl);                      \
     default:                                                                                       \
-        return ref ? sint_launch_t<TT, TIER_FP64, true, true>(a, grid, s)                          \
-                   : sint_launch_t<TT, TIER_FP64, false, true>(a, grid, s);                        \
+        return ref ? sint_launch_t<TT, TIER_FP64, true, true>(a, grid, s, pdl)                          \
+                   : sint_launch_t<TT, TIER_FP64, false, true>(a, grid, s, pdl);                        \
     }
     if (tile == 32) { AMPS_SINT(32) }
     AMPS_SINT(16)
