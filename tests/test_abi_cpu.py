@@ -132,3 +132,49 @@ def test_stochastic_half_rounding_is_a_kobayashi_option():
     assert w.Params.preset("graingrowth", 0, half_arith=w.HALF_SR).check()[0] == 1
     assert w.Params.preset("sintering", 0, half_arith=w.HALF_SR).check()[0] == 1
     assert w.Params.preset("kobayashi", 2, half_arith=4).check()[0] == 1
+
+
+# the reference-named half2 and adaptive wrappers: (name, pointer arguments, trailing ints)
+_WRAPPERS = [
+    ("amps_graingrowth_kernel1_lowpure", 5, 0), ("amps_graingrowth_dataprepare_half2", 2, 0),
+    ("amps_snowflake_kernel1_purelow", 8, 0), ("amps_snowflake_kernel2_purelow", 8, 0),
+    ("amps_graingrowth_kernel1_mix", 12, 2), ("amps_graingrowth_data_sychro_duringcomputation", 6, 0),
+    ("amps_graingrowth_data_sychro_aftercomputation", 3, 0), ("amps_graingrowth_highdata_to_low", 2, 0),
+    ("amps_graingrowth_kernel1_conversion", 3, 1), ("amps_graingrowth_monitor2_lastdata_store", 2, 0),
+    ("amps_snowflake_kernel1_mix", 18, 1), ("amps_snowflake_mix_kernel2", 17, 1),
+    ("amps_snowflake_kernel2_conversion", 5, 1),
+    ("amps_sintering_con1_mix", 14, 1), ("amps_sintering_con2_mix", 11, 1), ("amps_sintering_phi1_mix", 13, 1),
+    ("amps_sintering_phi2_mix", 13, 1), ("amps_sintering_con2_conversion", 3, 1),
+    ("amps_sintering_data_sychro_duringcomputation", 8, 0), ("amps_sintering_dataprepare", 2, 0),
+    ("amps_sintering_data_sychro_aftercomputation", 3, 0),
+]
+
+
+@pytest.mark.parametrize("name,nptr,nint", _WRAPPERS)
+def test_reference_named_wrappers_validate_before_any_launch(name, nptr, nint):
+    """Every half2 / adaptive wrapper refuses, before touching the device, a
+    grid it cannot run (odd nx, zero-flux, a tile that does not divide the
+    sides or is above 32) and a null array: AMPS_ERR_INVALID (1)."""
+    import ctypes
+    w = amps()
+    f = getattr(w.lib(), name)
+    f.argtypes = [ctypes.POINTER(w.Params)] + [ctypes.c_void_p] * nptr + [ctypes.c_int] * nint + [ctypes.c_void_p]
+    f.restype = ctypes.c_int
+    model = "sintering" if "sintering" in name else ("kobayashi" if "snowflake" in name else "graingrowth")
+    preset = {"sintering": 5, "kobayashi": 2, "graingrowth": 1}[model]
+    fake = [ctypes.c_void_p(256 * (k + 1)) for k in range(nptr)]  # never dereferenced on the host
+    ints = [0] * nint
+    bad = [dict(nx=510), dict(nx=511), dict(bc=w.BC_NOFLUX), dict(tile=12), dict(tile=64)]
+    if "lowpure" in name or "purelow" in name or "half2" in name:
+        bad = [dict(nx=511), dict(bc=w.BC_NOFLUX)]  # untiled: any even periodic grid
+    for kw in bad:
+        p = w.Params.preset(model, preset, **kw)
+        assert f(ctypes.byref(p), *fake, *ints, None) == 1, kw
+    p = w.Params.preset(model, preset)
+    for k in range(nptr):
+        if name in ("amps_graingrowth_kernel1_mix", "amps_snowflake_kernel1_mix", "amps_sintering_con1_mix") and k == (
+                1 if "sintering" not in name else 2):
+            continue  # the snapshot array may be null unless the temporal monitor is on
+        args = list(fake)
+        args[k] = None
+        assert f(ctypes.byref(p), *args, *ints, None) == 1, (name, k)
