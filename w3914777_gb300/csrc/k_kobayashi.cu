@@ -112,8 +112,8 @@ constexpr int TIER_LO = -1;
 
 // One tile of one step at tier TIER (smraw: the kernel's dynamic shared
 // memory, kob_smem<T, TIER> bytes; red / ntier: its static scratch; NT
-// threads).
-template <int T, int TIER, bool REF, int NT = kKobThreads>
+// threads).  MON = false compiles the monitor out (steps without it).
+template <int T, int TIER, bool REF, int NT = kKobThreads, bool MON = true>
 __device__ __forceinline__ void kob_tile(const StepArgs &a, unsigned char *smraw, double *red, uint8_t *ntier,
                                          int tile)
 {
@@ -168,7 +168,7 @@ __device__ __forceinline__ void kob_tile(const StepArgs &a, unsigned char *smraw
     // same metric, without FP64 operations per cell)
     using MA = typename std::conditional<TIER == TIER_FP64, MonAcc, MonAccF>::type;
     MA mon;
-    const bool mon_on = a.monitor_now != 0;
+    const bool mon_on = MON && a.monitor_now != 0;
     if (mon_on) mon_reset(a, mon);
     const int mslot = 0;
     for (int u = threadIdx.x; u < T * T; u += NT) {
@@ -290,7 +290,7 @@ __global__ void __launch_bounds__(kKobThreads) kob_step_kernel(StepArgs a)
 // launched to run alongside it (disjoint tiles and output stores; both read
 // the previous step's state only); its last CTA waits for the FP64 grid
 // before it exits, so this grid completes after both.
-template <int T>
+template <int T, bool MON>
 __global__ void __launch_bounds__(kKobThreads) kob_step_lo_kernel(StepArgs a)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
@@ -298,7 +298,7 @@ __global__ void __launch_bounds__(kKobThreads) kob_step_lo_kernel(StepArgs a)
     __shared__ uint8_t ntier[9];
     const int tile = blockIdx.x;
     const int tier = a.tier_out[tile];
-    if (tier != TIER_FP64) kob_tile<T, TIER_LO, false>(a, smraw, red, ntier, tile);
+    if (tier != TIER_FP64) kob_tile<T, TIER_LO, false, kKobThreads, MON>(a, smraw, red, ntier, tile);
     if (blockIdx.x == gridDim.x - 1) pdl_wait();
 }
 
@@ -335,18 +335,30 @@ cudaError_t kob_launch(int tile, int tier, bool ref, const StepArgs &a, int grid
 #undef AMPS_KOB
 }
 
+// the monitor steps take the variant with the monitor compiled in; the
+// others a kernel without its code (the step is instruction-fetch bound)
 cudaError_t kob_launch_lo(int tile, const StepArgs &a, int grid, cudaStream_t s, bool after64)
 {
+    const bool mon = a.monitor_now != 0;
     if (tile == 32)
-        return launch_kernel_nt(kob_step_lo_kernel<32>, grid, kKobThreads, kob_smem<32, TIER_FP32>(), s, after64, a);
-    return launch_kernel_nt(kob_step_lo_kernel<16>, grid, kKobThreads, kob_smem<16, TIER_FP32>(), s, after64, a);
+        return mon ? launch_kernel_nt(kob_step_lo_kernel<32, true>, grid, kKobThreads, kob_smem<32, TIER_FP32>(), s,
+                                      after64, a)
+                   : launch_kernel_nt(kob_step_lo_kernel<32, false>, grid, kKobThreads, kob_smem<32, TIER_FP32>(), s,
+                                      after64, a);
+    return mon ? launch_kernel_nt(kob_step_lo_kernel<16, true>, grid, kKobThreads, kob_smem<16, TIER_FP32>(), s,
+                                  after64, a)
+               : launch_kernel_nt(kob_step_lo_kernel<16, false>, grid, kKobThreads, kob_smem<16, TIER_FP32>(), s,
+                                  after64, a);
 }
 
 cudaError_t kob_prepare_lo(int tile)
 {
     const auto attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
-    return tile == 32 ? cudaFuncSetAttribute(kob_step_lo_kernel<32>, attr, kMaxDynSmem)
-                      : cudaFuncSetAttribute(kob_step_lo_kernel<16>, attr, kMaxDynSmem);
+    cudaError_t e = tile == 32 ? cudaFuncSetAttribute(kob_step_lo_kernel<32, true>, attr, kMaxDynSmem)
+                               : cudaFuncSetAttribute(kob_step_lo_kernel<16, true>, attr, kMaxDynSmem);
+    if (e != cudaSuccess) return e;
+    return tile == 32 ? cudaFuncSetAttribute(kob_step_lo_kernel<32, false>, attr, kMaxDynSmem)
+                      : cudaFuncSetAttribute(kob_step_lo_kernel<16, false>, attr, kMaxDynSmem);
 }
 
 cudaError_t kob_prepare(int tile, int tier, bool ref)
