@@ -112,8 +112,9 @@ constexpr int TIER_LO = -1;
 
 // One tile of one step at tier TIER (smraw: the kernel's dynamic shared
 // memory, kob_smem<T, TIER> bytes; red / ntier: its static scratch; NT
-// threads).  MON = false compiles the monitor out (steps without it).
-template <int T, int TIER, bool REF, int NT = kKobThreads, bool MON = true>
+// threads).  MON = false compiles the monitor out (steps without it), SR =
+// false the stochastic rounding of half tiles (runs without AMPS_HALF_SR).
+template <int T, int TIER, bool REF, int NT = kKobThreads, bool MON = true, bool SR = true>
 __device__ __forceinline__ void kob_tile(const StepArgs &a, unsigned char *smraw, double *red, uint8_t *ntier,
                                          int tile)
 {
@@ -215,7 +216,7 @@ __device__ __forceinline__ void kob_tile(const StepArgs &a, unsigned char *smraw
             tn = __dadd_rn(__dadd_rn(t0, __dmul_rn(ph.dt, lt)), __dmul_rn(ph.kappa, __dsub_rn(pn, p0)));
         } else {
             // storage rounding: to nearest, or (half tiles, AMPS_HALF_SR) stochastic
-            const bool sr = half && a.half_arith == AMPS_HALF_SR;
+            const bool sr = SR && half && a.half_arith == AMPS_HALF_SR;
             auto rnd = [&](CT v) -> CT {
                 if (half && sr) return (CT)__half2float(half_sr((float)v, sr_bits(ph.seed, step, g)));
                 if (TIER == TIER_LO) return half ? (CT)__half2float(__float2half_rn((float)v)) : v;
@@ -290,7 +291,7 @@ __global__ void __launch_bounds__(kKobThreads) kob_step_kernel(StepArgs a)
 // launched to run alongside it (disjoint tiles and output stores; both read
 // the previous step's state only); its last CTA waits for the FP64 grid
 // before it exits, so this grid completes after both.
-template <int T, bool MON>
+template <int T, bool MON, bool SR>
 __global__ void __launch_bounds__(kKobThreads) kob_step_lo_kernel(StepArgs a)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
@@ -298,7 +299,7 @@ __global__ void __launch_bounds__(kKobThreads) kob_step_lo_kernel(StepArgs a)
     __shared__ uint8_t ntier[9];
     const int tile = blockIdx.x;
     const int tier = a.tier_out[tile];
-    if (tier != TIER_FP64) kob_tile<T, TIER_LO, false, kKobThreads, MON>(a, smraw, red, ntier, tile);
+    if (tier != TIER_FP64) kob_tile<T, TIER_LO, false, kKobThreads, MON, SR>(a, smraw, red, ntier, tile);
     if (blockIdx.x == gridDim.x - 1) pdl_wait();
 }
 
@@ -335,31 +336,36 @@ cudaError_t kob_launch(int tile, int tier, bool ref, const StepArgs &a, int grid
 #undef AMPS_KOB
 }
 
-// the monitor steps take the variant with the monitor compiled in; the
-// others a kernel without its code (the step is instruction-fetch bound)
-cudaError_t kob_launch_lo(int tile, const StepArgs &a, int grid, cudaStream_t s, bool after64)
+// the monitor steps take the variant with the monitor compiled in, runs
+// with stochastic rounding the one with it; the others a kernel without
+// that code (the step is instruction-fetch bound)
+template <int T>
+static cudaError_t kob_launch_lo_t(const StepArgs &a, int grid, cudaStream_t s, bool after64)
 {
-    const bool mon = a.monitor_now != 0;
-    if (tile == 32)
-        return mon ? launch_kernel_nt(kob_step_lo_kernel<32, true>, grid, kKobThreads, kob_smem<32, TIER_FP32>(), s,
-                                      after64, a)
-                   : launch_kernel_nt(kob_step_lo_kernel<32, false>, grid, kKobThreads, kob_smem<32, TIER_FP32>(), s,
-                                      after64, a);
-    return mon ? launch_kernel_nt(kob_step_lo_kernel<16, true>, grid, kKobThreads, kob_smem<16, TIER_FP32>(), s,
-                                  after64, a)
-               : launch_kernel_nt(kob_step_lo_kernel<16, false>, grid, kKobThreads, kob_smem<16, TIER_FP32>(), s,
-                                  after64, a);
+    const size_t smem = kob_smem<T, TIER_FP32>();
+    const bool mon = a.monitor_now != 0, sr = a.half_arith == AMPS_HALF_SR;
+    if (sr) return mon ? launch_kernel_nt(kob_step_lo_kernel<T, true, true>, grid, kKobThreads, smem, s, after64, a)
+                       : launch_kernel_nt(kob_step_lo_kernel<T, false, true>, grid, kKobThreads, smem, s, after64, a);
+    return mon ? launch_kernel_nt(kob_step_lo_kernel<T, true, false>, grid, kKobThreads, smem, s, after64, a)
+               : launch_kernel_nt(kob_step_lo_kernel<T, false, false>, grid, kKobThreads, smem, s, after64, a);
 }
 
-cudaError_t kob_prepare_lo(int tile)
+cudaError_t kob_launch_lo(int tile, const StepArgs &a, int grid, cudaStream_t s, bool after64)
+{
+    return tile == 32 ? kob_launch_lo_t<32>(a, grid, s, after64) : kob_launch_lo_t<16>(a, grid, s, after64);
+}
+
+template <int T> static cudaError_t kob_prepare_lo_t()
 {
     const auto attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
-    cudaError_t e = tile == 32 ? cudaFuncSetAttribute(kob_step_lo_kernel<32, true>, attr, kMaxDynSmem)
-                               : cudaFuncSetAttribute(kob_step_lo_kernel<16, true>, attr, kMaxDynSmem);
-    if (e != cudaSuccess) return e;
-    return tile == 32 ? cudaFuncSetAttribute(kob_step_lo_kernel<32, false>, attr, kMaxDynSmem)
-                      : cudaFuncSetAttribute(kob_step_lo_kernel<16, false>, attr, kMaxDynSmem);
+    cudaError_t e = cudaFuncSetAttribute(kob_step_lo_kernel<T, true, true>, attr, kMaxDynSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(kob_step_lo_kernel<T, false, true>, attr, kMaxDynSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(kob_step_lo_kernel<T, true, false>, attr, kMaxDynSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(kob_step_lo_kernel<T, false, false>, attr, kMaxDynSmem);
+    return e;
 }
+
+cudaError_t kob_prepare_lo(int tile) { return tile == 32 ? kob_prepare_lo_t<32>() : kob_prepare_lo_t<16>(); }
 
 cudaError_t kob_prepare(int tile, int tier, bool ref)
 {
