@@ -16,6 +16,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <cmath>
 #include <map>
 #include <memory>
 #include <new>
@@ -193,6 +194,9 @@ static Phys make_phys(const amps_params &p)
         k[KB_EPSB] = ph.epsb; k[KB_DELTA] = ph.delta; k[KB_ED] = -ph.epsb * ph.aniso * ph.delta;
         k[KB_M] = ph.alpha / ph.pi; k[KB_GAMA] = ph.gama; k[KB_TEQ] = ph.teq; k[KB_NOISE] = ph.noise;
         k[KB_DTT] = ph.dt / ph.tau; k[KB_KAPPA] = ph.kappa; k[KB_DT] = ph.dt; k[KB_INV] = ph.inv_dxdy;
+        const bool even = ph.aniso >= 2 && ph.aniso <= 16 && ph.aniso == 2 * std::floor(ph.aniso / 2);
+        k[KB_MODE] = even ? ph.aniso : 0;
+        k[KB_C0] = std::cos(ph.aniso * ph.theta0); k[KB_S0] = std::sin(ph.aniso * ph.theta0);
     } else if (p.model == AMPS_SINTERING) {
         k[SN_INV] = ph.inv_dxdy; k[SN_B] = ph.B; k[SN_A2] = 2.0 * ph.A; k[SN_HCM] = 0.5 * ph.coefm;
         k[SN_DVOL] = ph.dvol; k[SN_DVAP] = ph.dvap; k[SN_DSUR] = ph.dsur; k[SN_DGRB] = ph.dgrb; k[SN_DT] = ph.dt;

@@ -53,9 +53,11 @@ struct Phys {
 
 enum KConst {
     // Kobayashi: 0.5/dx, 0.5/dy, aniso, theta0, epsb, delta, -epsb*aniso*delta,
-    // alpha/pi, gama, teq, noise, dt/tau, kappa, dt, 1/dxdy
+    // alpha/pi, gama, teq, noise, dt/tau, kappa, dt, 1/dxdy; the anisotropy
+    // mode when it is an even integer 2..16 (else 0), cos and sin of
+    // aniso*theta0
     KB_HX, KB_HY, KB_ANISO, KB_THETA0, KB_EPSB, KB_DELTA, KB_ED, KB_M, KB_GAMA, KB_TEQ, KB_NOISE, KB_DTT,
-    KB_KAPPA, KB_DT, KB_INV,
+    KB_KAPPA, KB_DT, KB_INV, KB_MODE, KB_C0, KB_S0,
     // sintering: 1/dxdy, B, 2A, 0.5*coefm, dvol, dvap, dsur, dgrb, dt, 12B, dt*coefl, 0.5*coefk
     SN_INV = 0, SN_B, SN_A2, SN_HCM, SN_DVOL, SN_DVAP, SN_DSUR, SN_DGRB, SN_DT, SN_B12, SN_DTL, SN_HCK,
     KCONST_MAX = 24

@@ -57,17 +57,65 @@ template <typename CT> __device__ __forceinline__ CT k_atan(CT v) { return atan(
 // the step is a fixed-latency critical path, and 25-30% slower at 1024^2 and
 // 2048^2, where the bands' shared ring rows cost throughput.)
 
+// cos(a*theta) and sin(a*theta) for theta = atan2(y, x) and an even
+// integer a, without trigonometric functions: the a-th power of the unit
+// vector (x + iy) / |(x, y)| (de Moivre's formula), by repeated squaring.
+// (x, y) is first scaled by a power of two (exact) so that x^2 + y^2 can
+// neither underflow nor overflow.  A zero gradient stands for theta = 0 --
+// for an even a the same cos and sin as atan2's +-0 and +-pi there.
+__device__ __forceinline__ void kob_rot(float x, float y, int a, float &ca, float &sa)
+{
+    float c = 1.f, s = 0.f;
+    const float m = fmaxf(fabsf(x), fabsf(y));
+    if (m > 0.f) {
+        int ex;
+        frexpf(m, &ex);
+        x = ldexpf(x, -ex);
+        y = ldexpf(y, -ex);
+        const float ir = rsqrtf(fmaf(x, x, y * y));
+        c = x * ir;
+        s = y * ir;
+    }
+    float pr = 1.f, pi = 0.f;  // the product so far
+    for (int n = a;;) {
+        if (n & 1) {
+            const float t = fmaf(pr, c, -pi * s);
+            pi = fmaf(pr, s, pi * c);
+            pr = t;
+        }
+        n >>= 1;
+        if (!n) break;
+        const float t = fmaf(c, c, -s * s);
+        s = 2.f * c * s;
+        c = t;
+    }
+    ca = pr;
+    sa = pi;
+}
+
 // Phase A at one cell (snowflake/function.h:30-34): P at the cell's phi,
-// row stride ps.
-template <typename CT>
+// row stride ps.  POLY (float tiles, an even integer anisotropy mode):
+// cos and sin of aniso*(theta - theta0) by kob_rot and the angle-difference
+// identities, the same quantities without atan2/cos/sin, whose long code
+// bounds the instruction fetch of this latency-bound step.
+template <typename CT, bool POLY = false>
 __device__ __forceinline__ void kob_aniso(const CT *P, int ps, const Phys &ph, CT &phx, CT &phy, CT &e, CT &ed)
 {
     const CT pe = P[1], pw = P[-1], pn = P[ps], pso = P[-ps];
     phx = (pe - pw) * kc<CT>(ph, KB_HX);
     phy = (pn - pso) * kc<CT>(ph, KB_HY);
-    const CT arg = kc<CT>(ph, KB_ANISO) * (k_atan2<CT>(phy, phx) - kc<CT>(ph, KB_THETA0));
-    e = kc<CT>(ph, KB_EPSB) * fma(kc<CT>(ph, KB_DELTA), k_cos<CT>(arg), CT(1));
-    ed = kc<CT>(ph, KB_ED) * k_sin<CT>(arg);
+    if constexpr (POLY && std::is_same<CT, float>::value) {
+        float ca, sa;
+        kob_rot(phx, phy, (int)ph.kf[KB_MODE], ca, sa);
+        const float c0 = ph.kf[KB_C0], s0 = ph.kf[KB_S0];
+        const float cosv = fmaf(ca, c0, sa * s0), sinv = fmaf(sa, c0, -ca * s0);
+        e = kc<CT>(ph, KB_EPSB) * fmaf(kc<CT>(ph, KB_DELTA), cosv, 1.f);
+        ed = kc<CT>(ph, KB_ED) * sinv;
+    } else {
+        const CT arg = kc<CT>(ph, KB_ANISO) * (k_atan2<CT>(phy, phx) - kc<CT>(ph, KB_THETA0));
+        e = kc<CT>(ph, KB_EPSB) * fma(kc<CT>(ph, KB_DELTA), k_cos<CT>(arg), CT(1));
+        ed = kc<CT>(ph, KB_ED) * k_sin<CT>(arg);
+    }
 }
 
 // Phase B at one cell (snowflake/function.h:54-59): P, Tm at the cell's phi
@@ -113,8 +161,9 @@ constexpr int TIER_LO = -1;
 // One tile of one step at tier TIER (smraw: the kernel's dynamic shared
 // memory, kob_smem<T, TIER> bytes; red / ntier: its static scratch; NT
 // threads).  MON = false compiles the monitor out (steps without it), SR =
-// false the stochastic rounding of half tiles (runs without AMPS_HALF_SR).
-template <int T, int TIER, bool REF, int NT = kKobThreads, bool MON = true, bool SR = true>
+// false the stochastic rounding of half tiles (runs without AMPS_HALF_SR);
+// POLY: float tiles take kob_aniso's trigonometry-free form.
+template <int T, int TIER, bool REF, int NT = kKobThreads, bool MON = true, bool SR = true, bool POLY = false>
 __device__ __forceinline__ void kob_tile(const StepArgs &a, unsigned char *smraw, double *red, uint8_t *ntier,
                                          int tile)
 {
@@ -155,7 +204,7 @@ __device__ __forceinline__ void kob_tile(const StepArgs &a, unsigned char *smraw
             e = __dmul_rn(ph.epsb, __dadd_rn(1.0, __dmul_rn(ph.delta, cos(arg))));
             ed = __dmul_rn(__dmul_rn(__dmul_rn(-ph.epsb, ph.aniso), ph.delta), sin(arg));
         } else {
-            kob_aniso<CT>(&S::at(sm, 0, r, cc), S::P, ph, phx, phy, e, ed);
+            kob_aniso<CT, POLY>(&S::at(sm, 0, r, cc), S::P, ph, phx, phy, e, ed);
         }
         const int o = u;
         px[o] = phx; py[o] = phy; ep[o] = e; epd[o] = ed;
@@ -272,7 +321,7 @@ __device__ __forceinline__ void kob_tile(const StepArgs &a, unsigned char *smraw
 // release the step's half/FP32 launch, which runs alongside (FP64 launch
 // first) -- so no grid of this step reads before the previous one has
 // written, and the launch itself overlaps the previous step.
-template <int T, int TIER, bool REF>
+template <int T, int TIER, bool REF, bool POLY>
 __global__ void __launch_bounds__(kKobThreads) kob_step_kernel(StepArgs a)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
@@ -281,7 +330,7 @@ __global__ void __launch_bounds__(kKobThreads) kob_step_kernel(StepArgs a)
     pdl_wait();
     pdl_trigger();
     if ((int)blockIdx.x >= a.count[TIER]) return;
-    kob_tile<T, TIER, REF>(a, smraw, red, ntier, a.list[blockIdx.x]);
+    kob_tile<T, TIER, REF, kKobThreads, true, true, POLY>(a, smraw, red, ntier, a.list[blockIdx.x]);
 }
 
 // The half and FP32 tiles of a step in one launch (one CTA per tile; FP64
@@ -291,7 +340,7 @@ __global__ void __launch_bounds__(kKobThreads) kob_step_kernel(StepArgs a)
 // launched to run alongside it (disjoint tiles and output stores; both read
 // the previous step's state only); its last CTA waits for the FP64 grid
 // before it exits, so this grid completes after both.
-template <int T, bool MON, bool SR>
+template <int T, bool MON, bool SR, bool POLY>
 __global__ void __launch_bounds__(kKobThreads) kob_step_lo_kernel(StepArgs a)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
@@ -299,7 +348,7 @@ __global__ void __launch_bounds__(kKobThreads) kob_step_lo_kernel(StepArgs a)
     __shared__ uint8_t ntier[9];
     const int tile = blockIdx.x;
     const int tier = a.tier_out[tile];
-    if (tier != TIER_FP64) kob_tile<T, TIER_LO, false, kKobThreads, MON, SR>(a, smraw, red, ntier, tile);
+    if (tier != TIER_FP64) kob_tile<T, TIER_LO, false, kKobThreads, MON, SR, POLY>(a, smraw, red, ntier, tile);
     if (blockIdx.x == gridDim.x - 1) pdl_wait();
 }
 
@@ -309,10 +358,10 @@ template <int T, int TIER> static size_t kob_smem()
     return (2 * (size_t)Stage<CT, T, 2>::FIELD + 4 * (size_t)(T + 2) * (T + 2)) * sizeof(CT);
 }
 
-template <int T, int TIER, bool REF>
+template <int T, int TIER, bool REF, bool POLY>
 static cudaError_t kob_launch_t(const StepArgs &a, int grid, cudaStream_t s, bool pdl)
 {
-    return launch_kernel_nt(kob_step_kernel<T, TIER, REF>, grid, kKobThreads, kob_smem<T, TIER>(), s, pdl, a);
+    return launch_kernel_nt(kob_step_kernel<T, TIER, REF, POLY>, grid, kKobThreads, kob_smem<T, TIER>(), s, pdl, a);
 }
 
 size_t kob_smem_bytes(int tile, int tier)
@@ -321,67 +370,93 @@ size_t kob_smem_bytes(int tile, int tier)
     return tier == TIER_FP64 ? kob_smem<16, TIER_FP64>() : kob_smem<16, TIER_FP32>();
 }
 
+// float tiles take the trigonometry-free anisotropy where the mode allows it
+static bool kob_poly(const StepArgs &a) { return a.ph.kf[KB_MODE] != 0.f; }
+
+template <int T>
+static cudaError_t kob_launch_tt(int tier, bool ref, const StepArgs &a, int grid, cudaStream_t s, bool pdl)
+{
+    const bool poly = kob_poly(a);
+    switch (tier) {
+    case TIER_HALF:
+        return poly ? kob_launch_t<T, TIER_HALF, false, true>(a, grid, s, pdl)
+                    : kob_launch_t<T, TIER_HALF, false, false>(a, grid, s, pdl);
+    case TIER_FP32:
+        return poly ? kob_launch_t<T, TIER_FP32, false, true>(a, grid, s, pdl)
+                    : kob_launch_t<T, TIER_FP32, false, false>(a, grid, s, pdl);
+    default:
+        return ref ? kob_launch_t<T, TIER_FP64, true, false>(a, grid, s, pdl)
+                   : kob_launch_t<T, TIER_FP64, false, false>(a, grid, s, pdl);
+    }
+}
+
 cudaError_t kob_launch(int tile, int tier, bool ref, const StepArgs &a, int grid, cudaStream_t s, bool pdl)
 {
-#define AMPS_KOB(TT)                                                                \
-    switch (tier) {                                                                 \
-    case TIER_HALF: return kob_launch_t<TT, TIER_HALF, false>(a, grid, s, pdl);     \
-    case TIER_FP32: return kob_launch_t<TT, TIER_FP32, false>(a, grid, s, pdl);     \
-    default:                                                                        \
-        return ref ? kob_launch_t<TT, TIER_FP64, true>(a, grid, s, pdl)             \
-                   : kob_launch_t<TT, TIER_FP64, false>(a, grid, s, pdl);           \
-    }
-    if (tile == 32) { AMPS_KOB(32) }
-    AMPS_KOB(16)
-#undef AMPS_KOB
+    return tile == 32 ? kob_launch_tt<32>(tier, ref, a, grid, s, pdl) : kob_launch_tt<16>(tier, ref, a, grid, s, pdl);
 }
 
 // the monitor steps take the variant with the monitor compiled in, runs
 // with stochastic rounding the one with it; the others a kernel without
 // that code (the step is instruction-fetch bound)
-template <int T>
-static cudaError_t kob_launch_lo_t(const StepArgs &a, int grid, cudaStream_t s, bool after64)
+template <int T, bool POLY>
+static cudaError_t kob_launch_lo_p(const StepArgs &a, int grid, cudaStream_t s, bool after64)
 {
     const size_t smem = kob_smem<T, TIER_FP32>();
     const bool mon = a.monitor_now != 0, sr = a.half_arith == AMPS_HALF_SR;
-    if (sr) return mon ? launch_kernel_nt(kob_step_lo_kernel<T, true, true>, grid, kKobThreads, smem, s, after64, a)
-                       : launch_kernel_nt(kob_step_lo_kernel<T, false, true>, grid, kKobThreads, smem, s, after64, a);
-    return mon ? launch_kernel_nt(kob_step_lo_kernel<T, true, false>, grid, kKobThreads, smem, s, after64, a)
-               : launch_kernel_nt(kob_step_lo_kernel<T, false, false>, grid, kKobThreads, smem, s, after64, a);
+    if (sr)
+        return mon ? launch_kernel_nt(kob_step_lo_kernel<T, true, true, POLY>, grid, kKobThreads, smem, s, after64, a)
+                   : launch_kernel_nt(kob_step_lo_kernel<T, false, true, POLY>, grid, kKobThreads, smem, s, after64, a);
+    return mon ? launch_kernel_nt(kob_step_lo_kernel<T, true, false, POLY>, grid, kKobThreads, smem, s, after64, a)
+               : launch_kernel_nt(kob_step_lo_kernel<T, false, false, POLY>, grid, kKobThreads, smem, s, after64, a);
 }
 
 cudaError_t kob_launch_lo(int tile, const StepArgs &a, int grid, cudaStream_t s, bool after64)
 {
-    return tile == 32 ? kob_launch_lo_t<32>(a, grid, s, after64) : kob_launch_lo_t<16>(a, grid, s, after64);
+    const bool poly = kob_poly(a);
+    if (tile == 32)
+        return poly ? kob_launch_lo_p<32, true>(a, grid, s, after64) : kob_launch_lo_p<32, false>(a, grid, s, after64);
+    return poly ? kob_launch_lo_p<16, true>(a, grid, s, after64) : kob_launch_lo_p<16, false>(a, grid, s, after64);
+}
+
+template <int T, bool POLY> static cudaError_t kob_prepare_lo_p()
+{
+    const auto attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    cudaError_t e = cudaFuncSetAttribute(kob_step_lo_kernel<T, true, true, POLY>, attr, kMaxDynSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(kob_step_lo_kernel<T, false, true, POLY>, attr, kMaxDynSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(kob_step_lo_kernel<T, true, false, POLY>, attr, kMaxDynSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(kob_step_lo_kernel<T, false, false, POLY>, attr, kMaxDynSmem);
+    return e;
 }
 
 template <int T> static cudaError_t kob_prepare_lo_t()
 {
-    const auto attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
-    cudaError_t e = cudaFuncSetAttribute(kob_step_lo_kernel<T, true, true>, attr, kMaxDynSmem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(kob_step_lo_kernel<T, false, true>, attr, kMaxDynSmem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(kob_step_lo_kernel<T, true, false>, attr, kMaxDynSmem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(kob_step_lo_kernel<T, false, false>, attr, kMaxDynSmem);
-    return e;
+    cudaError_t e = kob_prepare_lo_p<T, false>();
+    return e == cudaSuccess ? kob_prepare_lo_p<T, true>() : e;
 }
 
 cudaError_t kob_prepare_lo(int tile) { return tile == 32 ? kob_prepare_lo_t<32>() : kob_prepare_lo_t<16>(); }
 
-cudaError_t kob_prepare(int tile, int tier, bool ref)
+template <int T> static cudaError_t kob_prepare_t(int tier, bool ref)
 {
     const int lim = kMaxDynSmem;
     const auto attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
-#define AMPS_KOBP(TT)                                                                              \
-    switch (tier) {                                                                               \
-    case TIER_HALF: return cudaFuncSetAttribute(kob_step_kernel<TT, TIER_HALF, false>, attr, lim);  \
-    case TIER_FP32: return cudaFuncSetAttribute(kob_step_kernel<TT, TIER_FP32, false>, attr, lim);  \
-    default:                                                                                      \
-        return ref ? cudaFuncSetAttribute(kob_step_kernel<TT, TIER_FP64, true>, attr, lim)         \
-                   : cudaFuncSetAttribute(kob_step_kernel<TT, TIER_FP64, false>, attr, lim);       \
+    cudaError_t e;
+    switch (tier) {
+    case TIER_HALF:
+        e = cudaFuncSetAttribute(kob_step_kernel<T, TIER_HALF, false, false>, attr, lim);
+        return e == cudaSuccess ? cudaFuncSetAttribute(kob_step_kernel<T, TIER_HALF, false, true>, attr, lim) : e;
+    case TIER_FP32:
+        e = cudaFuncSetAttribute(kob_step_kernel<T, TIER_FP32, false, false>, attr, lim);
+        return e == cudaSuccess ? cudaFuncSetAttribute(kob_step_kernel<T, TIER_FP32, false, true>, attr, lim) : e;
+    default:
+        return ref ? cudaFuncSetAttribute(kob_step_kernel<T, TIER_FP64, true, false>, attr, lim)
+                   : cudaFuncSetAttribute(kob_step_kernel<T, TIER_FP64, false, false>, attr, lim);
     }
-    if (tile == 32) { AMPS_KOBP(32) }
-    AMPS_KOBP(16)
-#undef AMPS_KOBP
+}
+
+cudaError_t kob_prepare(int tile, int tier, bool ref)
+{
+    return tile == 32 ? kob_prepare_t<32>(tier, ref) : kob_prepare_t<16>(tier, ref);
 }
 
 }  // namespace amps
