@@ -14,34 +14,34 @@
 
 namespace amps {
 
+// Seeded uniform noise in [0, 1) of (step a, cell b): SplitMix64's mixing
+// function applied three times, the top 53 bits scaled by 2^-53.
+// noise_u01 split at its per-step key: noise_key(seed, a) is the part that
+// depends on the step only (computed once per tile), noise_u01_k(key, b)
+// the per-cell rest; noise_u01_k(noise_key(seed, a), b) == noise_u01(seed,
+// a, b) bit for bit.  Float: the 53-bit integer rounded once to float and
+// scaled by 2^-53 (exact), which is (float)noise_u01 -- without three FP64
+// operations per cell.
+__device__ __forceinline__ uint64_t noise_mix(uint64_t z)
+{
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+__device__ __forceinline__ uint64_t noise_key(uint64_t seed, uint64_t a) { return noise_mix(seed ^ noise_mix(a)); }
+template <typename CT> __device__ __forceinline__ CT noise_u01_k(uint64_t key, uint64_t b);
+template <> __device__ __forceinline__ double noise_u01_k<double>(uint64_t key, uint64_t b)
+{
+    return (double)(noise_mix(key + b) >> 11) * 0x1.0p-53;
+}
+template <> __device__ __forceinline__ float noise_u01_k<float>(uint64_t key, uint64_t b)
+{
+    return __ull2float_rn(noise_mix(key + b) >> 11) * 0x1.0p-53f;
+}
 __device__ __forceinline__ double noise_u01(uint64_t seed, uint64_t a, uint64_t b)
 {
-    auto mix = [](uint64_t z) {
-        z += 0x9E3779B97F4A7C15ull;
-        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-        return z ^ (z >> 31);
-    };
-    return (double)(mix(mix(seed ^ mix(a)) + b) >> 11) * 0x1.0p-53;
-}
-
-// noise_u01 at the tile's compute type.  Float: the 53-bit integer rounded
-// once to float and scaled by 2^-53 (exact), which is (float)noise_u01 --
-// without three FP64 operations per cell.
-template <typename CT> __device__ __forceinline__ CT noise_u01_t(uint64_t seed, uint64_t a, uint64_t b);
-template <> __device__ __forceinline__ double noise_u01_t<double>(uint64_t seed, uint64_t a, uint64_t b)
-{
-    return noise_u01(seed, a, b);
-}
-template <> __device__ __forceinline__ float noise_u01_t<float>(uint64_t seed, uint64_t a, uint64_t b)
-{
-    auto mix = [](uint64_t z) {
-        z += 0x9E3779B97F4A7C15ull;
-        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-        return z ^ (z >> 31);
-    };
-    return __ull2float_rn(mix(mix(seed ^ mix(a)) + b) >> 11) * 0x1.0p-53f;
+    return noise_u01_k<double>(noise_key(seed, a), b);
 }
 
 // x != 0 for a double parameter, by an integer test of its bits (no FP64 op)
@@ -126,7 +126,7 @@ __device__ __forceinline__ void kob_aniso(const CT *P, int ps, const Phys &ph, C
 // update does (snowflake/function.h:512-513 reads the new half phi).
 template <typename CT, typename RND>
 __device__ __forceinline__ void kob_update(const CT *P, const CT *Tm, int sp, const CT *px, const CT *py,
-                                           const CT *ep, const CT *epd, int o, int es, const Phys &ph, int64_t step,
+                                           const CT *ep, const CT *epd, int o, int es, const Phys &ph, uint64_t nkey,
                                            int64_t g, RND rnd, CT &pn, CT &tn)
 {
     const CT p0 = P[0], t0 = Tm[0];
@@ -141,7 +141,7 @@ __device__ __forceinline__ void kob_update(const CT *P, const CT *Tm, int sp, co
     const CT m = kc<CT>(ph, KB_M) * k_atan<CT>(kc<CT>(ph, KB_GAMA) * (kc<CT>(ph, KB_TEQ) - t0));
     CT drive = p0 - CT(0.5) + m;
     if (nonzero(ph.noise))
-        drive += kc<CT>(ph, KB_NOISE) * (noise_u01_t<CT>(ph.seed, (uint64_t)step, (uint64_t)g) - CT(0.5));
+        drive += kc<CT>(ph, KB_NOISE) * (noise_u01_k<CT>(nkey, (uint64_t)g) - CT(0.5));
     const CT inner = term1 + term2 + ep[o] * ep[o] * lp + p0 * (CT(1) - p0) * drive;
     pn = rnd(fma(kc<CT>(ph, KB_DTT), inner, p0));
     tn = fma(kc<CT>(ph, KB_KAPPA), pn - p0, fma(kc<CT>(ph, KB_DT), lt, t0));
@@ -213,6 +213,7 @@ __device__ __forceinline__ void kob_tile(const StepArgs &a, unsigned char *smraw
 
     // phase B: snowflake/function.h:54-59 on the tile
     const int64_t step = *a.step_base + a.step_off;
+    const uint64_t nkey = noise_key(ph.seed, (uint64_t)step);  // the noise's per-step part
     double metric = 0.0;
     // half/FP32 tiles fold their float values into a float accumulator (the
     // same metric, without FP64 operations per cell)
@@ -271,7 +272,7 @@ __device__ __forceinline__ void kob_tile(const StepArgs &a, unsigned char *smraw
                 if (TIER == TIER_LO) return half ? (CT)__half2float(__float2half_rn((float)v)) : v;
                 return round_to_tier<TIER == TIER_LO ? TIER_FP32 : TIER>(v);
             };
-            kob_update<CT>(P, Tm, S::P, px, py, ep, epd, o, E, ph, step, g, rnd, pn, tn);
+            kob_update<CT>(P, Tm, S::P, px, py, ep, epd, o, E, ph, nkey, g, rnd, pn, tn);
             if (half && sr)
                 tn = (CT)__half2float(half_sr((float)tn, sr_bits(ph.seed, step, (uint64_t)(a.n + g))));
         }
