@@ -1,5 +1,5 @@
-"""Ensemble of grain-growth runs (amps_ensemble_*): one persistent launch per
-step over every member's tiles must give each member exactly the results
+"""Ensemble of grain-growth runs (amps_ensemble_*): a step's launches over
+every member's tiles (one per group of members) must give each member exactly the results
 amps_run gives it alone -- fields, tier maps, statistics -- for members of
 different sizes, field counts, coefficients and time steps, in adaptive and
 plain modes, over whole and partial cadence periods, with and without
@@ -148,3 +148,24 @@ def test_ensemble_rejects_incompatible_members():
         amps.Ensemble([a, c])
     for s in (a, b, k, c):
         s.close()
+
+
+def test_ensemble_groups_past_the_launch_cap_match_individual_runs():
+    """More members than one launch carries (40 step-argument records in
+    the kernel's parameter space): 45 members of Q = 4 and 8, which share an
+    occupancy class and so split into two launches of that class, and 3 of
+    Q = 16 in a class of their own -- every member still exactly its single
+    run, adaptive, over two whole periods and a partial one."""
+    base = small_members(mixed())[0]
+    params = []
+    for i in range(48):
+        q = 16 if i >= 45 else (4 if i % 2 else 8)
+        side = 32 + 16 * (i % 5)  # 32..96, partial tiles included
+        p = base.replace(nx=side, ny=side, nfields=q, seed=500 + i)
+        params.append(p)
+    alone = run_alone(params, 25)
+    together = run_together(params, 25, chunks=[20, 5])
+    for k, ((fa, ta, sa), (fb, tb, sb)) in enumerate(zip(alone, together)):
+        assert np.array_equal(fa, fb), k
+        assert np.array_equal(ta, tb), k
+        assert sa == sb, k
