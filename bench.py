@@ -472,8 +472,8 @@ def run_reference_cuda(steps=2000):
     """The reference's own CUDA kernels on this GPU beside the library, at the
     reference's own configurations (its parameter files: 512^2, 16^2 tiles):
     grain growth para1 (Q = 2), the Kobayashi dendrite para2 and sintering
-    para5 (two particles), plain FP64 and AMSTENCIL at the sweep scripts'
-    thresholds.  The reference: its device
+    para5 (two particles): plain FP64, AMSTENCIL at the sweep scripts'
+    thresholds and (grain growth, Kobayashi) the all-half2 purelow runs.  The reference: its device
     code built from its sources for sm_103a (baseline/_ref/*.cubin), its host
     loops restated around driver-API launches (baseline/ref_cuda.cpp), timed
     by its own event window (step 5 to the end; one device synchronisation
@@ -512,6 +512,11 @@ def run_reference_cuda(steps=2000):
         gg[f"ours_mixed_monitor{m}_{thr:g}"] = ours(amps.Params.preset(
             "graingrowth", 1, mode="end2end_mix", monitor=m, monitor_samples=0, monitor_field=1, thr_lo=thr,
             thr_hi=thr, ref_order=1, half_arith=amps.HALF_REF, ref_snapshot=1))
+    if refcuda.available("graingrowth_purelow"):
+        gg["ref_purelow_half2"] = rate(refcuda.gg_purelow(total)[2])
+        gg["ours_purelow"] = ours(amps.Params.preset("graingrowth", 1, mode="purelow"))
+        gg["ours_purelow_half_ref"] = ours(amps.Params.preset("graingrowth", 1, mode="purelow",
+                                                              half_arith=amps.HALF_REF))
     out["graingrowth_para1"] = gg
     kob = {"ref_plain_fp64": rate(refcuda.kob_pure(total)[2]),
            "ours_plain_fp64_reference_order": ours(amps.Params.preset("kobayashi", 2, mode="purehigh", ref_order=1)),
@@ -521,6 +526,9 @@ def run_reference_cuda(steps=2000):
         kob[f"ours_mixed_monitor{m}_{thr:g}"] = ours(amps.Params.preset(
             "kobayashi", 2, mode="end2end_mix", monitor=m, monitor_samples=0, monitor_field=0, thr_lo=thr,
             thr_hi=thr, ref_order=1))
+    if refcuda.available("snowflake_purelow"):
+        kob["ref_purelow_half2"] = rate(refcuda.kob_purelow(total)[2])
+        kob["ours_purelow"] = ours(amps.Params.preset("kobayashi", 2, mode="purelow"))
     out["kobayashi_para2"] = kob
     if refcuda.available("sintering_pure") and refcuda.available("sintering_mix"):
         f0 = amps.init_host(amps.Params.preset("sintering", 5, mode="purehigh", ref_order=1), amps.INIT_REFERENCE)

@@ -149,9 +149,12 @@ __device__ __forceinline__ void kob_update(const CT *P, const CT *Tm, int sp, co
 
 // Threads per Kobayashi tile CTA.  A 512^2 grid is 256 tiles of 32^2, so
 // at 256 threads a tile the step ran one partial wave at ~14 warps per SM,
-// latency-bound; 512 threads a tile double the warps in flight (44 registers
-// a thread: two CTAs per SM).
-constexpr int kKobThreads = 512;
+// latency-bound; 512 threads a tile double the warps in flight (two cells a
+// thread).  A 16^2 half/FP32 tile keeps one cell a thread (256): 512 would
+// leave half of them idle in phase B and fit fewer CTAs on an SM.  A 16^2
+// FP64 tile keeps 512, so that its phase A (FP64 atan2/cos/sin on the 18^2
+// ring, the tier's critical path) takes one pass.
+template <int T, int TIER> constexpr int kob_threads() { return T == 32 || TIER == TIER_FP64 ? 512 : 256; }
 
 // TIER of kob_tile for the half/FP32 launch: half or FP32 at run time, one
 // copy of the tile code (with its long inlined atan2/cos/sin/atan chain) for
@@ -163,7 +166,7 @@ constexpr int TIER_LO = -1;
 // threads).  MON = false compiles the monitor out (steps without it), SR =
 // false the stochastic rounding of half tiles (runs without AMPS_HALF_SR);
 // POLY: float tiles take kob_aniso's trigonometry-free form.
-template <int T, int TIER, bool REF, int NT = kKobThreads, bool MON = true, bool SR = true, bool POLY = false>
+template <int T, int TIER, bool REF, int NT = kob_threads<T, TIER>(), bool MON = true, bool SR = true, bool POLY = false>
 __device__ __forceinline__ void kob_tile(const StepArgs &a, unsigned char *smraw, double *red, uint8_t *ntier,
                                          int tile)
 {
@@ -323,15 +326,15 @@ __device__ __forceinline__ void kob_tile(const StepArgs &a, unsigned char *smraw
 // first) -- so no grid of this step reads before the previous one has
 // written, and the launch itself overlaps the previous step.
 template <int T, int TIER, bool REF, bool POLY>
-__global__ void __launch_bounds__(kKobThreads) kob_step_kernel(StepArgs a)
+__global__ void __launch_bounds__(kob_threads<T, TIER>()) kob_step_kernel(StepArgs a)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
-    __shared__ double red[kKobThreads / 32];
+    __shared__ double red[kob_threads<T, TIER>() / 32];
     __shared__ uint8_t ntier[9];
     pdl_wait();
     pdl_trigger();
     if ((int)blockIdx.x >= a.count[TIER]) return;
-    kob_tile<T, TIER, REF, kKobThreads, true, true, POLY>(a, smraw, red, ntier, a.list[blockIdx.x]);
+    kob_tile<T, TIER, REF, kob_threads<T, TIER>(), true, true, POLY>(a, smraw, red, ntier, a.list[blockIdx.x]);
 }
 
 // The half and FP32 tiles of a step in one launch (one CTA per tile; FP64
@@ -342,14 +345,15 @@ __global__ void __launch_bounds__(kKobThreads) kob_step_kernel(StepArgs a)
 // the previous step's state only); its last CTA waits for the FP64 grid
 // before it exits, so this grid completes after both.
 template <int T, bool MON, bool SR, bool POLY>
-__global__ void __launch_bounds__(kKobThreads) kob_step_lo_kernel(StepArgs a)
+__global__ void __launch_bounds__(kob_threads<T, TIER_LO>()) kob_step_lo_kernel(StepArgs a)
 {
     extern __shared__ __align__(16) unsigned char smraw[];
-    __shared__ double red[kKobThreads / 32];
+    __shared__ double red[kob_threads<T, TIER_LO>() / 32];
     __shared__ uint8_t ntier[9];
     const int tile = blockIdx.x;
     const int tier = a.tier_out[tile];
-    if (tier != TIER_FP64) kob_tile<T, TIER_LO, false, kKobThreads, MON, SR, POLY>(a, smraw, red, ntier, tile);
+    if (tier != TIER_FP64)
+        kob_tile<T, TIER_LO, false, kob_threads<T, TIER_LO>(), MON, SR, POLY>(a, smraw, red, ntier, tile);
     if (blockIdx.x == gridDim.x - 1) pdl_wait();
 }
 
@@ -362,7 +366,8 @@ template <int T, int TIER> static size_t kob_smem()
 template <int T, int TIER, bool REF, bool POLY>
 static cudaError_t kob_launch_t(const StepArgs &a, int grid, cudaStream_t s, bool pdl)
 {
-    return launch_kernel_nt(kob_step_kernel<T, TIER, REF, POLY>, grid, kKobThreads, kob_smem<T, TIER>(), s, pdl, a);
+    return launch_kernel_nt(kob_step_kernel<T, TIER, REF, POLY>, grid, kob_threads<T, TIER>(), kob_smem<T, TIER>(), s,
+                            pdl, a);
 }
 
 size_t kob_smem_bytes(int tile, int tier)
@@ -403,12 +408,13 @@ template <int T, bool POLY>
 static cudaError_t kob_launch_lo_p(const StepArgs &a, int grid, cudaStream_t s, bool after64)
 {
     const size_t smem = kob_smem<T, TIER_FP32>();
+    constexpr int nt = kob_threads<T, TIER_LO>();
     const bool mon = a.monitor_now != 0, sr = a.half_arith == AMPS_HALF_SR;
     if (sr)
-        return mon ? launch_kernel_nt(kob_step_lo_kernel<T, true, true, POLY>, grid, kKobThreads, smem, s, after64, a)
-                   : launch_kernel_nt(kob_step_lo_kernel<T, false, true, POLY>, grid, kKobThreads, smem, s, after64, a);
-    return mon ? launch_kernel_nt(kob_step_lo_kernel<T, true, false, POLY>, grid, kKobThreads, smem, s, after64, a)
-               : launch_kernel_nt(kob_step_lo_kernel<T, false, false, POLY>, grid, kKobThreads, smem, s, after64, a);
+        return mon ? launch_kernel_nt(kob_step_lo_kernel<T, true, true, POLY>, grid, nt, smem, s, after64, a)
+                   : launch_kernel_nt(kob_step_lo_kernel<T, false, true, POLY>, grid, nt, smem, s, after64, a);
+    return mon ? launch_kernel_nt(kob_step_lo_kernel<T, true, false, POLY>, grid, nt, smem, s, after64, a)
+               : launch_kernel_nt(kob_step_lo_kernel<T, false, false, POLY>, grid, nt, smem, s, after64, a);
 }
 
 cudaError_t kob_launch_lo(int tile, const StepArgs &a, int grid, cudaStream_t s, bool after64)
