@@ -478,7 +478,8 @@ def run_reference_cuda(steps=2000):
     loops restated around driver-API launches (baseline/ref_cuda.cpp), timed
     by its own event window (step 5 to the end; one device synchronisation
     per step, as its programs do).  The library: amps_run of the same
-    configuration (reference order, the same monitor and threshold), wall
+    configuration (reference order, the same monitor and threshold; and, as
+    `ours_mixed_fma_*`, the same run in the library's own arithmetic), wall
     clock around run + synchronize.  Rates in Gcell-updates/s."""
     import time
     from w3914777_gb300 import amps
@@ -512,6 +513,12 @@ def run_reference_cuda(steps=2000):
         gg[f"ours_mixed_monitor{m}_{thr:g}"] = ours(amps.Params.preset(
             "graingrowth", 1, mode="end2end_mix", monitor=m, monitor_samples=0, monitor_field=1, thr_lo=thr,
             thr_hi=thr, ref_order=1, half_arith=amps.HALF_REF, ref_snapshot=1))
+        # the same run in the library's own arithmetic (FMA-form FP64 tiles,
+        # float arithmetic on half tiles): the reference order keeps
+        # pow(eta, 3) on the FP64 pipe, which paces the adaptive step
+        gg[f"ours_mixed_fma_monitor{m}_{thr:g}"] = ours(amps.Params.preset(
+            "graingrowth", 1, mode="end2end_mix", monitor=m, monitor_samples=0, monitor_field=1, thr_lo=thr,
+            thr_hi=thr, ref_order=0))
     if refcuda.available("graingrowth_purelow"):
         gg["ref_purelow_half2"] = rate(refcuda.gg_purelow(total)[2])
         gg["ours_purelow"] = ours(amps.Params.preset("graingrowth", 1, mode="purelow"))
@@ -526,6 +533,9 @@ def run_reference_cuda(steps=2000):
         kob[f"ours_mixed_monitor{m}_{thr:g}"] = ours(amps.Params.preset(
             "kobayashi", 2, mode="end2end_mix", monitor=m, monitor_samples=0, monitor_field=0, thr_lo=thr,
             thr_hi=thr, ref_order=1))
+        kob[f"ours_mixed_fma_monitor{m}_{thr:g}"] = ours(amps.Params.preset(
+            "kobayashi", 2, mode="end2end_mix", monitor=m, monitor_samples=0, monitor_field=0, thr_lo=thr,
+            thr_hi=thr, ref_order=0))
     if refcuda.available("snowflake_purelow"):
         kob["ref_purelow_half2"] = rate(refcuda.kob_purelow(total)[2])
         kob["ours_purelow"] = ours(amps.Params.preset("kobayashi", 2, mode="purelow"))
@@ -541,6 +551,9 @@ def run_reference_cuda(steps=2000):
             sint[f"ours_mixed_monitor{m}_{thr:g}"] = ours(amps.Params.preset(
                 "sintering", 5, mode="end2end_mix", monitor=m, monitor_samples=0, monitor_field=0, thr_lo=thr,
                 thr_hi=thr, ref_order=1, half_arith=amps.HALF_REF))
+            sint[f"ours_mixed_fma_monitor{m}_{thr:g}"] = ours(amps.Params.preset(
+                "sintering", 5, mode="end2end_mix", monitor=m, monitor_samples=0, monitor_field=0, thr_lo=thr,
+                thr_hi=thr, ref_order=0))
         out["sintering_para5"] = sint
     return out
 

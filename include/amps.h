@@ -221,7 +221,9 @@ AMPS_API int amps_get_fields(amps_handle *h, void *dst, int dtype, int on_device
  * kernels, one per tier in use, with the monitor (get_max_diff1/2) fused into
  * the epilogue of every cadence-th step, then get_type, and the tier
  * conversion done in-register by the next step.  Whole cadence periods are
- * replayed from a CUDA graph. */
+ * replayed from a CUDA graph, on the handle's stream (a handle on the
+ * default stream captures its graphs on a private stream and replays them
+ * on the default stream). */
 AMPS_API int amps_run(amps_handle *h, int nsteps);
 /* Enable (1) / disable (0) CUDA-graph replay of whole periods (default 1). */
 AMPS_API int amps_set_graphs(amps_handle *h, int enable);

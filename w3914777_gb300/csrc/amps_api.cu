@@ -67,6 +67,9 @@ struct amps_handle {
     double *d_stage = nullptr, *d_partials = nullptr, *d_out = nullptr;
     double *h_pinned = nullptr;  // nf*n doubles, page-locked
     cudaStream_t own = nullptr, stream = nullptr;
+    // private stream on which a handle working on the default stream (which
+    // cannot be captured) captures its period graphs; replayed on the default stream
+    cudaStream_t cap = nullptr;
 
     int64_t step = 0;
     int64_t launches = 0;  // kernels enqueued by the run loop (graph replays add their graph's count)
@@ -232,6 +235,7 @@ static void free_all(amps_handle *h)
         if (q) cudaFree(q);
     if (h->h_pinned) cudaFreeHost(h->h_pinned);
     if (h->own) cudaStreamDestroy(h->own);
+    if (h->cap) cudaStreamDestroy(h->cap);
 }
 
 extern "C" int amps_create(const amps_params *p, amps_handle **out)
@@ -863,18 +867,28 @@ extern "C" int amps_run(amps_handle *h, int nsteps)
             e = cudaGraphLaunch(ex, h->stream);
             cudaGraphExecDestroy(ex);  // freed once the launch completes
             if (e != cudaSuccess) FAIL(h, AMPS_ERR_CUDA, "graph launch: %s", cudaGetErrorString(e));
-        } else if (h->graphs && !h->profiling && k0 == 0 && cnt == cad && h->stream != nullptr) {
+        } else if (h->graphs && !h->profiling && k0 == 0 && cnt == cad) {
             const int key = h->parity | (h->transition ? 2 : 0) | (h->all_fp64 ? 4 : 0);
             auto it = h->graph.find(key);
             if (it == h->graph.end()) {
                 const int par0 = h->parity;
                 const bool tr0 = h->transition, all0 = h->all_fp64;
                 const int64_t n0 = h->launches;
-                cudaGraph_t gr;
-                CK(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-                int r = enqueue_chunk(h, 0, cad);
-                cudaError_t e = cudaStreamEndCapture(h->stream, &gr);
-                if (r) return r;
+                // the default stream cannot be captured: capture on a private
+                // stream (the period's launches go to h->stream meanwhile)
+                // and replay the graph on the default stream below
+                cudaStream_t user = h->stream;
+                if (!user && !h->cap) CK(h, cudaStreamCreateWithFlags(&h->cap, cudaStreamNonBlocking));
+                if (!user) h->stream = h->cap;
+                cudaGraph_t gr = nullptr;
+                cudaError_t e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
+                int r = e == cudaSuccess ? enqueue_chunk(h, 0, cad) : AMPS_OK;
+                if (e == cudaSuccess) e = cudaStreamEndCapture(h->stream, &gr);
+                h->stream = user;
+                if (r) {
+                    if (gr) cudaGraphDestroy(gr);
+                    return r;
+                }
                 if (e != cudaSuccess) FAIL(h, AMPS_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
                 cudaGraphExec_t ex;
                 e = cudaGraphInstantiate(&ex, gr, 0);
