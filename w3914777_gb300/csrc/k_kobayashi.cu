@@ -221,9 +221,11 @@ __device__ __forceinline__ void kob_tile(const StepArgs &a, unsigned char *smraw
     // half/FP32 tiles fold their float values into a float accumulator (the
     // same metric, without FP64 operations per cell)
     using MA = typename std::conditional<TIER == TIER_FP64, MonAcc, MonAccF>::type;
-    MA mon;
+    MA mon, m2;  // phi's samples, T's (fed by the same pass)
     const bool mon_on = MON && a.monitor_now != 0;
+    const bool mon_t = mon_on && (a.mfield < 0 || a.mfield == 1);
     if (mon_on) mon_reset(a, mon);
+    if (mon_t) mon_reset(a, m2);
     const int mslot = 0;
     for (int u = threadIdx.x; u < T * T; u += NT) {
         const int i = u % T, j = u / T;
@@ -294,25 +296,19 @@ __device__ __forceinline__ void kob_tile(const StepArgs &a, unsigned char *smraw
         }
         if (mon_on && (a.mfield <= 0))
             mon_add<T>(a, mon, mslot, tile, j, i, g, pn, p0, snap_prefetch<T>(a, mslot, tile, j, i, g));
+        if (mon_t) {
+            // the second monitored field (T) at its stored value
+            CT tv;
+            if constexpr (TIER == TIER_LO) tv = half ? (CT)__half2float(__float2half_rn((float)tn)) : tn;
+            else tv = round_to_tier<TIER>(tn);
+            const int slot = a.mfield < 0 ? 1 : 0;
+            mon_add<T>(a, m2, slot, tile, j, i, g, tv, t0, snap_prefetch<T>(a, slot, tile, j, i, g));
+        }
     }
     if (mon_on) {
         metric = mon_finish<NT>(a, mon, red, metric);
-        if (a.mfield < 0 || a.mfield == 1) {
-            // second monitored field (T): a second pass over the stored values
-            MA m2;
-            mon_reset(a, m2);
-            __syncthreads();
-            for (int u = threadIdx.x; u < T * T; u += NT) {
-                const int i = u % T, j = u / T;
-                const int64_t g = (int64_t)(y0 + j) * a.nx + x0 + i;
-                CT v;
-                if constexpr (TIER == TIER_FP64) v = ((const double *)a.out[2])[a.n + g];
-                else if (!half) v = ((const float *)a.out[1])[a.n + g];
-                else v = __half2float(((const __half *)a.out[0])[a.n + g]);
-                const int slot = a.mfield < 0 ? 1 : 0;
-                mon_add<T>(a, m2, slot, tile, j, i, g, v, S::at(sm, 1, j + R, i + S::O),
-                           snap_prefetch<T>(a, slot, tile, j, i, g));
-            }
+        if (mon_t) {
+            __syncthreads();  // red is reused
             metric = mon_finish<NT>(a, m2, red, metric);
         }
         if (threadIdx.x == 0) a.metric[tile] = metric;
