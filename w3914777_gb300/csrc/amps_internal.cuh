@@ -611,6 +611,7 @@ __device__ __forceinline__ double snap_prefetch(const StepArgs &a, int mslot, in
 // Per-tile monitor accumulator for one field, reduced at the end of the field.
 struct MonAcc {
     double mn, mx, dmax;
+    float dmaxf;  // kind 3: the largest |(float)v - (float)old|, scaled by the cadence once per tile
     int bad;
 };
 
@@ -623,7 +624,8 @@ template <int T>
 __device__ __forceinline__ void mon_add(const StepArgs &a, MonAcc &m, int mslot, int tile, int row, int col,
                                         int64_t gidx, double v, double old, double snapv)
 {
-    if (!(v == v) || isinf(v)) m.bad = 1;
+    // NaN or infinite: the exponent field all ones (integer test, off the FP64 pipe)
+    if ((__double2hiint(v) & 0x7ff00000) == 0x7ff00000) m.bad = 1;
     const int si = sample_index<T>(a.monitor_kind == 1 ? 1 : 2, a.samples, row, col);
     if (si < 0) return;
     if (a.monitor_kind == 1) {
@@ -633,7 +635,8 @@ __device__ __forceinline__ void mon_add(const StepArgs &a, MonAcc &m, int mslot,
         m.dmax = fmax(m.dmax, fabs(snapv - v));
         *snap_ptr<T>(a, mslot, tile, gidx, si) = v;
     } else {
-        m.dmax = fmax(m.dmax, (double)fabsf((float)v - (float)old) * a.cadence);
+        // max_i (x_i * cadence) = (max_i x_i) * cadence: rounding is monotone
+        m.dmaxf = fmaxf(m.dmaxf, fabsf((float)v - (float)old));
     }
 }
 
@@ -774,6 +777,7 @@ __device__ __forceinline__ void mon_reset(const StepArgs &a, MonAcc &m)
     m.mn = a.samples ? INFINITY : 1.0;
     m.mx = a.samples ? -INFINITY : 0.0;
     m.dmax = 0.0;
+    m.dmaxf = 0.f;
     m.bad = 0;
 }
 
@@ -786,8 +790,10 @@ __device__ __forceinline__ double mon_finish(const StepArgs &a, MonAcc &m, doubl
         const double mx = block_max<NT>(m.mx, red);
         const double mn = block_min<NT>(m.mn, red);
         v = mx - mn;
-    } else {
+    } else if (a.monitor_kind == 2) {
         v = block_max<NT>(m.dmax, red);
+    } else {
+        v = (double)block_maxf<NT>(m.dmaxf, reinterpret_cast<float *>(red)) * a.cadence;
     }
     if (__syncthreads_or(m.bad) && threadIdx.x == 0) atomicOr(a.flags, 1);
     return fmax(metric, v);
