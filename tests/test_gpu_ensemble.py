@@ -169,3 +169,31 @@ def test_ensemble_groups_past_the_launch_cap_match_individual_runs():
         assert np.array_equal(fa, fb), k
         assert np.array_equal(ta, tb), k
         assert sa == sb, k
+
+
+@pytest.mark.parametrize("mode", ["adaptive", "fp32", "half"])
+def test_ensemble_split_tiles_match_individual_runs(mode, monkeypatch):
+    """Split tiles (opt-in, AMPS_ENS_PAIR=1): members of 16 fields run
+    their non-monitor steps as two-CTA clusters (8 fields each, the sum of
+    squares from both halves' staging in field order).  Whole and ragged
+    members, interior tiles (tensor copies) and edge tiles, every tier and
+    mixed neighbourhoods: each member exactly its run alone, with split and
+    with whole tiles."""
+    base = small_members(mixed())[0]
+    extra = {"adaptive": {}, "fp32": dict(mode=amps.PUREHIGH, high_tier=amps.TIER_FP32),
+             "half": dict(mode=amps.PURELOW)}[mode]
+    params = []
+    for i, (side, q) in enumerate([(160, 16), (130, 16), (97, 16), (64, 16), (224, 16), (96, 8)]):
+        p = base.replace(nx=side, ny=side, nfields=q, seed=700 + i, **extra)
+        params.append(p)
+    alone = run_alone(params, 25)
+    for pair in ("1", "0"):
+        monkeypatch.setenv("AMPS_ENS_PAIR", pair)
+        together = run_together(params, 25, chunks=[20, 5])
+        for k, ((fa, ta, sa), (fb, tb, sb)) in enumerate(zip(alone, together)):
+            assert np.array_equal(fa, fb), (pair, k)
+            assert np.array_equal(ta, tb), (pair, k)
+            assert sa == sb, (pair, k)
+    if mode == "adaptive":
+        steps_per_tier = np.sum([st["tile_steps"] for _, _, st in alone[:5]], axis=0)
+        assert np.count_nonzero(steps_per_tier) == 3

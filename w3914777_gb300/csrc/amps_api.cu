@@ -151,13 +151,14 @@ static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
 // [nf][ny][nx] float array (nx: the storage's row pitch, ny: its rows) ->
 // box {40 columns, 34 rows, nf fields}: a 32x32 tile with a 1-cell halo and
 // its columns padded to 16-byte boundaries.
-static bool encode_field_map(CUtensorMap *tm, void *base, int nx, int ny, int nf)
+// boxf: fields per box (0: all nf)
+static bool encode_field_map(CUtensorMap *tm, void *base, int nx, int ny, int nf, int boxf = 0)
 {
     auto enc = tensor_map_encoder();
     if (!enc) return false;
     const cuuint64_t dims[3] = {(cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nf};
     const cuuint64_t strides[2] = {(cuuint64_t)nx * 4, (cuuint64_t)nx * ny * 4};
-    const cuuint32_t box[3] = {40, 34, (cuuint32_t)nf};
+    const cuuint32_t box[3] = {40, 34, (cuuint32_t)(boxf > 0 ? boxf : nf)};
     const cuuint32_t es[3] = {1, 1, 1};
     return enc(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
                CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
@@ -1271,12 +1272,15 @@ struct amps_ensemble {
         size_t smem = 0;
         cudaStream_t s = nullptr;  // its branch of a period graph
         cudaEvent_t done = nullptr;
+        bool pair = false;         // non-monitor steps as split tiles (gg_launch_ens_pair)
+        size_t smem_pair = 0;
     };
     std::vector<Group> groups;
     cudaEvent_t fork = nullptr;
     ClassifyArgs *d_cls = nullptr;      // whole periods: advance = stat_steps = cadence
     ClassifyArgs *d_cls_tmp = nullptr;  // partial periods (eager)
-    CUtensorMap *d_tmaps = nullptr;     // members' FP32 tensor maps [member][parity] (bulk staging)
+    CUtensorMap *d_tmaps = nullptr;     // members' FP32 tensor maps [member][box: all fields, split][parity]
+    std::vector<uint8_t> map8;          // [member]: its split-tile maps were encoded
     bool graphs = true;
     std::map<std::vector<uint8_t>, cudaGraphExec_t> periods;
     std::unique_ptr<EnsLaunch> launch;  // host staging of one launch's parameters
@@ -1377,6 +1381,22 @@ extern "C" int amps_ensemble_create(amps_handle *const *members, int count, amps
         g.members.push_back(order[i]);
         g.first.push_back(g.first.back() + h->ntiles);
     }
+    // split tiles (opt-in, AMPS_ENS_PAIR=1): a group whose members all have
+    // 2 * kPairFields fields runs its non-monitor steps as two-CTA clusters,
+    // half the fields each (32^2 tiles, the library's order).  Measured slower
+    // than whole tiles on the 64-member workload (43.9 against 53.7 Gcell/s:
+    // the two cluster barriers a tile cost more than the doubled occupancy
+    // gains), so whole tiles stay the default.
+    const char *pv = getenv("AMPS_ENS_PAIR");
+    bool any_pair = false;
+    for (auto &g : e->groups) {
+        bool all = e->T == 32 && !e->ref && pv && pv[0] == '1';
+        for (int mi : g.members) all = all && e->m[mi]->nf == 2 * kPairFields;
+        g.pair = all;
+        g.smem_pair = all ? gg_ens_smem_bytes(32, kPairFields) : 0;
+        any_pair |= all;
+    }
+    if (ce == cudaSuccess && any_pair) ce = gg_prepare_ens_pair(gg_ens_smem_bytes(32, kPairFields));
     for (auto &g : e->groups) {
         if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&g.s, cudaStreamNonBlocking);
         if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&g.done, cudaEventDisableTiming);
@@ -1388,13 +1408,20 @@ extern "C" int amps_ensemble_create(amps_handle *const *members, int count, amps
     if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&e->capture, cudaStreamNonBlocking);
     if (ce == cudaSuccess && e->T == 32) {
         // the members' tensor maps, in global memory where the ensemble kernel reads them
-        std::vector<CUtensorMap> maps((size_t)2 * count);
+        e->map8.assign(count, 0);
+        std::vector<CUtensorMap> maps((size_t)4 * count);
         memset(maps.data(), 0, sizeof(CUtensorMap) * maps.size());
-        for (int i = 0; i < count; ++i)
-            if (members[i]->tma_stage) {
-                maps[2 * i] = members[i]->tm[0];
-                maps[2 * i + 1] = members[i]->tm[1];
-            }
+        for (int i = 0; i < count; ++i) {
+            amps_handle *h = members[i];
+            if (!h->tma_stage) continue;
+            maps[4 * i] = h->tm[0];
+            maps[4 * i + 1] = h->tm[1];
+            if (h->nf == 2 * kPairFields)
+                e->map8[i] = encode_field_map(&maps[4 * i + 2], h->store[TIER_FP32][0], h->px, h->nty * h->T, h->nf,
+                                              kPairFields) &&
+                             encode_field_map(&maps[4 * i + 3], h->store[TIER_FP32][1], h->px, h->nty * h->T, h->nf,
+                                              kPairFields);
+        }
         ce = cudaMalloc(&e->d_tmaps, sizeof(CUtensorMap) * maps.size());
         if (ce == cudaSuccess)
             ce = cudaMemcpy(e->d_tmaps, maps.data(), sizeof(CUtensorMap) * maps.size(), cudaMemcpyHostToDevice);
@@ -1452,7 +1479,11 @@ static std::vector<StepArgs> ens_tables(const amps_ensemble *e, int k0, int cnt)
         for (int s = 0; s < cnt; ++s) {
             const bool mon = e->mixed && period_end && s == cnt - 1;
             t[(size_t)s * M + i] = step_args(h, par, tr, k0 + s, mon);
-            if (e->d_tmaps && h->tma_stage) t[(size_t)s * M + i].tmap = e->d_tmaps + 2 * i + par;
+            if (e->d_tmaps && h->tma_stage) {
+                t[(size_t)s * M + i].tmap = e->d_tmaps + 4 * i + par;
+                // split-tile boxes where they were encoded (else per-thread copies)
+                if (e->map8[i]) t[(size_t)s * M + i].tmap8 = e->d_tmaps + 4 * i + 2 + par;
+            }
             par ^= 1;
             tr = false;
         }
@@ -1472,7 +1503,8 @@ static int ens_launch(amps_ensemble *e, const amps_ensemble::Group &g, const std
         L.m[j] = tab[(size_t)k * M + g.members[j]];
     }
     L.first[L.count] = g.first[L.count];
-    ECK(e, gg_launch_ens(e->T, e->ref, mon, L, g.smem, s));
+    if (g.pair && !mon) ECK(e, gg_launch_ens_pair(L, g.smem_pair, s));
+    else ECK(e, gg_launch_ens(e->T, e->ref, mon, L, g.smem, s));
     return AMPS_OK;
 }
 

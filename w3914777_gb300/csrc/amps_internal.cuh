@@ -91,6 +91,7 @@ struct StepArgs {
     int half_arith;           // grain growth: AMPS_HALF_FP32 / _REF / _HFMA2 (half tiles' arithmetic)
     int tma_stage;            // grain growth: the launch carries a tensor map of the FP32 input (bulk staging)
     const CUtensorMap *tmap;  // ensemble steps: the member's tensor map of its FP32 input in global memory (or null)
+    const CUtensorMap *tmap8; // ensemble split tiles: the same input with boxes of kPairFields fields (or null)
     double *metric;           // [ntiles]
     double *snap;             // temporal snapshot: [nmon][ntiles][16] or [nmon][n]
     int *flags;               // bit 0: NaN/Inf seen; bit 1: a bounded device wait gave up
@@ -112,6 +113,27 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t by
 {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
 }
+// ---- thread-block clusters (the two CTAs of a split tile) --------------------
+// Every thread of both CTAs executes each barrier phase (aligned forms).
+__device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
+__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
+// The address of this CTA's shared-memory location p in the shared memory of cluster CTA `rank`.
+__device__ __forceinline__ uint32_t cluster_map(const void *p, uint32_t rank)
+{
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(smem_u32(p)), "r"(rank));
+    return r;
+}
+__device__ __forceinline__ float4 ld_cluster_f4(uint32_t addr)
+{
+    float4 v;
+    asm volatile("ld.shared::cluster.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+                 : "r"(addr)
+                 : "memory");
+    return v;
+}
+
 // 3-D tiled tensor load of one box into shared memory, completing on `bar`.
 __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *tm, int x, int y, int z, uint64_t *bar)
 {
@@ -290,6 +312,10 @@ template <int TIER, typename CT> __device__ __forceinline__ void store_tier(cons
 // ---- staged halo tile in shared memory ----------------------------------------
 // Field f occupies rows 0..T+2R-1 of pitch P = T + 2*O, the interior starting
 // at column O (16-byte aligned), the halo at O-R..O-1 and O+T..O+T+R-1.
+// Fields per CTA of a split grain-growth tile (ensemble members with twice
+// as many fields run a non-monitor step's tile as a two-CTA cluster).
+constexpr int kPairFields = 8;
+
 template <typename CT, int T, int R> struct Stage {
     static constexpr int O = 16 / sizeof(CT) >= R ? 16 / sizeof(CT) : R;
     static constexpr int P = T + 2 * O;
@@ -483,7 +509,7 @@ __device__ __forceinline__ void stage_band(const StepArgs &a, CT *dst, const uin
     }
 }
 
-// Stage fields [0, nfs) of a tile whose whole 3x3 neighbourhood holds FP32
+// Stage fields [f0, f0 + nfs) of a tile whose whole 3x3 neighbourhood holds FP32
 // input (no conversion) with an R-cell halo, by asynchronous global->shared
 // copies: 16-byte copies for the interior 8-cell row segments (L2 only, the
 // values are read once from global memory) and 4-byte copies for the halo
@@ -492,7 +518,7 @@ __device__ __forceinline__ void stage_band(const StepArgs &a, CT *dst, const uin
 // the final wait issued here (WAIT = false: committed, not waited for --
 // cp_async_wait_all before the shared memory is read or reused).
 template <int T, int R, bool WAIT = true>
-__device__ __forceinline__ void stage_tile_async32(const StepArgs &a, float *sm, int tx, int ty, int nfs)
+__device__ __forceinline__ void stage_tile_async32(const StepArgs &a, float *sm, int tx, int ty, int nfs, int f0 = 0)
 {
     using S = Stage<float, T, R>;
     constexpr int SEG = T / 8;
@@ -517,7 +543,7 @@ __device__ __forceinline__ void stage_tile_async32(const StepArgs &a, float *sm,
             seg = false;
         }
         for (int f = 0; f < nfs; ++f) {
-            const float *g = src + (int64_t)f * a.n + goff;
+            const float *g = src + (int64_t)(f0 + f) * a.n + goff;
             const uint32_t d = smem_u32(sm + f * S::FIELD + soff);
             if (seg) {
                 asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(g) : "memory");

@@ -70,6 +70,11 @@ size_t gg_ens_smem_bytes(int tile, int max_nf);
 cudaError_t gg_prepare_ens(int tile, bool ref, size_t max_smem);
 cudaError_t gg_ens_occupancy(int tile, bool ref, size_t smem, int *blocks_per_sm);
 cudaError_t gg_launch_ens(int tile, bool ref, bool monitor, const EnsLaunch &L, size_t smem, cudaStream_t s);
+// Split tiles (32^2, the library's order, non-monitor steps): every member of
+// L has 2 * kPairFields fields, and each tile runs as a two-CTA cluster of
+// kPairFields fields each (grid: two CTAs per work item of L.first).
+cudaError_t gg_prepare_ens_pair(size_t smem);
+cudaError_t gg_launch_ens_pair(const EnsLaunch &L, size_t smem, cudaStream_t s);
 size_t kob_smem_bytes(int tile, int tier);
 size_t sint_smem_bytes(int tile, int tier, int nf, bool mu64);
 

@@ -132,15 +132,18 @@ __device__ __forceinline__ void gg_tile_lo(const StepArgs &a, const float *sm, i
 // temporal, 3: rate; the spatial range takes gg_tile_lo_impl): the tile
 // metric is a maximum over fields and cells, so each thread folds every
 // field it computes into one accumulator and the block reduces once.
-template <int TIER, int RPT, int MK = 0>
+// PH > 0: one CTA of a split tile -- staging slots 0..PH-1 hold fields
+// [f0, f0 + PH), and the caller has formed `ss` over every field.
+template <int TIER, int RPT, int MK = 0, int PH = 0>
 __device__ __forceinline__ void gg_tile_lo_rows(const StepArgs &a, const float *sm, float *ss, int tile, int tx,
-                                                int ty, double *red)
+                                                int ty, double *red, int f0 = 0)
 {
+    static_assert(PH == 0 || MK == 0, "split tiles run the steps without a monitor");
     constexpr int T = 32, CPT = 4, GPR = T / CPT;
     using S = Stage<float, T, 1>;
     float *smm = const_cast<float *>(sm);
-    const int nf = a.nf;
-    {
+    const int nf = PH ? PH : a.nf;
+    if constexpr (PH == 0) {
         const int row = threadIdx.x / GPR, c = (threadIdx.x % GPR) * CPT;
         float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
         for (int f = 0; f < nf; ++f) {
@@ -151,8 +154,8 @@ __device__ __forceinline__ void gg_tile_lo_rows(const StepArgs &a, const float *
             acc.w = fmaf(q.w, q.w, acc.w);
         }
         *reinterpret_cast<float4 *>(ss + row * T + c) = acc;
+        __syncthreads();
     }
-    __syncthreads();
     static_assert(T % RPT == 0 && (T / RPT) * GPR * RPT == kThreads, "RPT groups of T/RPT x GPR threads");
     const int group = threadIdx.x / (kThreads / RPT), t = threadIdx.x % (kThreads / RPT);
     const int r0 = RPT * (t / GPR), c0 = (t % GPR) * CPT;  // tile-local rows r0 .. r0+RPT-1
@@ -196,7 +199,7 @@ __device__ __forceinline__ void gg_tile_lo_rows(const StepArgs &a, const float *
                 out[k] = fmaf(-dtm, fmaf(-kap, lap, dfd), e);
             }
             const int64_t gi = gbase + (int64_t)i * a.px;
-            store_cells<TIER, CPT>(a, (int64_t)f * a.n + gi, out);
+            store_cells<TIER, CPT>(a, (int64_t)(f0 + f) * a.n + gi, out);
             if constexpr (MK != 0) {
                 // a ragged grid's edge tile: cells past the domain are not samples
                 if (mon_f && r0 + i < min(T, a.ny - ty * T)) {
@@ -233,8 +236,11 @@ __device__ __forceinline__ double ld_nb64(const StepArgs &a, const uint8_t *nt, 
 // FP64 tile: direct loads through L1 with a rolling 3-row window, FP64
 // arithmetic; REF keeps the reference's expression order and rounding
 // (graingrowth/function.h:20-23).
-template <int T, bool REF, bool PARTIAL = false>
-__device__ __forceinline__ void gg_tile_fp64(const StepArgs &a, const uint8_t *nt, int tile, int tx, int ty, double *red)
+// PH > 0: this CTA updates fields [f0, f0 + PH) of the tile (one CTA of a
+// split tile; the sum of squares still covers every field).
+template <int T, bool REF, bool PARTIAL = false, int PH = 0>
+__device__ __forceinline__ void gg_tile_fp64(const StepArgs &a, const uint8_t *nt, int tile, int tx, int ty, double *red,
+                                             int f0 = 0)
 {
     constexpr bool partial = PARTIAL;  // a ragged grid's edge tile: owner-tier loads
     constexpr int RPT = T * T / kThreads;
@@ -256,7 +262,7 @@ __device__ __forceinline__ void gg_tile_fp64(const StepArgs &a, const uint8_t *n
     const int64_t gbase = (int64_t)(y0 + r0) * a.px + x0 + col;
     double metric = 0.0;
     MonAcc mon;
-    for (int f = 0; f < nf; ++f) {
+    for (int f = PH ? f0 : 0; f < (PH ? f0 + PH : nf); ++f) {
         const bool mon_f = a.monitor_now && (a.mfield < 0 || a.mfield == f);
         const int mslot = a.mfield < 0 ? f : 0;
         if (mon_f) mon_reset(a, mon);
@@ -322,11 +328,11 @@ __device__ __forceinline__ void gg_tile_fp64(const StepArgs &a, const uint8_t *n
 }
 
 // The FP64 tile of a ragged grid's edge, out of line (off the whole tiles' registers).
-template <int T, bool REF>
+template <int T, bool REF, int PH = 0>
 __device__ __noinline__ void gg_tile_fp64_partial(const StepArgs &a, const uint8_t *nt, int tile, int tx, int ty,
-                                                  double *red)
+                                                  double *red, int f0 = 0)
 {
-    gg_tile_fp64<T, REF, true>(a, nt, tile, tx, ty, red);
+    gg_tile_fp64<T, REF, true, PH>(a, nt, tile, tx, ty, red, f0);
 }
 
 __device__ __forceinline__ __half2 gg_hconst(const Phys &ph, int i)
@@ -453,9 +459,10 @@ __device__ __forceinline__ bool gg_partial_tile(const StepArgs &a, int T, int tx
 }
 
 // The patch of a partial tile's staging (Stage<CT, T, 1> layout, fields
-// [0, nf)); the caller synchronises before and after.
+// [f0, f0 + nfs) in slots 0..nfs-1; nfs < 0: all); the caller synchronises
+// before and after.
 template <typename CT, int T>
-__device__ __noinline__ void patch_ragged(const StepArgs &a, CT *sm, int tx, int ty)
+__device__ __noinline__ void patch_ragged(const StepArgs &a, CT *sm, int tx, int ty, int f0 = 0, int nfs = -1)
 {
     using S = Stage<CT, T, 1>;
     const int x0 = tx * T, y0 = ty * T;
@@ -470,7 +477,8 @@ __device__ __noinline__ void patch_ragged(const StepArgs &a, CT *sm, int tx, int
         const int tier = a.tier_in[(gy / T) * a.ntx + gx / T];
         const int64_t o = (int64_t)gy * a.px + gx;
         CT *d = &S::at(sm, 0, ly + 1, S::O + lx);
-        for (int f = 0; f < a.nf; ++f) d[f * S::FIELD] = load_tier<CT>(a, tier, (int64_t)f * a.n + o);
+        const int nl = nfs < 0 ? a.nf : nfs;
+        for (int f = 0; f < nl; ++f) d[f * S::FIELD] = load_tier<CT>(a, tier, (int64_t)(f0 + f) * a.n + o);
     }
 }
 
